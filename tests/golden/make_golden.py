@@ -1,0 +1,118 @@
+"""Regenerate the golden fixtures in this directory from the reference's own
+CPU code (oracle/_ref/libref.so, built in place from the reference tree by
+oracle/build_ref.sh). Run from the repository root where the reference tree
+exists:
+
+    python tests/golden/make_golden.py
+
+Fixtures:
+  dext_fused_cases.npz    the 48 frames of tests/spots/test_dext_fused.cc
+                          (8 sizes x 3 means x {u16, u32}, seeds 1..24, the
+                          reference's own generator) with dext<T>()'s output
+  dext_device_frames.npz  the 7 frames of tests/spots/test_dext_gpu.cc
+                          (synthetic_frame.hh make_frame) with dext<u16>()'s
+                          output and dext<u32>()'s output on the frame widened
+                          to 32 bits
+  sweep_small.npz         a 12-frame 256 x 320 uint32 sweep from this
+                          package's generator, with dext<u32>() per frame and
+                          dials_spots::Labeller's spots, kept pixels and
+                          counts in 3-D and 2-D, and with frame 7 missing (a gap)
+  refl_small.refl         refl::write of the 3-D spot table of sweep_small,
+                          shoeboxes on (byte-exact writer fixture)
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+sys.path.insert(0, os.path.join(REPO, "dials-metal_gb300"))
+
+import oracle as O  # noqa: E402
+
+FUSED_SIZES = [(1, 1), (5, 7), (32, 32), (33, 65), (100, 37), (67, 300), (257, 511), (64, 96)]
+DEVICE_FRAMES = [("exact tile", 32, 32, 1, 12.0, False),
+                 ("under one tile", 19, 27, 2, 8.0, False),
+                 ("ragged", 200, 301, 3, 15.0, False),
+                 ("ragged, masked", 200, 301, 4, 15.0, True),
+                 ("dark", 128, 128, 5, 1.0, False),
+                 ("module", 512, 1030, 6, 20.0, True)]
+
+
+def fused_cases():
+    out = {}
+    meta = []
+    seed = 1
+    i = 0
+    for (h, w) in FUSED_SIZES:
+        for mean in (0.3, 2.0, 12.0):
+            for dt in (np.uint16, np.uint32):
+                f = O.ref_fused_make(h, w, seed, mean, dt)
+                out[f"frame_{i}"] = f
+                out[f"signal_{i}"] = O.ref_dext(f)
+                meta.append((h, w, seed, mean, 16 if dt == np.uint16 else 32))
+                i += 1
+            seed += 1
+    out["meta"] = np.array(meta, dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, "dext_fused_cases.npz"), **out)
+    return i
+
+
+def device_frames():
+    out = {}
+    names = []
+    for i, (name, h, w, seed, bg, masked) in enumerate(DEVICE_FRAMES):
+        f = O.ref_make_frame(h, w, seed, bg, masked)
+        out[f"frame_{i}"] = f
+        out[f"signal16_{i}"] = O.ref_dext(f)
+        out[f"signal32_{i}"] = O.ref_dext(f.astype(np.uint32))
+        names.append(name)
+    # The all-masked frame the device test builds by hand.
+    i = len(DEVICE_FRAMES)
+    f = np.full((64, 64), 0xFFFF, np.uint16)
+    out[f"frame_{i}"] = f
+    out[f"signal16_{i}"] = O.ref_dext(f)
+    out[f"signal32_{i}"] = O.ref_dext(np.full((64, 64), 0xFFFFFFFF, np.uint32))
+    names.append("entirely masked")
+    out["names"] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, "dext_device_frames.npz"), **out)
+    return len(names)
+
+
+def sweep_small():
+    from sfgb import synth
+    p = synth.preset("plain_1m", height=256, width=320, n_frames=12,
+                     spots_per_frame=25.0, row_band_start=100, row_band_len=3,
+                     col_band_start=200, col_band_len=2, n_hot=10, seed=77)
+    sw = synth.Sweep(p)
+    frames = np.stack([sw.frame(i) for i in range(p.n_frames)])
+    out = {"frames": frames}
+    signals = [O.ref_dext(f) for f in frames]
+    for i, s in enumerate(signals):
+        out[f"signal_{i}"] = s
+    for tag, two_d, skip in (("3d", False, None), ("2d", True, None), ("gap", False, 7)):
+        lab = O.RefLabeller(p.height, p.width, two_d=two_d)
+        for i, s in enumerate(signals):
+            if i == skip:
+                continue
+            lab.add(i, s)
+        r = lab.finish()
+        out[f"spots_{tag}"] = r.spots
+        out[f"pixels_{tag}"] = r.pixels
+        out[f"counts_{tag}"] = np.array([r.counts[k] for k in O.COUNT_NAMES], np.uint64)
+        if tag == "3d":
+            lab.write_refl(os.path.join(HERE, "refl_small.refl"), shoeboxes=True)
+    np.savez_compressed(os.path.join(HERE, "sweep_small.npz"), **out)
+    return len(out["spots_3d"])
+
+
+if __name__ == "__main__":
+    if not O.ref_available():
+        O.build(quiet=False)
+    if not O.ref_available():
+        sys.exit("the reference library could not be built (no reference tree?)")
+    print("fused cases:", fused_cases())
+    print("device frames:", device_frames())
+    print("sweep spots (3-D):", sweep_small())
