@@ -1,0 +1,456 @@
+// The C ABI (include/sf_api.h): device discovery, pinned host memory, and
+// the per-thread host-frame threshold that replaces gpu::find<T>
+// (src/spots/dext_cuda.cu:711-869), plus the device-resident entry points.
+
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "sf_api.h"
+#include "sf_common.cuh"
+#include "sf_threshold.cuh"
+
+namespace sf {
+
+thread_local std::string t_last_error;
+static bool g_profiling = false;
+thread_local sf_stage_times t_stage_times = {0, 0, 0, 0, 0, 0, 0};
+
+int fail(cudaError_t e, const char *what) {
+  t_last_error = std::string("CUDA: ") + what + ": " + cudaGetErrorString(e);
+  return SF_ECUDA;
+}
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Validates the parameters and precomputes the per-launch constants.
+int make_launch_params(const sf_threshold_params *in, LaunchParams *P) {
+  sf_threshold_params p;
+  if (in)
+    p = *in;
+  else
+    sf_default_params(&p);
+  if (p.algorithm != SF_DISPERSION_EXTENDED && p.algorithm != SF_DISPERSION)
+    return SF_EBADARG;
+  if (p.kernel_x != p.kernel_y || p.kernel_x < 2 || p.kernel_x > kMaxHalf)
+    return SF_EUNSUPPORTED;
+  if (p.min_local < 0 || !std::isfinite(p.gain) || !std::isfinite(p.sigma_b) ||
+      !std::isfinite(p.sigma_s))
+    return SF_EBADARG;
+  std::memset(P, 0, sizeof(*P));
+  P->algorithm = p.algorithm;
+  P->half = p.kernel_x;
+  P->gain = p.gain;
+  P->sigma_b = p.sigma_b;
+  P->sigma_s = p.sigma_s;
+  P->min_local = (uint32_t)p.min_local;
+  // value > global_threshold, as the smallest integer value that passes.
+  const double gt = p.global_threshold;
+  if (std::isnan(gt))
+    P->p_min = ~0ull;
+  else if (gt < 0.0)
+    P->p_min = 0;
+  else if (gt >= 4294967296.0)
+    P->p_min = ~0ull;
+  else
+    P->p_min = (uint64_t)std::floor(gt) + 1ull;
+  P->int_ok = p.gain == 1.0 && p.sigma_b == std::floor(p.sigma_b) &&
+              p.sigma_b >= 0.0 && p.sigma_b <= 1024.0 &&
+              p.sigma_s == std::floor(p.sigma_s) && p.sigma_s >= 0.0 &&
+              p.sigma_s <= 1024.0;
+  P->sigma_b_int = P->int_ok ? (uint32_t)p.sigma_b : 0;
+  P->sigma_s2_int = P->int_ok ? (uint32_t)(p.sigma_s * p.sigma_s) : 0;
+  for (int n = 0; n <= kMaxN0; n++) {
+    // The reference's sqrt(R(2) * (m - R(1))), correctly rounded on both
+    // sides of the bus.
+    const double r = std::sqrt(2.0 * ((double)n - 1.0));
+    P->root[n] = r;
+    P->rootf[n] = std::sqrt(2.0f * ((float)n - 1.0f));
+    if (n >= 1) {
+      const double scaled = std::ldexp(r, kRootShift); // exact
+      P->root_lo[n] = (uint32_t)std::floor(scaled);
+      P->root_hi[n] = (uint32_t)std::ceil(scaled);
+    }
+  }
+  return SF_OK;
+}
+
+struct WorkspaceLayout {
+  size_t staging, tile_base, row_total, total;
+};
+
+static WorkspaceLayout layout(size_t h, size_t w, size_t capacity) {
+  WorkspaceLayout L;
+  L.staging = 0;
+  size_t off = align_up(capacity * sizeof(sf_signal_pixel), 256);
+  L.tile_base = off;
+  off += align_up((size_t)tiles_x((int)w) * tiles_y((int)h) * sizeof(uint32_t), 256);
+  L.row_total = off;
+  off += align_up((size_t)tiles_y((int)h) * sizeof(uint32_t), 256);
+  L.total = off;
+  return L;
+}
+
+static bool shape_ok(size_t h, size_t w) {
+  // The kernels index in 32 bits, as the reference (dext.cc:17-23).
+  return h > 0 && w > 0 && h <= 0x7fffffffu / w;
+}
+
+template <typename T>
+static int threshold_device(const T *d_image, size_t h, size_t w,
+                            const sf_threshold_params *params,
+                            sf_signal_pixel *d_out, size_t capacity,
+                            uint32_t *d_bits, uint32_t *d_count,
+                            uint32_t *d_word_prefix, void *d_ws, size_t ws_bytes,
+                            cudaStream_t stream) {
+  if (!d_image || !d_out || !d_bits || !d_count || !d_ws || !shape_ok(h, w) ||
+      capacity > 0xffffffffu)
+    return SF_EBADARG;
+  LaunchParams P;
+  int rc = make_launch_params(params, &P);
+  if (rc != SF_OK)
+    return rc;
+  const WorkspaceLayout L = layout(h, w, capacity);
+  if (ws_bytes < L.total)
+    return SF_EBADARG;
+  unsigned char *ws = static_cast<unsigned char *>(d_ws);
+  FrameBuffers fb;
+  fb.bits = d_bits;
+  fb.staging = reinterpret_cast<sf_signal_pixel *>(ws + L.staging);
+  fb.out = d_out;
+  fb.word_prefix = d_word_prefix;
+  fb.tile_base = reinterpret_cast<uint32_t *>(ws + L.tile_base);
+  fb.row_total = reinterpret_cast<uint32_t *>(ws + L.row_total);
+  fb.total = d_count;
+  fb.capacity = (uint32_t)capacity;
+  cudaError_t e = launch_threshold<T>(d_image, (int)h, (int)w, P, fb, stream);
+  if (e != cudaSuccess)
+    return fail(e, "launching the threshold");
+  return SF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The per-thread host-frame path (gpu::find<T>).
+// ---------------------------------------------------------------------------
+
+class Workspace {
+public:
+  ~Workspace() {
+    if (stream_) {
+      cudaStreamSynchronize(stream_);
+      cudaStreamDestroy(stream_);
+    }
+    for (cudaEvent_t &ev : marks_)
+      if (ev)
+        cudaEventDestroy(ev);
+    cudaFree(image_);
+    cudaFree(bits_);
+    cudaFree(out_);
+    cudaFree(ws_);
+    cudaFree(count_);
+    if (host_count_)
+      cudaFreeHost(host_count_);
+  }
+
+  int reserve(size_t image_bytes, size_t h, size_t w, size_t capacity) {
+    cudaError_t e;
+    if (!stream_) {
+      if ((e = cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking)) != cudaSuccess)
+        return fail(e, "cudaStreamCreate");
+      if ((e = cudaMalloc(&count_, sizeof(uint32_t))) != cudaSuccess)
+        return fail(e, "cudaMalloc for the count");
+      if ((e = cudaMallocHost(&host_count_, sizeof(uint32_t))) != cudaSuccess)
+        return fail(e, "cudaMallocHost for the count");
+    }
+    const size_t bits_bytes = words_per_row((int)w) * h * sizeof(uint32_t);
+    const size_t ws_bytes = sf_workspace_bytes(h, w, capacity);
+    const size_t out_bytes = capacity * sizeof(sf_signal_pixel);
+    if (image_bytes <= image_cap_ && bits_bytes <= bits_cap_ &&
+        ws_bytes <= ws_cap_ && out_bytes <= out_cap_)
+      return SF_OK;
+    // Nothing may be in flight when the buffers go (dext_cuda.cu:508-511).
+    cudaStreamSynchronize(stream_);
+    if (image_bytes > image_cap_) {
+      cudaFree(image_);
+      image_ = nullptr;
+      image_cap_ = 0;
+      if ((e = cudaMalloc(&image_, image_bytes)) != cudaSuccess)
+        return fail(e, "cudaMalloc for the frame");
+      image_cap_ = image_bytes;
+    }
+    if (bits_bytes > bits_cap_) {
+      cudaFree(bits_);
+      bits_ = nullptr;
+      bits_cap_ = 0;
+      if ((e = cudaMalloc(&bits_, bits_bytes)) != cudaSuccess)
+        return fail(e, "cudaMalloc for the bitmask");
+      bits_cap_ = bits_bytes;
+    }
+    if (ws_bytes > ws_cap_) {
+      cudaFree(ws_);
+      ws_ = nullptr;
+      ws_cap_ = 0;
+      if ((e = cudaMalloc(&ws_, ws_bytes)) != cudaSuccess)
+        return fail(e, "cudaMalloc for the workspace");
+      ws_cap_ = ws_bytes;
+    }
+    if (out_bytes > out_cap_) {
+      cudaFree(out_);
+      out_ = nullptr;
+      out_cap_ = 0;
+      if ((e = cudaMalloc(&out_, out_bytes)) != cudaSuccess)
+        return fail(e, "cudaMalloc for the signal list");
+      out_cap_ = out_bytes;
+    }
+    return SF_OK;
+  }
+
+  cudaEvent_t *marks() {
+    if (!marks_[0])
+      for (cudaEvent_t &ev : marks_)
+        cudaEventCreate(&ev);
+    return marks_;
+  }
+
+  cudaStream_t stream_ = nullptr;
+  void *image_ = nullptr;
+  uint32_t *bits_ = nullptr;
+  sf_signal_pixel *out_ = nullptr;
+  void *ws_ = nullptr;
+  uint32_t *count_ = nullptr;
+  uint32_t *host_count_ = nullptr;
+  size_t image_cap_ = 0, bits_cap_ = 0, ws_cap_ = 0, out_cap_ = 0;
+  cudaEvent_t marks_[3] = {nullptr, nullptr, nullptr};
+};
+
+static Workspace &workspace() {
+  static thread_local Workspace ws;
+  return ws;
+}
+
+// Leaves the stream idle however find() is left (dext_cuda.cu:455-467).
+struct StreamGuard {
+  cudaStream_t s;
+  ~StreamGuard() {
+    if (s)
+      cudaStreamSynchronize(s);
+  }
+};
+
+template <typename T>
+static int find_host(const T *image, size_t h, size_t w,
+                     const sf_threshold_params *params, sf_signal_pixel *out,
+                     size_t capacity, size_t *found) {
+  if (found)
+    *found = 0;
+  if (!image || !found || (!out && capacity) || !shape_ok(h, w))
+    return SF_EBADARG;
+  if (capacity > 0xffffffffu)
+    capacity = 0xffffffffu;
+  LaunchParams P;
+  int rc = make_launch_params(params, &P);
+  if (rc != SF_OK)
+    return rc;
+  const size_t bytes = h * w * sizeof(T);
+  // The device list needs at least one record for the kernels' pointers.
+  const size_t dcap = capacity ? capacity : 1;
+  Workspace &ws = workspace();
+  if ((rc = ws.reserve(bytes, h, w, dcap)) != SF_OK)
+    return rc;
+  const cudaStream_t stream = ws.stream_;
+  StreamGuard idle{stream};
+  const bool timing = g_profiling;
+  cudaEvent_t *marks = timing ? ws.marks() : nullptr;
+  cudaError_t e;
+  if (timing)
+    cudaEventRecord(marks[0], stream);
+  if ((e = cudaMemcpyAsync(ws.image_, image, bytes, cudaMemcpyHostToDevice, stream)) !=
+      cudaSuccess)
+    return fail(e, "copying a frame to the device");
+  if (timing)
+    cudaEventRecord(marks[1], stream);
+  rc = threshold_device<T>(static_cast<const T *>(ws.image_), h, w, params, ws.out_,
+                           dcap, ws.bits_, ws.count_, nullptr, ws.ws_, ws.ws_cap_,
+                           stream);
+  if (rc != SF_OK)
+    return rc;
+  if (timing)
+    cudaEventRecord(marks[2], stream);
+  if ((e = cudaMemcpyAsync(ws.host_count_, ws.count_, sizeof(uint32_t),
+                           cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
+    return fail(e, "reading the signal count back");
+  if ((e = cudaStreamSynchronize(stream)) != cudaSuccess)
+    return fail(e, "cudaStreamSynchronize");
+  const size_t n = *ws.host_count_;
+  *found = n;
+  sf_stage_times times = {0, 0, 0, 0, 0, 0, 0};
+  if (timing) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, marks[0], marks[1]);
+    times.upload = ms;
+    cudaEventElapsedTime(&ms, marks[1], marks[2]);
+    times.fused = ms;
+  }
+  if (n > capacity) {
+    if (timing)
+      t_stage_times = times;
+    return SF_EOVERFLOW;
+  }
+  if (n) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if ((e = cudaMemcpyAsync(out, ws.out_, n * sizeof(sf_signal_pixel),
+                             cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
+      return fail(e, "copying the signal pixels back");
+    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess)
+      return fail(e, "cudaStreamSynchronize");
+    times.copy = std::chrono::duration<double, std::milli>(
+                     std::chrono::steady_clock::now() - t0)
+                     .count();
+  }
+  if (timing)
+    t_stage_times = times;
+  return SF_OK;
+}
+
+} // namespace sf
+
+using namespace sf;
+
+extern "C" {
+
+void sf_default_params(sf_threshold_params *p) {
+  if (!p)
+    return;
+  p->algorithm = SF_DISPERSION_EXTENDED;
+  p->kernel_x = 3;
+  p->kernel_y = 3;
+  p->gain = 1.0;
+  p->sigma_b = 6.0;
+  p->sigma_s = 3.0;
+  p->min_local = 2;
+  p->global_threshold = 0.0;
+}
+
+const char *sf_backend(void) { return "CUDA (GB300, sm_103a)"; }
+
+static std::once_flag g_probe_once;
+static int g_available = 0;
+static std::string g_reason;
+
+static void probe() {
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess) {
+    g_reason = std::string("no CUDA device: ") + cudaGetErrorString(e);
+    return;
+  }
+  if (count == 0) {
+    g_reason = "no CUDA device";
+    return;
+  }
+  int dev = 0, major = 0, minor = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  if (major != 10 || minor != 3) {
+    char buf[128];
+    std::snprintf(buf, sizeof(buf),
+                  "device %d is compute capability %d.%d; this build is sm_103a only",
+                  dev, major, minor);
+    g_reason = buf;
+    return;
+  }
+  g_available = 1;
+}
+
+int sf_available(void) {
+  std::call_once(g_probe_once, probe);
+  return g_available;
+}
+
+const char *sf_unavailable_reason(void) {
+  std::call_once(g_probe_once, probe);
+  return g_available ? "" : g_reason.c_str();
+}
+
+size_t sf_memory_free(void) {
+  size_t free_b = 0, total = 0;
+  if (cudaMemGetInfo(&free_b, &total) != cudaSuccess)
+    return 0;
+  return free_b;
+}
+
+void *sf_host_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess)
+    return nullptr;
+  return p;
+}
+
+void sf_host_free(void *pointer) {
+  if (pointer)
+    cudaFreeHost(pointer);
+}
+
+const char *sf_last_error(void) { return t_last_error.c_str(); }
+
+int sf_find_u32(const uint32_t *image, size_t height, size_t width,
+                sf_signal_pixel *out, size_t capacity, size_t *found) {
+  return find_host<uint32_t>(image, height, width, nullptr, out, capacity, found);
+}
+int sf_find_u16(const uint16_t *image, size_t height, size_t width,
+                sf_signal_pixel *out, size_t capacity, size_t *found) {
+  return find_host<uint16_t>(image, height, width, nullptr, out, capacity, found);
+}
+int sf_find_u32_params(const uint32_t *image, size_t height, size_t width,
+                       const sf_threshold_params *params, sf_signal_pixel *out,
+                       size_t capacity, size_t *found) {
+  return find_host<uint32_t>(image, height, width, params, out, capacity, found);
+}
+int sf_find_u16_params(const uint16_t *image, size_t height, size_t width,
+                       const sf_threshold_params *params, sf_signal_pixel *out,
+                       size_t capacity, size_t *found) {
+  return find_host<uint16_t>(image, height, width, params, out, capacity, found);
+}
+
+void sf_profile_stages(int on) { g_profiling = on != 0; }
+int sf_profiling(void) { return g_profiling ? 1 : 0; }
+void sf_last_stage_times(sf_stage_times *out) {
+  if (out)
+    *out = t_stage_times;
+}
+
+size_t sf_workspace_bytes(size_t height, size_t width, size_t capacity) {
+  if (!shape_ok(height, width))
+    return 0;
+  return layout(height, width, capacity).total;
+}
+
+int sf_threshold_u32_device(const uint32_t *d_image, size_t height, size_t width,
+                            const sf_threshold_params *params,
+                            sf_signal_pixel *d_out, size_t capacity,
+                            uint32_t *d_bits, uint32_t *d_count,
+                            uint32_t *d_word_prefix, void *d_workspace,
+                            size_t workspace_bytes, void *stream) {
+  return threshold_device<uint32_t>(d_image, height, width, params, d_out, capacity,
+                                    d_bits, d_count, d_word_prefix, d_workspace,
+                                    workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+int sf_threshold_u16_device(const uint16_t *d_image, size_t height, size_t width,
+                            const sf_threshold_params *params,
+                            sf_signal_pixel *d_out, size_t capacity,
+                            uint32_t *d_bits, uint32_t *d_count,
+                            uint32_t *d_word_prefix, void *d_workspace,
+                            size_t workspace_bytes, void *stream) {
+  return threshold_device<uint16_t>(d_image, height, width, params, d_out, capacity,
+                                    d_bits, d_count, d_word_prefix, d_workspace,
+                                    workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+} // extern "C"

@@ -1,0 +1,238 @@
+"""ctypes bindings of the C ABI (include/sf_api.h, libsfgb.so).
+
+The host-frame calls mirror the reference's threshold backend
+(src/spots/dext_gpu.hh): `find()` is gpu::find<T>, returning the signal
+pixels ascending by index, with the same 0 / -1 / -2 status meanings turned
+into Python exceptions the way mxi_find turns them into runtime errors
+(src/spots/find_spots.cc:410-416). The device calls take torch CUDA tensors
+and enqueue on the current torch stream.
+
+There is no CPU fallback: if the library is missing or no sm_103a device is
+present these raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _paths
+
+SF_OK, SF_EBADARG, SF_EOVERFLOW, SF_ECUDA, SF_EUNSUPPORTED = 0, -1, -2, -3, -4
+DISPERSION_EXTENDED, DISPERSION = 0, 1
+
+# src/spots/signal_pixel.hh:20-28
+SIGNAL_DTYPE = np.dtype([("index", "<u4"), ("value", "<u4"), ("background", "<f4"),
+                         ("population", "<u2"), ("reserved", "<u2")])
+
+
+class ThresholdParams(ctypes.Structure):
+    _fields_ = [("algorithm", ctypes.c_int), ("kernel_x", ctypes.c_int),
+                ("kernel_y", ctypes.c_int), ("gain", ctypes.c_double),
+                ("sigma_b", ctypes.c_double), ("sigma_s", ctypes.c_double),
+                ("min_local", ctypes.c_int), ("global_threshold", ctypes.c_double)]
+
+
+class StageTimes(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("upload", "stage0", "stage1", "stage2", "fused", "copy", "sort")]
+
+
+@dataclass
+class Params:
+    """Threshold parameters. Defaults are the reference's fixed ones."""
+    algorithm: int = DISPERSION_EXTENDED
+    kernel_x: int = 3
+    kernel_y: int = 3
+    gain: float = 1.0
+    sigma_b: float = 6.0
+    sigma_s: float = 3.0
+    min_local: int = 2
+    global_threshold: float = 0.0
+
+    def c(self) -> ThresholdParams:
+        return ThresholdParams(self.algorithm, self.kernel_x, self.kernel_y, self.gain,
+                               self.sigma_b, self.sigma_s, self.min_local,
+                               self.global_threshold)
+
+
+class SpotFinderError(RuntimeError):
+    pass
+
+
+class OverflowError_(SpotFinderError):
+    """More signal pixels than the output holds (status -2)."""
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        path = _paths.core_lib()
+        if not os.path.exists(path):
+            raise SpotFinderError(f"{path} is not built; run __graft_entry__.build()")
+        L = ctypes.CDLL(path)
+        vp, sz, u32p = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p
+        L.sf_default_params.argtypes = [ctypes.POINTER(ThresholdParams)]
+        L.sf_backend.restype = ctypes.c_char_p
+        L.sf_available.restype = ctypes.c_int
+        L.sf_unavailable_reason.restype = ctypes.c_char_p
+        L.sf_memory_free.restype = sz
+        L.sf_host_alloc.argtypes = [sz]
+        L.sf_host_alloc.restype = vp
+        L.sf_host_free.argtypes = [vp]
+        L.sf_last_error.restype = ctypes.c_char_p
+        for name in ("sf_find_u32", "sf_find_u16"):
+            getattr(L, name).argtypes = [vp, sz, sz, vp, sz, ctypes.POINTER(sz)]
+            getattr(L, name).restype = ctypes.c_int
+        for name in ("sf_find_u32_params", "sf_find_u16_params"):
+            getattr(L, name).argtypes = [vp, sz, sz, ctypes.POINTER(ThresholdParams), vp,
+                                         sz, ctypes.POINTER(sz)]
+            getattr(L, name).restype = ctypes.c_int
+        L.sf_profile_stages.argtypes = [ctypes.c_int]
+        L.sf_profiling.restype = ctypes.c_int
+        L.sf_last_stage_times.argtypes = [ctypes.POINTER(StageTimes)]
+        L.sf_workspace_bytes.argtypes = [sz, sz, sz]
+        L.sf_workspace_bytes.restype = sz
+        for name in ("sf_threshold_u32_device", "sf_threshold_u16_device"):
+            getattr(L, name).argtypes = [vp, sz, sz, ctypes.POINTER(ThresholdParams), vp,
+                                         sz, u32p, u32p, u32p, vp, sz, vp]
+            getattr(L, name).restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def backend() -> str:
+    return lib().sf_backend().decode()
+
+
+def available() -> bool:
+    return bool(lib().sf_available())
+
+
+def unavailable_reason() -> str:
+    return lib().sf_unavailable_reason().decode()
+
+
+def last_error() -> str:
+    return lib().sf_last_error().decode()
+
+
+def _check(rc: int, what: str) -> None:
+    if rc == SF_OK:
+        return
+    if rc == SF_EOVERFLOW:
+        raise OverflowError_(f"{what}: more signal pixels than the output holds")
+    if rc == SF_EBADARG:
+        raise ValueError(f"{what}: bad argument")
+    if rc == SF_EUNSUPPORTED:
+        raise SpotFinderError(f"{what}: unsupported by this backend")
+    raise SpotFinderError(f"{what}: {last_error()}")
+
+
+def find(frame: np.ndarray, params: Params | None = None,
+         capacity: int | None = None) -> np.ndarray:
+    """Threshold one host frame (uint16/uint32, (h, w)); the signal pixels
+    ascending by index. capacity defaults to the reference's device bound,
+    one record per 16 bytes of frame (src/spots/dext_cuda.cu:741)."""
+    frame = np.ascontiguousarray(frame)
+    if frame.ndim != 2:
+        raise ValueError("a frame is two-dimensional")
+    h, w = frame.shape
+    if capacity is None:
+        capacity = max(1, frame.nbytes // 16)
+    out = np.empty(capacity, SIGNAL_DTYPE)
+    found = ctypes.c_size_t(0)
+    L = lib()
+    if frame.dtype == np.uint32:
+        fn, fnp = L.sf_find_u32, L.sf_find_u32_params
+    elif frame.dtype == np.uint16:
+        fn, fnp = L.sf_find_u16, L.sf_find_u16_params
+    else:
+        raise TypeError("frames are uint16 or uint32")
+    if params is None:
+        rc = fn(frame.ctypes.data, h, w, out.ctypes.data, capacity, ctypes.byref(found))
+    else:
+        p = params.c()
+        rc = fnp(frame.ctypes.data, h, w, ctypes.byref(p), out.ctypes.data, capacity,
+                 ctypes.byref(found))
+    _check(rc, "threshold")
+    return out[:found.value].copy()
+
+
+def profile_stages(on: bool) -> None:
+    lib().sf_profile_stages(int(on))
+
+
+def last_stage_times() -> dict:
+    t = StageTimes()
+    lib().sf_last_stage_times(ctypes.byref(t))
+    return {n: getattr(t, n) for n, _ in StageTimes._fields_}
+
+
+class DeviceThreshold:
+    """Device-resident threshold of frames already in HBM (torch tensors).
+
+    Holds the output list, bitmask, count and workspace for frames of one
+    shape, and enqueues on the given (default: current) torch stream.
+    """
+
+    def __init__(self, height: int, width: int, capacity: int | None = None,
+                 params: Params | None = None, dtype=None, word_prefix: bool = False):
+        import torch
+        self.h, self.w = height, width
+        self.capacity = capacity if capacity is not None else max(1, height * width // 4)
+        self.params = (params or Params()).c()
+        dev = torch.device("cuda")
+        self.out = torch.empty(self.capacity * 16, dtype=torch.uint8, device=dev)
+        self.words_per_row = (width + 31) // 32
+        self.bits = torch.empty(self.words_per_row * height, dtype=torch.int32, device=dev)
+        self.count = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.word_prefix = (torch.empty(self.words_per_row * height, dtype=torch.int32,
+                                        device=dev) if word_prefix else None)
+        nbytes = lib().sf_workspace_bytes(height, width, self.capacity)
+        if nbytes == 0:
+            raise ValueError("frame shape rejected")
+        self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+
+    def __call__(self, image, stream=None) -> None:
+        import torch
+        if image.device.type != "cuda" or not image.is_contiguous():
+            raise ValueError("a contiguous CUDA tensor")
+        if tuple(image.shape[-2:]) != (self.h, self.w):
+            raise ValueError("frame shape differs from this threshold's")
+        s = stream if stream is not None else torch.cuda.current_stream()
+        L = lib()
+        if image.dtype in (torch.int32, torch.uint32):
+            fn = L.sf_threshold_u32_device
+        elif image.dtype in (torch.int16, torch.uint16):
+            fn = L.sf_threshold_u16_device
+        else:
+            raise TypeError("frames are 16- or 32-bit")
+        rc = fn(image.data_ptr(), self.h, self.w, ctypes.byref(self.params),
+                self.out.data_ptr(), self.capacity, self.bits.data_ptr(),
+                self.count.data_ptr(),
+                self.word_prefix.data_ptr() if self.word_prefix is not None else None,
+                self.workspace.data_ptr(), self.workspace.numel(), s.cuda_stream)
+        _check(rc, "device threshold")
+
+    def result(self) -> np.ndarray:
+        """Synchronise and return the signal list (host copy)."""
+        import torch
+        torch.cuda.current_stream().synchronize()
+        n = int(self.count.item()) & 0xffffffff
+        if n > self.capacity:
+            raise OverflowError_(f"{n} signal pixels, capacity {self.capacity}")
+        raw = self.out[: n * 16].cpu().numpy()
+        return raw.view(SIGNAL_DTYPE).copy()
+
+    def mask(self) -> np.ndarray:
+        """The strong-pixel mask as booleans (h, w) (host copy)."""
+        words = self.bits.cpu().numpy().view(np.uint32).reshape(self.h, self.words_per_row)
+        bits = np.unpackbits(words.view(np.uint8).reshape(self.h, -1), axis=1,
+                             bitorder="little")
+        return bits[:, : self.w].astype(bool)
