@@ -61,7 +61,7 @@ def test_ragged_shapes(api, h, w):
                      spots_per_frame=max(1.0, h * w / 2000.0), n_hot=3, seed=h * 1000 + w)
     f = synth.Sweep(p).frame(0)[:h, :w].copy()
     for frame in (f, np.minimum(f, 0xFFFD).astype(np.uint16)):
-        _same(api.find(frame), O.dext(frame), f"{h}x{w} {frame.dtype}")
+        _same(api.find(frame, capacity=h * w), O.dext(frame), f"{h}x{w} {frame.dtype}")
 
 
 @pytest.mark.parametrize("params", [
@@ -69,19 +69,22 @@ def test_ragged_shapes(api, h, w):
     dict(algorithm=1), dict(algorithm=1, kernel_x=2, kernel_y=2),
     dict(gain=1.5), dict(gain=0.8, sigma_b=4.5, sigma_s=2.5),
     dict(min_local=5), dict(min_local=0), dict(global_threshold=3.0),
-    dict(global_threshold=2.5), dict(sigma_b=3.0, sigma_s=2.0)])
+    dict(global_threshold=2.5), dict(global_threshold=50.0), dict(min_local=30),
+    dict(sigma_b=3.0, sigma_s=2.0)])
 def test_parameters_against_oracle(api, params):
     # No reference test pins these settings; the oracle restatement is the
     # specification (it equals the reference at the defaults).
     from sfgb import synth
-    sw = synth.Sweep(synth.preset("batch_4m", height=300, width=420, n_frames=2, seed=5))
+    sw = synth.Sweep(synth.preset("batch_4m", height=300, width=420, n_frames=2, seed=5,
+                                  spots_per_frame=40.0, n_hot=15, row_band_start=77,
+                                  row_band_len=3))
     f = sw.frame(1)
     P = api.Params(**params)
     po = O.Params(**params)
-    _same(api.find(f, P), O.dext(f, po), f"{params} u32")
+    _same(api.find(f, P, capacity=f.size), O.dext(f, po), f"{params} u32")
     f16 = np.minimum(f, 0xFFFD).astype(np.uint16)
     f16[f == 0xFFFFFFFF] = 0xFFFF
-    _same(api.find(f16, P), O.dext(f16, po), f"{params} u16")
+    _same(api.find(f16, P, capacity=f.size), O.dext(f16, po), f"{params} u16")
 
 
 def test_sums_of_squares_wrap(api):
@@ -94,7 +97,7 @@ def test_sums_of_squares_wrap(api):
     f[mix] = low[mix]
     f[::7, ::5] = 3
     f[10:20, 10:20] = 0xFFFFFFFE
-    _same(api.find(f), O.dext(f), "wrapping sums")
+    _same(api.find(f, capacity=f.size), O.dext(f), "wrapping sums")
 
 
 def test_bright_dense_frame(api):
@@ -103,7 +106,7 @@ def test_bright_dense_frame(api):
     from sfgb import synth
     p = synth.preset("dense_16m", height=520, width=700, n_frames=2, spots_per_frame=400.0)
     f = synth.Sweep(p).frame(0)
-    _same(api.find(f), O.dext(f), "dense")
+    _same(api.find(f, capacity=f.size), O.dext(f), "dense")
 
 
 def test_all_masked_and_all_zero(api):
