@@ -454,3 +454,84 @@ int sf_threshold_u16_device(const uint16_t *d_image, size_t height, size_t width
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// The device threshold for callers that cannot allocate device memory.
+//
+// Some callers may not call cudaMalloc at all: a plugin running inside a host
+// application whose own allocator owns every byte of device memory, or a
+// detector-stream loop that must not stall acquisition on the device-wide
+// synchronisation an allocation can cause. For them the threshold's scratch
+// (the unordered signal list, the per-tile bases and the per-tile-row counts)
+// lives in a fixed array in this library's device image instead of a
+// caller-supplied workspace. The array is part of the module, so every GPU
+// that loads the library holds it until the process exits.
+// ---------------------------------------------------------------------------
+
+namespace sf {
+
+// 8 MiB of staging (524,288 signal records of 16 bytes) plus 1 MiB for the
+// per-tile bookkeeping, which covers every frame shape up to and beyond the
+// EIGER2 16M (4362 x 4148, 17,810 tiles).
+constexpr size_t kNoAllocCapacity = 524288;
+constexpr size_t kNoAllocScratchBytes = kNoAllocCapacity * sizeof(sf_signal_pixel) + (1u << 20);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// The device address of g_noalloc_scratch, looked up once per device. In host
+// code the array's name only stands in for the symbol; its address on the
+// device comes from cudaGetSymbolAddress, with that device current.
+constexpr int kNoAllocMaxDevices = 64;
+static void *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+static std::mutex g_noalloc_mutex;
+
+static int noalloc_scratch(void **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+    return fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kNoAllocMaxDevices) {
+    t_last_error = "device index beyond the scratch table";
+    return SF_EBADARG;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return fail(e, "cudaGetSymbolAddress for the fixed scratch");
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return SF_OK;
+}
+
+} // namespace sf
+
+extern "C" int sf_threshold_u32_device_noalloc(
+    const uint32_t *d_image, size_t height, size_t width,
+    const sf_threshold_params *params, sf_signal_pixel *d_out, size_t capacity,
+    uint32_t *d_bits, uint32_t *d_count, uint32_t *d_word_prefix, void *stream) {
+  using namespace sf;
+  if (!shape_ok(height, width))
+    return SF_EBADARG;
+  if (capacity > kNoAllocCapacity) {
+    t_last_error = "capacity above the fixed scratch's 524288 records";
+    return SF_EBADARG;
+  }
+  if (layout(height, width, capacity).total > kNoAllocScratchBytes) {
+    t_last_error = "frame too large for the fixed scratch's tile bookkeeping";
+    return SF_EBADARG;
+  }
+  void *scratch = nullptr;
+  const int rc = noalloc_scratch(&scratch);
+  if (rc != SF_OK)
+    return rc;
+  // threshold_device clears the per-tile-row counts and the total on the
+  // stream before the kernels run; the staging list and tile bases are
+  // written before they are read, so nothing else needs to start at zero.
+  return threshold_device<uint32_t>(d_image, height, width, params, d_out, capacity,
+                                    d_bits, d_count, d_word_prefix, scratch,
+                                    kNoAllocScratchBytes,
+                                    static_cast<cudaStream_t>(stream));
+}

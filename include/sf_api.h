@@ -139,6 +139,31 @@ int sf_threshold_u16_device(const uint16_t *d_image, size_t height,
                             uint32_t *d_word_prefix, void *d_workspace,
                             size_t workspace_bytes, void *stream);
 
+/*
+ * sf_threshold_u32_device as above, for callers that cannot allocate device
+ * memory: a plugin inside a host application whose own allocator owns all
+ * device memory, or a detector-stream loop that must not stall on an
+ * allocation. It has no counterpart in the reference. Its scratch is a fixed
+ * 9 MiB array inside this library (held on every GPU that loads the library
+ * until exit), so it takes no workspace and calls no allocator; the caller
+ * still passes the frame and every output.
+ *   - capacity may be at most 524288 records; larger capacities, or frames
+ *     whose per-tile bookkeeping would not fit, return -1 with the reason in
+ *     sf_last_error().
+ *   - The first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - Every call shares the one array: calls whose work overlaps on the GPU
+ *     (different streams, or different host threads) race and corrupt each
+ *     other's results. Serialise them, e.g. on one stream.
+ */
+int sf_threshold_u32_device_noalloc(const uint32_t *d_image, size_t height,
+                                    size_t width,
+                                    const sf_threshold_params *params,
+                                    sf_signal_pixel *d_out, size_t capacity,
+                                    uint32_t *d_bits, uint32_t *d_count,
+                                    uint32_t *d_word_prefix, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
