@@ -1,0 +1,1149 @@
+// 3-D spot labelling on the device: the streaming grouping of
+// src/spots/dials_spots.cc (Labeller::add / flush / emit / finish), for a
+// batch of frames at a time.
+//
+// State carried between batches is the reference's: the "live" pixels of
+// every component that still touches the newest frame, in (frame, index)
+// order, each pointing straight at its component's first pixel
+// (dials_spots.cc:199-218). A batch of B frames is appended to that pool in
+// order and joined in one union-find pass -- left neighbour in the row,
+// the pixel above, the same pixel on the previous frame when the frames are
+// consecutive (dials_spots.cc:106-137) -- with every link toward the lower
+// position, so a root is its component's first pixel (:36-55).
+//
+// What the reference emits at each flush is the components with no pixel on
+// the frame just added, in order of first pixel (:162-194). Over a batch that
+// is: every component whose last frame is not the batch's last frame, ordered
+// by (last frame, first pixel), which a stable partition of the closing roots
+// by last frame produces. Each emitted component's members are sorted back
+// into (frame, index) order and the reference's emit() arithmetic runs over
+// them sequentially in double, so the spot table is the reference's bit for
+// bit (:221-360).
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <climits>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "sf_api.h"
+#include "sf_common.cuh"
+#include "sf_label.cuh"
+#include "sf_scan.cuh"
+
+namespace sf {
+
+extern thread_local std::string t_last_error;
+int fail(cudaError_t e, const char *what);
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr int kThreads = 256;
+constexpr int kGrid = 2 * 152;          // persistent grid-stride launches
+constexpr int kWarpSortMax = 1024;      // members sorted by one warp
+constexpr int kBlockSortMax = 8192;     // members sorted by one block
+constexpr int kUnionRetries = 1 << 20;  // cap on a union's CAS retries
+
+enum : uint32_t {
+  kErrLiveFull = 1u,   // more open pixels than the live pool holds
+  kErrUnion = 2u,      // a union did not settle within kUnionRetries
+  kErrSpotSize = 4u,   // an accepted spot larger than kBlockSortMax
+  kErrOutFull = 8u,    // more spots / kept pixels than the batch outputs hold
+};
+
+enum { kCntSignal = 0, kCntGroups, kCntSmall, kCntLarge, kCntSeparated, kCntAccepted };
+
+struct LabelStatus {
+  uint32_t error;
+  uint32_t n_live;      // open pixels carried into the next batch
+  uint32_t prev_start;  // first live position of the last added frame
+  uint32_t n_total;     // n_live + the batch's pixels
+  uint32_t n_closing, n_cand, n_cand_pixels, n_accept, n_accept_pixels, n_open;
+  uint32_t frame_off[kLabelMaxBatch + 1];
+  unsigned long long counts[6];
+};
+
+struct BatchArgs {
+  int nb;
+  int finishing;        // close everything (finish(), dials_spots.cc:147-151)
+  int two_d;
+  uint32_t width, npix;
+  uint32_t min_size, max_size;
+  double max_separation;
+  int32_t frames[kLabelMaxBatch];
+  uint8_t link_prev[kLabelMaxBatch];
+};
+
+// ---------------------------------------------------------------------------
+// Union-find (dials_spots.cc:36-55), lock-free: a link is a CAS on a root
+// toward the smaller position, and finds halve paths.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t uf_find(uint32_t *parent, uint32_t x) {
+  volatile uint32_t *vp = parent;
+  while (true) {
+    const uint32_t p = vp[x];
+    if (p == x)
+      return x;
+    const uint32_t gp = vp[p];
+    if (gp == p)
+      return p;
+    vp[x] = gp; // gp is an ancestor of x: a benign shortcut
+    x = gp;
+  }
+}
+
+__device__ __forceinline__ void uf_unite(uint32_t *parent, uint32_t a, uint32_t b,
+                                         LabelStatus *st) {
+  for (int it = 0; it < kUnionRetries; it++) {
+    a = uf_find(parent, a);
+    b = uf_find(parent, b);
+    if (a == b)
+      return;
+    if (a < b) {
+      const uint32_t t = a;
+      a = b;
+      b = t;
+    }
+    const uint32_t old = atomicCAS(&parent[a], a, b);
+    if (old == a)
+      return;
+  }
+  atomicOr(&st->error, kErrUnion);
+}
+
+__device__ __forceinline__ uint32_t lower_bound(const uint32_t *v, uint32_t lo, uint32_t hi,
+                                                uint32_t key) {
+  while (lo < hi) {
+    const uint32_t mid = lo + ((hi - lo) >> 1);
+    if (v[mid] < key)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels of one batch, in launch order.
+// ---------------------------------------------------------------------------
+
+__global__ void k_offsets(LabelStatus *st, const uint32_t *__restrict__ counts,
+                          const BatchArgs a, uint32_t capacity) {
+  if (threadIdx.x != 0 || st->error)
+    return;
+  uint32_t off = 0;
+  for (int j = 0; j < a.nb; j++) {
+    st->frame_off[j] = off;
+    off += counts[j];
+  }
+  st->frame_off[a.nb] = off;
+  const unsigned long long total = (unsigned long long)st->n_live + off;
+  if (total > capacity) {
+    st->error |= kErrLiveFull;
+    return;
+  }
+  st->n_total = (uint32_t)total;
+  st->counts[kCntSignal] += off;
+}
+
+__global__ void k_append(LabelStatus *st, const sf_signal_pixel *__restrict__ lists,
+                         size_t stride, const BatchArgs a, int32_t *frame,
+                         uint32_t *index, uint32_t *value, uint32_t *parent) {
+  if (st->error)
+    return;
+  const int j = blockIdx.y;
+  const uint32_t n = st->frame_off[j + 1] - st->frame_off[j];
+  const uint32_t base = st->n_live + st->frame_off[j];
+  const sf_signal_pixel *list = lists + (size_t)j * stride;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const sf_signal_pixel s = list[i];
+    const uint32_t p = base + i;
+    frame[p] = a.frames[j];
+    index[p] = s.index;
+    value[p] = s.value;
+    parent[p] = p;
+  }
+}
+
+// dials_spots.cc:106-137: left (same row), above (same frame), and the same
+// index on the previous frame when it is the one before.
+__global__ void k_link(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ index,
+                       uint32_t *parent) {
+  if (st->error)
+    return;
+  const int j = blockIdx.y;
+  const uint32_t start = st->n_live + st->frame_off[j];
+  const uint32_t end = st->n_live + st->frame_off[j + 1];
+  uint32_t plo = 0, phi = 0;
+  if (a.link_prev[j]) {
+    plo = j == 0 ? st->prev_start : st->n_live + st->frame_off[j - 1];
+    phi = j == 0 ? st->n_live : start;
+  }
+  for (uint32_t p = start + blockIdx.x * blockDim.x + threadIdx.x; p < end;
+       p += gridDim.x * blockDim.x) {
+    const uint32_t idx = index[p];
+    if (p > start && idx % a.width != 0 && index[p - 1] == idx - 1)
+      uf_unite(parent, p, p - 1, st);
+    if (idx >= a.width) {
+      const uint32_t t = idx - a.width;
+      const uint32_t q = lower_bound(index, start, p, t);
+      if (q < p && index[q] == t)
+        uf_unite(parent, p, q, st);
+    }
+    if (phi > plo) {
+      const uint32_t q = lower_bound(index, plo, phi, idx);
+      if (q < phi && index[q] == idx)
+        uf_unite(parent, p, q, st);
+    }
+  }
+}
+
+__global__ void k_flatten(LabelStatus *st, uint32_t *parent, uint32_t *root, int32_t *zlast,
+                          uint32_t *csize, uint32_t *candid) {
+  if (st->error)
+    return;
+  const uint32_t n = st->n_total;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += gridDim.x * blockDim.x) {
+    uint32_t r = p;
+    while (parent[r] != r)
+      r = parent[r];
+    root[p] = r;
+    zlast[p] = INT_MIN;
+    csize[p] = 0;
+    candid[p] = kNone;
+  }
+}
+
+__global__ void k_comp_stats(LabelStatus *st, const uint32_t *__restrict__ root,
+                             const int32_t *__restrict__ frame, int32_t *zlast,
+                             uint32_t *csize) {
+  if (st->error)
+    return;
+  const uint32_t n = st->n_total;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += gridDim.x * blockDim.x) {
+    const uint32_t r = root[p];
+    atomicMax(&zlast[r], frame[p]);
+    atomicAdd(&csize[r], 1u);
+  }
+}
+
+__device__ __forceinline__ bool closes(const BatchArgs &a, int32_t z) {
+  return a.finishing || a.two_d || z < a.frames[a.nb - 1];
+}
+
+// Emission event of a component that closes: at finish() one flush; else the
+// add() of the frame after its last one (dials_spots.cc:65-69, :144).
+__device__ __forceinline__ uint32_t bucket_of(const BatchArgs &a, int32_t z) {
+  if (a.finishing || z < a.frames[0])
+    return 0;
+  int lo = 0, hi = a.nb - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (a.frames[mid] < z)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return 1u + (uint32_t)lo;
+}
+
+__global__ void k_closing_flags(LabelStatus *st, const BatchArgs a,
+                                const uint32_t *__restrict__ root,
+                                const int32_t *__restrict__ zlast, uint32_t *flag,
+                                uint32_t *open) {
+  if (st->error)
+    return;
+  const uint32_t n = st->n_total;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += gridDim.x * blockDim.x) {
+    const uint32_t r = root[p];
+    const bool c = closes(a, zlast[r]);
+    flag[p] = (r == p && c) ? 1u : 0u;
+    open[p] = c ? 0u : 1u;
+  }
+}
+
+__global__ void k_closing_list(LabelStatus *st, const BatchArgs a,
+                               const uint32_t *__restrict__ flag,
+                               const uint32_t *__restrict__ pos,
+                               const int32_t *__restrict__ zlast, uint32_t *clist,
+                               uint32_t *cbucket) {
+  if (st->error)
+    return;
+  const uint32_t n = st->n_total;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += gridDim.x * blockDim.x) {
+    if (flag[p]) {
+      const uint32_t k = pos[p];
+      clist[k] = p;
+      cbucket[k] = bucket_of(a, zlast[p]);
+    }
+  }
+}
+
+// Stable partition of the closing roots by emission event.
+constexpr int kBuckets = kLabelMaxBatch + 1;
+
+__global__ void __launch_bounds__(kThreads)
+k_bucket_hist(LabelStatus *st, const uint32_t *__restrict__ cbucket, uint32_t *hist) {
+  if (st->error)
+    return;
+  __shared__ uint32_t h[kBuckets];
+  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x)
+    h[b] = 0;
+  __syncthreads();
+  uint32_t lo, hi;
+  scan_chunk(st->n_closing, &lo, &hi);
+  for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x)
+    atomicAdd(&h[cbucket[k]], 1u);
+  __syncthreads();
+  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x)
+    hist[blockIdx.x * kBuckets + b] = h[b];
+}
+
+// Exclusive scan over (bucket, block) in bucket-major order, in place.
+__global__ void __launch_bounds__(1024) k_bucket_offsets(LabelStatus *st, uint32_t *hist) {
+  if (st->error)
+    return;
+  __shared__ uint32_t btotal[kBuckets];
+  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) {
+    uint32_t run = 0;
+    for (int blk = 0; blk < kGrid; blk++) {
+      const uint32_t v = hist[blk * kBuckets + b];
+      hist[blk * kBuckets + b] = run;
+      run += v;
+    }
+    btotal[b] = run;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int b = 0; b < kBuckets; b++) {
+      const uint32_t v = btotal[b];
+      btotal[b] = run;
+      run += v;
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x)
+    for (int blk = 0; blk < kGrid; blk++)
+      hist[blk * kBuckets + b] += btotal[b];
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_bucket_scatter(LabelStatus *st, const uint32_t *__restrict__ clist,
+                 const uint32_t *__restrict__ cbucket, const uint32_t *__restrict__ hist,
+                 uint32_t *order) {
+  if (st->error)
+    return;
+  constexpr int W = kThreads / 32;
+  __shared__ uint32_t wcnt[W][kBuckets];
+  __shared__ uint32_t running[kBuckets];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x)
+    running[b] = hist[blockIdx.x * kBuckets + b];
+  uint32_t lo, hi;
+  scan_chunk(st->n_closing, &lo, &hi);
+  for (uint32_t base = lo; base < hi; base += blockDim.x) {
+    for (int i = threadIdx.x; i < W * kBuckets; i += blockDim.x)
+      (&wcnt[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t k = base + threadIdx.x;
+    const bool valid = k < hi;
+    const uint32_t b = valid ? cbucket[k] : kBuckets; // kBuckets: no bucket
+    const unsigned m = __match_any_sync(0xffffffffu, b);
+    const uint32_t rank = __popc(m & ((1u << lane) - 1u));
+    if (valid && rank == 0)
+      wcnt[warp][b] = __popc(m);
+    __syncthreads();
+    // Exclusive prefix over warps, per bucket; the running totals advance.
+    for (int bb = threadIdx.x; bb < kBuckets; bb += blockDim.x) {
+      uint32_t run = running[bb];
+      for (int w = 0; w < W; w++) {
+        const uint32_t v = wcnt[w][bb];
+        wcnt[w][bb] = run;
+        run += v;
+      }
+      running[bb] = run;
+    }
+    __syncthreads();
+    if (valid)
+      order[wcnt[warp][b] + rank] = clist[k];
+    __syncthreads();
+  }
+}
+
+// Size filters (dials_spots.cc:224-231) over the closing components in
+// emission order.
+__global__ void k_size_filter(LabelStatus *st, const BatchArgs a,
+                              const uint32_t *__restrict__ order,
+                              const uint32_t *__restrict__ csize, uint32_t *cflag) {
+  if (st->error)
+    return;
+  const uint32_t n = st->n_closing;
+  uint32_t small = 0, large = 0, groups = 0;
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += gridDim.x * blockDim.x) {
+    const uint32_t sz = csize[order[e]];
+    groups++;
+    const bool s = sz < a.min_size, l = sz > a.max_size;
+    small += s;
+    large += !s && l;
+    cflag[e] = (!s && !l) ? 1u : 0u;
+  }
+  for (int o = 16; o; o >>= 1) {
+    small += __shfl_xor_sync(0xffffffffu, small, o);
+    large += __shfl_xor_sync(0xffffffffu, large, o);
+    groups += __shfl_xor_sync(0xffffffffu, groups, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (groups)
+      atomicAdd(&st->counts[kCntGroups], (unsigned long long)groups);
+    if (small)
+      atomicAdd(&st->counts[kCntSmall], (unsigned long long)small);
+    if (large)
+      atomicAdd(&st->counts[kCntLarge], (unsigned long long)large);
+  }
+}
+
+__global__ void k_cand_list(LabelStatus *st, const uint32_t *__restrict__ order,
+                            const uint32_t *__restrict__ csize,
+                            const uint32_t *__restrict__ cflag,
+                            const uint32_t *__restrict__ cpos, uint32_t *cand_root,
+                            uint32_t *cand_n, uint32_t *candid, uint32_t *cursor) {
+  if (st->error)
+    return;
+  const uint32_t n = st->n_closing;
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += gridDim.x * blockDim.x) {
+    if (cflag[e]) {
+      const uint32_t c = cpos[e], r = order[e];
+      cand_root[c] = r;
+      cand_n[c] = csize[r];
+      candid[r] = c;
+      cursor[c] = 0;
+    }
+  }
+}
+
+__global__ void k_gather(LabelStatus *st, const uint32_t *__restrict__ root,
+                         const uint32_t *__restrict__ candid,
+                         const uint32_t *__restrict__ cand_off, uint32_t *cursor,
+                         uint32_t *members) {
+  if (st->error)
+    return;
+  const uint32_t n = st->n_total;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += gridDim.x * blockDim.x) {
+    const uint32_t c = candid[root[p]];
+    if (c != kNone) {
+      const uint32_t slot = atomicAdd(&cursor[c], 1u);
+      members[cand_off[c] + slot] = p;
+    }
+  }
+}
+
+// Bitonic sort of m values (padded to a power of two with kNone) in shared
+// memory by `nt` cooperating threads numbered t.
+__device__ void bitonic_sort(uint32_t *s, int m, int t, int nt, bool warp_only) {
+  int size = 1;
+  while (size < m)
+    size <<= 1;
+  for (int i = m + t; i < size; i += nt)
+    s[i] = kNone;
+  if (warp_only)
+    __syncwarp();
+  else
+    __syncthreads();
+  for (int k = 2; k <= size; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = t; i < size; i += nt) {
+        const int l = i ^ j;
+        if (l > i) {
+          const uint32_t x = s[i], y = s[l];
+          const bool up = (i & k) == 0;
+          if ((x > y) == up) {
+            s[i] = y;
+            s[l] = x;
+          }
+        }
+      }
+      if (warp_only)
+        __syncwarp();
+      else
+        __syncthreads();
+    }
+  }
+}
+
+// The reference's emit() (dials_spots.cc:240-353) over members sorted into
+// (frame, index) order, sequentially in double: the same operations in the
+// same order. Returns false if the peak-centroid filter rejects it.
+__device__ bool emit_spot(const uint32_t *mem, uint32_t n, const int32_t *frame,
+                          const uint32_t *index, const uint32_t *value, uint32_t width,
+                          double max_separation, sf_spot *spot) {
+  double sum = 0.0, sum_sq = 0.0;
+  double weighted[3] = {0.0, 0.0, 0.0};
+  int32_t x0 = 0, x1 = 0, y0 = 0, y1 = 0, z0 = 0, z1 = 0;
+  uint32_t peak_value = 0;
+  double peak[3] = {0.0, 0.0, 0.0};
+  for (uint32_t k = 0; k < n; k++) {
+    const uint32_t q = mem[k];
+    const uint32_t idx = index[q];
+    const int32_t x = (int32_t)(idx % width), y = (int32_t)(idx / width), z = frame[q];
+    if (k == 0) {
+      x0 = x, x1 = x + 1, y0 = y, y1 = y + 1, z0 = z, z1 = z + 1;
+    } else {
+      x0 = x < x0 ? x : x0;
+      x1 = x + 1 > x1 ? x + 1 : x1;
+      y0 = y < y0 ? y : y0;
+      y1 = y + 1 > y1 ? y + 1 : y1;
+      z0 = z < z0 ? z : z0;
+      z1 = z + 1 > z1 ? z + 1 : z1;
+    }
+    const uint32_t v = value[q];
+    const double val = (double)v;
+    const double pos[3] = {__dadd_rn((double)x, 0.5), __dadd_rn((double)y, 0.5),
+                           __dadd_rn((double)z, 0.5)};
+    sum = __dadd_rn(sum, val);
+    sum_sq = __dadd_rn(sum_sq, __dmul_rn(val, val));
+    for (int ax = 0; ax < 3; ax++)
+      weighted[ax] = __dadd_rn(weighted[ax], __dmul_rn(val, pos[ax]));
+    if (v > peak_value) {
+      peak_value = v;
+      peak[0] = pos[0], peak[1] = pos[1], peak[2] = pos[2];
+    }
+  }
+  sf_spot s;
+  s.bbox[0] = x0, s.bbox[1] = x1, s.bbox[2] = y0, s.bbox[3] = y1, s.bbox[4] = z0,
+  s.bbox[5] = z1;
+  s.intensity = sum;
+  s.intensity_variance = sum;
+  s.n_signal = n;
+  s.first = 0;
+  s.variance[0] = s.variance[1] = s.variance[2] = 0.0;
+  const double pixel_variance = 1.0 / 12.0;
+  if (sum > 0.0) {
+    for (int ax = 0; ax < 3; ax++)
+      s.position[ax] = __ddiv_rn(weighted[ax], sum);
+    double delta_sq[3] = {0.0, 0.0, 0.0};
+    for (uint32_t k = 0; k < n; k++) {
+      const uint32_t q = mem[k];
+      const uint32_t idx = index[q];
+      const double val = (double)value[q];
+      const double pos[3] = {__dadd_rn((double)(idx % width), 0.5),
+                             __dadd_rn((double)(idx / width), 0.5),
+                             __dadd_rn((double)frame[q], 0.5)};
+      for (int ax = 0; ax < 3; ax++) {
+        const double d = __dsub_rn(pos[ax], s.position[ax]);
+        delta_sq[ax] = __dadd_rn(delta_sq[ax], __dmul_rn(__dmul_rn(val, d), d));
+      }
+    }
+    const double ss = __dmul_rn(sum, sum);
+    if (ss > sum_sq) {
+      for (int ax = 0; ax < 3; ax++) {
+        const double var = __ddiv_rn(__dmul_rn(delta_sq[ax], sum), __dsub_rn(ss, sum_sq));
+        s.variance[ax] = __dadd_rn(__ddiv_rn(var, sum), pixel_variance);
+      }
+    } else {
+      for (int ax = 0; ax < 3; ax++)
+        s.variance[ax] = pixel_variance;
+    }
+    if (s.bbox[5] == s.bbox[4] + 1)
+      s.position[2] = __dadd_rn((double)s.bbox[4], 0.5);
+  } else {
+    s.position[0] = __ddiv_rn((double)(s.bbox[1] + s.bbox[0]), 2.0);
+    s.position[1] = __ddiv_rn((double)(s.bbox[3] + s.bbox[2]), 2.0);
+    s.position[2] = __ddiv_rn((double)(s.bbox[5] + s.bbox[4]), 2.0);
+  }
+  *spot = s;
+  if (max_separation > 0.0) {
+    const double dx = __dsub_rn(peak[0], s.position[0]);
+    const double dy = __dsub_rn(peak[1], s.position[1]);
+    const double dz = __dsub_rn(peak[2], s.position[2]);
+    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    if (__dsqrt_rn(d2) > max_separation)
+      return false;
+  }
+  return true;
+}
+
+// One warp per candidate of up to kWarpSortMax members (or one block per
+// candidate of up to kBlockSortMax): sort the members into (frame, index)
+// order, write them back, run emit() and record acceptance.
+template <bool BLOCK>
+__global__ void __launch_bounds__(kThreads)
+k_sort_accept(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ cand_n,
+              const uint32_t *__restrict__ cand_off, uint32_t *members,
+              const int32_t *__restrict__ frame, const uint32_t *__restrict__ index,
+              const uint32_t *__restrict__ value, uint32_t *acc, uint32_t *acc_n) {
+  if (st->error)
+    return;
+  extern __shared__ __align__(16) uint32_t s_sort[];
+  const uint32_t ncand = st->n_cand;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  uint32_t separated = 0;
+  if (!BLOCK) {
+    uint32_t *s = s_sort + warp * kWarpSortMax;
+    for (uint32_t c = blockIdx.x * nwarps + warp; c < ncand; c += gridDim.x * nwarps) {
+      const uint32_t n = cand_n[c];
+      if (n > (uint32_t)kWarpSortMax)
+        continue;
+      uint32_t *m = members + cand_off[c];
+      for (uint32_t i = lane; i < n; i += 32)
+        s[i] = m[i];
+      __syncwarp();
+      bitonic_sort(s, (int)n, lane, 32, true);
+      for (uint32_t i = lane; i < n; i += 32)
+        m[i] = s[i];
+      __syncwarp();
+      if (lane == 0) {
+        sf_spot spot;
+        const bool ok = emit_spot(s, n, frame, index, value, a.width, a.max_separation, &spot);
+        acc[c] = ok ? 1u : 0u;
+        acc_n[c] = ok ? n : 0u;
+        separated += ok ? 0u : 1u;
+      }
+      __syncwarp();
+    }
+  } else {
+    __shared__ sf_spot s_spot;
+    __shared__ uint32_t s_ok;
+    for (uint32_t c = blockIdx.x; c < ncand; c += gridDim.x) {
+      const uint32_t n = cand_n[c];
+      if (n <= (uint32_t)kWarpSortMax)
+        continue;
+      if (n > (uint32_t)kBlockSortMax) {
+        if (threadIdx.x == 0) {
+          atomicOr(&st->error, kErrSpotSize);
+          acc[c] = 0;
+          acc_n[c] = 0;
+        }
+        continue;
+      }
+      uint32_t *m = members + cand_off[c];
+      for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        s_sort[i] = m[i];
+      __syncthreads();
+      bitonic_sort(s_sort, (int)n, threadIdx.x, blockDim.x, false);
+      for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        m[i] = s_sort[i];
+      if (threadIdx.x == 0) {
+        s_ok = emit_spot(s_sort, n, frame, index, value, a.width, a.max_separation, &s_spot)
+                   ? 1u : 0u;
+        acc[c] = s_ok;
+        acc_n[c] = s_ok ? n : 0u;
+        separated += s_ok ? 0u : 1u;
+      }
+      __syncthreads();
+    }
+  }
+  if (separated)
+    atomicAdd(&st->counts[kCntSeparated], (unsigned long long)separated);
+}
+
+// Accepted spots and their pixels into the batch outputs (dials_spots.cc:
+// 355-359): spot k's pixels at acc_off[k] in member order.
+__global__ void __launch_bounds__(kThreads)
+k_write(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ cand_n,
+        const uint32_t *__restrict__ cand_off, const uint32_t *__restrict__ members,
+        const int32_t *__restrict__ frame, const uint32_t *__restrict__ index,
+        const uint32_t *__restrict__ value, const uint32_t *__restrict__ acc,
+        const uint32_t *__restrict__ acc_idx, const uint32_t *__restrict__ acc_off,
+        sf_spot *spots, size_t spots_cap, sf_pixel *pixels, size_t pixels_cap) {
+  if (st->error)
+    return;
+  const uint32_t ncand = st->n_cand;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  for (uint32_t c = blockIdx.x * nwarps + warp; c < ncand; c += gridDim.x * nwarps) {
+    if (!acc[c])
+      continue;
+    const uint32_t n = cand_n[c];
+    const uint32_t si = acc_idx[c], po = acc_off[c];
+    if (si >= spots_cap || (size_t)po + n > pixels_cap) {
+      if (lane == 0)
+        atomicOr(&st->error, kErrOutFull);
+      continue;
+    }
+    const uint32_t *m = members + cand_off[c];
+    for (uint32_t k = lane; k < n; k += 32) {
+      const uint32_t q = m[k];
+      sf_pixel px;
+      px.frame = frame[q];
+      px.index = index[q];
+      px.value = value[q];
+      pixels[po + k] = px;
+    }
+    if (lane == 0) {
+      sf_spot spot;
+      emit_spot(m, n, frame, index, value, a.width, a.max_separation, &spot);
+      spot.first = po; // batch-local; the host adds the run's offset
+      spots[si] = spot;
+    }
+  }
+}
+
+__global__ void k_compact(LabelStatus *st, const uint32_t *__restrict__ open,
+                          const uint32_t *__restrict__ newpos,
+                          const uint32_t *__restrict__ root, const int32_t *__restrict__ frame,
+                          const uint32_t *__restrict__ index, const uint32_t *__restrict__ value,
+                          int32_t *frame2, uint32_t *index2, uint32_t *value2,
+                          uint32_t *parent2) {
+  if (st->error)
+    return;
+  const uint32_t n = st->n_total;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += gridDim.x * blockDim.x) {
+    if (open[p]) {
+      const uint32_t q = newpos[p];
+      frame2[q] = frame[p];
+      index2[q] = index[p];
+      value2[q] = value[p];
+      parent2[q] = newpos[root[p]];
+    }
+  }
+}
+
+__global__ void k_end_batch(LabelStatus *st, const BatchArgs a) {
+  if (threadIdx.x != 0 || st->error)
+    return;
+  st->counts[kCntAccepted] += st->n_accept;
+  st->n_live = st->n_open;
+  if (st->n_open == 0) {
+    st->prev_start = 0;
+  } else {
+    // Every pixel of the last frame belongs to a component still open, and
+    // they are the tail of the pool (dials_spots.cc:378-380).
+    const uint32_t last = st->frame_off[a.nb] - st->frame_off[a.nb - 1];
+    st->prev_start = st->n_open - last;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+
+template <typename T> static cudaError_t dalloc(T **p, size_t n) {
+  return cudaMalloc(reinterpret_cast<void **>(p), (n ? n : 1) * sizeof(T));
+}
+
+struct Labeller {
+  size_t height = 0, width = 0, capacity = 0, spots_cap = 0;
+  sf_label_options opt;
+  cudaStream_t own_stream = nullptr;
+  bool started = false;
+  int64_t last_frame = 0;
+  bool finished = false;
+  // Live pool, ping-pong.
+  int32_t *frame[2] = {nullptr, nullptr};
+  uint32_t *index[2] = {nullptr, nullptr}, *value[2] = {nullptr, nullptr};
+  uint32_t *parent[2] = {nullptr, nullptr};
+  int cur = 0;
+  // Scratch sized by capacity.
+  uint32_t *root = nullptr, *csize = nullptr, *candid = nullptr, *flag = nullptr,
+           *open = nullptr, *posa = nullptr, *posb = nullptr, *clist = nullptr,
+           *cbucket = nullptr, *order = nullptr, *cflag = nullptr, *cpos = nullptr,
+           *cand_root = nullptr, *cand_n = nullptr, *cand_off = nullptr, *cursor = nullptr,
+           *members = nullptr, *acc = nullptr, *acc_n = nullptr, *acc_idx = nullptr,
+           *acc_off = nullptr, *hist = nullptr, *block_sums = nullptr;
+  int32_t *zlast = nullptr;
+  LabelStatus *st = nullptr;
+  LabelStatus *host_st = nullptr;
+  // Batch outputs, copied to the host vectors after every batch.
+  sf_spot *d_spots = nullptr;
+  sf_pixel *d_pixels = nullptr;
+  // Host-list upload staging.
+  sf_signal_pixel *d_list = nullptr;
+  size_t d_list_cap = 0;
+  uint32_t *d_counts = nullptr;
+  std::vector<sf_spot> spots;
+  std::vector<sf_pixel> pixels;
+  sf_counts counts{};
+  uint32_t live = 0;
+  std::string error;
+
+  ~Labeller() {
+    if (own_stream) {
+      cudaStreamSynchronize(own_stream);
+      cudaStreamDestroy(own_stream);
+    }
+    for (int i = 0; i < 2; i++) {
+      cudaFree(frame[i]);
+      cudaFree(index[i]);
+      cudaFree(value[i]);
+      cudaFree(parent[i]);
+    }
+    uint32_t *bufs[] = {root, csize, candid, flag, open, posa, posb, clist, cbucket,
+                        order, cflag, cpos, cand_root, cand_n, cand_off, cursor,
+                        members, acc, acc_n, acc_idx, acc_off, hist, block_sums, d_counts};
+    for (uint32_t *b : bufs)
+      cudaFree(b);
+    cudaFree(zlast);
+    cudaFree(st);
+    cudaFree(d_spots);
+    cudaFree(d_pixels);
+    cudaFree(d_list);
+    if (host_st)
+      cudaFreeHost(host_st);
+  }
+
+  int init() {
+    cudaError_t e;
+    const size_t n = capacity;
+#define SF_ALLOC(ptr, cnt)                                                               \
+  if ((e = dalloc(&(ptr), (cnt))) != cudaSuccess)                                        \
+    return fail(e, "cudaMalloc for the labeller");
+    for (int i = 0; i < 2; i++) {
+      SF_ALLOC(frame[i], n);
+      SF_ALLOC(index[i], n);
+      SF_ALLOC(value[i], n);
+      SF_ALLOC(parent[i], n);
+    }
+    SF_ALLOC(root, n);
+    SF_ALLOC(csize, n);
+    SF_ALLOC(candid, n);
+    SF_ALLOC(flag, n);
+    SF_ALLOC(open, n);
+    SF_ALLOC(posa, n);
+    SF_ALLOC(posb, n);
+    SF_ALLOC(clist, n);
+    SF_ALLOC(cbucket, n);
+    SF_ALLOC(order, n);
+    SF_ALLOC(cflag, n);
+    SF_ALLOC(cpos, n);
+    SF_ALLOC(cand_root, n);
+    SF_ALLOC(cand_n, n);
+    SF_ALLOC(cand_off, n);
+    SF_ALLOC(cursor, n);
+    SF_ALLOC(members, n);
+    SF_ALLOC(acc, n);
+    SF_ALLOC(acc_n, n);
+    SF_ALLOC(acc_idx, n);
+    SF_ALLOC(acc_off, n);
+    SF_ALLOC(hist, (size_t)kGrid * kBuckets);
+    SF_ALLOC(block_sums, kScanBlocks);
+    SF_ALLOC(zlast, n);
+    // At most one accepted spot per min_spot_size pixels closed in a batch.
+    spots_cap = n / (opt.min_spot_size ? opt.min_spot_size : 1) + 1;
+    SF_ALLOC(d_spots, spots_cap);
+    SF_ALLOC(d_pixels, n);
+    SF_ALLOC(d_counts, kLabelMaxBatch);
+#undef SF_ALLOC
+    if ((e = cudaMalloc(&st, sizeof(LabelStatus))) != cudaSuccess)
+      return fail(e, "cudaMalloc for the labeller status");
+    if ((e = cudaMallocHost(&host_st, sizeof(LabelStatus))) != cudaSuccess)
+      return fail(e, "cudaMallocHost for the labeller status");
+    if ((e = cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking)) != cudaSuccess)
+      return fail(e, "cudaStreamCreate");
+    if ((e = cudaMemsetAsync(st, 0, sizeof(LabelStatus), own_stream)) != cudaSuccess)
+      return fail(e, "clearing the labeller status");
+    if ((e = cudaStreamSynchronize(own_stream)) != cudaSuccess)
+      return fail(e, "cudaStreamSynchronize");
+    return SF_OK;
+  }
+
+  // Enqueue one batch: frames[j]'s list at lists + j * stride, count counts[j].
+  int run_batch(const int64_t *frames, int nb, const sf_signal_pixel *lists,
+                size_t stride, const uint32_t *counts_dev, bool finishing,
+                cudaStream_t s) {
+    BatchArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.nb = nb;
+    a.finishing = finishing ? 1 : 0;
+    a.two_d = opt.two_d ? 1 : 0;
+    a.width = (uint32_t)width;
+    a.npix = (uint32_t)(height * width);
+    a.min_size = (uint32_t)std::min<size_t>(opt.min_spot_size, 0xffffffffu);
+    a.max_size = (uint32_t)std::min<size_t>(opt.max_spot_size, 0xffffffffu);
+    a.max_separation = opt.max_separation;
+    int64_t prev = last_frame;
+    bool have_prev = started;
+    for (int j = 0; j < nb; j++) {
+      a.frames[j] = (int32_t)frames[j];
+      a.link_prev[j] = (!opt.two_d && have_prev && frames[j] == prev + 1) ? 1 : 0;
+      prev = frames[j];
+      have_prev = true;
+    }
+    if (nb == 0) { // finish(): one flush of everything, nothing appended
+      a.nb = 1;
+      a.frames[0] = (int32_t)(last_frame + 1);
+      a.link_prev[0] = 0;
+    }
+    const int c = cur, o = 1 - cur;
+    const dim3 g2(kGrid / 4 > 0 ? kGrid / 4 : 1, a.nb);
+    cudaError_t e;
+    k_offsets<<<1, 32, 0, s>>>(st, counts_dev, a, (uint32_t)capacity);
+    k_append<<<g2, kThreads, 0, s>>>(st, lists, stride, a, frame[c], index[c], value[c],
+                                     parent[c]);
+    k_link<<<g2, kThreads, 0, s>>>(st, a, index[c], parent[c]);
+    k_flatten<<<kGrid, kThreads, 0, s>>>(st, parent[c], root, zlast, csize, candid);
+    k_comp_stats<<<kGrid, kThreads, 0, s>>>(st, root, frame[c], zlast, csize);
+    k_closing_flags<<<kGrid, kThreads, 0, s>>>(st, a, root, zlast, flag, open);
+    const uint32_t *err = &st->error;
+    if ((e = exclusive_scan(flag, posa, &st->n_total, &st->n_closing, block_sums, err, s)) !=
+        cudaSuccess)
+      return fail(e, "labeller scan");
+    k_closing_list<<<kGrid, kThreads, 0, s>>>(st, a, flag, posa, zlast, clist, cbucket);
+    k_bucket_hist<<<kGrid, kThreads, 0, s>>>(st, cbucket, hist);
+    k_bucket_offsets<<<1, 128, 0, s>>>(st, hist);
+    k_bucket_scatter<<<kGrid, kThreads, 0, s>>>(st, clist, cbucket, hist, order);
+    k_size_filter<<<kGrid, kThreads, 0, s>>>(st, a, order, csize, cflag);
+    if ((e = exclusive_scan(cflag, cpos, &st->n_closing, &st->n_cand, block_sums, err, s)) !=
+        cudaSuccess)
+      return fail(e, "labeller scan");
+    k_cand_list<<<kGrid, kThreads, 0, s>>>(st, order, csize, cflag, cpos, cand_root, cand_n,
+                                           candid, cursor);
+    if ((e = exclusive_scan(cand_n, cand_off, &st->n_cand, &st->n_cand_pixels, block_sums,
+                            err, s)) != cudaSuccess)
+      return fail(e, "labeller scan");
+    k_gather<<<kGrid, kThreads, 0, s>>>(st, root, candid, cand_off, cursor, members);
+    k_sort_accept<false><<<kGrid, kThreads, (kThreads / 32) * kWarpSortMax * 4, s>>>(
+        st, a, cand_n, cand_off, members, frame[c], index[c], value[c], acc, acc_n);
+    k_sort_accept<true><<<kGrid / 2, kThreads, kBlockSortMax * 4, s>>>(
+        st, a, cand_n, cand_off, members, frame[c], index[c], value[c], acc, acc_n);
+    if ((e = exclusive_scan(acc, acc_idx, &st->n_cand, &st->n_accept, block_sums, err, s)) !=
+        cudaSuccess)
+      return fail(e, "labeller scan");
+    if ((e = exclusive_scan(acc_n, acc_off, &st->n_cand, &st->n_accept_pixels, block_sums,
+                            err, s)) != cudaSuccess)
+      return fail(e, "labeller scan");
+    k_write<<<kGrid, kThreads, 0, s>>>(st, a, cand_n, cand_off, members, frame[c], index[c],
+                                       value[c], acc, acc_idx, acc_off, d_spots, spots_cap,
+                                       d_pixels, capacity);
+    if ((e = exclusive_scan(open, posb, &st->n_total, &st->n_open, block_sums, err, s)) !=
+        cudaSuccess)
+      return fail(e, "labeller scan");
+    k_compact<<<kGrid, kThreads, 0, s>>>(st, open, posb, root, frame[c], index[c], value[c],
+                                         frame[o], index[o], value[o], parent[o]);
+    k_end_batch<<<1, 32, 0, s>>>(st, a);
+    if ((e = cudaGetLastError()) != cudaSuccess)
+      return fail(e, "launching the labeller");
+    return collect(s, nb > 0 ? frames[nb - 1] : last_frame, nb > 0);
+  }
+
+  // Read the batch's status and outputs back and append them to the run.
+  int collect(cudaStream_t s, int64_t newest, bool added) {
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(host_st, st, sizeof(LabelStatus), cudaMemcpyDeviceToHost, s)) !=
+        cudaSuccess)
+      return fail(e, "reading the labeller status");
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess)
+      return fail(e, "cudaStreamSynchronize");
+    if (host_st->error) {
+      const uint32_t err = host_st->error;
+      t_last_error = (err & kErrLiveFull)
+                         ? "more signal pixels held open at once than the labeller's "
+                           "capacity"
+                     : (err & kErrSpotSize)
+                         ? "a spot within the size limits is larger than 8192 pixels"
+                     : (err & kErrOutFull) ? "labeller outputs overflowed"
+                                           : "a union did not settle";
+      return SF_EOVERFLOW;
+    }
+    const uint32_t na = host_st->n_accept, npx = host_st->n_accept_pixels;
+    const size_t s0 = spots.size(), p0 = pixels.size();
+    spots.resize(s0 + na);
+    pixels.resize(p0 + npx);
+    if (na &&
+        (e = cudaMemcpyAsync(spots.data() + s0, d_spots, na * sizeof(sf_spot),
+                             cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+      return fail(e, "reading spots back");
+    if (npx &&
+        (e = cudaMemcpyAsync(pixels.data() + p0, d_pixels, npx * sizeof(sf_pixel),
+                             cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+      return fail(e, "reading spot pixels back");
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess)
+      return fail(e, "cudaStreamSynchronize");
+    for (size_t i = s0; i < spots.size(); i++)
+      spots[i].first += p0;
+    const unsigned long long *c = host_st->counts;
+    counts.signal_pixels = c[kCntSignal];
+    counts.groups = c[kCntGroups];
+    counts.too_small = c[kCntSmall];
+    counts.too_large = c[kCntLarge];
+    counts.separated = c[kCntSeparated];
+    counts.accepted = c[kCntAccepted];
+    live = host_st->n_live;
+    cur = 1 - cur;
+    if (added) {
+      started = true;
+      last_frame = newest;
+    }
+    return SF_OK;
+  }
+};
+
+} // namespace sf
+
+using namespace sf;
+
+struct sf_labeller {
+  Labeller impl;
+};
+
+extern "C" {
+
+void sf_default_label_options(sf_label_options *o) {
+  if (!o)
+    return;
+  o->min_spot_size = 3;
+  o->max_spot_size = 1000;
+  o->max_separation = 2.0;
+  o->two_d = 0;
+}
+
+sf_labeller *sf_label_open(size_t height, size_t width, const sf_label_options *options,
+                           size_t live_capacity) {
+  sf_label_options o;
+  if (options)
+    o = *options;
+  else
+    sf_default_label_options(&o);
+  // dials_spots.cc:21-30
+  if (height == 0 || width == 0 || height > 0x7fffffffu / width) {
+    t_last_error = "dials_spots: a frame with no pixels in it";
+    return nullptr;
+  }
+  if (o.max_spot_size < o.min_spot_size) {
+    t_last_error = "max_spot_size is below min_spot_size, so nothing can be accepted";
+    return nullptr;
+  }
+  if (o.min_spot_size == 0) {
+    t_last_error = "min_spot_size must be at least 1";
+    return nullptr;
+  }
+  sf_labeller *l = new (std::nothrow) sf_labeller;
+  if (!l)
+    return nullptr;
+  l->impl.height = height;
+  l->impl.width = width;
+  l->impl.opt = o;
+  l->impl.capacity = live_capacity ? live_capacity : (size_t)(1u << 22);
+  if (l->impl.capacity > 0x7fffffffu)
+    l->impl.capacity = 0x7fffffffu;
+  if (l->impl.init() != SF_OK) {
+    delete l;
+    return nullptr;
+  }
+  return l;
+}
+
+void sf_label_close(sf_labeller *l) { delete l; }
+
+int sf_label_add(sf_labeller *l, int64_t frame, const sf_signal_pixel *signal, size_t n) {
+  if (!l || (!signal && n))
+    return SF_EBADARG;
+  Labeller &L = l->impl;
+  // dials_spots.cc:58-63, :79-95: order and range checks, on the host.
+  if (L.finished || (L.started && frame <= L.last_frame)) {
+    t_last_error = "frames must be added in ascending order";
+    return SF_EBADARG;
+  }
+  const uint64_t npix = (uint64_t)L.height * L.width;
+  for (size_t i = 0; i < n; i++) {
+    if (signal[i].index >= npix || (i && signal[i].index <= signal[i - 1].index)) {
+      t_last_error = "signal pixels off the frame or not ascending by index";
+      return SF_EBADARG;
+    }
+  }
+  cudaError_t e;
+  if (n > L.d_list_cap) {
+    cudaFree(L.d_list);
+    L.d_list = nullptr;
+    L.d_list_cap = 0;
+    if ((e = cudaMalloc(&L.d_list, n * sizeof(sf_signal_pixel))) != cudaSuccess)
+      return fail(e, "cudaMalloc for the signal list");
+    L.d_list_cap = n;
+  }
+  const uint32_t cnt = (uint32_t)n;
+  if (n && (e = cudaMemcpyAsync(L.d_list, signal, n * sizeof(sf_signal_pixel),
+                                cudaMemcpyHostToDevice, L.own_stream)) != cudaSuccess)
+    return fail(e, "copying the signal list");
+  if ((e = cudaMemcpyAsync(L.d_counts, &cnt, sizeof(uint32_t), cudaMemcpyHostToDevice,
+                           L.own_stream)) != cudaSuccess)
+    return fail(e, "copying the count");
+  return L.run_batch(&frame, 1, L.d_list, n, L.d_counts, false, L.own_stream);
+}
+
+int sf_label_add_device(sf_labeller *l, const int64_t *frames, size_t n_frames,
+                        const sf_signal_pixel *d_lists, size_t list_stride,
+                        const uint32_t *d_counts, void *stream) {
+  if (!l || !frames || !d_lists || !d_counts || n_frames == 0 ||
+      n_frames > (size_t)kLabelMaxBatch)
+    return SF_EBADARG;
+  Labeller &L = l->impl;
+  int64_t prev = L.last_frame;
+  bool have = L.started;
+  if (L.finished)
+    return SF_EBADARG;
+  for (size_t j = 0; j < n_frames; j++) {
+    if (have && frames[j] <= prev) {
+      t_last_error = "frames must be added in ascending order";
+      return SF_EBADARG;
+    }
+    prev = frames[j];
+    have = true;
+  }
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : L.own_stream;
+  return L.run_batch(frames, (int)n_frames, d_lists, list_stride, d_counts, false, s);
+}
+
+int sf_label_finish(sf_labeller *l) {
+  if (!l)
+    return SF_EBADARG;
+  Labeller &L = l->impl;
+  if (L.finished || !L.started) {
+    L.finished = true;
+    return SF_OK;
+  }
+  cudaError_t e;
+  const uint32_t zero = 0;
+  if ((e = cudaMemcpyAsync(L.d_counts, &zero, sizeof(uint32_t), cudaMemcpyHostToDevice,
+                           L.own_stream)) != cudaSuccess)
+    return fail(e, "copying the count");
+  const int rc = L.run_batch(nullptr, 0, L.d_list ? L.d_list : nullptr, 0, L.d_counts, true,
+                             L.own_stream);
+  L.finished = true;
+  return rc;
+}
+
+size_t sf_label_n_spots(const sf_labeller *l) { return l ? l->impl.spots.size() : 0; }
+size_t sf_label_n_pixels(const sf_labeller *l) { return l ? l->impl.pixels.size() : 0; }
+size_t sf_label_live(const sf_labeller *l) { return l ? l->impl.live : 0; }
+
+int sf_label_spots(const sf_labeller *l, sf_spot *out, size_t capacity) {
+  if (!l || (!out && capacity))
+    return SF_EBADARG;
+  const auto &v = l->impl.spots;
+  if (capacity < v.size())
+    return SF_EOVERFLOW;
+  if (!v.empty())
+    std::memcpy(out, v.data(), v.size() * sizeof(sf_spot));
+  return SF_OK;
+}
+
+int sf_label_pixels(const sf_labeller *l, sf_pixel *out, size_t capacity) {
+  if (!l || (!out && capacity))
+    return SF_EBADARG;
+  const auto &v = l->impl.pixels;
+  if (capacity < v.size())
+    return SF_EOVERFLOW;
+  if (!v.empty())
+    std::memcpy(out, v.data(), v.size() * sizeof(sf_pixel));
+  return SF_OK;
+}
+
+void sf_label_counts(const sf_labeller *l, sf_counts *out) {
+  if (l && out)
+    *out = l->impl.counts;
+}
+
+} // extern "C"

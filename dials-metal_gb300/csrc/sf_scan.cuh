@@ -1,0 +1,129 @@
+// Device-wide exclusive scan of uint32 values whose count lives on the
+// device, so a pipeline of kernels never has to read a size back to the host.
+// Three launches on a fixed grid: per-block chunk sums, a one-block scan of
+// those, then each block rescans its chunk with its offset.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sf {
+
+constexpr int kScanBlocks = 512;
+constexpr int kScanThreads = 512;
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and writes the block total to *total (all threads see it).
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *total) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_total;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o)
+      incl += t;
+  }
+  if (lane == 31)
+    s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = lane < nwarps ? s_warp[lane] : 0u;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o)
+        wi += t;
+    }
+    if (lane < nwarps)
+      s_warp[lane] = wi - w;
+    if (lane == 31)
+      s_total = wi;
+  }
+  __syncthreads();
+  const uint32_t r = s_warp[warp] + incl - v;
+  *total = s_total;
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ void scan_chunk(uint32_t n, uint32_t *lo, uint32_t *hi) {
+  const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  *lo = min(n, blockIdx.x * chunk);
+  *hi = min(n, *lo + chunk);
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+scan_sums(const uint32_t *__restrict__ in, const uint32_t *__restrict__ d_n,
+          uint32_t *__restrict__ block_sums, const uint32_t *__restrict__ d_error) {
+  if (d_error && *d_error)
+    return;
+  uint32_t lo, hi;
+  scan_chunk(*d_n, &lo, &hi);
+  uint32_t acc = 0;
+  for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+    acc += in[i];
+  for (int o = 16; o; o >>= 1)
+    acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ uint32_t s[32];
+  if ((threadIdx.x & 31) == 0)
+    s[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+      t += s[w];
+    block_sums[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(kScanBlocks)
+scan_block_sums(uint32_t *__restrict__ block_sums, uint32_t *__restrict__ d_total,
+                const uint32_t *__restrict__ d_error) {
+  if (d_error && *d_error)
+    return;
+  uint32_t total;
+  const uint32_t v = threadIdx.x < kScanBlocks ? block_sums[threadIdx.x] : 0u;
+  const uint32_t e = block_exclusive_scan(v, &total);
+  if (threadIdx.x < kScanBlocks)
+    block_sums[threadIdx.x] = e;
+  if (threadIdx.x == 0 && d_total)
+    *d_total = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+scan_apply(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
+           const uint32_t *__restrict__ d_n, const uint32_t *__restrict__ block_sums,
+           const uint32_t *__restrict__ d_error) {
+  if (d_error && *d_error)
+    return;
+  uint32_t lo, hi;
+  scan_chunk(*d_n, &lo, &hi);
+  uint32_t carry = block_sums[blockIdx.x];
+  for (uint32_t base = lo; base < hi; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < hi ? in[i] : 0u;
+    uint32_t total;
+    const uint32_t e = block_exclusive_scan(v, &total);
+    if (i < hi)
+      out[i] = carry + e;
+    carry += total;
+  }
+}
+
+// out[i] = sum of in[0..i) for i < *d_n; *d_total = sum of all. `in` and
+// `out` may alias. block_sums holds kScanBlocks words. Skipped entirely when
+// *d_error is non-zero (d_error may be null).
+inline cudaError_t exclusive_scan(const uint32_t *in, uint32_t *out, const uint32_t *d_n,
+                                  uint32_t *d_total, uint32_t *block_sums,
+                                  const uint32_t *d_error, cudaStream_t stream) {
+  scan_sums<<<kScanBlocks, kScanThreads, 0, stream>>>(in, d_n, block_sums, d_error);
+  scan_block_sums<<<1, kScanBlocks, 0, stream>>>(block_sums, d_total, d_error);
+  scan_apply<<<kScanBlocks, kScanThreads, 0, stream>>>(in, out, d_n, block_sums, d_error);
+  return cudaGetLastError();
+}
+
+} // namespace sf

@@ -139,6 +139,85 @@ int sf_threshold_u16_device(const uint16_t *d_image, size_t height,
                             uint32_t *d_word_prefix, void *d_workspace,
                             size_t workspace_bytes, void *stream);
 
+/* ---- 3-D spot labelling (src/spots/dials_spots.hh) ---- */
+
+/* dials_spots::Pixel (src/spots/dials_spots.hh:50-54): a signal pixel of an
+ * accepted spot, kept for the shoebox. */
+typedef struct {
+  int32_t frame;
+  uint32_t index;
+  uint32_t value;
+} sf_pixel;
+
+/* dials_spots::Spot (src/spots/dials_spots.hh:57-79), same layout. */
+typedef struct {
+  int32_t bbox[6];            /* x0, x1, y0, y1, z0, z1; upper bounds exclusive */
+  double position[3];         /* xyzobs.px.value */
+  double variance[3];         /* xyzobs.px.variance */
+  double intensity;           /* intensity.sum.value */
+  double intensity_variance;  /* intensity.sum.variance */
+  uint32_t n_signal;
+  uint64_t first;             /* where its pixels start in the pixel list */
+} sf_spot;
+
+/* dials_spots::Options (src/spots/dials_spots.hh:81-95). */
+typedef struct {
+  size_t min_spot_size;   /* 3 */
+  size_t max_spot_size;   /* 1000 */
+  double max_separation;  /* 2.0; <= 0 turns the filter off */
+  int two_d;              /* 0 */
+} sf_label_options;
+
+/* dials_spots::Counts (src/spots/dials_spots.hh:99-106). */
+typedef struct {
+  uint64_t signal_pixels, groups, too_small, too_large, separated, accepted;
+} sf_counts;
+
+typedef struct sf_labeller sf_labeller;
+
+void sf_default_label_options(sf_label_options *options);
+
+/* Replaces dials_spots::Labeller::Labeller (src/spots/dials_spots.hh:110,
+ * dials_spots.cc:21-30): NULL, with the reason in sf_last_error(), on the
+ * errors the constructor throws for. live_capacity bounds the pixels held
+ * open at once plus one batch's (0: 4 Mi); exceeding it is reported by the
+ * add as -2. The labeller's device state is resident until sf_label_close. */
+sf_labeller *sf_label_open(size_t height, size_t width,
+                           const sf_label_options *options,
+                           size_t live_capacity);
+void sf_label_close(sf_labeller *labeller);
+
+/* Replaces Labeller::add (src/spots/dials_spots.hh:114,
+ * dials_spots.cc:57-145) for one frame's host list, ascending by index.
+ * -1 if the frame is out of order or the list is off the frame or not
+ * ascending (the reference throws there). */
+int sf_label_add(sf_labeller *labeller, int64_t frame,
+                 const sf_signal_pixel *signal, size_t n);
+
+/* Labeller::add for n_frames ascending frames at once, their lists already
+ * on the device (frame j's at d_lists + j * list_stride, its count in
+ * d_counts[j]), e.g. straight from sf_threshold_*_device; enqueued on
+ * `stream` (NULL: the labeller's own). At most 64 frames per call. No
+ * reference counterpart: the reference adds one host list at a time. */
+int sf_label_add_device(sf_labeller *labeller, const int64_t *frames,
+                        size_t n_frames, const sf_signal_pixel *d_lists,
+                        size_t list_stride, const uint32_t *d_counts,
+                        void *stream);
+
+/* Replaces Labeller::finish (src/spots/dials_spots.hh:117). */
+int sf_label_finish(sf_labeller *labeller);
+
+/* Replace Labeller::spots(), pixels(), counts(), live()
+ * (src/spots/dials_spots.hh:119-125). The copies return -2 if capacity is
+ * short. */
+size_t sf_label_n_spots(const sf_labeller *labeller);
+size_t sf_label_n_pixels(const sf_labeller *labeller);
+int sf_label_spots(const sf_labeller *labeller, sf_spot *out, size_t capacity);
+int sf_label_pixels(const sf_labeller *labeller, sf_pixel *out,
+                    size_t capacity);
+void sf_label_counts(const sf_labeller *labeller, sf_counts *out);
+size_t sf_label_live(const sf_labeller *labeller);
+
 /*
  * sf_threshold_u32_device as above, for callers that cannot allocate device
  * memory: a plugin inside a host application whose own allocator owns all
