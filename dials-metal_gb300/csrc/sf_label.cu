@@ -51,6 +51,7 @@ enum : uint32_t {
   kErrUnion = 2u,      // a union did not settle within kUnionRetries
   kErrSpotSize = 4u,   // an accepted spot larger than kBlockSortMax
   kErrOutFull = 8u,    // more spots / kept pixels than the batch outputs hold
+  kErrListOverflow = 16u, // an input list's count exceeds its stride
 };
 
 enum { kCntSignal = 0, kCntGroups, kCntSmall, kCntLarge, kCntSeparated, kCntAccepted };
@@ -131,12 +132,18 @@ __device__ __forceinline__ uint32_t lower_bound(const uint32_t *v, uint32_t lo, 
 // ---------------------------------------------------------------------------
 
 __global__ void k_offsets(LabelStatus *st, const uint32_t *__restrict__ counts,
-                          const BatchArgs a, uint32_t capacity) {
+                          size_t stride, const BatchArgs a, uint32_t capacity) {
   if (threadIdx.x != 0 || st->error)
     return;
   uint32_t off = 0;
   for (int j = 0; j < a.nb; j++) {
     st->frame_off[j] = off;
+    // A list whose count exceeds its stride is one that overflowed its
+    // threshold's capacity: it is incomplete, and refused.
+    if (counts[j] > stride) {
+      st->error |= kErrListOverflow;
+      return;
+    }
     off += counts[j];
   }
   st->frame_off[a.nb] = off;
@@ -880,7 +887,7 @@ struct Labeller {
     const int c = cur, o = 1 - cur;
     const dim3 g2(kGrid / 4 > 0 ? kGrid / 4 : 1, a.nb);
     cudaError_t e;
-    k_offsets<<<1, 32, 0, s>>>(st, counts_dev, a, (uint32_t)capacity);
+    k_offsets<<<1, 32, 0, s>>>(st, counts_dev, stride, a, (uint32_t)capacity);
     k_append<<<g2, kThreads, 0, s>>>(st, lists, stride, a, frame[c], index[c], value[c],
                                      parent[c]);
     k_link<<<g2, kThreads, 0, s>>>(st, a, index[c], parent[c]);
@@ -945,7 +952,10 @@ struct Labeller {
                      : (err & kErrSpotSize)
                          ? "a spot within the size limits is larger than 8192 pixels"
                      : (err & kErrOutFull) ? "labeller outputs overflowed"
-                                           : "a union did not settle";
+                     : (err & kErrListOverflow)
+                         ? "a signal list's count exceeds its capacity (the threshold "
+                           "overflowed)"
+                         : "a union did not settle";
       return SF_EOVERFLOW;
     }
     const uint32_t na = host_st->n_accept, npx = host_st->n_accept_pixels;
