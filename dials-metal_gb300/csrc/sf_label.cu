@@ -1102,7 +1102,9 @@ int sf_label_add_device(sf_labeller *l, const int64_t *frames, size_t n_frames,
     prev = frames[j];
     have = true;
   }
-  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : L.own_stream;
+  // The stream the lists were produced on; NULL is the legacy default stream,
+  // as for the threshold's device entry points.
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : cudaStreamLegacy;
   return L.run_batch(frames, (int)n_frames, d_lists, list_stride, d_counts, false, s);
 }
 

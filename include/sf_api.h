@@ -197,8 +197,10 @@ int sf_label_add(sf_labeller *labeller, int64_t frame,
 /* Labeller::add for n_frames ascending frames at once, their lists already
  * on the device (frame j's at d_lists + j * list_stride, its count in
  * d_counts[j]), e.g. straight from sf_threshold_*_device; enqueued on
- * `stream` (NULL: the labeller's own). At most 64 frames per call. No
- * reference counterpart: the reference adds one host list at a time. */
+ * `stream`, the stream that produced the lists (NULL: the legacy default
+ * stream), which is synchronised before the call returns. At most 64 frames
+ * per call. No reference counterpart: the reference adds one host list at a
+ * time. */
 int sf_label_add_device(sf_labeller *labeller, const int64_t *frames,
                         size_t n_frames, const sf_signal_pixel *d_lists,
                         size_t list_stride, const uint32_t *d_counts,
