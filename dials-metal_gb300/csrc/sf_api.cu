@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -13,6 +14,8 @@
 
 #include "sf_api.h"
 #include "sf_common.cuh"
+#include "sf_scan.cuh"
+#include "sf_stream.cuh"
 #include "sf_threshold.cuh"
 
 namespace sf {
@@ -80,18 +83,36 @@ int make_launch_params(const sf_threshold_params *in, LaunchParams *P) {
   return SF_OK;
 }
 
+// One workspace serves both threshold paths: the streaming path (32-bit
+// frames, dispersion_extended, gain 1 and integral sigmas) and the tile path
+// (everything else).
 struct WorkspaceLayout {
-  size_t staging, tile_base, row_total, total;
+  size_t staging, cand, scr1, prefix, wide, counters, block_sums, tile_base, row_total,
+      total;
+  size_t cand_cap;
 };
 
 static WorkspaceLayout layout(size_t h, size_t w, size_t capacity) {
   WorkspaceLayout L;
-  L.staging = 0;
-  size_t off = align_up(capacity * sizeof(sf_signal_pixel), 256);
-  L.tile_base = off;
-  off += align_up((size_t)tiles_x((int)w) * tiles_y((int)h) * sizeof(uint32_t), 256);
-  L.row_total = off;
-  off += align_up((size_t)tiles_y((int)h) * sizeof(uint32_t), 256);
+  const size_t words = (w + 31) / 32 * h;
+  // A frame with more eroded-mask candidates than twice the list capacity
+  // (plus slack) is not a frame of spots; it is refused like an overflow.
+  L.cand_cap = std::min(h * w, 2 * capacity + 65536);
+  size_t off = 0;
+  auto take = [&off](size_t bytes) {
+    const size_t at = off;
+    off += align_up(bytes ? bytes : 1, 256);
+    return at;
+  };
+  L.staging = take(capacity * sizeof(sf_signal_pixel));
+  L.cand = take(L.cand_cap * sizeof(uint32_t));
+  L.scr1 = take(words * sizeof(uint32_t));
+  L.prefix = take(words * sizeof(uint32_t));
+  L.wide = take((size_t)stream_units((int)h, (int)w) * 16);
+  L.counters = take(kCtrCount * sizeof(uint32_t));
+  L.block_sums = take(kScanBlocks * sizeof(uint32_t));
+  L.tile_base = take((size_t)tiles_x((int)w) * tiles_y((int)h) * sizeof(uint32_t));
+  L.row_total = take((size_t)tiles_y((int)h) * sizeof(uint32_t));
   L.total = off;
   return L;
 }
@@ -119,6 +140,26 @@ static int threshold_device(const T *d_image, size_t h, size_t w,
   if (ws_bytes < L.total)
     return SF_EBADARG;
   unsigned char *ws = static_cast<unsigned char *>(d_ws);
+  if (sizeof(T) == 4 && P.algorithm == SF_DISPERSION_EXTENDED && P.int_ok) {
+    StreamBuffers b;
+    b.bits = d_bits;
+    b.scr1 = reinterpret_cast<uint32_t *>(ws + L.scr1);
+    b.prefix = d_word_prefix ? d_word_prefix : reinterpret_cast<uint32_t *>(ws + L.prefix);
+    b.cand = reinterpret_cast<uint32_t *>(ws + L.cand);
+    b.cand_cap = (uint32_t)L.cand_cap;
+    b.counters = reinterpret_cast<uint32_t *>(ws + L.counters);
+    b.wide = reinterpret_cast<uint4 *>(ws + L.wide);
+    b.block_sums = reinterpret_cast<uint32_t *>(ws + L.block_sums);
+    b.staging = reinterpret_cast<sf_signal_pixel *>(ws + L.staging);
+    b.out = d_out;
+    b.capacity = (uint32_t)capacity;
+    b.count_out = d_count;
+    cudaError_t e = launch_stream(reinterpret_cast<const uint32_t *>(d_image), (int)h, (int)w,
+                                  P, b, stream);
+    if (e != cudaSuccess)
+      return fail(e, "launching the threshold");
+    return SF_OK;
+  }
   FrameBuffers fb;
   fb.bits = d_bits;
   fb.staging = reinterpret_cast<sf_signal_pixel *>(ws + L.staging);
@@ -470,11 +511,11 @@ int sf_threshold_u16_device(const uint16_t *d_image, size_t height, size_t width
 
 namespace sf {
 
-// 8 MiB of staging (524,288 signal records of 16 bytes) plus 1 MiB for the
-// per-tile bookkeeping, which covers every frame shape up to and beyond the
-// EIGER2 16M (4362 x 4148, 17,810 tiles).
+// 24 MiB: 8 MiB of staging (524,288 signal records of 16 bytes), the
+// candidate list for that capacity (4.25 MiB), and the per-word and per-tile
+// bookkeeping of frames up to 2^25 pixels (the EIGER2 16M is 18.1 M).
 constexpr size_t kNoAllocCapacity = 524288;
-constexpr size_t kNoAllocScratchBytes = kNoAllocCapacity * sizeof(sf_signal_pixel) + (1u << 20);
+constexpr size_t kNoAllocScratchBytes = (size_t)24 << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 

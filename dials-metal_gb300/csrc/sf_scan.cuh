@@ -56,7 +56,7 @@ __device__ __forceinline__ void scan_chunk(uint32_t n, uint32_t *lo, uint32_t *h
   *hi = min(n, *lo + chunk);
 }
 
-__global__ void __launch_bounds__(kScanThreads)
+static __global__ void __launch_bounds__(kScanThreads)
 scan_sums(const uint32_t *__restrict__ in, const uint32_t *__restrict__ d_n,
           uint32_t *__restrict__ block_sums, const uint32_t *__restrict__ d_error) {
   if (d_error && *d_error)
@@ -80,7 +80,7 @@ scan_sums(const uint32_t *__restrict__ in, const uint32_t *__restrict__ d_n,
   }
 }
 
-__global__ void __launch_bounds__(kScanBlocks)
+static __global__ void __launch_bounds__(kScanBlocks)
 scan_block_sums(uint32_t *__restrict__ block_sums, uint32_t *__restrict__ d_total,
                 const uint32_t *__restrict__ d_error) {
   if (d_error && *d_error)
@@ -94,7 +94,7 @@ scan_block_sums(uint32_t *__restrict__ block_sums, uint32_t *__restrict__ d_tota
     *d_total = total;
 }
 
-__global__ void __launch_bounds__(kScanThreads)
+static __global__ void __launch_bounds__(kScanThreads)
 scan_apply(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
            const uint32_t *__restrict__ d_n, const uint32_t *__restrict__ block_sums,
            const uint32_t *__restrict__ d_error) {

@@ -1,0 +1,67 @@
+// Internal interface of the streaming threshold (sf_stream.cu).
+//
+// The float decision of the dispersion test. With exact n, S (integers) and
+// Q~ = the float sum of the window's p^2 (13 roundings of non-negative terms
+// at most, so Q~ = Q (1 + e), |e| <= 13 u, u = 2^-24), the reference's test
+// at gain 1 and integral sigma_b is A > RN(X) with A = nQ - S(S + n - 1)
+// exact and X = S sigma_b r_n (the reference's double r_n). Writing
+// c = n - 1 + sigma_b r_n, A - X = nQ - S(S + c). Tables per n give floats
+// nf_hi >= n (1 + 2^-14), nf_lo <= n (1 - 2^-14) and c_lo <= c <= c_hi.
+//   RN(nf_hi Q~) <= RN(S~ RN(S~ + c_lo))     =>  nQ <= S(S + c): not signal
+//   RN(nf_lo Q~) >= RN(RN(1.0001 RN(S~ RN(S~ + c_hi))) + 2)
+//                                            =>  nQ >= S(S + c) + 1: signal
+// (the 2^-14 and 1.0001 margins exceed the few-u float errors by orders of
+// magnitude). Anything else is decided exactly. The packed sums hold while
+// every valid pixel is below 2^26 / n_max, which also keeps nQ < 2^53 and
+// S^2 < 2^52, where the reference's double left side is exactly A.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sf_common.cuh"
+
+namespace sf {
+
+constexpr int kStreamTW = 224;  // output columns per strip
+constexpr int kStreamSH = 96;   // output rows per strip segment
+
+// Counter words at the start of the stream workspace.
+enum {
+  kCtrTotal = 0,  // signal pixels found
+  kCtrCand,       // candidates found
+  kCtrWide,       // strip segments handed to the 64-bit path
+  kCtrWords,      // bitmask words of the frame
+  kCtrCount = 8
+};
+
+struct StreamTables {
+  uint32_t narrow_max;  // valid pixels at or above this take the 64-bit path
+  float nf_hi[kMaxN0 + 1], nf_lo[kMaxN0 + 1], c_lo[kMaxN0 + 1], c_hi[kMaxN0 + 1];
+};
+
+struct StreamBuffers {
+  uint32_t *bits;         // final strong mask (output)
+  uint32_t *scr1;         // eroded mask
+  uint32_t *prefix;       // per-word exclusive popcount prefix (maybe output)
+  uint32_t *cand;         // candidate pixel indices
+  uint32_t cand_cap;
+  uint32_t *counters;     // kCtrCount words
+  uint4 *wide;            // handed-over strip segments
+  uint32_t *block_sums;   // scan scratch
+  sf_signal_pixel *staging;
+  sf_signal_pixel *out;   // ascending list (output)
+  uint32_t capacity;
+  uint32_t *count_out;    // the caller's count word
+};
+
+inline int stream_units(int h, int w) {
+  return ((w + kStreamTW - 1) / kStreamTW) * ((h + kStreamSH - 1) / kStreamSH);
+}
+
+void make_stream_tables(const LaunchParams &P, StreamTables *T);
+
+cudaError_t launch_stream(const uint32_t *image, int h, int w, const LaunchParams &P,
+                          const StreamBuffers &b, cudaStream_t stream);
+
+} // namespace sf

@@ -225,11 +225,11 @@ size_t sf_label_live(const sf_labeller *labeller);
  * memory: a plugin inside a host application whose own allocator owns all
  * device memory, or a detector-stream loop that must not stall on an
  * allocation. It has no counterpart in the reference. Its scratch is a fixed
- * 9 MiB array inside this library (held on every GPU that loads the library
+ * 24 MiB array inside this library (held on every GPU that loads the library
  * until exit), so it takes no workspace and calls no allocator; the caller
  * still passes the frame and every output.
- *   - capacity may be at most 524288 records; larger capacities, or frames
- *     whose per-tile bookkeeping would not fit, return -1 with the reason in
+ *   - capacity may be at most 524288 records, and the frame at most about
+ *     2^25 pixels; beyond either it returns -1 with the reason in
  *     sf_last_error().
  *   - The first call on each device looks up the array's device address
  *     (cudaGetSymbolAddress) with that device current; make that first call
