@@ -37,6 +37,12 @@
 
 namespace sf {
 
+// Packed exact sums: the window count in the top bits (enough for the
+// largest window, (2K+1)^2 pixels), the sum in the rest.
+constexpr int pack_shift(int K) {
+  return (2 * K + 1) * (2 * K + 1) < 32 ? 27 : (2 * K + 1) * (2 * K + 1) < 64 ? 26 : 25;
+}
+
 template <int K> struct SG {
   static constexpr int E = K - 1;          // erosion radius
   static constexpr int R1 = 2 * K - 1;     // pixel halo of the eroded mask
@@ -54,6 +60,9 @@ template <int K> struct SG {
   static constexpr int N0 = (2 * K + 1) * (2 * K + 1);
   static constexpr int F4 = LW / 4;        // float4 per loaded row
   static constexpr int CCAP = 2048;        // block candidate buffer
+  static constexpr uint32_t PS = pack_shift(K);
+  static constexpr uint32_t MASK = (1u << PS) - 1u;
+  static_assert(N0 < (1 << (32 - PS)), "the count fits above the sum");
   static_assert(TW % 32 == 0, "strip width is whole words");
   static_assert(S0W <= NT, "one thread per stage-0 column");
   static_assert(A >= R1 && A % 4 == 0, "pad");
@@ -61,9 +70,6 @@ template <int K> struct SG {
   static_assert(A - R1 + 7 + 2 * K <= 19, "a segment's windows lie in its 20 loaded values");
 };
 
-// Packed exact sums: count in the top 6 bits, sum in the low 26.
-constexpr uint32_t kPackShift = 26;
-constexpr uint32_t kSumMask = (1u << kPackShift) - 1u;
 
 __device__ __forceinline__ float u23_to_float(uint32_t v) {
   // Exact for v < 2^23: the bits of 2^23 + v, less 2^23.
@@ -202,7 +208,7 @@ stream_stage01(const uint32_t *__restrict__ image, int height, int width, int ve
         const bool valid = v[e] < 0xFFFFFFFEu;
         wide |= valid && v[e] >= narrow;
         const uint32_t pv = valid && v[e] < narrow ? v[e] : 0u;
-        packed[e] = valid ? ((1u << kPackShift) | pv) : 0u;
+        packed[e] = valid ? ((1u << G::PS) | pv) : 0u;
         const float f = u23_to_float(pv);
         qq[e] = __fmul_rn(f, f);
       }
@@ -295,8 +301,8 @@ stream_stage01(const uint32_t *__restrict__ image, int height, int width, int ve
         const int rr = ((row % G::RING) + G::RING) % G::RING;
         const uint32_t me = own ? s.ns[rr][cj] : 0u;
         const bool masked = me == 0u;
-        const uint32_t n = vns >> kPackShift;
-        const uint32_t S = vns & kSumMask;
+        const uint32_t n = vns >> G::PS;
+        const uint32_t S = vns & G::MASK;
         bool bit = masked, defer = false;
         if (!masked) {
           // Surely not: nQ <= S (S + c_lo) with every float error bounded
@@ -351,7 +357,7 @@ stream_stage01(const uint32_t *__restrict__ image, int height, int width, int ve
           for (int dx = -K; dx <= K; dx++) {
             const uint32_t v = s.ns[rr][c + dx];
             if (v) {
-              const unsigned long long p = v & kSumMask;
+              const unsigned long long p = v & G::MASK;
               n++;
               S += p;
               Q += p * p;
@@ -402,7 +408,7 @@ stream_stage01(const uint32_t *__restrict__ image, int height, int width, int ve
         }
         const int rr = ((row % G::RING) + G::RING) % G::RING;
         const uint32_t pk = s.ns[rr][c + G::A];
-        const bool cnd = b && !((mreg >> k) & 1u) && (uint64_t)(pk & kSumMask) >= P.p_min;
+        const bool cnd = b && !((mreg >> k) & 1u) && (uint64_t)(pk & G::MASK) >= P.p_min;
         const unsigned cm = __ballot_sync(0xffffffffu, cnd);
         if (cm) {
           uint32_t base = 0;
@@ -664,7 +670,8 @@ static float round_up(double v) {
 void make_stream_tables(const LaunchParams &P, StreamTables *T) {
   const int K = P.half;
   const int n0 = (2 * K + 1) * (2 * K + 1);
-  T->narrow_max = (uint32_t)(((1u << kPackShift) - 1u) / (uint32_t)n0);
+  const int ps = K == 2 ? pack_shift(2) : K == 3 ? pack_shift(3) : pack_shift(4);
+  T->narrow_max = (uint32_t)(((1u << ps) - 1u) / (uint32_t)n0);
   for (int n = 0; n <= kMaxN0; n++) {
     const bool testable = n >= 1 && (uint32_t)n >= P.min_local && n <= n0;
     // c = n - 1 + sigma_b r_n with the reference's double r_n; the margins

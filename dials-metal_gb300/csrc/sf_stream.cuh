@@ -11,9 +11,10 @@
 //   RN(nf_lo Q~) >= RN(RN(1.0001 RN(S~ RN(S~ + c_hi))) + 2)
 //                                            =>  nQ >= S(S + c) + 1: signal
 // (the 2^-14 and 1.0001 margins exceed the few-u float errors by orders of
-// magnitude). Anything else is decided exactly. The packed sums hold while
-// every valid pixel is below 2^26 / n_max, which also keeps nQ < 2^53 and
-// S^2 < 2^52, where the reference's double left side is exactly A.
+// magnitude). Anything else is decided exactly. The packed sums (count above
+// a 27-, 26- or 25-bit sum for K = 2, 3, 4) hold while every valid pixel is
+// below 2^bits / n_max, which also keeps nQ < 2^53 and S^2 < 2^52, where the
+// reference's double left side is exactly A.
 #pragma once
 
 #include <cuda_runtime.h>
