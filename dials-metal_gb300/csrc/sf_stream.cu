@@ -31,6 +31,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+#include <cmath>
+
 #include "sf_common.cuh"
 #include "sf_scan.cuh"
 #include "sf_stream.cuh"
@@ -79,17 +82,17 @@ __device__ __forceinline__ float u23_to_float(uint32_t v) {
 template <int K>
 struct StreamSmem {
   using G = SG<K>;
-  uint32_t ns[G::RING][G::LWP];      // packed pixels: valid ? (1 << 26 | p) : 0
-  float q[G::STEP][G::LWP];          // p^2 (float), the step's rows
+  uint32_t ns[G::RING][G::LWP];      // packed pixels: valid ? (1 << PS | p) : 0
+  uint32_t q[G::STEP][G::LWP];       // p^2, the step's rows
   uint32_t hns[G::STEP][G::HW];      // row sums of packed pixels
-  float hq[G::STEP][G::HW];          // row sums of p^2
+  uint32_t hq[G::STEP][G::HW];       // row sums of p^2
   uint32_t vcol[G::S0W];             // vertical erosion words
   uint32_t fix[G::S0W];              // exact decisions that came out "signal"
   uint16_t defer[G::S0W * G::STEP];  // queued pixels: j * 8 + row-in-step
   uint32_t cand[G::CCAP];
   float nf_hi[G::N0 + 1], nf_lo[G::N0 + 1], c_lo[G::N0 + 1], c_hi[G::N0 + 1];
   uint32_t root_lo[G::N0 + 1], root_hi[G::N0 + 1];
-  uint32_t ndefer, ncand, wide;
+  uint32_t ndefer, ncand;
 };
 
 template <int K>
@@ -112,14 +115,45 @@ __device__ void flush_candidates(StreamSmem<K> &s, uint32_t *cand, uint32_t *cou
   __syncthreads();
 }
 
+// One step's raw pixels for this thread: float4 number tid and tid + 256 of
+// the step's 8 x F4.
 template <int K>
-__global__ void __launch_bounds__(256)
+__device__ __forceinline__ void load_step(const uint32_t *__restrict__ image, int height,
+                                          int width, int vec, int x0, int P0, uint4 v[2]) {
+  using G = SG<K>;
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int i = threadIdx.x + h * G::NT;
+    v[h] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+    if (i >= G::STEP * G::F4)
+      continue;
+    const int r = i / G::F4, c4 = i - r * G::F4;
+    const int gy = P0 + r, gx = x0 - G::A + 4 * c4;
+    if (gy < 0 || gy >= height)
+      continue;
+    const uint32_t *row = image + (size_t)gy * width;
+    if (vec && gx >= 0 && gx + 3 < width) {
+      v[h] = __ldg(reinterpret_cast<const uint4 *>(row + gx));
+    } else {
+      uint32_t t[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+#pragma unroll
+      for (int e = 0; e < 4; e++)
+        if (gx + e >= 0 && gx + e < width)
+          t[e] = __ldg(row + gx + e);
+      v[h] = make_uint4(t[0], t[1], t[2], t[3]);
+    }
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(256, 3)
 stream_stage01(const uint32_t *__restrict__ image, int height, int width, int vec,
                const __grid_constant__ LaunchParams P, const __grid_constant__ StreamTables T,
                uint32_t *__restrict__ scr1_bits, uint32_t *__restrict__ final_bits,
                uint32_t *__restrict__ cand, uint32_t cand_cap, uint32_t *__restrict__ counters,
                uint4 *__restrict__ wide_list) {
   using G = SG<K>;
+  constexpr int W0 = 2 * K + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   StreamSmem<K> &s = *reinterpret_cast<StreamSmem<K> *>(smem_raw);
   const int tid = threadIdx.x;
@@ -129,6 +163,9 @@ stream_stage01(const uint32_t *__restrict__ image, int height, int width, int ve
   const int y1 = min(height, y0 + kStreamSH);
   const int wpr = (width + 31) >> 5;
   const uint32_t narrow = T.narrow_max;
+  // The all-valid window's table entries, the common case.
+  const float nf_hi0 = T.nf_hi[G::N0], nf_lo0 = T.nf_lo[G::N0];
+  const float c_lo0 = T.c_lo[G::N0], c_hi0 = T.c_hi[G::N0];
 
   for (int i = tid; i <= G::N0; i += G::NT) {
     s.nf_hi[i] = T.nf_hi[i];
@@ -145,7 +182,6 @@ stream_stage01(const uint32_t *__restrict__ image, int height, int width, int ve
   if (tid == 0) {
     s.ndefer = 0;
     s.ncand = 0;
-    s.wide = 0;
   }
 
   // This thread's stage-0 column j (output column j - E), if any.
@@ -156,67 +192,56 @@ stream_stage01(const uint32_t *__restrict__ image, int height, int width, int ve
     j = tid - G::TW;
   else if (tid < G::TW + 2 * G::E)
     j = tid;
-  const int cj = G::A - G::E + j;  // its column in the loaded rows
+  const bool own = j >= 0;
+  const int cj = G::A - G::E + (own ? j : 0);  // its column in the loaded rows
 
-  // Row sums of the previous two steps, step-local order (index i = row
-  // P0 - 8 + i for old, P0 - 16 + i for old2).
-  uint32_t old_ns[8], old2_ns[8];
-  float old_q[8];
+  // Row sums of the previous two steps (index i = row P0 - 8 + i for old,
+  // P0 - 16 + i for old2).
+  uint32_t old_ns[8], old2_ns[8], old_q[8], old2_q[8];
 #pragma unroll
-  for (int i = 0; i < 8; i++) {
-    old_ns[i] = 0;
-    old2_ns[i] = 0;
-    old_q[i] = 0.0f;
-  }
-  uint32_t vns = 0;        // running column sum of the row sums (packed)
-  uint32_t sreg = 0;       // stage-0 mask, bit 0 = newest row
-  uint32_t mreg = 0;       // masked pixels, same rows
-  __syncthreads();
+  for (int i = 0; i < 8; i++)
+    old_ns[i] = old2_ns[i] = old_q[i] = old2_q[i] = 0u;
+  uint32_t vns = 0, vq = 0; // running column sums
+  uint32_t sreg = 0;        // stage-0 mask, bit 0 = newest row
+  uint32_t mreg = 0;        // masked pixels, same rows
 
   const int p_first = y0 - G::R1;
-  // Output rows of step t: scr1 rows (P + 7 - K) - k for k in [E, E + 8).
+  uint4 raw[2];
+  load_step<K>(image, height, width, vec, x0, p_first, raw);
+  __syncthreads();
+
+  // Ring rows are indexed by row - p_first (non-negative) modulo RING.
   for (int P0 = p_first;; P0 += G::STEP) {
     const int newest_v0 = P0 + 7 - K;
-    const int out_hi = newest_v0 - G::E;   // highest scr1 row this step
+    const int out_hi = newest_v0 - G::E;  // highest eroded row this step
     const int out_lo = out_hi - 7;
     if (out_lo >= y1)
       break;
+    const int rb = P0 - p_first;          // ring base for row P0
 
-    // -- pack 8 pixel rows [P0, P0 + 8) --------------------------------------
+    // -- pack the step's 8 pixel rows; prefetch the next step's ---------------
     bool wide = false;
-    for (int i = tid; i < G::STEP * G::F4; i += G::NT) {
-      const int r = i / G::F4, c4 = i - r * G::F4;
-      const int gy = P0 + r;
-      const int gx = x0 - G::A + 4 * c4;
-      uint32_t v[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
-      if (gy >= 0 && gy < height) {
-        const uint32_t *row = image + (size_t)gy * width;
-        if (vec && gx >= 0 && gx + 3 < width) {
-          const uint4 t4 = __ldg(reinterpret_cast<const uint4 *>(row + gx));
-          v[0] = t4.x, v[1] = t4.y, v[2] = t4.z, v[3] = t4.w;
-        } else {
 #pragma unroll
-          for (int e = 0; e < 4; e++)
-            if (gx + e >= 0 && gx + e < width)
-              v[e] = __ldg(row + gx + e);
+    for (int h = 0; h < 2; h++) {
+      const int i = tid + h * G::NT;
+      if (i < G::STEP * G::F4) {
+        const int r = i / G::F4, c4 = i - r * G::F4;
+        const uint32_t v[4] = {raw[h].x, raw[h].y, raw[h].z, raw[h].w};
+        uint32_t pk[4], qq[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const bool valid = v[e] < 0xFFFFFFFEu;
+          wide |= valid && v[e] >= narrow;
+          const uint32_t pv = valid && v[e] < narrow ? v[e] : 0u;
+          pk[e] = valid ? ((1u << G::PS) | pv) : 0u;
+          qq[e] = pv * pv;
         }
+        *reinterpret_cast<uint4 *>(&s.ns[(rb + r) & (G::RING - 1)][4 * c4]) =
+            make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        *reinterpret_cast<uint4 *>(&s.q[r][4 * c4]) = make_uint4(qq[0], qq[1], qq[2], qq[3]);
       }
-      uint32_t packed[4];
-      float qq[4];
-#pragma unroll
-      for (int e = 0; e < 4; e++) {
-        const bool valid = v[e] < 0xFFFFFFFEu;
-        wide |= valid && v[e] >= narrow;
-        const uint32_t pv = valid && v[e] < narrow ? v[e] : 0u;
-        packed[e] = valid ? ((1u << G::PS) | pv) : 0u;
-        const float f = u23_to_float(pv);
-        qq[e] = __fmul_rn(f, f);
-      }
-      const int rr = (gy % G::RING + G::RING) % G::RING;
-      *reinterpret_cast<uint4 *>(&s.ns[rr][4 * c4]) =
-          make_uint4(packed[0], packed[1], packed[2], packed[3]);
-      *reinterpret_cast<float4 *>(&s.q[r][4 * c4]) = make_float4(qq[0], qq[1], qq[2], qq[3]);
     }
+    load_step<K>(image, height, width, vec, x0, P0 + G::STEP, raw);
     if (__syncthreads_or(wide)) {
       // Rows from out_lo on are not yet written: hand the rest over.
       if (tid == 0) {
@@ -227,107 +252,98 @@ stream_stage01(const uint32_t *__restrict__ image, int height, int width, int ve
     }
 
     // -- row sums over 2K + 1 columns, 8 outputs per thread ------------------
-    for (int i = tid; i < G::STEP * G::NSEG; i += G::NT) {
-      const int r = i / G::NSEG, sg = i - r * G::NSEG;
-      const int rr = ((P0 + r) % G::RING + G::RING) % G::RING;
-      const int c0 = 8 * sg;  // aligned start; window starts at c0 + A - R1
-      uint32_t a[20];
-      float b[20];
+    if (tid < G::STEP * G::NSEG) {
+      const int r = tid / G::NSEG, sg = tid - r * G::NSEG;
+      const int ring_r = (rb + r) & (G::RING - 1);
+      const int c0 = 8 * sg;
+      uint32_t a[20], b[20];
 #pragma unroll
       for (int f = 0; f < 5; f++) {
-        const uint4 u = *reinterpret_cast<const uint4 *>(&s.ns[rr][c0 + 4 * f]);
-        const float4 w = *reinterpret_cast<const float4 *>(&s.q[r][c0 + 4 * f]);
+        const uint4 u = *reinterpret_cast<const uint4 *>(&s.ns[ring_r][c0 + 4 * f]);
+        const uint4 w = *reinterpret_cast<const uint4 *>(&s.q[r][c0 + 4 * f]);
         a[4 * f] = u.x, a[4 * f + 1] = u.y, a[4 * f + 2] = u.z, a[4 * f + 3] = u.w;
         b[4 * f] = w.x, b[4 * f + 1] = w.y, b[4 * f + 2] = w.z, b[4 * f + 3] = w.w;
       }
       constexpr int o = G::A - G::R1;
-      uint32_t hn[8];
-      float hq[8];
-      uint32_t run = 0;
+      uint32_t hn[8], hq[8];
+      uint32_t ra = 0, rq = 0;
 #pragma unroll
-      for (int d = 0; d <= 2 * K; d++)
-        run += a[o + d];
-      hn[0] = run;
+      for (int d = 0; d < W0; d++) {
+        ra += a[o + d];
+        rq += b[o + d];
+      }
+      hn[0] = ra;
+      hq[0] = rq;
 #pragma unroll
       for (int k = 1; k < 8; k++) {
-        run += a[o + k + 2 * K] - a[o + k - 1];
-        hn[k] = run;
-      }
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        float t = b[o + k];
-#pragma unroll
-        for (int d = 1; d <= 2 * K; d++)
-          t = __fadd_rn(t, b[o + k + d]);
-        hq[k] = t;
+        ra += a[o + k + 2 * K] - a[o + k - 1];
+        rq += b[o + k + 2 * K] - b[o + k - 1];
+        hn[k] = ra;
+        hq[k] = rq;
       }
       *reinterpret_cast<uint4 *>(&s.hns[r][c0]) = make_uint4(hn[0], hn[1], hn[2], hn[3]);
       *reinterpret_cast<uint4 *>(&s.hns[r][c0 + 4]) = make_uint4(hn[4], hn[5], hn[6], hn[7]);
-      *reinterpret_cast<float4 *>(&s.hq[r][c0]) = make_float4(hq[0], hq[1], hq[2], hq[3]);
-      *reinterpret_cast<float4 *>(&s.hq[r][c0 + 4]) = make_float4(hq[4], hq[5], hq[6], hq[7]);
+      *reinterpret_cast<uint4 *>(&s.hq[r][c0]) = make_uint4(hq[0], hq[1], hq[2], hq[3]);
+      *reinterpret_cast<uint4 *>(&s.hq[r][c0 + 4]) = make_uint4(hq[4], hq[5], hq[6], hq[7]);
     }
     __syncthreads();
 
     // -- column sums and the dispersion test, one thread per column ----------
     {
-      uint32_t cur_ns[8];
-      float cur_q[8];
-      const bool own = j >= 0;
+      uint32_t cur_ns[8], cur_q[8];
 #pragma unroll
       for (int r = 0; r < 8; r++) {
         cur_ns[r] = own ? s.hns[r][j] : 0u;
-        cur_q[r] = own ? s.hq[r][j] : 0.0f;
+        cur_q[r] = own ? s.hq[r][j] : 0u;
       }
 #pragma unroll
       for (int r = 0; r < 8; r++) {
-        // Column sums of rows r - 2K .. r (step-local), i.e. stage-0 row
-        // P0 + r - K.
-        {
-          // The row sum leaving the 2K + 1 window.
-          constexpr int W0 = 2 * K + 1;
-          const int d = r - W0;
-          const uint32_t leaving = d >= 0 ? cur_ns[d >= 0 ? d : 0]
-                                   : d >= -8 ? old_ns[8 + d >= 0 ? 8 + d : 0]
-                                             : old2_ns[16 + d >= 0 ? 16 + d : 0];
-          vns += cur_ns[r] - leaving;
-        }
-        float vq = cur_q[r];
-#pragma unroll
-        for (int d = 1; d <= 2 * K; d++) {
-          const int idx = r - d;
-          vq = __fadd_rn(vq, idx >= 0 ? cur_q[idx] : old_q[8 + idx]);
-        }
-        const int row = P0 + r - K;
-        const int rr = ((row % G::RING) + G::RING) % G::RING;
-        const uint32_t me = own ? s.ns[rr][cj] : 0u;
+        // The row sums leaving the 2K + 1 window (static indices).
+        constexpr int dummy = 0;
+        (void)dummy;
+        const int d = r - W0;
+        const uint32_t lns = d >= 0 ? cur_ns[d >= 0 ? d : 0]
+                             : d >= -8 ? old_ns[d >= -8 ? 8 + d : 0]
+                                       : old2_ns[16 + d >= 0 ? 16 + d : 0];
+        const uint32_t lq = d >= 0 ? cur_q[d >= 0 ? d : 0]
+                            : d >= -8 ? old_q[d >= -8 ? 8 + d : 0]
+                                      : old2_q[16 + d >= 0 ? 16 + d : 0];
+        vns += cur_ns[r] - lns;
+        vq += cur_q[r] - lq;
+        // Stage-0 row P0 + r - K.
+        const uint32_t me = s.ns[(rb + r - K + G::RING) & (G::RING - 1)][cj];
         const bool masked = me == 0u;
-        const uint32_t n = vns >> G::PS;
-        const uint32_t S = vns & G::MASK;
         bool bit = masked, defer = false;
         if (!masked) {
-          // Surely not: nQ <= S (S + c_lo) with every float error bounded
-          // (derivation in the header of sf_stream.cuh).
+          const uint32_t n = vns >> G::PS;
+          const uint32_t S = vns & G::MASK;
+          const bool full = n == (uint32_t)G::N0;
+          const float nhi = full ? nf_hi0 : s.nf_hi[n];
+          const float clo = full ? c_lo0 : s.c_lo[n];
           const float Sf = __uint2float_rn(S);
-          const float lhs_hi = __fmul_rn(s.nf_hi[n], vq);
-          const float rhs_lo = __fmul_rn(Sf, __fadd_rn(Sf, s.c_lo[n]));
-          if (!(lhs_hi <= rhs_lo)) {
-            // Surely: nQ >= S (S + c_hi) + 1, likewise.
-            const float lhs_lo = __fmul_rn(s.nf_lo[n], vq);
-            const float rhs_hi = __fmul_rn(Sf, __fadd_rn(Sf, s.c_hi[n]));
-            if (lhs_lo >= __fadd_rn(__fmul_rn(rhs_hi, 1.0001f), 2.0f))
+          const float Qf = __uint2float_rn(vq);
+          // Surely not: nQ <= S (S + c) (bounds in sf_stream.cuh).
+          if (!(__fmul_rn(nhi, Qf) <= __fmul_rn(Sf, __fadd_rn(Sf, clo)))) {
+            const float nlo = full ? nf_lo0 : s.nf_lo[n];
+            const float chi = full ? c_hi0 : s.c_hi[n];
+            // Surely: nQ >= S (S + c) + 1.
+            if (__fmul_rn(nlo, Qf) >=
+                __fadd_rn(__fmul_rn(__fmul_rn(Sf, __fadd_rn(Sf, chi)), 1.0001f), 2.0f))
               bit = true;
-            else
+            else {
+              const int row = P0 + r - K;
               // Rows beyond these only feed outputs outside the segment.
-              defer = row >= y0 - G::E && row < y1 + G::E;
+              defer = own && row >= y0 - G::E && row < y1 + G::E;
+            }
           }
         }
-        const unsigned dm = __ballot_sync(0xffffffffu, own && defer);
-        if (dm) {
+        if (__any_sync(0xffffffffu, defer)) {
+          const unsigned dm = __ballot_sync(0xffffffffu, defer);
           uint32_t base = 0;
           if (lane == 0)
             base = atomicAdd(&s.ndefer, (uint32_t)__popc(dm));
           base = __shfl_sync(0xffffffffu, base, 0);
-          if (own && defer)
+          if (defer)
             s.defer[base + __popc(dm & ((1u << lane) - 1u))] = (uint16_t)(j * 8 + r);
         }
         sreg = (sreg << 1) | (bit ? 1u : 0u);
@@ -337,25 +353,25 @@ stream_stage01(const uint32_t *__restrict__ image, int height, int width, int ve
       for (int r = 0; r < 8; r++) {
         old2_ns[r] = old_ns[r];
         old_ns[r] = cur_ns[r];
+        old2_q[r] = old_q[r];
         old_q[r] = cur_q[r];
       }
     }
     __syncthreads();
 
-    // -- the queued pixels, decided exactly -----------------------------------
+    // -- the queued pixels, decided exactly (rare) ----------------------------
     {
       const uint32_t nd = s.ndefer;
       for (uint32_t i = tid; i < nd; i += G::NT) {
         const uint32_t e = s.defer[i];
         const int jj = (int)(e >> 3), r = (int)(e & 7u);
-        const int row = P0 + r - K;
         const int c = G::A - G::E + jj;
         uint32_t n = 0;
         unsigned long long S = 0, Q = 0;
         for (int dy = -K; dy <= K; dy++) {
-          const int rr = (((row + dy) % G::RING) + G::RING) % G::RING;
+          const int ring_r = (rb + r - K + dy + G::RING) & (G::RING - 1);
           for (int dx = -K; dx <= K; dx++) {
-            const uint32_t v = s.ns[rr][c + dx];
+            const uint32_t v = s.ns[ring_r][c + dx];
             if (v) {
               const unsigned long long p = v & G::MASK;
               n++;
@@ -373,7 +389,7 @@ stream_stage01(const uint32_t *__restrict__ image, int height, int width, int ve
       s.ndefer = 0;
 
     // -- erosion ---------------------------------------------------------------
-    if (j >= 0) {
+    if (own) {
       sreg |= s.fix[j];
       s.fix[j] = 0u;
       uint32_t v = sreg;
@@ -393,21 +409,22 @@ stream_stage01(const uint32_t *__restrict__ image, int height, int width, int ve
         h &= s.vcol[c + G::E - d] & s.vcol[c + G::E + d];
       const uint32_t scr1 = h | mreg;
       const int gx = x0 + c;
+      const bool inside = gx < width;
+      const int widx = (x0 >> 5) + warp;
 #pragma unroll
       for (int k = G::E; k < G::E + 8; k++) {
         const int row = newest_v0 - k;
         if (row < y0 || row >= y1)
           continue;
-        const bool inside = gx < width;
         const bool b = inside && ((scr1 >> k) & 1u);
         const uint32_t word = __ballot_sync(0xffffffffu, b);
-        const int widx = (x0 >> 5) + warp;
         if (lane == 0 && widx < wpr) {
           scr1_bits[(size_t)row * wpr + widx] = word;
           final_bits[(size_t)row * wpr + widx] = 0u;
         }
-        const int rr = ((row % G::RING) + G::RING) % G::RING;
-        const uint32_t pk = s.ns[rr][c + G::A];
+        if (word == 0u)
+          continue;  // warp-uniform
+        const uint32_t pk = s.ns[(row - p_first) & (G::RING - 1)][c + G::A];
         const bool cnd = b && !((mreg >> k) & 1u) && (uint64_t)(pk & G::MASK) >= P.p_min;
         const unsigned cm = __ballot_sync(0xffffffffu, cnd);
         if (cm) {
@@ -578,12 +595,18 @@ stream_stage2(const uint32_t *__restrict__ image, int height, int width,
         const unsigned long long both =
             (unsigned long long)__ldg(brow + w0) |
             ((w0 + 1 < wpr) ? ((unsigned long long)__ldg(brow + w0 + 1) << 32) : 0ull);
-        for (int xx = xlo; xx <= xhi; xx++) {
-          const bool eroded = (both >> (xx - (w0 << 5))) & 1ull;
-          if (!eroded) {
-            // Masked pixels are in the eroded mask, so this one is valid.
+        const unsigned long long bg_bits = ~(both >> (xlo - (w0 << 5)));
+        // Row loads issued together, then summed.
+        uint32_t v[2 * K2 + 1];
+#pragma unroll
+        for (int d = 0; d <= 2 * K2; d++)
+          v[d] = (xlo + d <= xhi) ? __ldg(row + xlo + d) : 0u;
+#pragma unroll
+        for (int d = 0; d <= 2 * K2; d++) {
+          // Not in the eroded mask (masked pixels are in it), so valid.
+          if (xlo + d <= xhi && ((bg_bits >> d) & 1ull)) {
             n++;
-            S += __ldg(row + xx);
+            S += v[d];
           }
         }
       }
@@ -671,7 +694,13 @@ void make_stream_tables(const LaunchParams &P, StreamTables *T) {
   const int K = P.half;
   const int n0 = (2 * K + 1) * (2 * K + 1);
   const int ps = K == 2 ? pack_shift(2) : K == 3 ? pack_shift(3) : pack_shift(4);
-  T->narrow_max = (uint32_t)(((1u << ps) - 1u) / (uint32_t)n0);
+  // Exact 32-bit sums: the count and sum packed below 2^32, and the window's
+  // sum of p^2 below 2^32 (p < sqrt(2^32 / n0): 13107, 9362, 7282).
+  const uint32_t by_pack = (uint32_t)(((1u << ps) - 1u) / (uint32_t)n0);
+  uint32_t by_sq = (uint32_t)std::floor(std::sqrt(4294967295.0 / n0));
+  while ((uint64_t)by_sq * by_sq * (uint64_t)n0 > 0xFFFFFFFFull)
+    by_sq--;
+  T->narrow_max = std::min(by_pack, by_sq + 1);
   for (int n = 0; n <= kMaxN0; n++) {
     const bool testable = n >= 1 && (uint32_t)n >= P.min_local && n <= n0;
     // c = n - 1 + sigma_b r_n with the reference's double r_n; the margins
