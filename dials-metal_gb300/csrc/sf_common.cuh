@@ -122,9 +122,10 @@ __device__ __forceinline__ bool stage2_u32(uint32_t p, uint32_t n,
                                            unsigned long long S,
                                            const LaunchParams &P, float *bg) {
   if (n < P.min_local) {
+    // mean 0: sqrt(gain 0) is a zero, sigma_s times it a zero (both finite),
+    // and p >= 0 + 0 holds for every pixel.
     *bg = 0.0f;
-    // mean 0: p >= 0 + sigma_s sqrt(0) holds for any finite sigma_s.
-    return (double)p >= __dadd_rn(0.0, __dmul_rn(P.sigma_s, __dsqrt_rn(__dmul_rn(P.gain, 0.0))));
+    return true;
   }
   if (P.int_ok && S < (1ull << 24)) {
     *bg = __fdiv_rn((float)(uint32_t)S, (float)n);

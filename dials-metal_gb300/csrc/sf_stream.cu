@@ -1,32 +1,17 @@
 // The streaming threshold for 32-bit frames (the benchmark path).
 //
-// Stage 0 and the erosion of src/spots/dext.cc (:53-142) run in one pass
-// down vertical strips; stage 2 (:151-222) runs afterwards only at the
-// candidates the erosion leaves, which are a percent or so of the frame.
+// Stage 0 and the erosion of src/spots/dext.cc (:53-142) run in one pass in
+// which every warp walks down its own strip of rows; stage 2 (:151-222) runs
+// afterwards only at the candidates the erosion leaves, a percent or so of
+// the frame:
 //
-//   stream_stage01   One block per strip segment: 224 output columns by 96
-//                    output rows, walking down in steps of 8 rows. Each step
-//                    packs 8 new pixel rows into shared memory (count and sum
-//                    as n << 26 | S, exact; I^2 as float), takes row sums of
-//                    2K+1 columns, then one thread per column carries the
-//                    column sums down in registers and decides the dispersion
-//                    test for its pixel with a float bound: "surely not",
-//                    "surely", or near the threshold, in which case the pixel
-//                    is queued and decided exactly (uint64 sums, then the
-//                    reference's integer/double decision, sf_common.cuh). The
-//                    stage-0 mask lives in per-column shift registers, so the
-//                    erosion is a few shifts and ANDs. Out: the eroded mask
-//                    (bitmask), the final mask zeroed, and the candidates.
-//   stream_wide      The same outputs with 64-bit sums, for the rare strip
-//                    segments holding a valid pixel too large for the packed
-//                    sums (>= 2^26 / n_max); stream_stage01 hands them over
-//                    from the row where it met one.
-//   stream_stage2    One thread per candidate: the background count and sum
-//                    over the clipped (2K+5)^2 window, the Poisson test
-//                    (exact, sf_common.cuh), the record into a staging list and
-//                    the bit into the final mask.
-//   order_*          Popcount prefix of the final mask's words, then every
-//                    staged record scattered to its ascending position.
+//   seg_stage01   stage 0 + erosion, one warp per 240-column strip and run
+//                 of rows, no block barriers (described below)
+//   stream_wide   the same outputs with 64-bit sums, for the rare runs that
+//                 hold a valid pixel too large for the exact 32-bit sums
+//   seg_stage2    the background-only Poisson test at each candidate, exact
+//   order_*       a look-back scan of the final mask's popcounts, then every
+//                 staged record scattered to its ascending position
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -46,416 +31,305 @@ constexpr int pack_shift(int K) {
   return (2 * K + 1) * (2 * K + 1) < 32 ? 27 : (2 * K + 1) * (2 * K + 1) < 64 ? 26 : 25;
 }
 
-template <int K> struct SG {
-  static constexpr int E = K - 1;          // erosion radius
-  static constexpr int R1 = 2 * K - 1;     // pixel halo of the eroded mask
-  static constexpr int A = 8;              // left pad: >= R1, 16-byte aligned
-  static constexpr int TW = kStreamTW;     // output columns per strip (224)
-  static constexpr int LW = TW + 2 * A;    // loaded columns (240)
-  static constexpr int LWP = LW + 8;       // ring row stride (reads run past LW)
-  static constexpr int S0W = TW + 2 * E;   // stage-0 columns
-  static constexpr int NT = 256;
-  static constexpr int STEP = 8;
-  static constexpr int RING = 16;          // packed-pixel ring rows
-  static constexpr int NSEG = (S0W + 7) / 8;
-  static constexpr int HW = NSEG * 8;      // row-sum stride
-  static constexpr int NWORD = TW / 32;
-  static constexpr int N0 = (2 * K + 1) * (2 * K + 1);
-  static constexpr int F4 = LW / 4;        // float4 per loaded row
-  static constexpr int CCAP = 2048;        // block candidate buffer
+// ---------------------------------------------------------------------------
+// Stage 0 and the erosion, one warp per (strip, run of rows).
+//
+// Lane l owns the 8 columns [X + 8 l, X + 8 l + 8) and walks down the run one
+// pixel row at a time with no block barrier: it loads the 16 pixels
+// [X + 8 l - 4, X + 8 l + 12) of the row (four 16-byte loads, the next row's
+// prefetched), packs them (count and sum as n << PS | S, exact; p^2 exact in
+// 32 bits), takes its 8 row sums of 2K+1 columns in registers, and carries
+// 8 column sums down in registers; the row sum leaving the window comes back
+// from a small per-lane ring in shared memory. Each new stage-0 row gives 8
+// decisions (sf_stream.cuh), kept as 8-bit chunks in a 64-bit history; the
+// erosion ANDs 2E+1 chunks vertically, then across columns with the
+// neighbouring lanes' chunks (two shuffles). Lanes 0 and 31 are halo: they
+// feed their neighbours' erosion and write nothing, so a warp writes 240
+// columns. Pixels in the narrow range can take the near-threshold case exactly
+// inline, from the exact sums, since it is rare.
+// ---------------------------------------------------------------------------
+
+constexpr int kSegLanes = 32;
+constexpr int kSegOut = 240;          // output columns per warp
+constexpr int kSegWarps = 4;          // warps per block
+constexpr int kSegCand = 512;         // per-warp candidate buffer
+
+template <int K> struct SegG {
+  static constexpr int E = K - 1;
+  static constexpr int R1 = 2 * K - 1;
+  static constexpr int W0 = 2 * K + 1;
+  static constexpr int N0 = W0 * W0;
   static constexpr uint32_t PS = pack_shift(K);
   static constexpr uint32_t MASK = (1u << PS) - 1u;
-  static_assert(N0 < (1 << (32 - PS)), "the count fits above the sum");
-  static_assert(TW % 32 == 0, "strip width is whole words");
-  static_assert(S0W <= NT, "one thread per stage-0 column");
-  static_assert(A >= R1 && A % 4 == 0, "pad");
-  static_assert(8 * (NSEG - 1) + 19 < LWP, "row-sum reads stay in the row");
-  static_assert(A - R1 + 7 + 2 * K <= 19, "a segment's windows lie in its 20 loaded values");
+  static_assert(R1 <= 7, "eight rows of history");
 };
 
-
-__device__ __forceinline__ float u23_to_float(uint32_t v) {
-  // Exact for v < 2^23: the bits of 2^23 + v, less 2^23.
-  return __fsub_rn(__uint_as_float(v | 0x4B000000u), 8388608.0f);
-}
-
-template <int K>
-struct StreamSmem {
-  using G = SG<K>;
-  uint32_t ns[G::RING][G::LWP];      // packed pixels: valid ? (1 << PS | p) : 0
-  uint32_t q[G::STEP][G::LWP];       // p^2, the step's rows
-  uint32_t hns[G::STEP][G::HW];      // row sums of packed pixels
-  uint32_t hq[G::STEP][G::HW];       // row sums of p^2
-  uint32_t vcol[G::S0W];             // vertical erosion words
-  uint32_t fix[G::S0W];              // exact decisions that came out "signal"
-  uint16_t defer[G::S0W * G::STEP];  // queued pixels: j * 8 + row-in-step
-  uint32_t cand[G::CCAP];
-  float nf_hi[G::N0 + 1], nf_lo[G::N0 + 1], c_lo[G::N0 + 1], c_hi[G::N0 + 1];
-  uint32_t root_lo[G::N0 + 1], root_hi[G::N0 + 1];
-  uint32_t ndefer, ncand;
+template <int K> struct SegSmem {
+  using G = SegG<K>;
+  // ring[warp][slot][quad][lane] : uint4 = 4 of the 16 row sums
+  uint4 ring[kSegWarps][G::W0][4][kSegLanes];
+  uint32_t cand[kSegWarps][kSegCand];
+  uint32_t ncand[kSegWarps];
 };
 
-template <int K>
-__device__ void flush_candidates(StreamSmem<K> &s, uint32_t *cand, uint32_t *counters,
-                                 uint32_t cand_cap) {
-  // All threads; s.ncand stable (called between barriers).
-  const uint32_t n = s.ncand;
-  __shared__ uint32_t base;
-  if (threadIdx.x == 0)
-    base = n ? atomicAdd(&counters[kCtrCand], n) : 0u;
-  __syncthreads();
-  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-    const uint32_t g = base + i;
-    if (g < cand_cap)
-      cand[g] = s.cand[i];
-  }
-  __syncthreads();
-  if (threadIdx.x == 0)
-    s.ncand = 0;
-  __syncthreads();
-}
-
-// One step's raw pixels for this thread: float4 number tid and tid + 256 of
-// the step's 8 x F4.
-template <int K>
-__device__ __forceinline__ void load_step(const uint32_t *__restrict__ image, int height,
-                                          int width, int vec, int x0, int P0, uint4 v[2]) {
-  using G = SG<K>;
+__device__ __forceinline__ void seg_load(const uint32_t *__restrict__ image, int height, int width,
+                                         int vec, int cx, int p, uint32_t v[16]) {
 #pragma unroll
-  for (int h = 0; h < 2; h++) {
-    const int i = threadIdx.x + h * G::NT;
-    v[h] = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
-    if (i >= G::STEP * G::F4)
-      continue;
-    const int r = i / G::F4, c4 = i - r * G::F4;
-    const int gy = P0 + r, gx = x0 - G::A + 4 * c4;
-    if (gy < 0 || gy >= height)
-      continue;
-    const uint32_t *row = image + (size_t)gy * width;
+  for (int i = 0; i < 16; i++)
+    v[i] = 0xFFFFFFFFu;
+  if (p < 0 || p >= height)
+    return;
+  const uint32_t *row = image + (size_t)p * width;
+  const int x = cx - 4;
+#pragma unroll
+  for (int f = 0; f < 4; f++) {
+    const int gx = x + 4 * f;
     if (vec && gx >= 0 && gx + 3 < width) {
-      v[h] = __ldg(reinterpret_cast<const uint4 *>(row + gx));
+      const uint4 t = __ldg(reinterpret_cast<const uint4 *>(row + gx));
+      v[4 * f] = t.x, v[4 * f + 1] = t.y, v[4 * f + 2] = t.z, v[4 * f + 3] = t.w;
     } else {
-      uint32_t t[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
 #pragma unroll
       for (int e = 0; e < 4; e++)
         if (gx + e >= 0 && gx + e < width)
-          t[e] = __ldg(row + gx + e);
-      v[h] = make_uint4(t[0], t[1], t[2], t[3]);
+          v[4 * f + e] = __ldg(row + gx + e);
     }
   }
 }
 
 template <int K>
-__global__ void __launch_bounds__(256, 3)
-stream_stage01(const uint32_t *__restrict__ image, int height, int width, int vec,
-               const __grid_constant__ LaunchParams P, const __grid_constant__ StreamTables T,
-               uint32_t *__restrict__ scr1_bits, uint32_t *__restrict__ final_bits,
-               uint32_t *__restrict__ cand, uint32_t cand_cap, uint32_t *__restrict__ counters,
-               uint4 *__restrict__ wide_list) {
-  using G = SG<K>;
-  constexpr int W0 = 2 * K + 1;
+__device__ void seg_flush(SegSmem<K> &s, int warp, uint32_t *cand, uint32_t *counters,
+                          uint32_t cand_cap) {
+  __syncwarp();
+  const uint32_t n = s.ncand[warp];
+  uint32_t base = 0;
+  if ((threadIdx.x & 31) == 0)
+    base = n ? atomicAdd(&counters[kCtrCand], n) : 0u;
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (uint32_t i = threadIdx.x & 31; i < n; i += 32)
+    if (base + i < cand_cap)
+      cand[base + i] = s.cand[warp][i];
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0)
+    s.ncand[warp] = 0;
+  __syncwarp();
+}
+
+template <int K>
+__global__ void __launch_bounds__(kSegWarps * 32, 3)
+seg_stage01(const uint32_t *__restrict__ image, int height, int width, int vec, int nstrips,
+            int nruns, int run_rows, const __grid_constant__ LaunchParams P,
+            const __grid_constant__ StreamTables T, uint8_t *__restrict__ scr1_bytes,
+            uint8_t *__restrict__ final_bytes, uint32_t *__restrict__ cand, uint32_t cand_cap,
+            uint32_t *__restrict__ counters, uint4 *__restrict__ wide_list) {
+  using G = SegG<K>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  StreamSmem<K> &s = *reinterpret_cast<StreamSmem<K> *>(smem_raw);
-  const int tid = threadIdx.x;
-  const int lane = tid & 31, warp = tid >> 5;
-  const int x0 = blockIdx.x * G::TW;
-  const int y0 = blockIdx.y * kStreamSH;
-  const int y1 = min(height, y0 + kStreamSH);
-  const int wpr = (width + 31) >> 5;
+  SegSmem<K> &s = *reinterpret_cast<SegSmem<K> *>(smem_raw);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gw = blockIdx.x * kSegWarps + warp;
+  const int sx = gw % nstrips, ry = gw / nstrips;
+  if (ry >= nruns)
+    return;  // whole warp
+  const int X = kSegOut * sx - 8;
+  const int cx = X + 8 * lane;
+  const int ra = ry * run_rows;
+  const int rb = min(height, ra + run_rows);
+  const int bytes_per_row = ((width + 31) >> 5) * 4;
+  const bool writer = lane >= 1 && lane <= 30 && cx < bytes_per_row * 8;
   const uint32_t narrow = T.narrow_max;
-  // The all-valid window's table entries, the common case.
   const float nf_hi0 = T.nf_hi[G::N0], nf_lo0 = T.nf_lo[G::N0];
   const float c_lo0 = T.c_lo[G::N0], c_hi0 = T.c_hi[G::N0];
+  // Bits of this lane's columns that lie inside the frame.
+  const uint32_t inside8 = cx >= width ? 0u : (cx + 8 <= width ? 0xFFu : ((1u << (width - cx)) - 1u));
 
-  for (int i = tid; i <= G::N0; i += G::NT) {
-    s.nf_hi[i] = T.nf_hi[i];
-    s.nf_lo[i] = T.nf_lo[i];
-    s.c_lo[i] = T.c_lo[i];
-    s.c_hi[i] = T.c_hi[i];
-    s.root_lo[i] = P.root_lo[i];
-    s.root_hi[i] = P.root_hi[i];
-  }
-  for (int i = tid; i < G::RING * G::LWP; i += G::NT)
-    (&s.ns[0][0])[i] = 0u;
-  for (int i = tid; i < G::S0W; i += G::NT)
-    s.fix[i] = 0u;
-  if (tid == 0) {
-    s.ndefer = 0;
-    s.ncand = 0;
-  }
-
-  // This thread's stage-0 column j (output column j - E), if any.
-  int j = -1;
-  if (tid < G::TW)
-    j = tid + G::E;
-  else if (tid < G::TW + G::E)
-    j = tid - G::TW;
-  else if (tid < G::TW + 2 * G::E)
-    j = tid;
-  const bool own = j >= 0;
-  const int cj = G::A - G::E + (own ? j : 0);  // its column in the loaded rows
-
-  // Row sums of the previous two steps (index i = row P0 - 8 + i for old,
-  // P0 - 16 + i for old2).
-  uint32_t old_ns[8], old2_ns[8], old_q[8], old2_q[8];
+  if (lane == 0)
+    s.ncand[warp] = 0;
 #pragma unroll
-  for (int i = 0; i < 8; i++)
-    old_ns[i] = old2_ns[i] = old_q[i] = old2_q[i] = 0u;
-  uint32_t vns = 0, vq = 0; // running column sums
-  uint32_t sreg = 0;        // stage-0 mask, bit 0 = newest row
-  uint32_t mreg = 0;        // masked pixels, same rows
+  for (int sl = 0; sl < G::W0; sl++)
+#pragma unroll
+    for (int qd = 0; qd < 4; qd++)
+      s.ring[warp][sl][qd][lane] = make_uint4(0u, 0u, 0u, 0u);
+  __syncwarp();
 
-  const int p_first = y0 - G::R1;
-  uint4 raw[2];
-  load_step<K>(image, height, width, vec, x0, p_first, raw);
-  __syncthreads();
+  uint32_t vns[8], vq[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++)
+    vns[c] = vq[c] = 0u;
+  unsigned long long hval = 0ull;  // valid bits, 8 per row, newest row in byte 0
+  unsigned long long hs0 = 0ull;   // stage-0 bits, same layout (decision rows)
 
-  // Ring rows are indexed by row - p_first (non-negative) modulo RING.
-  for (int P0 = p_first;; P0 += G::STEP) {
-    const int newest_v0 = P0 + 7 - K;
-    const int out_hi = newest_v0 - G::E;  // highest eroded row this step
-    const int out_lo = out_hi - 7;
-    if (out_lo >= y1)
-      break;
-    const int rb = P0 - p_first;          // ring base for row P0
+  const int p0 = ra - G::R1, p1 = rb + G::R1;  // pixel rows [p0, p1)
+  uint32_t raw[16], nxt[16];
+  seg_load(image, height, width, vec, cx, p0, nxt);
+  int slot = 0;
+  for (int p = p0; p < p1; p++) {
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+      raw[i] = nxt[i];
+    if (p + 1 < p1)
+      seg_load(image, height, width, vec, cx, p + 1, nxt);
 
-    // -- pack the step's 8 pixel rows; prefetch the next step's ---------------
+    // Pack.
+    uint32_t ns[16], q[16];
     bool wide = false;
+    uint32_t valid8 = 0;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int i = tid + h * G::NT;
-      if (i < G::STEP * G::F4) {
-        const int r = i / G::F4, c4 = i - r * G::F4;
-        const uint32_t v[4] = {raw[h].x, raw[h].y, raw[h].z, raw[h].w};
-        uint32_t pk[4], qq[4];
-#pragma unroll
-        for (int e = 0; e < 4; e++) {
-          const bool valid = v[e] < 0xFFFFFFFEu;
-          wide |= valid && v[e] >= narrow;
-          const uint32_t pv = valid && v[e] < narrow ? v[e] : 0u;
-          pk[e] = valid ? ((1u << G::PS) | pv) : 0u;
-          qq[e] = pv * pv;
-        }
-        *reinterpret_cast<uint4 *>(&s.ns[(rb + r) & (G::RING - 1)][4 * c4]) =
-            make_uint4(pk[0], pk[1], pk[2], pk[3]);
-        *reinterpret_cast<uint4 *>(&s.q[r][4 * c4]) = make_uint4(qq[0], qq[1], qq[2], qq[3]);
-      }
+    for (int i = 0; i < 16; i++) {
+      const bool valid = raw[i] < 0xFFFFFFFEu;
+      wide |= valid && raw[i] >= narrow;
+      const uint32_t pv = valid && raw[i] < narrow ? raw[i] : 0u;
+      ns[i] = valid ? ((1u << G::PS) | pv) : 0u;
+      q[i] = pv * pv;
+      if (i >= 4 && i < 12)
+        valid8 |= (valid ? 1u : 0u) << (i - 4);
     }
-    load_step<K>(image, height, width, vec, x0, P0 + G::STEP, raw);
-    if (__syncthreads_or(wide)) {
-      // Rows from out_lo on are not yet written: hand the rest over.
-      if (tid == 0) {
+    if (__any_sync(0xffffffffu, wide)) {
+      // Rows from p - R1 on are not yet written: hand them over.
+      if (lane == 0) {
         const uint32_t k = atomicAdd(&counters[kCtrWide], 1u);
-        wide_list[k] = make_uint4((uint32_t)x0, (uint32_t)max(out_lo, y0), (uint32_t)y1, 0u);
+        const int xb = max(0, X + 8), xe = min(width, X + 8 + kSegOut);
+        wide_list[k] = make_uint4((uint32_t)xb, (uint32_t)xe, (uint32_t)max(ra, p - G::R1),
+                                  (uint32_t)rb);
       }
       break;
     }
+    hval = (hval << 8) | valid8;
 
-    // -- row sums over 2K + 1 columns, 8 outputs per thread ------------------
-    if (tid < G::STEP * G::NSEG) {
-      const int r = tid / G::NSEG, sg = tid - r * G::NSEG;
-      const int ring_r = (rb + r) & (G::RING - 1);
-      const int c0 = 8 * sg;
-      uint32_t a[20], b[20];
-#pragma unroll
-      for (int f = 0; f < 5; f++) {
-        const uint4 u = *reinterpret_cast<const uint4 *>(&s.ns[ring_r][c0 + 4 * f]);
-        const uint4 w = *reinterpret_cast<const uint4 *>(&s.q[r][c0 + 4 * f]);
-        a[4 * f] = u.x, a[4 * f + 1] = u.y, a[4 * f + 2] = u.z, a[4 * f + 3] = u.w;
-        b[4 * f] = w.x, b[4 * f + 1] = w.y, b[4 * f + 2] = w.z, b[4 * f + 3] = w.w;
-      }
-      constexpr int o = G::A - G::R1;
-      uint32_t hn[8], hq[8];
-      uint32_t ra = 0, rq = 0;
-#pragma unroll
-      for (int d = 0; d < W0; d++) {
-        ra += a[o + d];
-        rq += b[o + d];
-      }
-      hn[0] = ra;
-      hq[0] = rq;
-#pragma unroll
-      for (int k = 1; k < 8; k++) {
-        ra += a[o + k + 2 * K] - a[o + k - 1];
-        rq += b[o + k + 2 * K] - b[o + k - 1];
-        hn[k] = ra;
-        hq[k] = rq;
-      }
-      *reinterpret_cast<uint4 *>(&s.hns[r][c0]) = make_uint4(hn[0], hn[1], hn[2], hn[3]);
-      *reinterpret_cast<uint4 *>(&s.hns[r][c0 + 4]) = make_uint4(hn[4], hn[5], hn[6], hn[7]);
-      *reinterpret_cast<uint4 *>(&s.hq[r][c0]) = make_uint4(hq[0], hq[1], hq[2], hq[3]);
-      *reinterpret_cast<uint4 *>(&s.hq[r][c0 + 4]) = make_uint4(hq[4], hq[5], hq[6], hq[7]);
-    }
-    __syncthreads();
-
-    // -- column sums and the dispersion test, one thread per column ----------
+    // Row sums of 2K + 1 columns for the 8 columns.
+    constexpr int o = 4 - K;
+    uint32_t hn[8], hq[8];
     {
-      uint32_t cur_ns[8], cur_q[8];
+      uint32_t a = 0, b = 0;
 #pragma unroll
-      for (int r = 0; r < 8; r++) {
-        cur_ns[r] = own ? s.hns[r][j] : 0u;
-        cur_q[r] = own ? s.hq[r][j] : 0u;
+      for (int d = 0; d < G::W0; d++) {
+        a += ns[o + d];
+        b += q[o + d];
       }
+      hn[0] = a;
+      hq[0] = b;
 #pragma unroll
-      for (int r = 0; r < 8; r++) {
-        // The row sums leaving the 2K + 1 window (static indices).
-        constexpr int dummy = 0;
-        (void)dummy;
-        const int d = r - W0;
-        const uint32_t lns = d >= 0 ? cur_ns[d >= 0 ? d : 0]
-                             : d >= -8 ? old_ns[d >= -8 ? 8 + d : 0]
-                                       : old2_ns[16 + d >= 0 ? 16 + d : 0];
-        const uint32_t lq = d >= 0 ? cur_q[d >= 0 ? d : 0]
-                            : d >= -8 ? old_q[d >= -8 ? 8 + d : 0]
-                                      : old2_q[16 + d >= 0 ? 16 + d : 0];
-        vns += cur_ns[r] - lns;
-        vq += cur_q[r] - lq;
-        // Stage-0 row P0 + r - K.
-        const uint32_t me = s.ns[(rb + r - K + G::RING) & (G::RING - 1)][cj];
-        const bool masked = me == 0u;
-        bool bit = masked, defer = false;
-        if (!masked) {
-          const uint32_t n = vns >> G::PS;
-          const uint32_t S = vns & G::MASK;
-          const bool full = n == (uint32_t)G::N0;
-          const float nhi = full ? nf_hi0 : s.nf_hi[n];
-          const float clo = full ? c_lo0 : s.c_lo[n];
-          const float Sf = __uint2float_rn(S);
-          const float Qf = __uint2float_rn(vq);
-          // Surely not: nQ <= S (S + c) (bounds in sf_stream.cuh).
-          if (!(__fmul_rn(nhi, Qf) <= __fmul_rn(Sf, __fadd_rn(Sf, clo)))) {
-            const float nlo = full ? nf_lo0 : s.nf_lo[n];
-            const float chi = full ? c_hi0 : s.c_hi[n];
-            // Surely: nQ >= S (S + c) + 1.
-            if (__fmul_rn(nlo, Qf) >=
-                __fadd_rn(__fmul_rn(__fmul_rn(Sf, __fadd_rn(Sf, chi)), 1.0001f), 2.0f))
-              bit = true;
-            else {
-              const int row = P0 + r - K;
-              // Rows beyond these only feed outputs outside the segment.
-              defer = own && row >= y0 - G::E && row < y1 + G::E;
-            }
-          }
-        }
-        if (__any_sync(0xffffffffu, defer)) {
-          const unsigned dm = __ballot_sync(0xffffffffu, defer);
-          uint32_t base = 0;
-          if (lane == 0)
-            base = atomicAdd(&s.ndefer, (uint32_t)__popc(dm));
-          base = __shfl_sync(0xffffffffu, base, 0);
-          if (defer)
-            s.defer[base + __popc(dm & ((1u << lane) - 1u))] = (uint16_t)(j * 8 + r);
-        }
-        sreg = (sreg << 1) | (bit ? 1u : 0u);
-        mreg = (mreg << 1) | (masked ? 1u : 0u);
-      }
-#pragma unroll
-      for (int r = 0; r < 8; r++) {
-        old2_ns[r] = old_ns[r];
-        old_ns[r] = cur_ns[r];
-        old2_q[r] = old_q[r];
-        old_q[r] = cur_q[r];
+      for (int c = 1; c < 8; c++) {
+        a += ns[o + c + 2 * K] - ns[o + c - 1];
+        b += q[o + c + 2 * K] - q[o + c - 1];
+        hn[c] = a;
+        hq[c] = b;
       }
     }
-    __syncthreads();
 
-    // -- the queued pixels, decided exactly (rare) ----------------------------
+    // Column sums: the row sums of W0 rows ago come back from the ring.
     {
-      const uint32_t nd = s.ndefer;
-      for (uint32_t i = tid; i < nd; i += G::NT) {
-        const uint32_t e = s.defer[i];
-        const int jj = (int)(e >> 3), r = (int)(e & 7u);
-        const int c = G::A - G::E + jj;
-        uint32_t n = 0;
-        unsigned long long S = 0, Q = 0;
-        for (int dy = -K; dy <= K; dy++) {
-          const int ring_r = (rb + r - K + dy + G::RING) & (G::RING - 1);
-          for (int dx = -K; dx <= K; dx++) {
-            const uint32_t v = s.ns[ring_r][c + dx];
-            if (v) {
-              const unsigned long long p = v & G::MASK;
-              n++;
-              S += p;
-              Q += p * p;
-            }
-          }
-        }
-        if (stage0_u32(n, S, Q, P, s.root_lo, s.root_hi))
-          atomicOr(&s.fix[jj], 1u << (7 - r));
+      const uint4 l0 = s.ring[warp][slot][0][lane], l1 = s.ring[warp][slot][1][lane];
+      const uint4 l2 = s.ring[warp][slot][2][lane], l3 = s.ring[warp][slot][3][lane];
+      const uint32_t ln[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+      const uint32_t lq[8] = {l2.x, l2.y, l2.z, l2.w, l3.x, l3.y, l3.z, l3.w};
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        vns[c] += hn[c] - ln[c];
+        vq[c] += hq[c] - lq[c];
       }
+      s.ring[warp][slot][0][lane] = make_uint4(hn[0], hn[1], hn[2], hn[3]);
+      s.ring[warp][slot][1][lane] = make_uint4(hn[4], hn[5], hn[6], hn[7]);
+      s.ring[warp][slot][2][lane] = make_uint4(hq[0], hq[1], hq[2], hq[3]);
+      s.ring[warp][slot][3][lane] = make_uint4(hq[4], hq[5], hq[6], hq[7]);
+      slot = slot + 1 == G::W0 ? 0 : slot + 1;
     }
-    __syncthreads();
-    if (tid == 0)
-      s.ndefer = 0;
+    if (p < p0 + 2 * K)
+      continue;  // the column sums are not yet full windows (warp-uniform)
 
-    // -- erosion ---------------------------------------------------------------
-    if (own) {
-      sreg |= s.fix[j];
-      s.fix[j] = 0u;
-      uint32_t v = sreg;
+    // Stage-0 row p - K: eight decisions.
+    uint32_t s8 = 0;
+    const uint32_t vrow = (uint32_t)(hval >> (8 * K)) & 0xFFu;
 #pragma unroll
-      for (int d = 1; d <= G::E; d++)
-        v &= (sreg >> d) & (sreg << d);
-      s.vcol[j] = v;
-    }
-    __syncthreads();
-
-    // -- eroded mask, zeroed final mask, candidates (output columns) ---------
-    if (warp < G::NWORD) {
-      const int c = tid;  // output column c, stage-0 column c + E
-      uint32_t h = s.vcol[c + G::E];
-#pragma unroll
-      for (int d = 1; d <= G::E; d++)
-        h &= s.vcol[c + G::E - d] & s.vcol[c + G::E + d];
-      const uint32_t scr1 = h | mreg;
-      const int gx = x0 + c;
-      const bool inside = gx < width;
-      const int widx = (x0 >> 5) + warp;
-#pragma unroll
-      for (int k = G::E; k < G::E + 8; k++) {
-        const int row = newest_v0 - k;
-        if (row < y0 || row >= y1)
-          continue;
-        const bool b = inside && ((scr1 >> k) & 1u);
-        const uint32_t word = __ballot_sync(0xffffffffu, b);
-        if (lane == 0 && widx < wpr) {
-          scr1_bits[(size_t)row * wpr + widx] = word;
-          final_bits[(size_t)row * wpr + widx] = 0u;
-        }
-        if (word == 0u)
-          continue;  // warp-uniform
-        const uint32_t pk = s.ns[(row - p_first) & (G::RING - 1)][c + G::A];
-        const bool cnd = b && !((mreg >> k) & 1u) && (uint64_t)(pk & G::MASK) >= P.p_min;
-        const unsigned cm = __ballot_sync(0xffffffffu, cnd);
-        if (cm) {
-          uint32_t base = 0;
-          if (lane == 0)
-            base = atomicAdd(&s.ncand, (uint32_t)__popc(cm));
-          base = __shfl_sync(0xffffffffu, base, 0);
-          if (cnd)
-            s.cand[base + __popc(cm & ((1u << lane) - 1u))] =
-                (uint32_t)row * (uint32_t)width + (uint32_t)gx;
+    for (int c = 0; c < 8; c++) {
+      bool bit = !((vrow >> c) & 1u);  // masked pixels are set
+      if (!bit) {
+        const uint32_t n = vns[c] >> G::PS, S = vns[c] & G::MASK;
+        const bool full = n == (uint32_t)G::N0;
+        const float nhi = full ? nf_hi0 : T.nf_hi[n];
+        const float clo = full ? c_lo0 : T.c_lo[n];
+        const float Sf = __uint2float_rn(S), Qf = __uint2float_rn(vq[c]);
+        if (!(__fmul_rn(nhi, Qf) <= __fmul_rn(Sf, __fadd_rn(Sf, clo)))) {
+          const float nlo = full ? nf_lo0 : T.nf_lo[n];
+          const float chi = full ? c_hi0 : T.c_hi[n];
+          if (__fmul_rn(nlo, Qf) >=
+              __fadd_rn(__fmul_rn(__fmul_rn(Sf, __fadd_rn(Sf, chi)), 1.0001f), 2.0f))
+            bit = true;
+          else  // near the threshold: decide exactly (rare)
+            bit = stage0_u32(n, (unsigned long long)S, (unsigned long long)vq[c], P,
+                             P.root_lo, P.root_hi);
         }
       }
+      s8 |= (bit ? 1u : 0u) << c;
     }
-    __syncthreads();
-    if (s.ncand > G::CCAP - G::TW * 8)
-      flush_candidates<K>(s, cand, counters, cand_cap);
+    hs0 = (hs0 << 8) | s8;
+    if (p < p0 + 2 * K + 2 * G::E)
+      continue;  // the erosion needs 2E more decision rows (warp-uniform)
+
+    // Erosion of row p - R1: vertical AND of 2E + 1 chunks, then across
+    // columns with the neighbours' chunks.
+    uint32_t v8 = 0xFFu;
+#pragma unroll
+    for (int b = 0; b <= 2 * G::E; b++)
+      v8 &= (uint32_t)(hs0 >> (8 * b)) & 0xFFu;
+    const uint32_t left = __shfl_up_sync(0xffffffffu, v8, 1);
+    const uint32_t right = __shfl_down_sync(0xffffffffu, v8, 1);
+    const uint32_t all = (right << 16) | (v8 << 8) | left;
+    uint32_t h8 = 0xFFu;
+#pragma unroll
+    for (int d = -G::E; d <= G::E; d++)
+      h8 &= (all >> (8 + d)) & 0xFFu;
+    const uint32_t masked8 = ~(uint32_t)(hval >> (8 * G::R1)) & 0xFFu;
+    const uint32_t scr1 = (h8 | masked8) & inside8;
+    const int re = p - G::R1;
+    const bool out_row = re >= ra && re < rb;
+    if (out_row && writer) {
+      scr1_bytes[(size_t)re * bytes_per_row + (cx >> 3)] = (uint8_t)scr1;
+      final_bytes[(size_t)re * bytes_per_row + (cx >> 3)] = 0;
+    }
+    // Candidates: eroded, not masked, above the global threshold.
+    uint32_t c8 = (out_row && writer) ? (scr1 & ~masked8) : 0u;
+    if (__any_sync(0xffffffffu, c8 != 0u)) {
+      if (c8) {
+        const uint32_t *row = image + (size_t)re * width;
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+          if (((c8 >> c) & 1u) && (uint64_t)__ldg(row + cx + c) < P.p_min)
+            c8 &= ~(1u << c);
+      }
+      const uint32_t cnt = __popc(c8);
+      uint32_t incl = cnt;
+#pragma unroll
+      for (int o2 = 1; o2 < 32; o2 <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o2);
+        if (lane >= o2)
+          incl += t;
+      }
+      const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+      if (s.ncand[warp] + total > (uint32_t)kSegCand)
+        seg_flush<K>(s, warp, cand, counters, cand_cap);
+      const uint32_t base = s.ncand[warp] + incl - cnt;
+      uint32_t k = 0;
+      for (int c = 0; c < 8; c++)
+        if ((c8 >> c) & 1u)
+          s.cand[warp][base + k++] = (uint32_t)re * (uint32_t)width + (uint32_t)(cx + c);
+      __syncwarp();
+      if (lane == 0)
+        s.ncand[warp] += total;
+      __syncwarp();
+    }
   }
-  __syncthreads();
-  flush_candidates<K>(s, cand, counters, cand_cap);
+  seg_flush<K>(s, warp, cand, counters, cand_cap);
 }
 
 // ---------------------------------------------------------------------------
-// Segments holding a pixel too large for the packed sums: 32 x 32 tiles of
-// the eroded mask with exact 64-bit sums, from the row the streaming block
-// stopped at.
+// Runs holding a pixel too large for the exact 32-bit sums: 32 x 32 tiles of
+// the eroded mask with 64-bit sums, for the columns [xb, xe) and rows
+// [yb, ye) a warp handed over.
 // ---------------------------------------------------------------------------
 template <int K>
 __global__ void __launch_bounds__(256)
-stream_wide(const uint32_t *__restrict__ image, int height, int width,
-            const __grid_constant__ LaunchParams P, uint32_t *__restrict__ scr1_bits,
-            uint32_t *__restrict__ final_bits, uint32_t *__restrict__ cand,
+stream_wide(const uint32_t *__restrict__ image, int height, int width, int run_rows,
+            const __grid_constant__ LaunchParams P, uint8_t *__restrict__ scr1_bytes,
+            uint8_t *__restrict__ final_bytes, uint32_t *__restrict__ cand,
             uint32_t cand_cap, uint32_t *__restrict__ counters,
             const uint4 *__restrict__ wide_list) {
   constexpr int E = K - 1, R1 = 2 * K - 1;
@@ -466,25 +340,23 @@ stream_wide(const uint32_t *__restrict__ image, int height, int width,
   __shared__ uint8_t scr0[S0][S0];
   __shared__ uint32_t rlo[kMaxN0 + 1], rhi[kMaxN0 + 1];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wpr = (width + 31) >> 5;
+  const int bytes_per_row = ((width + 31) >> 5) * 4;
   for (int i = tid; i <= kMaxN0; i += blockDim.x) {
     rlo[i] = P.root_lo[i];
     rhi[i] = P.root_hi[i];
   }
   const uint32_t nwide = counters[kCtrWide];
-  // Work items: (entry, tile column, tile row), tiles of 32 rows from the
-  // entry's first row.
-  constexpr int TPS = kStreamTW / TS; // tile columns per strip
-  constexpr int TPR = (kStreamSH + TS - 1) / TS + 1;
+  constexpr int TPS = (kSegOut + TS - 1) / TS;  // tile columns per entry
+  const int TPR = (run_rows + TS - 1) / TS;      // tile rows per entry
   for (uint32_t item = blockIdx.x; item < nwide * TPS * TPR; item += gridDim.x) {
     const uint4 w = wide_list[item / (TPS * TPR)];
     const int rem = (int)(item % (TPS * TPR));
     const int tcol = rem % TPS, trow = rem / TPS;
-    const int tx0 = (int)w.x + tcol * TS;
-    const int ty0 = (int)w.y + trow * TS;
-    if (ty0 >= (int)w.z || tx0 >= width)
-      continue;
-    const int ty1 = min((int)w.z, ty0 + TS);
+    const int xb = (int)w.x, xe = (int)w.y, yb = (int)w.z, ye = (int)w.w;
+    const int tx0 = xb + tcol * TS, ty0 = yb + trow * TS;
+    if (ty0 >= ye || tx0 >= xe)
+      continue;  // block-uniform
+    const int ty1 = min(ye, ty0 + TS);
     __syncthreads();
     for (int i = tid; i < IW * IW; i += blockDim.x) {
       const int r = i / IW, c = i - r * IW;
@@ -523,10 +395,8 @@ stream_wide(const uint32_t *__restrict__ image, int height, int width,
       scr0[r][c] = (sig || pix[r + K][c + K] >= 0xFFFFFFFEu) ? 1 : 0;
     }
     __syncthreads();
-    // Eroded mask of the 32 x 32 tile: warp w handles rows w, w + 8, ...
     for (int r = warp; r < TS; r += blockDim.x >> 5) {
-      const int gy = ty0 + r;
-      const int c = lane;
+      const int gy = ty0 + r, c = lane, gx = tx0 + c;
       const uint32_t v = pix[r + R1][c + R1];
       bool m = true;
       if (v < 0xFFFFFFFEu) {
@@ -538,12 +408,14 @@ stream_wide(const uint32_t *__restrict__ image, int height, int width,
               break;
             }
       }
-      const bool inside = gy < ty1 && tx0 + c < width;
-      const bool b = inside && m;
+      const bool b = gy < ty1 && gx < min(xe, width) && m;
       const uint32_t word = __ballot_sync(0xffffffffu, b);
-      if (lane == 0 && gy < ty1 && (tx0 >> 5) < wpr) {
-        scr1_bits[(size_t)gy * wpr + (tx0 >> 5)] = word;
-        final_bits[(size_t)gy * wpr + (tx0 >> 5)] = 0u;
+      if (gy < ty1 && lane < 4) {
+        const int bx = tx0 + 8 * lane;
+        if (bx < xe && (bx >> 3) < bytes_per_row) {
+          scr1_bytes[(size_t)gy * bytes_per_row + (bx >> 3)] = (uint8_t)(word >> (8 * lane));
+          final_bytes[(size_t)gy * bytes_per_row + (bx >> 3)] = 0;
+        }
       }
       const bool cnd = b && v < 0xFFFFFFFEu && (uint64_t)v >= P.p_min;
       const unsigned cm = __ballot_sync(0xffffffffu, cnd);
@@ -554,62 +426,69 @@ stream_wide(const uint32_t *__restrict__ image, int height, int width,
         base = __shfl_sync(0xffffffffu, base, 0);
         const uint32_t g = base + __popc(cm & ((1u << lane) - 1u));
         if (cnd && g < cand_cap)
-          cand[g] = (uint32_t)gy * (uint32_t)width + (uint32_t)(tx0 + c);
+          cand[g] = (uint32_t)gy * (uint32_t)width + (uint32_t)gx;
       }
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// Stage 2 at the candidates.
+// Stage 2 at the candidates, four lanes to a candidate: each lane sums a
+// quarter of the (2K + 5) rows of the clipped window, two shuffles add them.
 // ---------------------------------------------------------------------------
 template <int K>
 __global__ void __launch_bounds__(256)
-stream_stage2(const uint32_t *__restrict__ image, int height, int width,
-              const __grid_constant__ LaunchParams P, const uint32_t *__restrict__ scr1_bits,
-              uint32_t *__restrict__ final_bits, const uint32_t *__restrict__ cand,
-              uint32_t cand_cap, uint32_t *__restrict__ counters,
-              sf_signal_pixel *__restrict__ staging, uint32_t capacity) {
-  constexpr int K2 = K + 2;
+seg_stage2(const uint32_t *__restrict__ image, int height, int width,
+           const __grid_constant__ LaunchParams P, const uint32_t *__restrict__ scr1_words,
+           uint32_t *__restrict__ final_words, const uint32_t *__restrict__ cand,
+           uint32_t cand_cap, uint32_t *__restrict__ counters,
+           sf_signal_pixel *__restrict__ staging, uint32_t capacity) {
+  constexpr int K2 = K + 2, WW = 2 * K2 + 1;
   const int wpr = (width + 31) >> 5;
   const uint32_t nc = min(counters[kCtrCand], cand_cap);
-  const int lane = threadIdx.x & 31;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < nc; base += gridDim.x * blockDim.x) {
-    const uint32_t i = base + threadIdx.x;
-    bool sig = false;
-    sf_signal_pixel rec;
-    uint32_t idx = 0;
-    if (i < nc) {
+  const int lane = threadIdx.x & 31, sub = lane & 3;
+  const uint32_t per_pass = (gridDim.x * blockDim.x) >> 2;
+  for (uint32_t base = (blockIdx.x * blockDim.x) >> 2; base < nc + 0; base += per_pass) {
+    const uint32_t i = base + (threadIdx.x >> 2);
+    const bool live = i < nc;
+    uint32_t idx = 0, p = 0, n = 0;
+    unsigned long long S = 0;
+    if (live) {
       idx = cand[i];
       const int y = (int)(idx / (uint32_t)width), x = (int)(idx % (uint32_t)width);
-      const uint32_t p = __ldg(image + idx);
-      uint32_t n = 0;
-      unsigned long long S = 0;
-      const int ylo = max(0, y - K2), yhi = min(height - 1, y + K2);
+      p = __ldg(image + idx);
       const int xlo = max(0, x - K2), xhi = min(width - 1, x + K2);
-      for (int yy = ylo; yy <= yhi; yy++) {
+      const int w0 = xlo >> 5;
+      for (int dy = -K2 + sub; dy <= K2; dy += 4) {
+        const int yy = y + dy;
+        if (yy < 0 || yy >= height)
+          continue;
         const uint32_t *row = image + (size_t)yy * width;
-        const uint32_t *brow = scr1_bits + (size_t)yy * wpr;
-        // The eroded mask over [xlo, xhi] from at most two words.
-        const int w0 = xlo >> 5;
+        const uint32_t *brow = scr1_words + (size_t)yy * wpr;
         const unsigned long long both =
             (unsigned long long)__ldg(brow + w0) |
             ((w0 + 1 < wpr) ? ((unsigned long long)__ldg(brow + w0 + 1) << 32) : 0ull);
-        const unsigned long long bg_bits = ~(both >> (xlo - (w0 << 5)));
-        // Row loads issued together, then summed.
-        uint32_t v[2 * K2 + 1];
+        const unsigned long long bgb = ~(both >> (xlo - (w0 << 5)));
+        uint32_t v[WW];
 #pragma unroll
-        for (int d = 0; d <= 2 * K2; d++)
+        for (int d = 0; d < WW; d++)
           v[d] = (xlo + d <= xhi) ? __ldg(row + xlo + d) : 0u;
 #pragma unroll
-        for (int d = 0; d <= 2 * K2; d++) {
-          // Not in the eroded mask (masked pixels are in it), so valid.
-          if (xlo + d <= xhi && ((bg_bits >> d) & 1ull)) {
+        for (int d = 0; d < WW; d++)
+          if (xlo + d <= xhi && ((bgb >> d) & 1ull)) {
+            // Not in the eroded mask, so valid (masked pixels are in it).
             n++;
             S += v[d];
           }
-        }
       }
+    }
+    n += __shfl_xor_sync(0xffffffffu, n, 1);
+    S += __shfl_xor_sync(0xffffffffu, S, 1);
+    n += __shfl_xor_sync(0xffffffffu, n, 2);
+    S += __shfl_xor_sync(0xffffffffu, S, 2);
+    bool sig = false;
+    sf_signal_pixel rec;
+    if (live && sub == 0) {
       float bg;
       sig = stage2_u32(p, n, S, P, &bg);
       rec.index = idx;
@@ -628,30 +507,96 @@ stream_stage2(const uint32_t *__restrict__ image, int height, int width,
         const uint32_t slot = b + __popc(m & ((1u << lane) - 1u));
         if (slot < capacity)
           staging[slot] = rec;
-        atomicOr(&final_bits[(size_t)(idx / (uint32_t)width) * wpr + (idx % (uint32_t)width) / 32],
-                 1u << ((idx % (uint32_t)width) & 31u));
+        const uint32_t y = idx / (uint32_t)width, x = idx % (uint32_t)width;
+        atomicOr(&final_words[(size_t)y * wpr + (x >> 5)], 1u << (x & 31u));
       }
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// Ordering: popcounts of the final mask's words, their exclusive scan, then
-// each staged record to its ascending position.
+// Ordering. One pass of a decoupled look-back scan over the popcounts of the
+// final mask's words (tiles claimed in order with an atomic, each waiting only
+// on tiles claimed before it, every wait bounded), then each staged record to
+// its ascending position.
 // ---------------------------------------------------------------------------
-__global__ void order_popc(const uint32_t *__restrict__ bits, const uint32_t *__restrict__ nwords,
-                           uint32_t *__restrict__ out) {
-  const uint32_t n = *nwords;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    out[i] = __popc(bits[i]);
+constexpr int kScanTile = kScanTileWords;
+constexpr unsigned long long kAggFlag = 1ull << 32, kIncFlag = 2ull << 32;
+constexpr int kLookbackSpins = 1 << 22;
+
+__global__ void __launch_bounds__(512)
+order_lookback(const uint32_t *__restrict__ bits, uint32_t nwords,
+               uint32_t *__restrict__ prefix, uint32_t *__restrict__ counters,
+               unsigned long long *__restrict__ status) {
+  __shared__ uint32_t s_tile, s_prefix;
+  if (threadIdx.x == 0)
+    s_tile = atomicAdd(&counters[kCtrTiles], 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t w0 = tile * kScanTile;
+  constexpr int PER = kScanTile / 512;
+  uint32_t c[PER], local = 0;
+#pragma unroll
+  for (int k = 0; k < PER; k++) {
+    const uint32_t w = w0 + threadIdx.x * PER + k;
+    c[k] = w < nwords ? __popc(bits[w]) : 0u;
+    local += c[k];
+  }
+  uint32_t total;
+  const uint32_t excl = block_exclusive_scan(local, &total);
+  if (threadIdx.x == 0) {
+    volatile unsigned long long *vs = status;
+    if (tile == 0) {
+      atomicExch(&status[0], kIncFlag | total);
+      s_prefix = 0;
+    } else {
+      atomicExch(&status[tile], kAggFlag | total);
+      uint32_t run = 0;
+      int t = (int)tile - 1;
+      while (t >= 0) {
+        unsigned long long v = vs[t];
+        int spins = 0;
+        while (!(v >> 32) && spins < kLookbackSpins) {
+          __nanosleep(32);
+          v = vs[t];
+          spins++;
+        }
+        if (!(v >> 32)) {
+          atomicOr(&counters[kCtrError], 1u);  // a predecessor never published
+          break;
+        }
+        run += (uint32_t)v;
+        if ((v >> 32) == 2ull)
+          break;
+        t--;
+      }
+      __threadfence();
+      atomicExch(&status[tile], kIncFlag | (run + total));
+      s_prefix = run;
+    }
+  }
+  __syncthreads();
+  uint32_t run = s_prefix + excl;
+#pragma unroll
+  for (int k = 0; k < PER; k++) {
+    const uint32_t w = w0 + threadIdx.x * PER + k;
+    if (w < nwords)
+      prefix[w] = run;
+    run += c[k];
+  }
 }
 
 __global__ void order_scatter(int width, const uint32_t *__restrict__ bits,
                               const uint32_t *__restrict__ prefix,
-                              const uint32_t *__restrict__ counters,
+                              const uint32_t *__restrict__ counters, uint32_t cand_cap,
                               const sf_signal_pixel *__restrict__ staging, uint32_t capacity,
-                              sf_signal_pixel *__restrict__ out) {
-  const uint32_t n = min(counters[kCtrTotal], capacity);
+                              sf_signal_pixel *__restrict__ out, uint32_t *__restrict__ count_out) {
+  const uint32_t total = counters[kCtrTotal];
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    // The signal found; all ones if a list overflowed or the scan failed, as
+    // for a count above capacity (the list is then incomplete).
+    *count_out = (counters[kCtrCand] > cand_cap || counters[kCtrError]) ? 0xFFFFFFFFu : total;
+  const uint32_t n = min(total, capacity);
   const int wpr = (width + 31) >> 5;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const sf_signal_pixel rec = staging[i];
@@ -661,16 +606,6 @@ __global__ void order_scatter(int width, const uint32_t *__restrict__ bits,
     if (dst < capacity)
       out[dst] = rec;
   }
-}
-
-__global__ void set_word_count(uint32_t *counters, uint32_t nwords) {
-  counters[kCtrWords] = nwords;
-}
-
-// The caller's count: the signal found, or all ones if the candidate list
-// overflowed (the list is then incomplete, as for a count above capacity).
-__global__ void finish_count(const uint32_t *counters, uint32_t cand_cap, uint32_t *out) {
-  *out = counters[kCtrCand] > cand_cap ? 0xFFFFFFFFu : counters[kCtrTotal];
 }
 
 // ---------------------------------------------------------------------------
@@ -718,11 +653,11 @@ void make_stream_tables(const LaunchParams &P, StreamTables *T) {
 template <int K>
 static cudaError_t launch_stream_k(const uint32_t *image, int h, int w, const LaunchParams &P,
                                    const StreamBuffers &b, cudaStream_t stream) {
-  using S = StreamSmem<K>;
+  using S = SegSmem<K>;
   static bool configured = false;
   cudaError_t e;
   if (!configured) {
-    e = cudaFuncSetAttribute(stream_stage01<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(seg_stage01<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(S));
     if (e != cudaSuccess)
       return e;
@@ -731,34 +666,33 @@ static cudaError_t launch_stream_k(const uint32_t *image, int h, int w, const La
   StreamTables T;
   make_stream_tables(P, &T);
   const int vec = (w % 4 == 0 && reinterpret_cast<uintptr_t>(image) % 16 == 0) ? 1 : 0;
-  const dim3 g1((w + kStreamTW - 1) / kStreamTW, (h + kStreamSH - 1) / kStreamSH);
-  stream_stage01<K><<<g1, 256, sizeof(S), stream>>>(image, h, w, vec, P, T, b.scr1, b.bits,
-                                                     b.cand, b.cand_cap, b.counters, b.wide);
-  stream_wide<K><<<2 * 152, 256, 0, stream>>>(image, h, w, P, b.scr1, b.bits, b.cand,
+  const SegGeometry g = seg_geometry(h, w);
+  const int warps = g.nstrips * g.nruns;
+  uint8_t *scr1 = reinterpret_cast<uint8_t *>(b.scr1);
+  uint8_t *fin = reinterpret_cast<uint8_t *>(b.bits);
+  seg_stage01<K><<<(warps + kSegWarps - 1) / kSegWarps, kSegWarps * 32, sizeof(S), stream>>>(
+      image, h, w, vec, g.nstrips, g.nruns, g.run_rows, P, T, scr1, fin, b.cand, b.cand_cap,
+      b.counters, b.wide);
+  stream_wide<K><<<2 * 152, 256, 0, stream>>>(image, h, w, g.run_rows, P, scr1, fin, b.cand,
                                                b.cand_cap, b.counters, b.wide);
-  stream_stage2<K><<<4 * 152, 256, 0, stream>>>(image, h, w, P, b.scr1, b.bits, b.cand,
-                                                 b.cand_cap, b.counters, b.staging,
-                                                 b.capacity);
+  seg_stage2<K><<<8 * 152, 256, 0, stream>>>(image, h, w, P, b.scr1, b.bits, b.cand,
+                                              b.cand_cap, b.counters, b.staging, b.capacity);
   const uint32_t nwords = (uint32_t)(((size_t)w + 31) / 32 * h);
-  order_popc<<<2 * 152, 512, 0, stream>>>(b.bits, b.counters + kCtrWords, b.prefix);
-  e = exclusive_scan(b.prefix, b.prefix, b.counters + kCtrWords, nullptr, b.block_sums,
-                     nullptr, stream);
-  if (e != cudaSuccess)
-    return e;
-  order_scatter<<<2 * 152, 256, 0, stream>>>(w, b.bits, b.prefix, b.counters, b.staging,
-                                             b.capacity, b.out);
-  finish_count<<<1, 1, 0, stream>>>(b.counters, b.cand_cap, b.count_out);
-  (void)nwords;
+  order_lookback<<<(unsigned)scan_tiles(h, w), 512, 0, stream>>>(b.bits, nwords, b.prefix,
+                                                                  b.counters, b.status);
+  order_scatter<<<2 * 152, 256, 0, stream>>>(w, b.bits, b.prefix, b.counters, b.cand_cap,
+                                             b.staging, b.capacity, b.out, b.count_out);
   return cudaGetLastError();
 }
 
 cudaError_t launch_stream(const uint32_t *image, int h, int w, const LaunchParams &P,
                           const StreamBuffers &b, cudaStream_t stream) {
-  cudaError_t e = cudaMemsetAsync(b.counters, 0, kCtrCount * sizeof(uint32_t), stream);
+  // The counters and the scan status words are contiguous.
+  cudaError_t e = cudaMemsetAsync(
+      b.counters, 0, kCtrCount * sizeof(uint32_t) + scan_tiles(h, w) * sizeof(unsigned long long),
+      stream);
   if (e != cudaSuccess)
     return e;
-  const uint32_t nwords = (uint32_t)(((size_t)w + 31) / 32 * h);
-  set_word_count<<<1, 1, 0, stream>>>(b.counters, nwords);
   switch (P.half) {
   case 2:
     return launch_stream_k<2>(image, h, w, P, b, stream);

@@ -24,17 +24,36 @@
 
 namespace sf {
 
-constexpr int kStreamTW = 224;  // output columns per strip
-constexpr int kStreamSH = 96;   // output rows per strip segment
-
-// Counter words at the start of the stream workspace.
+// Counter words at the start of the stream workspace, followed by the
+// look-back scan's per-tile status words.
 enum {
   kCtrTotal = 0,  // signal pixels found
   kCtrCand,       // candidates found
-  kCtrWide,       // strip segments handed to the 64-bit path
-  kCtrWords,      // bitmask words of the frame
+  kCtrWide,       // runs handed to the 64-bit path
+  kCtrTiles,      // scan tiles claimed
+  kCtrError,      // a bounded wait gave up
   kCtrCount = 8
 };
+
+constexpr int kScanTileWords = 4096;
+
+// Strips of 240 output columns (one warp each) by runs of rows: as many runs
+// as fill the GPU once (3 blocks of 4 warps on each of 152 SMs), each at least
+// 16 rows.
+struct SegGeometry {
+  int nstrips, nruns, run_rows;
+};
+inline SegGeometry seg_geometry(int h, int w) {
+  SegGeometry g;
+  g.nstrips = (w + 239) / 240;
+  const int target = 1800;
+  int nruns = (target + g.nstrips - 1) / g.nstrips;
+  g.run_rows = (h + nruns - 1) / nruns;
+  if (g.run_rows < 16)
+    g.run_rows = 16;
+  g.nruns = (h + g.run_rows - 1) / g.run_rows;
+  return g;
+}
 
 struct StreamTables {
   uint32_t narrow_max;  // valid pixels at or above this take the 64-bit path
@@ -48,8 +67,8 @@ struct StreamBuffers {
   uint32_t *cand;         // candidate pixel indices
   uint32_t cand_cap;
   uint32_t *counters;     // kCtrCount words
-  uint4 *wide;            // handed-over strip segments
-  uint32_t *block_sums;   // scan scratch
+  uint4 *wide;            // handed-over runs
+  unsigned long long *status;  // look-back status, right after the counters
   sf_signal_pixel *staging;
   sf_signal_pixel *out;   // ascending list (output)
   uint32_t capacity;
@@ -57,7 +76,13 @@ struct StreamBuffers {
 };
 
 inline int stream_units(int h, int w) {
-  return ((w + kStreamTW - 1) / kStreamTW) * ((h + kStreamSH - 1) / kStreamSH);
+  const SegGeometry g = seg_geometry(h, w);
+  return g.nstrips * g.nruns;
+}
+
+inline size_t scan_tiles(int h, int w) {
+  const size_t words = ((size_t)w + 31) / 32 * h;
+  return (words + kScanTileWords - 1) / kScanTileWords;
 }
 
 void make_stream_tables(const LaunchParams &P, StreamTables *T);
