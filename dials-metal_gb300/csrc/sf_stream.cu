@@ -186,7 +186,9 @@ seg_stage01(const uint32_t *__restrict__ image, int height, int width, int vec, 
       // Rows from p - R1 on are not yet written: hand them over.
       if (lane == 0) {
         const uint32_t k = atomicAdd(&counters[kCtrWide], 1u);
-        const int xb = max(0, X + 8), xe = min(width, X + 8 + kSegOut);
+        // Up to the end of the row's last mask word: the columns past the
+        // frame are written as zeros there, as the lanes here would have.
+        const int xb = max(0, X + 8), xe = min(bytes_per_row * 8, X + 8 + kSegOut);
         wide_list[k] = make_uint4((uint32_t)xb, (uint32_t)xe, (uint32_t)max(ra, p - G::R1),
                                   (uint32_t)rb);
       }
