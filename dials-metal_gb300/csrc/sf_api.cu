@@ -109,8 +109,7 @@ static WorkspaceLayout layout(size_t h, size_t w, size_t capacity) {
   L.scr1 = take(words * sizeof(uint32_t));
   L.prefix = take(words * sizeof(uint32_t));
   L.wide = take((size_t)stream_units((int)h, (int)w) * 16);
-  L.counters = take(kCtrCount * sizeof(uint32_t) +
-                    scan_tiles((int)h, (int)w) * sizeof(unsigned long long));
+  L.counters = take(kCtrCount * sizeof(uint32_t));
   L.block_sums = take(kScanBlocks * sizeof(uint32_t));
   L.tile_base = take((size_t)tiles_x((int)w) * tiles_y((int)h) * sizeof(uint32_t));
   L.row_total = take((size_t)tiles_y((int)h) * sizeof(uint32_t));
@@ -150,8 +149,7 @@ static int threshold_device(const T *d_image, size_t h, size_t w,
     b.cand_cap = (uint32_t)L.cand_cap;
     b.counters = reinterpret_cast<uint32_t *>(ws + L.counters);
     b.wide = reinterpret_cast<uint4 *>(ws + L.wide);
-    b.status = reinterpret_cast<unsigned long long *>(ws + L.counters +
-                                                      kCtrCount * sizeof(uint32_t));
+    b.block_sums = reinterpret_cast<uint32_t *>(ws + L.block_sums);
     b.staging = reinterpret_cast<sf_signal_pixel *>(ws + L.staging);
     b.out = d_out;
     b.capacity = (uint32_t)capacity;

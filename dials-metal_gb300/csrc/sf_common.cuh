@@ -118,6 +118,16 @@ __device__ __forceinline__ bool stage0_u32(uint32_t n, unsigned long long S,
 // midpoint, far more than the 2^-53 a double rounding moves it. So the
 // background is an IEEE float division, exact in its inputs for S < 2^24.
 // ---------------------------------------------------------------------------
+// The reference's double sequence (dext.cc:204-206), out of line: callers
+// reach it rarely and should not issue it otherwise.
+static __device__ __noinline__ bool stage2_double(uint32_t p, uint32_t n, unsigned long long S,
+                                                  const LaunchParams &P, float *bg) {
+  const double mean = __ddiv_rn(__ull2double_rn(S), (double)n);
+  *bg = __double2float_rn(mean);
+  const double t = __dadd_rn(mean, __dmul_rn(P.sigma_s, __dsqrt_rn(__dmul_rn(P.gain, mean))));
+  return (double)p >= t;
+}
+
 __device__ __forceinline__ bool stage2_u32(uint32_t p, uint32_t n,
                                            unsigned long long S,
                                            const LaunchParams &P, float *bg) {
@@ -141,10 +151,7 @@ __device__ __forceinline__ bool stage2_u32(uint32_t p, uint32_t n,
     if (E < -8192)
       return false;
   }
-  const double mean = __ddiv_rn(__ull2double_rn(S), (double)n);
-  *bg = __double2float_rn(mean);
-  const double t = __dadd_rn(mean, __dmul_rn(P.sigma_s, __dsqrt_rn(__dmul_rn(P.gain, mean))));
-  return (double)p >= t;
+  return stage2_double(p, n, S, P, bg);
 }
 
 // ---------------------------------------------------------------------------

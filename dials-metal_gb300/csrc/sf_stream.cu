@@ -19,9 +19,13 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cooperative_groups.h>
+
 #include "sf_common.cuh"
 #include "sf_scan.cuh"
 #include "sf_stream.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace sf {
 
@@ -114,6 +118,19 @@ __device__ void seg_flush(SegSmem<K> &s, int warp, uint32_t *cand, uint32_t *cou
   __syncwarp();
 }
 
+// The cases the "surely not" bound leaves: the "surely" bound, then, near the
+// threshold, the exact decision. Kept out of line so the common path does not
+// carry (or issue) it.
+template <int K>
+__device__ __noinline__ bool seg_rare_decision(uint32_t n, uint32_t S, uint32_t Q, float Sf,
+                                               float Qf, const LaunchParams &P,
+                                               const StreamTables &T) {
+  if (__fmul_rn(T.nf_lo[n], Qf) >=
+      __fadd_rn(__fmul_rn(__fmul_rn(Sf, __fadd_rn(Sf, T.c_hi[n])), 1.0001f), 2.0f))
+    return true;
+  return stage0_u32(n, (unsigned long long)S, (unsigned long long)Q, P, P.root_lo, P.root_hi);
+}
+
 template <int K>
 __global__ void __launch_bounds__(kSegWarps * 32, 3)
 seg_stage01(const uint32_t *__restrict__ image, int height, int width, int vec, int nstrips,
@@ -136,8 +153,7 @@ seg_stage01(const uint32_t *__restrict__ image, int height, int width, int vec, 
   const int bytes_per_row = ((width + 31) >> 5) * 4;
   const bool writer = lane >= 1 && lane <= 30 && cx < bytes_per_row * 8;
   const uint32_t narrow = T.narrow_max;
-  const float nf_hi0 = T.nf_hi[G::N0], nf_lo0 = T.nf_lo[G::N0];
-  const float c_lo0 = T.c_lo[G::N0], c_hi0 = T.c_hi[G::N0];
+  const float nf_hi0 = T.nf_hi[G::N0], c_lo0 = T.c_lo[G::N0];
   // Bits of this lane's columns that lie inside the frame.
   const uint32_t inside8 = cx >= width ? 0u : (cx + 8 <= width ? 0xFFu : ((1u << (width - cx)) - 1u));
 
@@ -249,16 +265,8 @@ seg_stage01(const uint32_t *__restrict__ image, int height, int width, int vec, 
         const float nhi = full ? nf_hi0 : T.nf_hi[n];
         const float clo = full ? c_lo0 : T.c_lo[n];
         const float Sf = __uint2float_rn(S), Qf = __uint2float_rn(vq[c]);
-        if (!(__fmul_rn(nhi, Qf) <= __fmul_rn(Sf, __fadd_rn(Sf, clo)))) {
-          const float nlo = full ? nf_lo0 : T.nf_lo[n];
-          const float chi = full ? c_hi0 : T.c_hi[n];
-          if (__fmul_rn(nlo, Qf) >=
-              __fadd_rn(__fmul_rn(__fmul_rn(Sf, __fadd_rn(Sf, chi)), 1.0001f), 2.0f))
-            bit = true;
-          else  // near the threshold: decide exactly (rare)
-            bit = stage0_u32(n, (unsigned long long)S, (unsigned long long)vq[c], P,
-                             P.root_lo, P.root_hi);
-        }
+        if (!(__fmul_rn(nhi, Qf) <= __fmul_rn(Sf, __fadd_rn(Sf, clo))))
+          bit = seg_rare_decision<K>(n, S, vq[c], Sf, Qf, P, T);
       }
       s8 |= (bit ? 1u : 0u) << c;
     }
@@ -517,88 +525,59 @@ seg_stage2(const uint32_t *__restrict__ image, int height, int width,
 }
 
 // ---------------------------------------------------------------------------
-// Ordering. One pass of a decoupled look-back scan over the popcounts of the
-// final mask's words (tiles claimed in order with an atomic, each waiting only
-// on tiles claimed before it, every wait bounded), then each staged record to
-// its ascending position.
+// Ordering, one cooperative kernel with one block per SM: each block sums
+// the popcounts of its share of the final mask's words; after a grid-wide
+// barrier each block adds its predecessors' sums and writes the exclusive
+// prefix of every word it owns; after a second barrier every staged record is
+// scattered to its ascending position.
 // ---------------------------------------------------------------------------
-constexpr int kScanTile = kScanTileWords;
-constexpr unsigned long long kAggFlag = 1ull << 32, kIncFlag = 2ull << 32;
-constexpr int kLookbackSpins = 1 << 22;
+constexpr int kOrderThreads = 1024;
 
-__global__ void __launch_bounds__(512)
-order_lookback(const uint32_t *__restrict__ bits, uint32_t nwords,
-               uint32_t *__restrict__ prefix, uint32_t *__restrict__ counters,
-               unsigned long long *__restrict__ status) {
-  __shared__ uint32_t s_tile, s_prefix;
-  if (threadIdx.x == 0)
-    s_tile = atomicAdd(&counters[kCtrTiles], 1u);
-  __syncthreads();
-  const uint32_t tile = s_tile;
-  const uint32_t w0 = tile * kScanTile;
-  constexpr int PER = kScanTile / 512;
-  uint32_t c[PER], local = 0;
-#pragma unroll
-  for (int k = 0; k < PER; k++) {
-    const uint32_t w = w0 + threadIdx.x * PER + k;
-    c[k] = w < nwords ? __popc(bits[w]) : 0u;
-    local += c[k];
-  }
+__global__ void __launch_bounds__(kOrderThreads)
+order_coop(int width, const uint32_t *__restrict__ bits, uint32_t nwords,
+           uint32_t *__restrict__ prefix, uint32_t *__restrict__ block_sums,
+           const uint32_t *__restrict__ counters, uint32_t cand_cap,
+           const sf_signal_pixel *__restrict__ staging, uint32_t capacity,
+           sf_signal_pixel *__restrict__ out, uint32_t *__restrict__ count_out) {
+  cg::grid_group grid = cg::this_grid();
+  const uint32_t chunk = (nwords + gridDim.x - 1) / gridDim.x;
+  const uint32_t lo = min(nwords, blockIdx.x * chunk), hi = min(nwords, lo + chunk);
+  uint32_t acc = 0;
+  for (uint32_t w = lo + threadIdx.x; w < hi; w += blockDim.x)
+    acc += __popc(bits[w]);
   uint32_t total;
-  const uint32_t excl = block_exclusive_scan(local, &total);
-  if (threadIdx.x == 0) {
-    volatile unsigned long long *vs = status;
-    if (tile == 0) {
-      atomicExch(&status[0], kIncFlag | total);
-      s_prefix = 0;
-    } else {
-      atomicExch(&status[tile], kAggFlag | total);
-      uint32_t run = 0;
-      int t = (int)tile - 1;
-      while (t >= 0) {
-        unsigned long long v = vs[t];
-        int spins = 0;
-        while (!(v >> 32) && spins < kLookbackSpins) {
-          __nanosleep(32);
-          v = vs[t];
-          spins++;
-        }
-        if (!(v >> 32)) {
-          atomicOr(&counters[kCtrError], 1u);  // a predecessor never published
-          break;
-        }
-        run += (uint32_t)v;
-        if ((v >> 32) == 2ull)
-          break;
-        t--;
-      }
-      __threadfence();
-      atomicExch(&status[tile], kIncFlag | (run + total));
-      s_prefix = run;
-    }
+  (void)block_exclusive_scan(acc, &total);
+  if (threadIdx.x == 0)
+    block_sums[blockIdx.x] = total;
+  grid.sync();
+  __shared__ uint32_t s_base;
+  if (threadIdx.x < 32) {
+    uint32_t b = 0;
+    for (uint32_t i = threadIdx.x; i < blockIdx.x; i += 32)
+      b += block_sums[i];
+    for (int o = 16; o; o >>= 1)
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    if (threadIdx.x == 0)
+      s_base = b;
   }
   __syncthreads();
-  uint32_t run = s_prefix + excl;
-#pragma unroll
-  for (int k = 0; k < PER; k++) {
-    const uint32_t w = w0 + threadIdx.x * PER + k;
-    if (w < nwords)
-      prefix[w] = run;
-    run += c[k];
+  uint32_t carry = s_base;
+  for (uint32_t base = lo; base < hi; base += blockDim.x) {
+    const uint32_t w = base + threadIdx.x;
+    const uint32_t c = w < hi ? __popc(bits[w]) : 0u;
+    uint32_t t;
+    const uint32_t e = block_exclusive_scan(c, &t);
+    if (w < hi)
+      prefix[w] = carry + e;
+    carry += t;
   }
-}
-
-__global__ void order_scatter(int width, const uint32_t *__restrict__ bits,
-                              const uint32_t *__restrict__ prefix,
-                              const uint32_t *__restrict__ counters, uint32_t cand_cap,
-                              const sf_signal_pixel *__restrict__ staging, uint32_t capacity,
-                              sf_signal_pixel *__restrict__ out, uint32_t *__restrict__ count_out) {
-  const uint32_t total = counters[kCtrTotal];
+  grid.sync();
+  const uint32_t found = counters[kCtrTotal];
   if (blockIdx.x == 0 && threadIdx.x == 0)
-    // The signal found; all ones if a list overflowed or the scan failed, as
-    // for a count above capacity (the list is then incomplete).
-    *count_out = (counters[kCtrCand] > cand_cap || counters[kCtrError]) ? 0xFFFFFFFFu : total;
-  const uint32_t n = min(total, capacity);
+    // The signal found; all ones if the candidate list overflowed, as for a
+    // count above capacity (the list is then incomplete).
+    *count_out = counters[kCtrCand] > cand_cap ? 0xFFFFFFFFu : found;
+  const uint32_t n = min(found, capacity);
   const int wpr = (width + 31) >> 5;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const sf_signal_pixel rec = staging[i];
@@ -652,6 +631,23 @@ void make_stream_tables(const LaunchParams &P, StreamTables *T) {
   }
 }
 
+// One block per SM for the cooperative ordering kernel.
+static int order_blocks() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, order_coop, kOrderThreads, 0);
+    n = sms * (per > 0 ? 1 : 0);
+    if (n <= 0)
+      n = 1;
+    if (n > kScanBlocks)
+      n = kScanBlocks;
+  }
+  return n;
+}
+
 template <int K>
 static cudaError_t launch_stream_k(const uint32_t *image, int h, int w, const LaunchParams &P,
                                    const StreamBuffers &b, cudaStream_t stream) {
@@ -679,20 +675,25 @@ static cudaError_t launch_stream_k(const uint32_t *image, int h, int w, const La
                                                b.cand_cap, b.counters, b.wide);
   seg_stage2<K><<<8 * 152, 256, 0, stream>>>(image, h, w, P, b.scr1, b.bits, b.cand,
                                               b.cand_cap, b.counters, b.staging, b.capacity);
-  const uint32_t nwords = (uint32_t)(((size_t)w + 31) / 32 * h);
-  order_lookback<<<(unsigned)scan_tiles(h, w), 512, 0, stream>>>(b.bits, nwords, b.prefix,
-                                                                  b.counters, b.status);
-  order_scatter<<<2 * 152, 256, 0, stream>>>(w, b.bits, b.prefix, b.counters, b.cand_cap,
-                                             b.staging, b.capacity, b.out, b.count_out);
+  uint32_t nwords = (uint32_t)(((size_t)w + 31) / 32 * h);
+  int width = w;
+  uint32_t cand_cap = b.cand_cap, capacity = b.capacity;
+  const uint32_t *bits_c = b.bits;
+  const uint32_t *counters_c = b.counters;
+  const sf_signal_pixel *staging_c = b.staging;
+  void *args[] = {&width,    &bits_c,    &nwords,    (void *)&b.prefix, (void *)&b.block_sums,
+                  &counters_c, &cand_cap, &staging_c, &capacity,         (void *)&b.out,
+                  (void *)&b.count_out};
+  e = cudaLaunchCooperativeKernel((void *)order_coop, dim3(order_blocks()), dim3(kOrderThreads),
+                                  args, 0, stream);
+  if (e != cudaSuccess)
+    return e;
   return cudaGetLastError();
 }
 
 cudaError_t launch_stream(const uint32_t *image, int h, int w, const LaunchParams &P,
                           const StreamBuffers &b, cudaStream_t stream) {
-  // The counters and the scan status words are contiguous.
-  cudaError_t e = cudaMemsetAsync(
-      b.counters, 0, kCtrCount * sizeof(uint32_t) + scan_tiles(h, w) * sizeof(unsigned long long),
-      stream);
+  cudaError_t e = cudaMemsetAsync(b.counters, 0, kCtrCount * sizeof(uint32_t), stream);
   if (e != cudaSuccess)
     return e;
   switch (P.half) {

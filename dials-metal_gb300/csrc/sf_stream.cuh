@@ -24,18 +24,13 @@
 
 namespace sf {
 
-// Counter words at the start of the stream workspace, followed by the
-// look-back scan's per-tile status words.
+// Counter words at the start of the stream workspace.
 enum {
   kCtrTotal = 0,  // signal pixels found
   kCtrCand,       // candidates found
   kCtrWide,       // runs handed to the 64-bit path
-  kCtrTiles,      // scan tiles claimed
-  kCtrError,      // a bounded wait gave up
   kCtrCount = 8
 };
-
-constexpr int kScanTileWords = 4096;
 
 // Strips of 240 output columns (one warp each) by runs of rows: as many runs
 // as fill the GPU once (3 blocks of 4 warps on each of 152 SMs), each at least
@@ -68,7 +63,7 @@ struct StreamBuffers {
   uint32_t cand_cap;
   uint32_t *counters;     // kCtrCount words
   uint4 *wide;            // handed-over runs
-  unsigned long long *status;  // look-back status, right after the counters
+  uint32_t *block_sums;   // per-block sums of the ordering kernel
   sf_signal_pixel *staging;
   sf_signal_pixel *out;   // ascending list (output)
   uint32_t capacity;
@@ -80,10 +75,6 @@ inline int stream_units(int h, int w) {
   return g.nstrips * g.nruns;
 }
 
-inline size_t scan_tiles(int h, int w) {
-  const size_t words = ((size_t)w + 31) / 32 * h;
-  return (words + kScanTileWords - 1) / kScanTileWords;
-}
 
 void make_stream_tables(const LaunchParams &P, StreamTables *T);
 
