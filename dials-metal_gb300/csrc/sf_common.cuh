@@ -146,9 +146,20 @@ __device__ __forceinline__ bool stage2_u32(uint32_t p, uint32_t n,
       return true; // p - mean > 2^23.6 > sigma_s sqrt(mean) + any rounding
     const long long E =
         d * d - (long long)P.sigma_s2_int * (long long)S * (long long)n;
-    if (E > 8192)
+    // |p - t| beyond the double sequence's error err <= 2^-50 t means
+    // |E| > n^2 err (err + 2 sigma_s sqrt(mean)); bound that from above in
+    // float with generous slack (mean < 2^24 here).
+    const float mu = __fdiv_ru((float)(uint32_t)S, (float)n);
+    const float rt = __fsqrt_ru(mu) * 1.001f + 1.0f;
+    const float ss = (float)P.sigma_s;
+    const float t = mu + ss * rt + 1.0f;
+    const float err = t * 0x1p-49f;
+    const float nn = (float)n * (float)n;
+    const float bound = nn * err * (err + 2.0f * ss * rt) * 2.0f + 1.0f;
+    const float Ef = (float)E;
+    if (Ef > bound)
       return true;
-    if (E < -8192)
+    if (Ef < -bound)
       return false;
   }
   return stage2_double(p, n, S, P, bg);

@@ -77,25 +77,25 @@ template <int K> struct SegSmem {
 };
 
 __device__ __forceinline__ void seg_load(const uint32_t *__restrict__ image, int height, int width,
-                                         int vec, int cx, int p, uint32_t v[16]) {
+                                         bool interior, int cx, int p, uint32_t v[16]) {
+  if (p < 0 || p >= height) {
 #pragma unroll
-  for (int i = 0; i < 16; i++)
-    v[i] = 0xFFFFFFFFu;
-  if (p < 0 || p >= height)
+    for (int i = 0; i < 16; i++)
+      v[i] = 0xFFFFFFFFu;
     return;
-  const uint32_t *row = image + (size_t)p * width;
-  const int x = cx - 4;
+  }
+  const uint32_t *row = image + (size_t)p * width + (cx - 4);
+  if (interior) {
 #pragma unroll
-  for (int f = 0; f < 4; f++) {
-    const int gx = x + 4 * f;
-    if (vec && gx >= 0 && gx + 3 < width) {
-      const uint4 t = __ldg(reinterpret_cast<const uint4 *>(row + gx));
+    for (int f = 0; f < 4; f++) {
+      const uint4 t = __ldg(reinterpret_cast<const uint4 *>(row) + f);
       v[4 * f] = t.x, v[4 * f + 1] = t.y, v[4 * f + 2] = t.z, v[4 * f + 3] = t.w;
-    } else {
+    }
+  } else {
 #pragma unroll
-      for (int e = 0; e < 4; e++)
-        if (gx + e >= 0 && gx + e < width)
-          v[4 * f + e] = __ldg(row + gx + e);
+    for (int i = 0; i < 16; i++) {
+      const int gx = cx - 4 + i;
+      v[i] = (gx >= 0 && gx < width) ? __ldg(row + i) : 0xFFFFFFFFu;
     }
   }
 }
@@ -118,17 +118,187 @@ __device__ void seg_flush(SegSmem<K> &s, int warp, uint32_t *cand, uint32_t *cou
   __syncwarp();
 }
 
-// The cases the "surely not" bound leaves: the "surely" bound, then, near the
-// threshold, the exact decision. Kept out of line so the common path does not
-// carry (or issue) it.
-template <int K>
-__device__ __noinline__ bool seg_rare_decision(uint32_t n, uint32_t S, uint32_t Q, float Sf,
-                                               float Qf, const LaunchParams &P,
-                                               const StreamTables &T) {
-  if (__fmul_rn(T.nf_lo[n], Qf) >=
-      __fadd_rn(__fmul_rn(__fmul_rn(Sf, __fadd_rn(Sf, T.c_hi[n])), 1.0001f), 2.0f))
-    return true;
+// The exact decision for the thin band neither float bound settles. Out of
+// line: the common path neither carries nor issues it.
+static __device__ __noinline__ bool seg_exact(uint32_t n, uint32_t S, uint32_t Q,
+                                              const LaunchParams &P) {
   return stage0_u32(n, (unsigned long long)S, (unsigned long long)Q, P, P.root_lo, P.root_hi);
+}
+
+// Everything a lane carries from row to row.
+template <int K> struct SegState {
+  uint32_t vns[8], vq[8];
+  unsigned long long hval, hs0;
+  int slot;
+};
+
+// One pixel row p for this lane. Returns false when the warp must hand the
+// rest of its run to the 64-bit path.
+template <int K>
+__device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const uint32_t raw[16],
+                                        int p, int p0, int ra, int rb, int cx, int X,
+                                        int width, int bytes_per_row, bool writer,
+                                        uint32_t inside8, int warp, int lane,
+                                        const LaunchParams &P, const StreamTables &T,
+                                        float nf_hi0, float c_lo0, float nf_lo0, float c_hi0,
+                                        const uint32_t *__restrict__ image,
+                                        uint8_t *__restrict__ scr1_bytes,
+                                        uint8_t *__restrict__ final_bytes, uint32_t *cand,
+                                        uint32_t cand_cap, uint32_t *counters,
+                                        uint4 *wide_list) {
+  using G = SegG<K>;
+  constexpr int o = 4 - K;               // first of the 8 + 2K pixels used
+  const uint32_t narrow = T.narrow_max;
+
+  // Pack the pixels the row sums use.
+  uint32_t ns[16], q[16];
+  bool wide = false;
+  uint32_t valid8 = 0;
+#pragma unroll
+  for (int i = o; i < o + 8 + 2 * K; i++) {
+    const uint32_t v = raw[i];
+    const bool small = v < narrow;
+    wide |= !small && v < 0xFFFFFFFEu;
+    ns[i] = small ? (v | (1u << G::PS)) : 0u;
+    const uint32_t pv = small ? v : 0u;
+    q[i] = pv * pv;
+    if (i >= 4 && i < 12)
+      valid8 |= (v < 0xFFFFFFFEu ? 1u : 0u) << (i - 4);
+  }
+  if (__any_sync(0xffffffffu, wide)) {
+    if (lane == 0) {
+      const uint32_t k = atomicAdd(&counters[kCtrWide], 1u);
+      // Up to the end of the row's last mask word: the columns past the
+      // frame are written as zeros there, as the lanes here would have.
+      const int xb = max(0, X + 8), xe = min(bytes_per_row * 8, X + 8 + kSegOut);
+      wide_list[k] =
+          make_uint4((uint32_t)xb, (uint32_t)xe, (uint32_t)max(ra, p - G::R1), (uint32_t)rb);
+    }
+    return false;
+  }
+  st.hval = (st.hval << 8) | valid8;
+
+  // Row sums of 2K + 1 columns for the 8 columns.
+  uint32_t hn[8], hq[8];
+  {
+    uint32_t a = 0, b = 0;
+#pragma unroll
+    for (int d = 0; d < G::W0; d++) {
+      a += ns[o + d];
+      b += q[o + d];
+    }
+    hn[0] = a;
+    hq[0] = b;
+#pragma unroll
+    for (int c = 1; c < 8; c++) {
+      a += ns[o + c + 2 * K] - ns[o + c - 1];
+      b += q[o + c + 2 * K] - q[o + c - 1];
+      hn[c] = a;
+      hq[c] = b;
+    }
+  }
+
+  // Column sums: the row sums of W0 rows ago come back from the ring.
+  {
+    uint4 *r = &s.ring[warp][st.slot][0][lane];
+    const uint4 l0 = r[0], l1 = r[32], l2 = r[64], l3 = r[96];
+    const uint32_t ln[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+    const uint32_t lq[8] = {l2.x, l2.y, l2.z, l2.w, l3.x, l3.y, l3.z, l3.w};
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      st.vns[c] += hn[c] - ln[c];
+      st.vq[c] += hq[c] - lq[c];
+    }
+    r[0] = make_uint4(hn[0], hn[1], hn[2], hn[3]);
+    r[32] = make_uint4(hn[4], hn[5], hn[6], hn[7]);
+    r[64] = make_uint4(hq[0], hq[1], hq[2], hq[3]);
+    r[96] = make_uint4(hq[4], hq[5], hq[6], hq[7]);
+    st.slot = st.slot + 1 == G::W0 ? 0 : st.slot + 1;
+  }
+  if (p < p0 + 2 * K)
+    return true;  // the column sums are not yet full windows (warp-uniform)
+
+  // Stage-0 row p - K: eight decisions.
+  uint32_t s8 = 0;
+  const uint32_t vrow = (uint32_t)(st.hval >> (8 * K)) & 0xFFu;
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    bool bit = !((vrow >> c) & 1u);  // masked pixels are set
+    if (!bit) {
+      const uint32_t n = st.vns[c] >> G::PS, S = st.vns[c] & G::MASK;
+      const bool full = n == (uint32_t)G::N0;
+      const float Sf = __uint2float_rn(S), Qf = __uint2float_rn(st.vq[c]);
+      // Surely not: nQ <= S (S + c) (bounds in sf_stream.cuh).
+      if (!(__fmul_rn(full ? nf_hi0 : T.nf_hi[n], Qf) <=
+            __fmul_rn(Sf, __fadd_rn(Sf, full ? c_lo0 : T.c_lo[n])))) {
+        // Surely: nQ >= S (S + c) + 1; otherwise decide exactly (rare).
+        if (__fmul_rn(full ? nf_lo0 : T.nf_lo[n], Qf) >=
+            __fadd_rn(__fmul_rn(__fmul_rn(Sf, __fadd_rn(Sf, full ? c_hi0 : T.c_hi[n])), 1.0001f),
+                      2.0f))
+          bit = true;
+        else
+          bit = seg_exact(n, S, st.vq[c], P);
+      }
+    }
+    s8 |= (bit ? 1u : 0u) << c;
+  }
+  st.hs0 = (st.hs0 << 8) | s8;
+  if (p < p0 + 2 * K + 2 * G::E)
+    return true;  // the erosion needs 2E more decision rows (warp-uniform)
+
+  // Erosion of row p - R1: vertical AND of 2E + 1 chunks, then across columns
+  // with the neighbours' chunks.
+  uint32_t v8 = 0xFFu;
+#pragma unroll
+  for (int b = 0; b <= 2 * G::E; b++)
+    v8 &= (uint32_t)(st.hs0 >> (8 * b)) & 0xFFu;
+  const uint32_t left = __shfl_up_sync(0xffffffffu, v8, 1);
+  const uint32_t right = __shfl_down_sync(0xffffffffu, v8, 1);
+  const uint32_t all = (right << 16) | (v8 << 8) | left;
+  uint32_t h8 = 0xFFu;
+#pragma unroll
+  for (int d = -G::E; d <= G::E; d++)
+    h8 &= (all >> (8 + d)) & 0xFFu;
+  const uint32_t masked8 = ~(uint32_t)(st.hval >> (8 * G::R1)) & 0xFFu;
+  const uint32_t scr1 = (h8 | masked8) & inside8;
+  const int re = p - G::R1;
+  const bool out_row = re >= ra && re < rb;
+  if (out_row && writer) {
+    scr1_bytes[(size_t)re * bytes_per_row + (cx >> 3)] = (uint8_t)scr1;
+    final_bytes[(size_t)re * bytes_per_row + (cx >> 3)] = 0;
+  }
+  // Candidates: eroded, not masked, above the global threshold.
+  uint32_t c8 = (out_row && writer) ? (scr1 & ~masked8) : 0u;
+  if (__any_sync(0xffffffffu, c8 != 0u)) {
+    if (c8) {
+      const uint32_t *row = image + (size_t)re * width;
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+        if (((c8 >> c) & 1u) && (uint64_t)__ldg(row + cx + c) < P.p_min)
+          c8 &= ~(1u << c);
+    }
+    const uint32_t cnt = __popc(c8);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o2 = 1; o2 < 32; o2 <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o2);
+      if (lane >= o2)
+        incl += t;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (s.ncand[warp] + total > (uint32_t)kSegCand)
+      seg_flush<K>(s, warp, cand, counters, cand_cap);
+    const uint32_t base = s.ncand[warp] + incl - cnt;
+    uint32_t k = 0;
+    for (int c = 0; c < 8; c++)
+      if ((c8 >> c) & 1u)
+        s.cand[warp][base + k++] = (uint32_t)re * (uint32_t)width + (uint32_t)(cx + c);
+    __syncwarp();
+    if (lane == 0)
+      s.ncand[warp] += total;
+    __syncwarp();
+  }
+  return true;
 }
 
 template <int K>
@@ -152,10 +322,12 @@ seg_stage01(const uint32_t *__restrict__ image, int height, int width, int vec, 
   const int rb = min(height, ra + run_rows);
   const int bytes_per_row = ((width + 31) >> 5) * 4;
   const bool writer = lane >= 1 && lane <= 30 && cx < bytes_per_row * 8;
-  const uint32_t narrow = T.narrow_max;
+  const bool interior = vec && cx - 4 >= 0 && cx + 12 <= width;
   const float nf_hi0 = T.nf_hi[G::N0], c_lo0 = T.c_lo[G::N0];
+  const float nf_lo0 = T.nf_lo[G::N0], c_hi0 = T.c_hi[G::N0];
   // Bits of this lane's columns that lie inside the frame.
-  const uint32_t inside8 = cx >= width ? 0u : (cx + 8 <= width ? 0xFFu : ((1u << (width - cx)) - 1u));
+  const uint32_t inside8 =
+      cx >= width ? 0u : (cx + 8 <= width ? 0xFFu : ((1u << (width - cx)) - 1u));
 
   if (lane == 0)
     s.ncand[warp] = 0;
@@ -166,166 +338,32 @@ seg_stage01(const uint32_t *__restrict__ image, int height, int width, int vec, 
       s.ring[warp][sl][qd][lane] = make_uint4(0u, 0u, 0u, 0u);
   __syncwarp();
 
-  uint32_t vns[8], vq[8];
+  SegState<K> st;
 #pragma unroll
   for (int c = 0; c < 8; c++)
-    vns[c] = vq[c] = 0u;
-  unsigned long long hval = 0ull;  // valid bits, 8 per row, newest row in byte 0
-  unsigned long long hs0 = 0ull;   // stage-0 bits, same layout (decision rows)
+    st.vns[c] = st.vq[c] = 0u;
+  st.hval = st.hs0 = 0ull;
+  st.slot = 0;
 
   const int p0 = ra - G::R1, p1 = rb + G::R1;  // pixel rows [p0, p1)
-  uint32_t raw[16], nxt[16];
-  seg_load(image, height, width, vec, cx, p0, nxt);
-  int slot = 0;
-  for (int p = p0; p < p1; p++) {
-#pragma unroll
-    for (int i = 0; i < 16; i++)
-      raw[i] = nxt[i];
+  uint32_t A[16], B[16];
+  seg_load(image, height, width, interior, cx, p0, A);
+  for (int p = p0; p < p1; p += 2) {
+    // Two rows per pass, the loads alternating between A and B.
     if (p + 1 < p1)
-      seg_load(image, height, width, vec, cx, p + 1, nxt);
-
-    // Pack.
-    uint32_t ns[16], q[16];
-    bool wide = false;
-    uint32_t valid8 = 0;
-#pragma unroll
-    for (int i = 0; i < 16; i++) {
-      const bool valid = raw[i] < 0xFFFFFFFEu;
-      wide |= valid && raw[i] >= narrow;
-      const uint32_t pv = valid && raw[i] < narrow ? raw[i] : 0u;
-      ns[i] = valid ? ((1u << G::PS) | pv) : 0u;
-      q[i] = pv * pv;
-      if (i >= 4 && i < 12)
-        valid8 |= (valid ? 1u : 0u) << (i - 4);
-    }
-    if (__any_sync(0xffffffffu, wide)) {
-      // Rows from p - R1 on are not yet written: hand them over.
-      if (lane == 0) {
-        const uint32_t k = atomicAdd(&counters[kCtrWide], 1u);
-        // Up to the end of the row's last mask word: the columns past the
-        // frame are written as zeros there, as the lanes here would have.
-        const int xb = max(0, X + 8), xe = min(bytes_per_row * 8, X + 8 + kSegOut);
-        wide_list[k] = make_uint4((uint32_t)xb, (uint32_t)xe, (uint32_t)max(ra, p - G::R1),
-                                  (uint32_t)rb);
-      }
+      seg_load(image, height, width, interior, cx, p + 1, B);
+    if (!seg_row<K>(s, st, A, p, p0, ra, rb, cx, X, width, bytes_per_row, writer, inside8,
+                    warp, lane, P, T, nf_hi0, c_lo0, nf_lo0, c_hi0, image, scr1_bytes,
+                    final_bytes, cand, cand_cap, counters, wide_list))
       break;
-    }
-    hval = (hval << 8) | valid8;
-
-    // Row sums of 2K + 1 columns for the 8 columns.
-    constexpr int o = 4 - K;
-    uint32_t hn[8], hq[8];
-    {
-      uint32_t a = 0, b = 0;
-#pragma unroll
-      for (int d = 0; d < G::W0; d++) {
-        a += ns[o + d];
-        b += q[o + d];
-      }
-      hn[0] = a;
-      hq[0] = b;
-#pragma unroll
-      for (int c = 1; c < 8; c++) {
-        a += ns[o + c + 2 * K] - ns[o + c - 1];
-        b += q[o + c + 2 * K] - q[o + c - 1];
-        hn[c] = a;
-        hq[c] = b;
-      }
-    }
-
-    // Column sums: the row sums of W0 rows ago come back from the ring.
-    {
-      const uint4 l0 = s.ring[warp][slot][0][lane], l1 = s.ring[warp][slot][1][lane];
-      const uint4 l2 = s.ring[warp][slot][2][lane], l3 = s.ring[warp][slot][3][lane];
-      const uint32_t ln[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
-      const uint32_t lq[8] = {l2.x, l2.y, l2.z, l2.w, l3.x, l3.y, l3.z, l3.w};
-#pragma unroll
-      for (int c = 0; c < 8; c++) {
-        vns[c] += hn[c] - ln[c];
-        vq[c] += hq[c] - lq[c];
-      }
-      s.ring[warp][slot][0][lane] = make_uint4(hn[0], hn[1], hn[2], hn[3]);
-      s.ring[warp][slot][1][lane] = make_uint4(hn[4], hn[5], hn[6], hn[7]);
-      s.ring[warp][slot][2][lane] = make_uint4(hq[0], hq[1], hq[2], hq[3]);
-      s.ring[warp][slot][3][lane] = make_uint4(hq[4], hq[5], hq[6], hq[7]);
-      slot = slot + 1 == G::W0 ? 0 : slot + 1;
-    }
-    if (p < p0 + 2 * K)
-      continue;  // the column sums are not yet full windows (warp-uniform)
-
-    // Stage-0 row p - K: eight decisions.
-    uint32_t s8 = 0;
-    const uint32_t vrow = (uint32_t)(hval >> (8 * K)) & 0xFFu;
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-      bool bit = !((vrow >> c) & 1u);  // masked pixels are set
-      if (!bit) {
-        const uint32_t n = vns[c] >> G::PS, S = vns[c] & G::MASK;
-        const bool full = n == (uint32_t)G::N0;
-        const float nhi = full ? nf_hi0 : T.nf_hi[n];
-        const float clo = full ? c_lo0 : T.c_lo[n];
-        const float Sf = __uint2float_rn(S), Qf = __uint2float_rn(vq[c]);
-        if (!(__fmul_rn(nhi, Qf) <= __fmul_rn(Sf, __fadd_rn(Sf, clo))))
-          bit = seg_rare_decision<K>(n, S, vq[c], Sf, Qf, P, T);
-      }
-      s8 |= (bit ? 1u : 0u) << c;
-    }
-    hs0 = (hs0 << 8) | s8;
-    if (p < p0 + 2 * K + 2 * G::E)
-      continue;  // the erosion needs 2E more decision rows (warp-uniform)
-
-    // Erosion of row p - R1: vertical AND of 2E + 1 chunks, then across
-    // columns with the neighbours' chunks.
-    uint32_t v8 = 0xFFu;
-#pragma unroll
-    for (int b = 0; b <= 2 * G::E; b++)
-      v8 &= (uint32_t)(hs0 >> (8 * b)) & 0xFFu;
-    const uint32_t left = __shfl_up_sync(0xffffffffu, v8, 1);
-    const uint32_t right = __shfl_down_sync(0xffffffffu, v8, 1);
-    const uint32_t all = (right << 16) | (v8 << 8) | left;
-    uint32_t h8 = 0xFFu;
-#pragma unroll
-    for (int d = -G::E; d <= G::E; d++)
-      h8 &= (all >> (8 + d)) & 0xFFu;
-    const uint32_t masked8 = ~(uint32_t)(hval >> (8 * G::R1)) & 0xFFu;
-    const uint32_t scr1 = (h8 | masked8) & inside8;
-    const int re = p - G::R1;
-    const bool out_row = re >= ra && re < rb;
-    if (out_row && writer) {
-      scr1_bytes[(size_t)re * bytes_per_row + (cx >> 3)] = (uint8_t)scr1;
-      final_bytes[(size_t)re * bytes_per_row + (cx >> 3)] = 0;
-    }
-    // Candidates: eroded, not masked, above the global threshold.
-    uint32_t c8 = (out_row && writer) ? (scr1 & ~masked8) : 0u;
-    if (__any_sync(0xffffffffu, c8 != 0u)) {
-      if (c8) {
-        const uint32_t *row = image + (size_t)re * width;
-#pragma unroll
-        for (int c = 0; c < 8; c++)
-          if (((c8 >> c) & 1u) && (uint64_t)__ldg(row + cx + c) < P.p_min)
-            c8 &= ~(1u << c);
-      }
-      const uint32_t cnt = __popc(c8);
-      uint32_t incl = cnt;
-#pragma unroll
-      for (int o2 = 1; o2 < 32; o2 <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o2);
-        if (lane >= o2)
-          incl += t;
-      }
-      const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-      if (s.ncand[warp] + total > (uint32_t)kSegCand)
-        seg_flush<K>(s, warp, cand, counters, cand_cap);
-      const uint32_t base = s.ncand[warp] + incl - cnt;
-      uint32_t k = 0;
-      for (int c = 0; c < 8; c++)
-        if ((c8 >> c) & 1u)
-          s.cand[warp][base + k++] = (uint32_t)re * (uint32_t)width + (uint32_t)(cx + c);
-      __syncwarp();
-      if (lane == 0)
-        s.ncand[warp] += total;
-      __syncwarp();
-    }
+    if (p + 1 >= p1)
+      break;
+    if (p + 2 < p1)
+      seg_load(image, height, width, interior, cx, p + 2, A);
+    if (!seg_row<K>(s, st, B, p + 1, p0, ra, rb, cx, X, width, bytes_per_row, writer,
+                    inside8, warp, lane, P, T, nf_hi0, c_lo0, nf_lo0, c_hi0, image,
+                    scr1_bytes, final_bytes, cand, cand_cap, counters, wide_list))
+      break;
   }
   seg_flush<K>(s, warp, cand, counters, cand_cap);
 }
@@ -469,9 +507,12 @@ seg_stage2(const uint32_t *__restrict__ image, int height, int width,
       p = __ldg(image + idx);
       const int xlo = max(0, x - K2), xhi = min(width - 1, x + K2);
       const int w0 = xlo >> 5;
-      for (int dy = -K2 + sub; dy <= K2; dy += 4) {
+      constexpr int ROWS = (WW + 3) / 4;  // rows per lane
+#pragma unroll
+      for (int k = 0; k < ROWS; k++) {
+        const int dy = -K2 + sub + 4 * k;
         const int yy = y + dy;
-        if (yy < 0 || yy >= height)
+        if (dy > K2 || yy < 0 || yy >= height)
           continue;
         const uint32_t *row = image + (size_t)yy * width;
         const uint32_t *brow = scr1_words + (size_t)yy * wpr;
