@@ -221,25 +221,20 @@ def run_ours(args):
     frames = make_pool(pool_n, seed_offset=rank)
     pool = torch.stack([torch.from_numpy(f.view(np.int32)) for f in frames]).to(dev)
     stream = torch.cuda.Stream(device=dev)
-    dt = api.DeviceThreshold(H, W)
+    batch = api.DeviceBatch(H, W, B)
 
-    def step(i0: int, events=None):
-        with torch.cuda.stream(stream):
-            for j in range(B):
-                k = (i0 + j) % pool_n
-                if events is not None:
-                    events[j][0].record(stream)
-                dt(pool[k], stream=stream)
-                if events is not None:
-                    events[j][1].record(stream)
+    def step(i0: int):
+        views = [pool[(i0 + j) % pool_n] for j in range(B)]
+        batch(views, stream=stream)
 
-    for w in range(args.warmup):
-        step(w * B)
+    with torch.cuda.stream(stream):
+        for w in range(args.warmup):
+            step(w * B)
     stream.synchronize()
-    n_signal = int(dt.count.item())
+    n_signal = int(batch.counts[:B].double().mean().item())
 
-    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(B)] for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
     clocks = ClockSampler(local, os.path.join(REPO, "gpurun_out", "bench_clocks.csv")
                           if os.path.isdir(os.path.join(REPO, "gpurun_out")) else None)
     clocks.start()
@@ -247,10 +242,13 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    start.record(stream)
-    for s in range(args.steps):
-        step((args.warmup + s) * B, ev[s])
-    end.record(stream)
+    with torch.cuda.stream(stream):
+        start.record(stream)
+        for s in range(args.steps):
+            ev[s][0].record(stream)
+            step((args.warmup + s) * B)
+            ev[s][1].record(stream)
+        end.record(stream)
     torch.cuda.synchronize(dev)
     if world > 1:
         torch.distributed.barrier()
@@ -259,55 +257,83 @@ def run_ours(args):
     elapsed_ms = max_over_ranks(elapsed_ms, world, dev)
     frames_done = sum_over_ranks(args.steps * B, world, dev)
     value = frames_done / (elapsed_ms / 1e3)
-    launch_ms = statistics.mean(a.elapsed_time(b) for row in ev for a, b in row)
+    launch_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
 
-    # Roofline of the threshold pass: algorithmic bytes per frame (the frame
-    # read once, the bitmask written, the signal list written).
-    algo_bytes = H * W * 4 + (H * W + 7) // 8 + 16 * n_signal
+    # Roofline of the threshold launch sequence: algorithmic bytes per frame
+    # (the frame read once, the bitmask written, the signal list written).
+    algo_bytes = B * (H * W * 4 + (H * W + 7) // 8 + 16 * n_signal)
     peak, peak_kind = measured_peak_gbs()
     achieved = algo_bytes / (launch_ms / 1e3) / 1e9
 
-    # End to end through the C ABI host-frame call (gpu::find drop-in).
+    # The plain per-frame device path (one launch sequence per frame).
+    single = api.DeviceThreshold(H, W)
+    with torch.cuda.stream(stream):
+        for j in range(4):
+            single(pool[j % pool_n], stream=stream)
+        stream.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n_single = max(B, 16)
+        a.record(stream)
+        for j in range(n_single):
+            single(pool[j % pool_n], stream=stream)
+        b.record(stream)
+    torch.cuda.synchronize(dev)
+    per_frame = n_single / (a.elapsed_time(b) / 1e3)
+    del single
+
+    # End to end through the C ABI host-frame call (gpu::find drop-in), from
+    # several host threads as mxi_find's -j workers call it.
     e2e = None
     if not args.no_e2e:
+        import ctypes
+        from concurrent.futures import ThreadPoolExecutor
+        L = api.lib()
         host = []
         for f in frames[: min(pool_n, 8)]:
-            ptr = api.lib().sf_host_alloc(f.nbytes)
+            ptr = L.sf_host_alloc(f.nbytes)
             if not ptr:
                 raise SystemExit("sf_host_alloc failed")
-            arr = np.ctypeslib.as_array((np.ctypeslib.ctypes.c_uint32 * f.size).from_address(ptr))
+            arr = np.ctypeslib.as_array((ctypes.c_uint32 * f.size).from_address(ptr))
             arr[:] = f.ravel()
-            host.append((ptr, arr.reshape(f.shape)))
-        out = np.empty(H * W // 4, api.SIGNAL_DTYPE)
-        import ctypes
-        found = ctypes.c_size_t(0)
-        L = api.lib()
+            host.append(ptr)
+        T = args.e2e_threads
+        outs = []
+        for _ in range(T):
+            ptr = L.sf_host_alloc(H * W // 4 * 16)
+            if not ptr:
+                raise SystemExit("sf_host_alloc failed")
+            outs.append(ptr)
+        tls = threading.local()
+        slot_lock = threading.Lock()
+        slots = list(range(T))
 
         def e2e_frame(k):
-            rc = L.sf_find_u32(host[k % len(host)][0], H, W, out.ctypes.data, len(out),
+            if not hasattr(tls, "slot"):
+                with slot_lock:
+                    tls.slot = slots.pop()
+            found = ctypes.c_size_t(0)
+            rc = L.sf_find_u32(host[k % len(host)], H, W, outs[tls.slot], H * W // 4,
                                ctypes.byref(found))
             if rc != 0:
                 raise SystemExit(f"sf_find_u32 failed: {rc} {api.last_error()}")
             return found.value
 
-        for w in range(args.warmup):
-            for j in range(B):
-                e2e_frame(w * B + j)
-        if world > 1:
-            torch.distributed.barrier()
-        t0 = time.perf_counter()
-        d2h = 0
-        for s in range(args.steps):
-            for j in range(B):
-                d2h += 4 + 16 * e2e_frame(s * B + j)
-        t1 = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=T) as ex:
+            list(ex.map(e2e_frame, range(max(args.warmup, 1) * max(B, T))))
+            if world > 1:
+                torch.distributed.barrier()
+            t0 = time.perf_counter()
+            n_e2e = args.steps * B
+            d2h = sum(4 + 16 * n for n in ex.map(e2e_frame, range(n_e2e)))
+            t1 = time.perf_counter()
         e_ms = max_over_ranks((t1 - t0) * 1e3, world, dev)
-        e2e = {"value": sum_over_ranks(args.steps * B, world, dev) / (e_ms / 1e3),
+        e2e = {"value": sum_over_ranks(n_e2e, world, dev) / (e_ms / 1e3),
                "unit": "frames/s", "h2d_bytes_per_step": B * H * W * 4,
                "d2h_bytes_per_step": int(d2h / args.steps),
-               "path": "sf_find_u32 (C ABI, gpu::find<uint32_t> drop-in), pinned host "
-                       "frames, copy + threshold + signal-list read-back per frame"}
-        for ptr, _ in host:
+               "path": f"sf_find_u32 (C ABI, gpu::find<uint32_t> drop-in) from {T} host "
+                       "threads, pinned host frames; per frame the copy in, the threshold "
+                       "and the signal list's read-back"}
+        for ptr in host + outs:
             L.sf_host_free(ptr)
 
     base = None
@@ -327,17 +353,21 @@ def run_ours(args):
                                      f"({pool_n * H * W * 4 / 1e9:.2f} GB), cycled",
                        "l2": "inputs larger than L2: each frame is 72.4 MB and "
                              "consecutive frames differ",
-                       "stage": "threshold (all three dext stages + ordered emit)",
-                       "signal_pixels_per_frame": n_signal},
+                       "stage": "threshold (all three dext stages + ordered emit), "
+                                f"{B} frames per launch sequence",
+                       "signal_pixels_per_frame": n_signal,
+                       "plain_per_frame_frames_per_s": per_frame,
+                       "batched_over_plain": value / per_frame},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind,
-                         "kernel": "threshold pass (threshold_tile + order_signal), "
-                                   "CUDA events around each launch",
+                         "kernel": "threshold launch sequence of a batch (seg_stage01, "
+                                   "stream_wide, seg_stage2, order_sums, order_prefix, "
+                                   "order_scatter), CUDA events around each batch",
                          "algorithmic_bytes_per_launch": algo_bytes,
                          "launch_ms": launch_ms, "traffic": args.traffic},
             "cpu_baseline": base, "e2e": e2e, "clocks": clock,
-            "gpu_launches": 2 * args.steps * B,
+            "gpu_launches": 6 * args.steps,
         }
         print(json.dumps(line))
     if world > 1:
@@ -356,6 +386,7 @@ def main(argv=None):
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-threads", type=int, default=4)
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per threshold launch from an ncu capture")
     args = ap.parse_args(argv)

@@ -24,6 +24,47 @@ thread_local std::string t_last_error;
 static bool g_profiling = false;
 thread_local sf_stage_times t_stage_times = {0, 0, 0, 0, 0, 0, 0};
 
+// Events around the kernel groups of the calling thread's last profiled
+// launch; read (after they complete) by sf_last_stage_times.
+struct DeviceMarks {
+  StreamMarks m = {nullptr, nullptr, nullptr, nullptr};
+  bool pending = false, staged = false;
+  ~DeviceMarks() {
+    for (cudaEvent_t e : {m.start, m.stage01, m.stage2, m.order})
+      if (e)
+        cudaEventDestroy(e);
+  }
+  const StreamMarks *arm() {
+    if (!m.start)
+      for (cudaEvent_t *e : {&m.start, &m.stage01, &m.stage2, &m.order})
+        cudaEventCreate(e);
+    pending = true;
+    return &m;
+  }
+  // Moves the device stage times of the last launch into *t (zeros where a
+  // launch recorded no stage boundaries).
+  void collect(sf_stage_times *t) {
+    if (!pending)
+      return;
+    pending = false;
+    if (cudaEventSynchronize(m.order) != cudaSuccess)
+      return;
+    float ms = 0.0f;
+    t->stage0 = t->stage1 = t->stage2 = t->sort = 0.0;
+    if (staged) {
+      cudaEventElapsedTime(&ms, m.start, m.stage01);
+      t->stage0 = ms;
+      cudaEventElapsedTime(&ms, m.stage01, m.stage2);
+      t->stage2 = ms;
+      cudaEventElapsedTime(&ms, m.stage2, m.order);
+      t->sort = ms;
+    }
+    cudaEventElapsedTime(&ms, m.start, m.order);
+    t->fused = ms;
+  }
+};
+thread_local DeviceMarks t_marks;
+
 int fail(cudaError_t e, const char *what) {
   t_last_error = std::string("CUDA: ") + what + ": " + cudaGetErrorString(e);
   return SF_ECUDA;
@@ -84,17 +125,16 @@ int make_launch_params(const sf_threshold_params *in, LaunchParams *P) {
 }
 
 // One workspace serves both threshold paths: the streaming path (32-bit
-// frames, dispersion_extended, gain 1 and integral sigmas) and the tile path
-// (everything else).
+// frames, dispersion_extended, gain 1 and integral sigmas; one frame or a
+// batch) and the tile path (everything else, one frame at a time).
 struct WorkspaceLayout {
-  size_t staging, cand, scr1, prefix, wide, counters, block_sums, tile_base, row_total,
-      total;
-  size_t cand_cap;
+  size_t staging, cand, res, scr1, wide, counters, block_sums, tile_base, row_total, total;
+  size_t cand_cap, words;
 };
 
-static WorkspaceLayout layout(size_t h, size_t w, size_t capacity) {
+static WorkspaceLayout layout(size_t h, size_t w, size_t capacity, size_t nframes = 1) {
   WorkspaceLayout L;
-  const size_t words = (w + 31) / 32 * h;
+  L.words = (w + 31) / 32 * h;
   // A frame with more eroded-mask candidates than twice the list capacity
   // (plus slack) is not a frame of spots; it is refused like an overflow.
   L.cand_cap = std::min(h * w, 2 * capacity + 65536);
@@ -104,13 +144,13 @@ static WorkspaceLayout layout(size_t h, size_t w, size_t capacity) {
     off += align_up(bytes ? bytes : 1, 256);
     return at;
   };
-  L.staging = take(capacity * sizeof(sf_signal_pixel));
-  L.cand = take(L.cand_cap * sizeof(uint32_t));
-  L.scr1 = take(words * sizeof(uint32_t));
-  L.prefix = take(words * sizeof(uint32_t));
-  L.wide = take((size_t)stream_units((int)h, (int)w) * 16);
-  L.counters = take(kCtrCount * sizeof(uint32_t));
-  L.block_sums = take(kScanBlocks * sizeof(uint32_t));
+  L.staging = take(capacity * sizeof(sf_signal_pixel));  // the tile path's, one frame
+  L.cand = take(nframes * L.cand_cap * sizeof(uint32_t));
+  L.res = take(nframes * L.cand_cap * sizeof(uint2));
+  L.scr1 = take(nframes * L.words * sizeof(uint32_t));
+  L.wide = take(stream_wide_entries((int)h, (int)w, (int)nframes) * 2 * sizeof(uint4));
+  L.counters = take(counter_words((int)nframes) * sizeof(uint32_t));
+  L.block_sums = take((size_t)std::max(kScanBlocks, stream_order_blocks()) * sizeof(uint32_t));
   L.tile_base = take((size_t)tiles_x((int)w) * tiles_y((int)h) * sizeof(uint32_t));
   L.row_total = take((size_t)tiles_y((int)h) * sizeof(uint32_t));
   L.total = off;
@@ -122,6 +162,83 @@ static bool shape_ok(size_t h, size_t w) {
   return h > 0 && w > 0 && h <= 0x7fffffffu / w;
 }
 
+static bool stream_path(size_t elem, const LaunchParams &P) {
+  return elem == 4 && P.algorithm == SF_DISPERSION_EXTENDED && P.int_ok;
+}
+
+// Frames d_images[0 .. n) (device pointers): lists at d_out + j * capacity,
+// masks at d_bits + j * words, counts at d_counts[j].
+template <typename T>
+static int threshold_frames(const T *const *d_images, size_t n, size_t h, size_t w,
+                            const sf_threshold_params *params, sf_signal_pixel *d_out,
+                            size_t capacity, uint32_t *d_bits, uint32_t *d_counts,
+                            uint32_t *d_word_prefix, void *d_ws, size_t ws_bytes,
+                            int run_rows, cudaStream_t stream) {
+  if (!d_images || n == 0 || n > (size_t)kMaxBatch || !d_out || !d_bits || !d_counts || !d_ws ||
+      !shape_ok(h, w) || capacity > 0xffffffffu)
+    return SF_EBADARG;
+  for (size_t j = 0; j < n; j++)
+    if (!d_images[j])
+      return SF_EBADARG;
+  LaunchParams P;
+  int rc = make_launch_params(params, &P);
+  if (rc != SF_OK)
+    return rc;
+  const bool streamed = stream_path(sizeof(T), P);
+  const WorkspaceLayout L = layout(h, w, capacity, streamed ? n : 1);
+  if (ws_bytes < L.total)
+    return SF_EBADARG;
+  unsigned char *ws = static_cast<unsigned char *>(d_ws);
+  if (streamed) {
+    FramePtrs F;
+    for (size_t j = 0; j < n; j++)
+      F.image[j] = reinterpret_cast<const uint32_t *>(d_images[j]);
+    StreamBuffers b;
+    b.bits = d_bits;
+    b.words = L.words;
+    b.scr1 = reinterpret_cast<uint32_t *>(ws + L.scr1);
+    b.prefix = d_word_prefix;
+    b.cand = reinterpret_cast<uint32_t *>(ws + L.cand);
+    b.res = reinterpret_cast<uint2 *>(ws + L.res);
+    b.cand_cap = (uint32_t)L.cand_cap;
+    b.counters = reinterpret_cast<uint32_t *>(ws + L.counters);
+    b.wide = reinterpret_cast<uint4 *>(ws + L.wide);
+    b.block_sums = reinterpret_cast<uint32_t *>(ws + L.block_sums);
+    b.capacity = (uint32_t)capacity;
+    b.out = d_out;
+    b.out_stride = capacity;
+    b.count_out = d_counts;
+    const StreamMarks *marks = g_profiling ? t_marks.arm() : nullptr;
+    t_marks.staged = true;
+    cudaError_t e = launch_stream(F, (int)n, (int)h, (int)w, P, b, run_rows, stream, marks);
+    if (e != cudaSuccess)
+      return fail(e, "launching the threshold");
+    return SF_OK;
+  }
+  const StreamMarks *marks = g_profiling ? t_marks.arm() : nullptr;
+  t_marks.staged = false;
+  if (marks)
+    cudaEventRecord(marks->start, stream);
+  // The tile path, one frame after another on the stream.
+  for (size_t j = 0; j < n; j++) {
+    FrameBuffers fb;
+    fb.bits = d_bits + j * L.words;
+    fb.staging = reinterpret_cast<sf_signal_pixel *>(ws + L.staging);
+    fb.out = d_out + j * capacity;
+    fb.word_prefix = d_word_prefix ? d_word_prefix + j * L.words : nullptr;
+    fb.tile_base = reinterpret_cast<uint32_t *>(ws + L.tile_base);
+    fb.row_total = reinterpret_cast<uint32_t *>(ws + L.row_total);
+    fb.total = d_counts + j;
+    fb.capacity = (uint32_t)capacity;
+    cudaError_t e = launch_threshold<T>(d_images[j], (int)h, (int)w, P, fb, stream);
+    if (e != cudaSuccess)
+      return fail(e, "launching the threshold");
+  }
+  if (marks)
+    cudaEventRecord(marks->order, stream);
+  return SF_OK;
+}
+
 template <typename T>
 static int threshold_device(const T *d_image, size_t h, size_t w,
                             const sf_threshold_params *params,
@@ -129,50 +246,11 @@ static int threshold_device(const T *d_image, size_t h, size_t w,
                             uint32_t *d_bits, uint32_t *d_count,
                             uint32_t *d_word_prefix, void *d_ws, size_t ws_bytes,
                             cudaStream_t stream) {
-  if (!d_image || !d_out || !d_bits || !d_count || !d_ws || !shape_ok(h, w) ||
-      capacity > 0xffffffffu)
+  if (!d_image)
     return SF_EBADARG;
-  LaunchParams P;
-  int rc = make_launch_params(params, &P);
-  if (rc != SF_OK)
-    return rc;
-  const WorkspaceLayout L = layout(h, w, capacity);
-  if (ws_bytes < L.total)
-    return SF_EBADARG;
-  unsigned char *ws = static_cast<unsigned char *>(d_ws);
-  if (sizeof(T) == 4 && P.algorithm == SF_DISPERSION_EXTENDED && P.int_ok) {
-    StreamBuffers b;
-    b.bits = d_bits;
-    b.scr1 = reinterpret_cast<uint32_t *>(ws + L.scr1);
-    b.prefix = d_word_prefix ? d_word_prefix : reinterpret_cast<uint32_t *>(ws + L.prefix);
-    b.cand = reinterpret_cast<uint32_t *>(ws + L.cand);
-    b.cand_cap = (uint32_t)L.cand_cap;
-    b.counters = reinterpret_cast<uint32_t *>(ws + L.counters);
-    b.wide = reinterpret_cast<uint4 *>(ws + L.wide);
-    b.block_sums = reinterpret_cast<uint32_t *>(ws + L.block_sums);
-    b.staging = reinterpret_cast<sf_signal_pixel *>(ws + L.staging);
-    b.out = d_out;
-    b.capacity = (uint32_t)capacity;
-    b.count_out = d_count;
-    cudaError_t e = launch_stream(reinterpret_cast<const uint32_t *>(d_image), (int)h, (int)w,
-                                  P, b, stream);
-    if (e != cudaSuccess)
-      return fail(e, "launching the threshold");
-    return SF_OK;
-  }
-  FrameBuffers fb;
-  fb.bits = d_bits;
-  fb.staging = reinterpret_cast<sf_signal_pixel *>(ws + L.staging);
-  fb.out = d_out;
-  fb.word_prefix = d_word_prefix;
-  fb.tile_base = reinterpret_cast<uint32_t *>(ws + L.tile_base);
-  fb.row_total = reinterpret_cast<uint32_t *>(ws + L.row_total);
-  fb.total = d_count;
-  fb.capacity = (uint32_t)capacity;
-  cudaError_t e = launch_threshold<T>(d_image, (int)h, (int)w, P, fb, stream);
-  if (e != cudaSuccess)
-    return fail(e, "launching the threshold");
-  return SF_OK;
+  const T *images[1] = {d_image};
+  return threshold_frames<T>(images, 1, h, w, params, d_out, capacity, d_bits, d_count,
+                             d_word_prefix, d_ws, ws_bytes, 0, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -334,8 +412,7 @@ static int find_host(const T *image, size_t h, size_t w,
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, marks[0], marks[1]);
     times.upload = ms;
-    cudaEventElapsedTime(&ms, marks[1], marks[2]);
-    times.fused = ms;
+    t_marks.collect(&times);
   }
   if (n > capacity) {
     if (timing)
@@ -462,6 +539,7 @@ int sf_find_u16_params(const uint16_t *image, size_t height, size_t width,
 void sf_profile_stages(int on) { g_profiling = on != 0; }
 int sf_profiling(void) { return g_profiling ? 1 : 0; }
 void sf_last_stage_times(sf_stage_times *out) {
+  t_marks.collect(&t_stage_times);
   if (out)
     *out = t_stage_times;
 }
@@ -494,6 +572,35 @@ int sf_threshold_u16_device(const uint16_t *d_image, size_t height, size_t width
                                     workspace_bytes, static_cast<cudaStream_t>(stream));
 }
 
+size_t sf_batch_workspace_bytes(size_t n_frames, size_t height, size_t width,
+                                size_t capacity) {
+  if (!shape_ok(height, width) || n_frames == 0 || n_frames > (size_t)kMaxBatch)
+    return 0;
+  return layout(height, width, capacity, n_frames).total;
+}
+
+int sf_threshold_u32_batch_device(const uint32_t *const *d_images, size_t n_frames,
+                                  size_t height, size_t width,
+                                  const sf_threshold_params *params, sf_signal_pixel *d_out,
+                                  size_t capacity, uint32_t *d_bits, uint32_t *d_counts,
+                                  uint32_t *d_word_prefix, void *d_workspace,
+                                  size_t workspace_bytes, void *stream) {
+  return threshold_frames<uint32_t>(d_images, n_frames, height, width, params, d_out, capacity,
+                                    d_bits, d_counts, d_word_prefix, d_workspace,
+                                    workspace_bytes, 0, static_cast<cudaStream_t>(stream));
+}
+
+int sf_threshold_u16_batch_device(const uint16_t *const *d_images, size_t n_frames,
+                                  size_t height, size_t width,
+                                  const sf_threshold_params *params, sf_signal_pixel *d_out,
+                                  size_t capacity, uint32_t *d_bits, uint32_t *d_counts,
+                                  uint32_t *d_word_prefix, void *d_workspace,
+                                  size_t workspace_bytes, void *stream) {
+  return threshold_frames<uint16_t>(d_images, n_frames, height, width, params, d_out, capacity,
+                                    d_bits, d_counts, d_word_prefix, d_workspace,
+                                    workspace_bytes, 0, static_cast<cudaStream_t>(stream));
+}
+
 } // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -511,9 +618,9 @@ int sf_threshold_u16_device(const uint16_t *d_image, size_t height, size_t width
 
 namespace sf {
 
-// 24 MiB: 8 MiB of staging (524,288 signal records of 16 bytes), the
-// candidate list for that capacity (4.25 MiB), and the per-word and per-tile
-// bookkeeping of frames up to 2^25 pixels (the EIGER2 16M is 18.1 M).
+// 24 MiB: 8 MiB of staging (524,288 signal records of 16 bytes) and the
+// per-word and per-tile bookkeeping (eroded mask, word prefixes, tile sums)
+// of frames up to 2^25 pixels (the EIGER2 16M is 18.1 M).
 constexpr size_t kNoAllocCapacity = 524288;
 constexpr size_t kNoAllocScratchBytes = (size_t)24 << 20;
 

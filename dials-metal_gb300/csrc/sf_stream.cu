@@ -1,4 +1,5 @@
-// The streaming threshold for 32-bit frames (the benchmark path).
+// The streaming threshold for 32-bit frames (the benchmark path), for one
+// frame or a batch of same-shaped frames per launch sequence.
 //
 // Stage 0 and the erosion of src/spots/dext.cc (:53-142) run in one pass in
 // which every warp walks down its own strip of rows; stage 2 (:151-222) runs
@@ -6,74 +7,92 @@
 // the frame:
 //
 //   seg_stage01   stage 0 + erosion, one warp per 240-column strip and run
-//                 of rows, no block barriers (described below)
+//                 of rows of one frame, no block barriers (described below);
+//                 writes the eroded mask and the candidate mask
 //   stream_wide   the same outputs with 64-bit sums, for the rare runs that
 //                 hold a valid pixel too large for the exact 32-bit sums
-//   seg_stage2    the background-only Poisson test at each candidate, exact
-//   order_*       a look-back scan of the final mask's popcounts, then every
-//                 staged record scattered to its ascending position
+//   mask_sums, mask_list
+//                 the candidates as an ascending list (two scans of the mask)
+//   seg_stage2    the background-only Poisson test at each candidate, exact;
+//                 clears the failures from the mask, which is then the final
+//                 strong-pixel mask
+//   pass_sums, pass_scatter
+//                 the passing candidates compacted in list order: the signal
+//                 list, ascending by index
+//   mask_prefix   (when asked for) each final-mask word's list position
 
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <algorithm>
 #include <cmath>
-
-#include <cooperative_groups.h>
+#include <mutex>
 
 #include "sf_common.cuh"
 #include "sf_scan.cuh"
 #include "sf_stream.cuh"
 
-namespace cg = cooperative_groups;
-
 namespace sf {
 
-// Packed exact sums: the window count in the top bits (enough for the
-// largest window, (2K+1)^2 pixels), the sum in the rest.
+// Packed exact sums: the window's masked-pixel count in the top bits (enough
+// for the largest window, (2K+1)^2 pixels), the sum of the valid ones in the
+// rest.
 constexpr int pack_shift(int K) {
   return (2 * K + 1) * (2 * K + 1) < 32 ? 27 : (2 * K + 1) * (2 * K + 1) < 64 ? 26 : 25;
 }
 
+// Fixed-point bits of the decision constants (sf_stream.cuh).
+constexpr int kDecShift = 8;
+
 // ---------------------------------------------------------------------------
-// Stage 0 and the erosion, one warp per (strip, run of rows).
+// Stage 0 and the erosion, one warp per (frame, strip, run of rows).
 //
 // Lane l owns the 8 columns [X + 8 l, X + 8 l + 8) and walks down the run one
 // pixel row at a time with no block barrier: it loads the 16 pixels
 // [X + 8 l - 4, X + 8 l + 12) of the row (four 16-byte loads, the next row's
-// prefetched), packs them (count and sum as n << PS | S, exact; p^2 exact in
-// 32 bits), takes its 8 row sums of 2K+1 columns in registers, and carries
-// 8 column sums down in registers; the row sum leaving the window comes back
-// from a small per-lane ring in shared memory. Each new stage-0 row gives 8
-// decisions (sf_stream.cuh), kept as 8-bit chunks in a 64-bit history; the
-// erosion ANDs 2E+1 chunks vertically, then across columns with the
-// neighbouring lanes' chunks (two shuffles). Lanes 0 and 31 are halo: they
-// feed their neighbours' erosion and write nothing, so a warp writes 240
-// columns. Pixels in the narrow range can take the near-threshold case exactly
-// inline, from the exact sums, since it is rare.
+// prefetched), takes its 8 row sums of 2K+1 columns in registers (masked
+// count and sum packed as m << PS | S, exact; p^2 exact in 32 bits), and
+// carries 8 column sums down in registers; the row sum leaving the window
+// comes back from a small per-lane ring in shared memory. A lane whose 8 + 2K
+// pixels are all valid and small (nearly all of them) packs nothing: its
+// masked count is 0. Each new stage-0 row gives 8 decisions (sf_stream.cuh)
+// from two 64-bit bounds per window without a branch (windows with masked
+// pixels read their constants from a small table); the rare windows between
+// the bounds are decided exactly, out of line. The decisions are kept as
+// 8-bit chunks in a 64-bit history; the erosion ANDs
+// 2E+1 chunks vertically, then across columns with the neighbouring lanes'
+// chunks (two shuffles). Lanes 0 and 31 are halo: they feed their
+// neighbours' erosion and write nothing, so a warp writes 240 columns.
 // ---------------------------------------------------------------------------
 
 constexpr int kSegLanes = 32;
 constexpr int kSegOut = 240;          // output columns per warp
-constexpr int kSegWarps = 4;          // warps per block
-constexpr int kSegCand = 512;         // per-warp candidate buffer
+constexpr int kSegWarps = 2;          // warps per block
 
 template <int K> struct SegG {
   static constexpr int E = K - 1;
   static constexpr int R1 = 2 * K - 1;
   static constexpr int W0 = 2 * K + 1;
   static constexpr int N0 = W0 * W0;
+  // Rows before a run's first output row: the windows fill (2K) and the
+  // erosion's decision rows (2E).
+  static constexpr int PRO = 2 * K + 2 * E;
   static constexpr uint32_t PS = pack_shift(K);
   static constexpr uint32_t MASK = (1u << PS) - 1u;
+  // Blocks per SM that shared memory and registers allow (the ring grows
+  // with K).
+  static constexpr int OCC = K == 2 ? 8 : K == 3 ? 7 : 5;
   static_assert(R1 <= 7, "eight rows of history");
+  static_assert(PRO == R1 + 2 * K - 1, "the first steady row outputs the run's first row");
 };
 
 template <int K> struct SegSmem {
   using G = SegG<K>;
   // ring[warp][slot][quad][lane] : uint4 = 4 of the 16 row sums
   uint4 ring[kSegWarps][G::W0][4][kSegLanes];
-  uint32_t cand[kSegWarps][kSegCand];
-  uint32_t ncand[kSegWarps];
+  // Decision constants by masked count m (window count N0 - m):
+  // {2^8 n or 0, clo, chi, 0}.
+  uint4 tab[G::N0 + 1];
 };
 
 __device__ __forceinline__ void seg_load(const uint32_t *__restrict__ image, int height, int width,
@@ -100,26 +119,21 @@ __device__ __forceinline__ void seg_load(const uint32_t *__restrict__ image, int
   }
 }
 
-template <int K>
-__device__ void seg_flush(SegSmem<K> &s, int warp, uint32_t *cand, uint32_t *counters,
-                          uint32_t cand_cap) {
-  __syncwarp();
-  const uint32_t n = s.ncand[warp];
-  uint32_t base = 0;
-  if ((threadIdx.x & 31) == 0)
-    base = n ? atomicAdd(&counters[kCtrCand], n) : 0u;
-  base = __shfl_sync(0xffffffffu, base, 0);
-  for (uint32_t i = threadIdx.x & 31; i < n; i += 32)
-    if (base + i < cand_cap)
-      cand[base + i] = s.cand[warp][i];
-  __syncwarp();
-  if ((threadIdx.x & 31) == 0)
-    s.ncand[warp] = 0;
-  __syncwarp();
-}
+// What one warp's run writes to, resolved once per warp.
+struct SegRun {
+  const uint32_t *image;
+  uint8_t *scr1_bytes, *final_bytes;
+  uint32_t *wide_ctr;
+  uint4 *wide_list;
+  int frame, height, width, bytes_per_row;
+  int X, cx, ra, rb, p0, warp, lane;
+  bool writer;
+  uint32_t inside8;
+  uint32_t nk0, clo0, chi0;  // decision constants of full windows
+};
 
-// The exact decision for the thin band neither float bound settles. Out of
-// line: the common path neither carries nor issues it.
+// The exact decision for the thin band neither bound settles. Out of line:
+// the common path neither carries nor issues it.
 static __device__ __noinline__ bool seg_exact(uint32_t n, uint32_t S, uint32_t Q,
                                               const LaunchParams &P) {
   return stage0_u32(n, (unsigned long long)S, (unsigned long long)Q, P, P.root_lo, P.root_hi);
@@ -132,65 +146,91 @@ template <int K> struct SegState {
   int slot;
 };
 
-// One pixel row p for this lane. Returns false when the warp must hand the
-// rest of its run to the 64-bit path.
-template <int K>
+// The two bounds of one window (sf_stream.cuh), branch-free:
+// maybe = 2^8 n Q > S (2^8 S + clo), sure = 2^8 n Q >= S (2^8 S + chi) + 2^9.
+__device__ __forceinline__ void seg_bounds(uint32_t S, uint32_t Q, uint32_t nk, uint32_t clo,
+                                           uint32_t chi, bool *maybe, bool *sure) {
+  const unsigned long long L = (unsigned long long)Q * nk;
+  const uint32_t tl = (S << kDecShift) + clo, th = (S << kDecShift) + chi;
+  *maybe = L > (unsigned long long)S * tl;
+  *sure = L >= (unsigned long long)S * th + (2ull << kDecShift);
+}
+
+// One pixel row p for this lane. Steady rows (every row past a run's first
+// PRO) output an eroded row; the first PRO rows only fill the windows and the
+// decision history. Returns false when the warp must hand the rest of its run
+// to the 64-bit path.
+template <int K, bool kSteady>
 __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const uint32_t raw[16],
-                                        int p, int p0, int ra, int rb, int cx, int X,
-                                        int width, int bytes_per_row, bool writer,
-                                        uint32_t inside8, int warp, int lane,
-                                        const LaunchParams &P, const StreamTables &T,
-                                        float nf_hi0, float c_lo0, float nf_lo0, float c_hi0,
-                                        const uint32_t *__restrict__ image,
-                                        uint8_t *__restrict__ scr1_bytes,
-                                        uint8_t *__restrict__ final_bytes, uint32_t *cand,
-                                        uint32_t cand_cap, uint32_t *counters,
-                                        uint4 *wide_list) {
+                                        int p, const SegRun &r, const LaunchParams &P,
+                                        const StreamTables &T) {
   using G = SegG<K>;
   constexpr int o = 4 - K;               // first of the 8 + 2K pixels used
+  constexpr int NP = 8 + 2 * K;
   const uint32_t narrow = T.narrow_max;
 
-  // Pack the pixels the row sums use.
-  uint32_t ns[16], q[16];
-  bool wide = false;
-  uint32_t valid8 = 0;
+  // The pixels the row sums use, as masked-count << PS | value and value^2.
+  uint32_t m4[4];
 #pragma unroll
-  for (int i = o; i < o + 8 + 2 * K; i++) {
-    const uint32_t v = raw[i];
-    const bool small = v < narrow;
-    wide |= !small && v < 0xFFFFFFFEu;
-    ns[i] = small ? (v | (1u << G::PS)) : 0u;
-    const uint32_t pv = small ? v : 0u;
-    q[i] = pv * pv;
-    if (i >= 4 && i < 12)
-      valid8 |= (v < 0xFFFFFFFEu ? 1u : 0u) << (i - 4);
+  for (int j = 0; j < 4; j++) {
+    uint32_t a = 0;
+#pragma unroll
+    for (int i = o + j; i < o + NP; i += 4)
+      a = max(a, raw[i]);
+    m4[j] = a;
+  }
+  const uint32_t mx = max(max(m4[0], m4[1]), max(m4[2], m4[3]));
+  uint32_t ns[16], q[16], valid8;
+  bool wide = false;
+  if (mx < narrow) {
+    // All valid and small (nearly every lane): no masked pixel to count.
+#pragma unroll
+    for (int i = o; i < o + NP; i++) {
+      ns[i] = raw[i];
+      q[i] = raw[i] * raw[i];
+    }
+    valid8 = 0xFFu;
+  } else {
+    valid8 = 0;
+#pragma unroll
+    for (int i = o; i < o + NP; i++) {
+      const uint32_t v = raw[i];
+      const bool small = v < narrow;
+      wide |= !small && v < 0xFFFFFFFEu;
+      ns[i] = small ? v : (1u << G::PS);
+      q[i] = small ? v * v : 0u;
+      if (i >= 4 && i < 12)
+        valid8 |= (v < 0xFFFFFFFEu ? 1u : 0u) << (i - 4);
+    }
   }
   if (__any_sync(0xffffffffu, wide)) {
-    if (lane == 0) {
-      const uint32_t k = atomicAdd(&counters[kCtrWide], 1u);
+    if (r.lane == 0) {
+      const uint32_t k = atomicAdd(r.wide_ctr, 1u);
       // Up to the end of the row's last mask word: the columns past the
       // frame are written as zeros there, as the lanes here would have.
-      const int xb = max(0, X + 8), xe = min(bytes_per_row * 8, X + 8 + kSegOut);
-      wide_list[k] =
-          make_uint4((uint32_t)xb, (uint32_t)xe, (uint32_t)max(ra, p - G::R1), (uint32_t)rb);
+      const int xb = max(0, r.X + 8), xe = min(r.bytes_per_row * 8, r.X + 8 + kSegOut);
+      r.wide_list[2 * k] =
+          make_uint4((uint32_t)xb, (uint32_t)xe, (uint32_t)max(r.ra, p - G::R1), (uint32_t)r.rb);
+      r.wide_list[2 * k + 1] = make_uint4((uint32_t)r.frame, 0u, 0u, 0u);
     }
     return false;
   }
   st.hval = (st.hval << 8) | valid8;
 
-  // Row sums of 2K + 1 columns for the 8 columns.
+  // Row sums of 2K + 1 columns for the 8 columns, as two sliding chains.
   uint32_t hn[8], hq[8];
-  {
+#pragma unroll
+  for (int h = 0; h < 8; h += 4) {
     uint32_t a = 0, b = 0;
 #pragma unroll
     for (int d = 0; d < G::W0; d++) {
-      a += ns[o + d];
-      b += q[o + d];
+      a += ns[o + h + d];
+      b += q[o + h + d];
     }
-    hn[0] = a;
-    hq[0] = b;
+    hn[h] = a;
+    hq[h] = b;
 #pragma unroll
-    for (int c = 1; c < 8; c++) {
+    for (int c = h + 1; c < h + 4; c++) {
       a += ns[o + c + 2 * K] - ns[o + c - 1];
       b += q[o + c + 2 * K] - q[o + c - 1];
       hn[c] = a;
@@ -200,8 +240,8 @@ __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const ui
 
   // Column sums: the row sums of W0 rows ago come back from the ring.
   {
-    uint4 *r = &s.ring[warp][st.slot][0][lane];
-    const uint4 l0 = r[0], l1 = r[32], l2 = r[64], l3 = r[96];
+    uint4 *rg = &s.ring[r.warp][st.slot][0][r.lane];
+    const uint4 l0 = rg[0], l1 = rg[32], l2 = rg[64], l3 = rg[96];
     const uint32_t ln[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
     const uint32_t lq[8] = {l2.x, l2.y, l2.z, l2.w, l3.x, l3.y, l3.z, l3.w};
 #pragma unroll
@@ -209,42 +249,53 @@ __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const ui
       st.vns[c] += hn[c] - ln[c];
       st.vq[c] += hq[c] - lq[c];
     }
-    r[0] = make_uint4(hn[0], hn[1], hn[2], hn[3]);
-    r[32] = make_uint4(hn[4], hn[5], hn[6], hn[7]);
-    r[64] = make_uint4(hq[0], hq[1], hq[2], hq[3]);
-    r[96] = make_uint4(hq[4], hq[5], hq[6], hq[7]);
+    rg[0] = make_uint4(hn[0], hn[1], hn[2], hn[3]);
+    rg[32] = make_uint4(hn[4], hn[5], hn[6], hn[7]);
+    rg[64] = make_uint4(hq[0], hq[1], hq[2], hq[3]);
+    rg[96] = make_uint4(hq[4], hq[5], hq[6], hq[7]);
     st.slot = st.slot + 1 == G::W0 ? 0 : st.slot + 1;
   }
-  if (p < p0 + 2 * K)
+  if (!kSteady && p < r.p0 + 2 * K)
     return true;  // the column sums are not yet full windows (warp-uniform)
 
-  // Stage-0 row p - K: eight decisions.
-  uint32_t s8 = 0;
+  // Stage-0 row p - K: eight decisions, maybe/sure bits without branches;
+  // masked pixels are set.
   const uint32_t vrow = (uint32_t)(st.hval >> (8 * K)) & 0xFFu;
+  uint32_t maybe8 = 0, sure8 = 0;
+  const uint32_t any_masked = (st.vns[0] | st.vns[1] | st.vns[2] | st.vns[3] | st.vns[4] |
+                               st.vns[5] | st.vns[6] | st.vns[7]) >> G::PS;
+  if (any_masked == 0) {
 #pragma unroll
-  for (int c = 0; c < 8; c++) {
-    bool bit = !((vrow >> c) & 1u);  // masked pixels are set
-    if (!bit) {
-      const uint32_t n = st.vns[c] >> G::PS, S = st.vns[c] & G::MASK;
-      const bool full = n == (uint32_t)G::N0;
-      const float Sf = __uint2float_rn(S), Qf = __uint2float_rn(st.vq[c]);
-      // Surely not: nQ <= S (S + c) (bounds in sf_stream.cuh).
-      if (!(__fmul_rn(full ? nf_hi0 : T.nf_hi[n], Qf) <=
-            __fmul_rn(Sf, __fadd_rn(Sf, full ? c_lo0 : T.c_lo[n])))) {
-        // Surely: nQ >= S (S + c) + 1; otherwise decide exactly (rare).
-        if (__fmul_rn(full ? nf_lo0 : T.nf_lo[n], Qf) >=
-            __fadd_rn(__fmul_rn(__fmul_rn(Sf, __fadd_rn(Sf, full ? c_hi0 : T.c_hi[n])), 1.0001f),
-                      2.0f))
-          bit = true;
-        else
-          bit = seg_exact(n, S, st.vq[c], P);
-      }
+    for (int c = 0; c < 8; c++) {
+      bool mb, su;
+      seg_bounds(st.vns[c], st.vq[c], r.nk0, r.clo0, r.chi0, &mb, &su);
+      maybe8 |= mb ? 1u << c : 0u;
+      sure8 |= su ? 1u << c : 0u;
     }
-    s8 |= (bit ? 1u : 0u) << c;
+  } else {
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const uint4 t = s.tab[st.vns[c] >> G::PS];
+      bool mb, su;
+      seg_bounds(st.vns[c] & G::MASK, st.vq[c], t.x, t.y, t.z, &mb, &su);
+      maybe8 |= mb ? 1u << c : 0u;
+      sure8 |= su ? 1u << c : 0u;
+    }
+  }
+  uint32_t s8 = (~vrow | sure8) & 0xFFu;
+  const uint32_t amb8 = maybe8 & ~sure8 & vrow;
+  if (amb8) {  // the thin band: exact, out of line (rare)
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const uint32_t x = st.vns[c];
+      if (((amb8 >> c) & 1u) &&
+          seg_exact((uint32_t)G::N0 - (x >> G::PS), x & G::MASK, st.vq[c], P))
+        s8 |= 1u << c;
+    }
   }
   st.hs0 = (st.hs0 << 8) | s8;
-  if (p < p0 + 2 * K + 2 * G::E)
-    return true;  // the erosion needs 2E more decision rows (warp-uniform)
+  if (!kSteady)
+    return true;  // the erosion needs 2E more decision rows
 
   // Erosion of row p - R1: vertical AND of 2E + 1 chunks, then across columns
   // with the neighbours' chunks.
@@ -260,77 +311,62 @@ __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const ui
   for (int d = -G::E; d <= G::E; d++)
     h8 &= (all >> (8 + d)) & 0xFFu;
   const uint32_t masked8 = ~(uint32_t)(st.hval >> (8 * G::R1)) & 0xFFu;
-  const uint32_t scr1 = (h8 | masked8) & inside8;
-  const int re = p - G::R1;
-  const bool out_row = re >= ra && re < rb;
-  if (out_row && writer) {
-    scr1_bytes[(size_t)re * bytes_per_row + (cx >> 3)] = (uint8_t)scr1;
-    final_bytes[(size_t)re * bytes_per_row + (cx >> 3)] = 0;
-  }
-  // Candidates: eroded, not masked, above the global threshold.
-  uint32_t c8 = (out_row && writer) ? (scr1 & ~masked8) : 0u;
-  if (__any_sync(0xffffffffu, c8 != 0u)) {
-    if (c8) {
-      const uint32_t *row = image + (size_t)re * width;
-#pragma unroll
-      for (int c = 0; c < 8; c++)
-        if (((c8 >> c) & 1u) && (uint64_t)__ldg(row + cx + c) < P.p_min)
-          c8 &= ~(1u << c);
-    }
-    const uint32_t cnt = __popc(c8);
-    uint32_t incl = cnt;
-#pragma unroll
-    for (int o2 = 1; o2 < 32; o2 <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o2);
-      if (lane >= o2)
-        incl += t;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    if (s.ncand[warp] + total > (uint32_t)kSegCand)
-      seg_flush<K>(s, warp, cand, counters, cand_cap);
-    const uint32_t base = s.ncand[warp] + incl - cnt;
-    uint32_t k = 0;
-    for (int c = 0; c < 8; c++)
-      if ((c8 >> c) & 1u)
-        s.cand[warp][base + k++] = (uint32_t)re * (uint32_t)width + (uint32_t)(cx + c);
-    __syncwarp();
-    if (lane == 0)
-      s.ncand[warp] += total;
-    __syncwarp();
+  const uint32_t scr1 = (h8 | masked8) & r.inside8;
+  const int re = p - G::R1;  // within [ra, rb) on every steady row
+  if (r.writer) {
+    // Candidates: eroded and not masked. The final mask starts as them and
+    // stage 2 clears those that fail (the global threshold among them).
+    const size_t at = (size_t)re * r.bytes_per_row + (r.cx >> 3);
+    r.scr1_bytes[at] = (uint8_t)scr1;
+    r.final_bytes[at] = (uint8_t)(scr1 & ~masked8);
   }
   return true;
 }
 
 template <int K>
-__global__ void __launch_bounds__(kSegWarps * 32, 3)
-seg_stage01(const uint32_t *__restrict__ image, int height, int width, int vec, int nstrips,
-            int nruns, int run_rows, const __grid_constant__ LaunchParams P,
+__global__ void __launch_bounds__(kSegWarps * 32, SegG<K>::OCC)
+seg_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int width, int vec,
+            int nstrips, int nruns, int run_rows, const __grid_constant__ LaunchParams P,
             const __grid_constant__ StreamTables T, uint8_t *__restrict__ scr1_bytes,
-            uint8_t *__restrict__ final_bytes, uint32_t *__restrict__ cand, uint32_t cand_cap,
-            uint32_t *__restrict__ counters, uint4 *__restrict__ wide_list) {
+            uint8_t *__restrict__ final_bytes, size_t mask_bytes, uint32_t *__restrict__ counters,
+            uint4 *__restrict__ wide_list) {
   using G = SegG<K>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SegSmem<K> &s = *reinterpret_cast<SegSmem<K> *>(smem_raw);
+  for (int m = threadIdx.x; m <= G::N0; m += blockDim.x)
+    s.tab[m] = make_uint4(T.nk[G::N0 - m], T.clo[G::N0 - m], T.chi[G::N0 - m], 0u);
+  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gw = blockIdx.x * kSegWarps + warp;
-  const int sx = gw % nstrips, ry = gw / nstrips;
-  if (ry >= nruns)
+  const int sx = gw % nstrips, t = gw / nstrips;
+  const int ry = t % nruns, f = t / nruns;
+  if (f >= nframes)
     return;  // whole warp
-  const int X = kSegOut * sx - 8;
-  const int cx = X + 8 * lane;
-  const int ra = ry * run_rows;
-  const int rb = min(height, ra + run_rows);
-  const int bytes_per_row = ((width + 31) >> 5) * 4;
-  const bool writer = lane >= 1 && lane <= 30 && cx < bytes_per_row * 8;
-  const bool interior = vec && cx - 4 >= 0 && cx + 12 <= width;
-  const float nf_hi0 = T.nf_hi[G::N0], c_lo0 = T.c_lo[G::N0];
-  const float nf_lo0 = T.nf_lo[G::N0], c_hi0 = T.c_hi[G::N0];
+  SegRun r;
+  r.frame = f;
+  r.image = F.image[f];
+  r.height = height;
+  r.width = width;
+  r.bytes_per_row = ((width + 31) >> 5) * 4;
+  r.scr1_bytes = scr1_bytes + (size_t)f * mask_bytes;
+  r.final_bytes = final_bytes + (size_t)f * mask_bytes;
+  r.wide_ctr = counters + kCtrWide;
+  r.wide_list = wide_list;
+  r.X = kSegOut * sx - 8;
+  r.cx = r.X + 8 * lane;
+  r.ra = ry * run_rows;
+  r.rb = min(height, r.ra + run_rows);
+  r.p0 = r.ra - G::R1;
+  r.warp = warp;
+  r.lane = lane;
+  r.writer = lane >= 1 && lane <= 30 && r.cx < r.bytes_per_row * 8;
   // Bits of this lane's columns that lie inside the frame.
-  const uint32_t inside8 =
-      cx >= width ? 0u : (cx + 8 <= width ? 0xFFu : ((1u << (width - cx)) - 1u));
+  r.inside8 = r.cx >= width ? 0u : (r.cx + 8 <= width ? 0xFFu : ((1u << (width - r.cx)) - 1u));
+  r.nk0 = T.nk[G::N0];
+  r.clo0 = T.clo[G::N0];
+  r.chi0 = T.chi[G::N0];
+  const bool interior = vec && r.cx - 4 >= 0 && r.cx + 12 <= width;
 
-  if (lane == 0)
-    s.ncand[warp] = 0;
 #pragma unroll
   for (int sl = 0; sl < G::W0; sl++)
 #pragma unroll
@@ -345,40 +381,45 @@ seg_stage01(const uint32_t *__restrict__ image, int height, int width, int vec, 
   st.hval = st.hs0 = 0ull;
   st.slot = 0;
 
-  const int p0 = ra - G::R1, p1 = rb + G::R1;  // pixel rows [p0, p1)
-  uint32_t A[16], B[16];
-  seg_load(image, height, width, interior, cx, p0, A);
-  for (int p = p0; p < p1; p += 2) {
-    // Two rows per pass, the loads alternating between A and B.
-    if (p + 1 < p1)
-      seg_load(image, height, width, interior, cx, p + 1, B);
-    if (!seg_row<K>(s, st, A, p, p0, ra, rb, cx, X, width, bytes_per_row, writer, inside8,
-                    warp, lane, P, T, nf_hi0, c_lo0, nf_lo0, c_hi0, image, scr1_bytes,
-                    final_bytes, cand, cand_cap, counters, wide_list))
-      break;
-    if (p + 1 >= p1)
-      break;
-    if (p + 2 < p1)
-      seg_load(image, height, width, interior, cx, p + 2, A);
-    if (!seg_row<K>(s, st, B, p + 1, p0, ra, rb, cx, X, width, bytes_per_row, writer,
-                    inside8, warp, lane, P, T, nf_hi0, c_lo0, nf_lo0, c_hi0, image,
-                    scr1_bytes, final_bytes, cand, cand_cap, counters, wide_list))
-      break;
+  // Pixel rows [p0, p1): the first PRO fill the windows and the history,
+  // then every row outputs one eroded row (two per pass, the loads of the
+  // next row prefetched into the other buffer).
+  const int p1 = r.rb + G::R1;
+  bool go = true;
+  for (int p = r.p0; go && p < r.p0 + G::PRO; p++) {
+    uint32_t v[16];
+    seg_load(r.image, height, width, interior, r.cx, p, v);
+    go = seg_row<K, false>(s, st, v, p, r, P, T);
   }
-  seg_flush<K>(s, warp, cand, counters, cand_cap);
+  if (go) {
+    uint32_t A[16], B[16];
+    int p = r.p0 + G::PRO;
+    seg_load(r.image, height, width, interior, r.cx, p, A);
+    for (; p < p1; p += 2) {
+      if (p + 1 < p1)
+        seg_load(r.image, height, width, interior, r.cx, p + 1, B);
+      if (!seg_row<K, true>(s, st, A, p, r, P, T))
+        break;
+      if (p + 1 >= p1)
+        break;
+      if (p + 2 < p1)
+        seg_load(r.image, height, width, interior, r.cx, p + 2, A);
+      if (!seg_row<K, true>(s, st, B, p + 1, r, P, T))
+        break;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Runs holding a pixel too large for the exact 32-bit sums: 32 x 32 tiles of
 // the eroded mask with 64-bit sums, for the columns [xb, xe) and rows
-// [yb, ye) a warp handed over.
+// [yb, ye) of the frame a warp handed over.
 // ---------------------------------------------------------------------------
 template <int K>
 __global__ void __launch_bounds__(256)
-stream_wide(const uint32_t *__restrict__ image, int height, int width, int run_rows,
-            const __grid_constant__ LaunchParams P, uint8_t *__restrict__ scr1_bytes,
-            uint8_t *__restrict__ final_bytes, uint32_t *__restrict__ cand,
-            uint32_t cand_cap, uint32_t *__restrict__ counters,
+stream_wide(const __grid_constant__ FramePtrs F, int height, int width, int run_rows,
+            const __grid_constant__ LaunchParams P, uint8_t *__restrict__ scr1_all,
+            uint8_t *__restrict__ final_all, size_t mask_bytes, uint32_t *__restrict__ counters,
             const uint4 *__restrict__ wide_list) {
   constexpr int E = K - 1, R1 = 2 * K - 1;
   constexpr int TS = 32, IW = TS + 2 * R1, S0 = IW - 2 * K;
@@ -397,7 +438,12 @@ stream_wide(const uint32_t *__restrict__ image, int height, int width, int run_r
   constexpr int TPS = (kSegOut + TS - 1) / TS;  // tile columns per entry
   const int TPR = (run_rows + TS - 1) / TS;      // tile rows per entry
   for (uint32_t item = blockIdx.x; item < nwide * TPS * TPR; item += gridDim.x) {
-    const uint4 w = wide_list[item / (TPS * TPR)];
+    const uint32_t k = item / (TPS * TPR);
+    const uint4 w = wide_list[2 * k];
+    const int f = (int)wide_list[2 * k + 1].x;
+    const uint32_t *image = F.image[f];
+    uint8_t *scr1_bytes = scr1_all + (size_t)f * mask_bytes;
+    uint8_t *final_bytes = final_all + (size_t)f * mask_bytes;
     const int rem = (int)(item % (TPS * TPR));
     const int tcol = rem % TPS, trow = rem / TPS;
     const int xb = (int)w.x, xe = (int)w.y, yb = (int)w.z, ye = (int)w.w;
@@ -458,151 +504,309 @@ stream_wide(const uint32_t *__restrict__ image, int height, int width, int run_r
       }
       const bool b = gy < ty1 && gx < min(xe, width) && m;
       const uint32_t word = __ballot_sync(0xffffffffu, b);
+      const unsigned cm = __ballot_sync(0xffffffffu, b && v < 0xFFFFFFFEu);
       if (gy < ty1 && lane < 4) {
         const int bx = tx0 + 8 * lane;
         if (bx < xe && (bx >> 3) < bytes_per_row) {
           scr1_bytes[(size_t)gy * bytes_per_row + (bx >> 3)] = (uint8_t)(word >> (8 * lane));
-          final_bytes[(size_t)gy * bytes_per_row + (bx >> 3)] = 0;
+          final_bytes[(size_t)gy * bytes_per_row + (bx >> 3)] = (uint8_t)(cm >> (8 * lane));
         }
       }
-      const bool cnd = b && v < 0xFFFFFFFEu && (uint64_t)v >= P.p_min;
-      const unsigned cm = __ballot_sync(0xffffffffu, cnd);
-      if (cm) {
-        uint32_t base = 0;
-        if (lane == 0)
-          base = atomicAdd(&counters[kCtrCand], (uint32_t)__popc(cm));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        const uint32_t g = base + __popc(cm & ((1u << lane) - 1u));
-        if (cnd && g < cand_cap)
-          cand[g] = (uint32_t)gy * (uint32_t)width + (uint32_t)gx;
-      }
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// Stage 2 at the candidates, four lanes to a candidate: each lane sums a
-// quarter of the (2K + 5) rows of the clipped window, two shuffles add them.
+// The candidate list: the set bits of the candidate mask (the final mask as
+// the first pass wrote it), ascending, from two scans over the mask words.
+// Every kernel below runs on a (block, frame) grid.
 // ---------------------------------------------------------------------------
-template <int K>
-__global__ void __launch_bounds__(256)
-seg_stage2(const uint32_t *__restrict__ image, int height, int width,
-           const __grid_constant__ LaunchParams P, const uint32_t *__restrict__ scr1_words,
-           uint32_t *__restrict__ final_words, const uint32_t *__restrict__ cand,
-           uint32_t cand_cap, uint32_t *__restrict__ counters,
-           sf_signal_pixel *__restrict__ staging, uint32_t capacity) {
-  constexpr int K2 = K + 2, WW = 2 * K2 + 1;
-  const int wpr = (width + 31) >> 5;
-  const uint32_t nc = min(counters[kCtrCand], cand_cap);
-  const int lane = threadIdx.x & 31, sub = lane & 3;
-  const uint32_t per_pass = (gridDim.x * blockDim.x) >> 2;
-  for (uint32_t base = (blockIdx.x * blockDim.x) >> 2; base < nc + 0; base += per_pass) {
-    const uint32_t i = base + (threadIdx.x >> 2);
-    const bool live = i < nc;
-    uint32_t idx = 0, p = 0, n = 0;
-    unsigned long long S = 0;
-    if (live) {
-      idx = cand[i];
-      const int y = (int)(idx / (uint32_t)width), x = (int)(idx % (uint32_t)width);
-      p = __ldg(image + idx);
-      const int xlo = max(0, x - K2), xhi = min(width - 1, x + K2);
-      const int w0 = xlo >> 5;
-      constexpr int ROWS = (WW + 3) / 4;  // rows per lane
-#pragma unroll
-      for (int k = 0; k < ROWS; k++) {
-        const int dy = -K2 + sub + 4 * k;
-        const int yy = y + dy;
-        if (dy > K2 || yy < 0 || yy >= height)
-          continue;
-        const uint32_t *row = image + (size_t)yy * width;
-        const uint32_t *brow = scr1_words + (size_t)yy * wpr;
-        const unsigned long long both =
-            (unsigned long long)__ldg(brow + w0) |
-            ((w0 + 1 < wpr) ? ((unsigned long long)__ldg(brow + w0 + 1) << 32) : 0ull);
-        const unsigned long long bgb = ~(both >> (xlo - (w0 << 5)));
-        uint32_t v[WW];
-#pragma unroll
-        for (int d = 0; d < WW; d++)
-          v[d] = (xlo + d <= xhi) ? __ldg(row + xlo + d) : 0u;
-#pragma unroll
-        for (int d = 0; d < WW; d++)
-          if (xlo + d <= xhi && ((bgb >> d) & 1ull)) {
-            // Not in the eroded mask, so valid (masked pixels are in it).
-            n++;
-            S += v[d];
-          }
-      }
-    }
-    n += __shfl_xor_sync(0xffffffffu, n, 1);
-    S += __shfl_xor_sync(0xffffffffu, S, 1);
-    n += __shfl_xor_sync(0xffffffffu, n, 2);
-    S += __shfl_xor_sync(0xffffffffu, S, 2);
-    bool sig = false;
-    sf_signal_pixel rec;
-    if (live && sub == 0) {
-      float bg;
-      sig = stage2_u32(p, n, S, P, &bg);
-      rec.index = idx;
-      rec.value = p;
-      rec.background = bg;
-      rec.population = (uint16_t)n;
-      rec.reserved = 0;
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, sig);
-    if (m) {
-      uint32_t b = 0;
-      if (lane == 0)
-        b = atomicAdd(&counters[kCtrTotal], (uint32_t)__popc(m));
-      b = __shfl_sync(0xffffffffu, b, 0);
-      if (sig) {
-        const uint32_t slot = b + __popc(m & ((1u << lane) - 1u));
-        if (slot < capacity)
-          staging[slot] = rec;
-        const uint32_t y = idx / (uint32_t)width, x = idx % (uint32_t)width;
-        atomicOr(&final_words[(size_t)y * wpr + (x >> 5)], 1u << (x & 31u));
-      }
-    }
-  }
+constexpr int kScanT = 1024;
+
+__device__ __forceinline__ void chunk_of(size_t n, uint32_t *lo, uint32_t *hi) {
+  const size_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  *lo = (uint32_t)min(n, (size_t)blockIdx.x * chunk);
+  *hi = (uint32_t)min(n, (size_t)*lo + chunk);
 }
 
-// ---------------------------------------------------------------------------
-// Ordering, one cooperative kernel with one block per SM: each block sums
-// the popcounts of its share of the final mask's words; after a grid-wide
-// barrier each block adds its predecessors' sums and writes the exclusive
-// prefix of every word it owns; after a second barrier every staged record is
-// scattered to its ascending position.
-// ---------------------------------------------------------------------------
-constexpr int kOrderThreads = 1024;
+// Sum of the block's predecessors' counts in its frame, and (block 0) the
+// frame's total.
+__device__ __forceinline__ uint32_t block_base(const uint32_t *__restrict__ block_sums,
+                                               uint32_t *total) {
+  __shared__ uint32_t s_base, s_total;
+  if (threadIdx.x < 32) {
+    const uint32_t *bs = block_sums + (size_t)blockIdx.y * gridDim.x;
+    uint32_t b = 0, t = 0;
+    for (uint32_t i = threadIdx.x; i < gridDim.x; i += 32) {
+      const uint32_t v = bs[i];
+      b += i < blockIdx.x ? v : 0u;
+      t += v;
+    }
+    for (int o = 16; o; o >>= 1) {
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+      t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    if (threadIdx.x == 0) {
+      s_base = b;
+      s_total = t;
+    }
+  }
+  __syncthreads();
+  *total = s_total;
+  return s_base;
+}
 
-__global__ void __launch_bounds__(kOrderThreads)
-order_coop(int width, const uint32_t *__restrict__ bits, uint32_t nwords,
-           uint32_t *__restrict__ prefix, uint32_t *__restrict__ block_sums,
-           const uint32_t *__restrict__ counters, uint32_t cand_cap,
-           const sf_signal_pixel *__restrict__ staging, uint32_t capacity,
-           sf_signal_pixel *__restrict__ out, uint32_t *__restrict__ count_out) {
-  cg::grid_group grid = cg::this_grid();
-  const uint32_t chunk = (nwords + gridDim.x - 1) / gridDim.x;
-  const uint32_t lo = min(nwords, blockIdx.x * chunk), hi = min(nwords, lo + chunk);
+// Popcounts of the block's share of a frame's mask words.
+__global__ void __launch_bounds__(kScanT)
+mask_sums(const uint32_t *__restrict__ bits_all, size_t words, uint32_t *__restrict__ block_sums) {
+  const uint32_t *bits = bits_all + (size_t)blockIdx.y * words;
+  uint32_t lo, hi;
+  chunk_of(words, &lo, &hi);
   uint32_t acc = 0;
   for (uint32_t w = lo + threadIdx.x; w < hi; w += blockDim.x)
     acc += __popc(bits[w]);
   uint32_t total;
   (void)block_exclusive_scan(acc, &total);
   if (threadIdx.x == 0)
-    block_sums[blockIdx.x] = total;
-  grid.sync();
-  __shared__ uint32_t s_base;
-  if (threadIdx.x < 32) {
-    uint32_t b = 0;
-    for (uint32_t i = threadIdx.x; i < blockIdx.x; i += 32)
-      b += block_sums[i];
-    for (int o = 16; o; o >>= 1)
-      b += __shfl_xor_sync(0xffffffffu, b, o);
-    if (threadIdx.x == 0)
-      s_base = b;
+    block_sums[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = total;
+}
+
+// The pixel index of every set bit of the block's share, in order.
+__global__ void __launch_bounds__(kScanT)
+mask_list(const uint32_t *__restrict__ bits_all, size_t words, int width,
+          const uint32_t *__restrict__ block_sums, uint32_t *__restrict__ cand_all,
+          uint32_t cand_cap, uint32_t *__restrict__ counters) {
+  const int f = blockIdx.y;
+  const uint32_t *bits = bits_all + (size_t)f * words;
+  uint32_t *cand = cand_all + (size_t)f * cand_cap;
+  uint32_t total;
+  uint32_t carry = block_base(block_sums, &total);
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand] = total;
+  const uint32_t wpr = ((uint32_t)width + 31u) >> 5;
+  uint32_t lo, hi;
+  chunk_of(words, &lo, &hi);
+  for (uint32_t base = lo; base < hi; base += blockDim.x) {
+    const uint32_t w = base + threadIdx.x;
+    uint32_t word = w < hi ? bits[w] : 0u;
+    uint32_t t;
+    uint32_t pos = carry + block_exclusive_scan(__popc(word), &t);
+    if (word) {
+      const uint32_t row = w / wpr;
+      const uint32_t first = row * (uint32_t)width + (w - row * wpr) * 32u;
+      while (word) {
+        const int b = __ffs(word) - 1;
+        word &= word - 1u;
+        if (pos < cand_cap)
+          cand[pos] = first + (uint32_t)b;
+        pos++;
+      }
+    }
+    carry += t;
   }
-  __syncthreads();
-  uint32_t carry = s_base;
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2 at the candidates, four lanes to a candidate: each lane sums a
+// quarter of the (2K + 5) rows of the clipped window, two shuffles add them.
+// Away from the frame's edges a lane reads a window row as four aligned
+// 16-byte loads (the 16 columns from the window's first column rounded down
+// to a multiple of 4) and the eroded-mask bits over them as a 64-bit pair,
+// every row's loads issued together. The result of candidate i goes to
+// res[i] (the background's bits; the population, and the pass bit at 16),
+// and a candidate that fails is cleared from the final mask.
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void s2_window(const uint32_t *__restrict__ image,
+                                          const uint32_t *__restrict__ scr1_words, int height,
+                                          int width, int wpr, int vec, int sub, int y, int x,
+                                          uint32_t *n_out, unsigned long long *S_out) {
+  constexpr int K2 = K + 2, WW = 2 * K2 + 1, ROWS = (WW + 3) / 4;
+  static_assert(WW + 3 <= 16, "a window row fits four aligned 16-byte loads");
+  uint32_t n = 0;
+  unsigned long long S = 0;
+  const int xa = (x - K2) & ~3;
+  if (vec && x - K2 >= 0 && xa + 16 <= width) {
+    const int off = (x - K2) - xa;
+    const int w0 = xa >> 5, sh = xa & 31;
+    const uint32_t win = ((1u << WW) - 1u) << off;
+    // Rows off the frame (or past the window) read a clamped row and count
+    // nothing.
+    uint32_t bgs[ROWS];
+    uint4 t[ROWS][4];
+#pragma unroll
+    for (int k = 0; k < ROWS; k++) {
+      const int dy = -K2 + sub + 4 * k;
+      const int yy = y + dy;
+      const bool in = dy <= K2 && yy >= 0 && yy < height;
+      const int yc = min(max(yy, 0), height - 1);
+      const uint4 *row = reinterpret_cast<const uint4 *>(image + (size_t)yc * width + xa);
+      const uint32_t *brow = scr1_words + (size_t)yc * wpr;
+      const uint32_t b0 = __ldg(brow + w0);
+      const uint32_t b1 = (w0 + 1 < wpr) ? __ldg(brow + w0 + 1) : 0u;
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        t[k][q] = __ldg(row + q);
+      const unsigned long long both = (unsigned long long)b0 | ((unsigned long long)b1 << 32);
+      bgs[k] = in ? (~(uint32_t)(both >> sh) & win) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < ROWS; k++) {
+      const uint32_t bg = bgs[k];
+      const uint32_t v[16] = {t[k][0].x, t[k][0].y, t[k][0].z, t[k][0].w,
+                              t[k][1].x, t[k][1].y, t[k][1].z, t[k][1].w,
+                              t[k][2].x, t[k][2].y, t[k][2].z, t[k][2].w,
+                              t[k][3].x, t[k][3].y, t[k][3].z, t[k][3].w};
+      // Not in the eroded mask, so valid (masked pixels are in it).
+      n += __popc(bg);
+#pragma unroll
+      for (int d = 0; d < 16; d++)
+        S += ((bg >> d) & 1u) ? v[d] : 0u;
+    }
+  } else {
+    const int xlo = max(0, x - K2), xhi = min(width - 1, x + K2);
+    const int w0 = xlo >> 5;
+#pragma unroll
+    for (int k = 0; k < ROWS; k++) {
+      const int dy = -K2 + sub + 4 * k;
+      const int yy = y + dy;
+      if (dy > K2 || yy < 0 || yy >= height)
+        continue;
+      const uint32_t *row = image + (size_t)yy * width;
+      const uint32_t *brow = scr1_words + (size_t)yy * wpr;
+      const unsigned long long both =
+          (unsigned long long)__ldg(brow + w0) |
+          ((w0 + 1 < wpr) ? ((unsigned long long)__ldg(brow + w0 + 1) << 32) : 0ull);
+      const unsigned long long bgb = ~(both >> (xlo - (w0 << 5)));
+#pragma unroll
+      for (int d = 0; d < WW; d++)
+        if (xlo + d <= xhi && ((bgb >> d) & 1ull)) {
+          n++;
+          S += __ldg(row + xlo + d);
+        }
+    }
+  }
+  *n_out = n;
+  *S_out = S;
+}
+
+template <int K>
+__global__ void __launch_bounds__(256)
+seg_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
+           const __grid_constant__ LaunchParams P, const uint32_t *__restrict__ scr1_all,
+           uint32_t *__restrict__ final_all, size_t words, const uint32_t *__restrict__ cand_all,
+           uint32_t cand_cap, const uint32_t *__restrict__ counters, uint2 *__restrict__ res_all) {
+  const int f = blockIdx.y;
+  const uint32_t *image = F.image[f];
+  const uint32_t *scr1_words = scr1_all + (size_t)f * words;
+  uint32_t *final_words = final_all + (size_t)f * words;
+  const uint32_t *cand = cand_all + (size_t)f * cand_cap;
+  uint2 *res = res_all + (size_t)f * cand_cap;
+  const int wpr = (width + 31) >> 5;
+  const uint32_t nc = min(counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand], cand_cap);
+  const int lane = threadIdx.x & 31, sub = lane & 3;
+  const uint32_t per_pass = (gridDim.x * blockDim.x) >> 2;
+  for (uint32_t base = (blockIdx.x * blockDim.x) >> 2; base < nc; base += per_pass) {
+    const uint32_t i = base + (threadIdx.x >> 2);
+    const bool live = i < nc;
+    uint32_t idx = 0, p = 0, n = 0;
+    unsigned long long S = 0;
+    int y = 0, x = 0;
+    if (live) {
+      idx = cand[i];
+      y = (int)(idx / (uint32_t)width);
+      x = (int)(idx - (uint32_t)y * (uint32_t)width);
+      p = __ldg(image + idx);
+      s2_window<K>(image, scr1_words, height, width, wpr, vec, sub, y, x, &n, &S);
+    }
+    n += __shfl_xor_sync(0xffffffffu, n, 1);
+    S += __shfl_xor_sync(0xffffffffu, S, 1);
+    n += __shfl_xor_sync(0xffffffffu, n, 2);
+    S += __shfl_xor_sync(0xffffffffu, S, 2);
+    if (live && sub == 0) {
+      float bg = 0.0f;
+      // dext.cc:205: only pixels above the global threshold are tested.
+      const bool sig = (uint64_t)p >= P.p_min && stage2_u32(p, n, S, P, &bg);
+      res[i] = make_uint2(__float_as_uint(bg), n | (sig ? 1u << 16 : 0u));
+      if (!sig)
+        atomicAnd(&final_words[(size_t)y * wpr + (x >> 5)], ~(1u << (x & 31)));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The ordered list: the passing candidates compacted in list order, which is
+// ascending pixel order (src/spots/dext.cc:212-220 emits in scan order).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kScanT)
+pass_sums(const uint2 *__restrict__ res_all, uint32_t cand_cap,
+          const uint32_t *__restrict__ counters, uint32_t *__restrict__ block_sums) {
+  const int f = blockIdx.y;
+  const uint2 *res = res_all + (size_t)f * cand_cap;
+  const uint32_t nc = min(counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand], cand_cap);
+  uint32_t lo, hi;
+  chunk_of(nc, &lo, &hi);
+  uint32_t acc = 0;
+  for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+    acc += (res[i].y >> 16) & 1u;
+  uint32_t total;
+  (void)block_exclusive_scan(acc, &total);
+  if (threadIdx.x == 0)
+    block_sums[(size_t)f * gridDim.x + blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanT)
+pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ cand_all,
+             uint32_t cand_cap, const uint2 *__restrict__ res_all,
+             const uint32_t *__restrict__ counters, const uint32_t *__restrict__ block_sums,
+             sf_signal_pixel *__restrict__ out_all, size_t out_stride, uint32_t capacity,
+             uint32_t *__restrict__ count_out) {
+  const int f = blockIdx.y;
+  const uint32_t *image = F.image[f];
+  const uint32_t *cand = cand_all + (size_t)f * cand_cap;
+  const uint2 *res = res_all + (size_t)f * cand_cap;
+  sf_signal_pixel *out = out_all + (size_t)f * out_stride;
+  const uint32_t ncand = counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand];
+  const uint32_t nc = min(ncand, cand_cap);
+  uint32_t total;
+  uint32_t carry = block_base(block_sums, &total);
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    // The signal found; all ones if the candidate list overflowed, as for a
+    // count above capacity (the list is then incomplete).
+    count_out[f] = ncand > cand_cap ? 0xFFFFFFFFu : total;
+  uint32_t lo, hi;
+  chunk_of(nc, &lo, &hi);
+  for (uint32_t base = lo; base < hi; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const uint2 r = i < hi ? res[i] : make_uint2(0u, 0u);
+    const uint32_t pass = (r.y >> 16) & 1u;
+    uint32_t t;
+    const uint32_t pos = carry + block_exclusive_scan(pass, &t);
+    if (pass && pos < capacity) {
+      const uint32_t idx = cand[i];
+      sf_signal_pixel rec;
+      rec.index = idx;
+      rec.value = __ldg(image + idx);
+      rec.background = __uint_as_float(r.x);
+      rec.population = (uint16_t)(r.y & 0xFFFFu);
+      rec.reserved = 0;
+      out[pos] = rec;
+    }
+    carry += t;
+  }
+}
+
+// Optional: per final-mask word, the list position of its first pixel.
+__global__ void __launch_bounds__(kScanT)
+mask_prefix(const uint32_t *__restrict__ bits_all, size_t words,
+            const uint32_t *__restrict__ block_sums, uint32_t *__restrict__ prefix_all) {
+  const int f = blockIdx.y;
+  const uint32_t *bits = bits_all + (size_t)f * words;
+  uint32_t *prefix = prefix_all + (size_t)f * words;
+  uint32_t total;
+  uint32_t carry = block_base(block_sums, &total);
+  uint32_t lo, hi;
+  chunk_of(words, &lo, &hi);
   for (uint32_t base = lo; base < hi; base += blockDim.x) {
     const uint32_t w = base + threadIdx.x;
     const uint32_t c = w < hi ? __popc(bits[w]) : 0u;
@@ -612,39 +816,54 @@ order_coop(int width, const uint32_t *__restrict__ bits, uint32_t nwords,
       prefix[w] = carry + e;
     carry += t;
   }
-  grid.sync();
-  const uint32_t found = counters[kCtrTotal];
-  if (blockIdx.x == 0 && threadIdx.x == 0)
-    // The signal found; all ones if the candidate list overflowed, as for a
-    // count above capacity (the list is then incomplete).
-    *count_out = counters[kCtrCand] > cand_cap ? 0xFFFFFFFFu : found;
-  const uint32_t n = min(found, capacity);
-  const int wpr = (width + 31) >> 5;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const sf_signal_pixel rec = staging[i];
-    const uint32_t y = rec.index / (uint32_t)width, x = rec.index % (uint32_t)width;
-    const size_t w = (size_t)y * wpr + (x >> 5);
-    const uint32_t dst = prefix[w] + __popc(bits[w] & ((1u << (x & 31u)) - 1u));
-    if (dst < capacity)
-      out[dst] = rec;
-  }
 }
 
 // ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
 
-static float round_down(double v) {
-  float f = (float)v;
-  if ((double)f > v)
-    f = nextafterf(f, -INFINITY);
-  return f;
+static int device_sms() {
+  static int cached = 0;
+  if (cached)
+    return cached;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      sms <= 0)
+    return 152;  // not cached: asked again once a device answers
+  cached = sms;
+  return cached;
 }
-static float round_up(double v) {
-  float f = (float)v;
-  if ((double)f < v)
-    f = nextafterf(f, INFINITY);
-  return f;
+
+// Blocks of the ordering kernels: about two per SM over the batch, never
+// more than kOrderMaxBlocks in all.
+constexpr int kOrderMaxBlocks = 1024;
+static int order_bpf(int nframes) {
+  const int want = (2 * device_sms() + nframes - 1) / nframes;
+  return std::max(1, std::min(want, kOrderMaxBlocks / nframes));
+}
+
+int stream_order_blocks() { return kOrderMaxBlocks; }
+
+size_t stream_wide_entries(int h, int w, int nframes) {
+  const size_t strips = (size_t)(w + kSegOut - 1) / kSegOut;
+  const size_t runs = (size_t)(h + kMinRunRows - 1) / kMinRunRows;
+  return (size_t)nframes * strips * runs;
+}
+
+SegGeometry seg_geometry(int h, int w, int nframes, int run_rows, int slots) {
+  SegGeometry g;
+  g.nstrips = (w + kSegOut - 1) / kSegOut;
+  if (run_rows <= 0) {
+    // As many runs as fit the resident warps in one wave: a second, partial
+    // wave would double the kernel's time.
+    const long long per = (long long)nframes * g.nstrips;
+    const long long nruns = std::max(1ll, (long long)slots / per);
+    run_rows = (int)((h + nruns - 1) / nruns);
+  }
+  g.run_rows = std::max(run_rows, kMinRunRows);
+  g.nruns = (h + g.run_rows - 1) / g.run_rows;
+  return g;
 }
 
 void make_stream_tables(const LaunchParams &P, StreamTables *T) {
@@ -660,90 +879,103 @@ void make_stream_tables(const LaunchParams &P, StreamTables *T) {
   T->narrow_max = std::min(by_pack, by_sq + 1);
   for (int n = 0; n <= kMaxN0; n++) {
     const bool testable = n >= 1 && (uint32_t)n >= P.min_local && n <= n0;
-    // c = n - 1 + sigma_b r_n with the reference's double r_n; the margins
-    // are 2^-14 relative on n, far above the ~2^-19 the float sums can err.
-    // The double sum itself may round, hence the 2^-40 widening.
-    const double c = testable ? (double)(n - 1) + (double)P.sigma_b_int * P.root[n] : 0.0;
-    T->c_lo[n] = testable ? round_down(c * (1.0 - 0x1p-40)) : 0.0f;
-    T->c_hi[n] = testable ? round_up(c * (1.0 + 0x1p-40)) : 0.0f;
-    T->nf_hi[n] = testable ? round_up((double)n * (1.0 + 1.0 / 16384.0)) : 0.0f;
-    // Untestable windows are never signal: nf_lo 0 keeps "surely" false.
-    T->nf_lo[n] = testable ? round_down((double)n * (1.0 - 1.0 / 16384.0)) : 0.0f;
+    // 2^8 (n - 1 + sigma_b r_n) bracketed from r_n's 2^-20 floor and ceiling.
+    const uint64_t sb = P.sigma_b_int;
+    const uint64_t lo = testable ? (sb * P.root_lo[n]) >> (kRootShift - kDecShift) : 0;
+    const uint64_t hi =
+        testable ? (sb * P.root_hi[n] + ((1ull << (kRootShift - kDecShift)) - 1)) >>
+                       (kRootShift - kDecShift)
+                 : 0;
+    const uint64_t base = testable ? (uint64_t)(n - 1) << kDecShift : 0;
+    T->clo[n] = (uint32_t)(base + lo);
+    T->chi[n] = (uint32_t)(base + hi);
+    // nk 0 makes every such window "surely not" (0 <= S (2^8 S + clo)).
+    T->nk[n] = testable ? (uint32_t)n << kDecShift : 0u;
   }
 }
 
-// One block per SM for the cooperative ordering kernel.
-static int order_blocks() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, order_coop, kOrderThreads, 0);
-    n = sms * (per > 0 ? 1 : 0);
-    if (n <= 0)
-      n = 1;
-    if (n > kScanBlocks)
-      n = kScanBlocks;
+template <int K> static int seg_slots() {
+  static int slots = 0;
+  if (!slots) {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, seg_stage01<K>, kSegWarps * 32,
+                                                  sizeof(SegSmem<K>));
+    slots = std::max(1, per) * kSegWarps * device_sms();
   }
-  return n;
+  return slots;
 }
 
 template <int K>
-static cudaError_t launch_stream_k(const uint32_t *image, int h, int w, const LaunchParams &P,
-                                   const StreamBuffers &b, cudaStream_t stream) {
+static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w,
+                                   const LaunchParams &P, const StreamBuffers &b, int run_rows,
+                                   cudaStream_t stream, const StreamMarks *marks) {
   using S = SegSmem<K>;
-  static bool configured = false;
-  cudaError_t e;
-  if (!configured) {
-    e = cudaFuncSetAttribute(seg_stage01<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(S));
-    if (e != cudaSuccess)
-      return e;
-    configured = true;
-  }
+  static std::once_flag configured;
+  static cudaError_t config_error = cudaSuccess;
+  std::call_once(configured, [] {
+    config_error = cudaFuncSetAttribute(
+        seg_stage01<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(S));
+  });
+  if (config_error != cudaSuccess)
+    return config_error;
   StreamTables T;
   make_stream_tables(P, &T);
-  const int vec = (w % 4 == 0 && reinterpret_cast<uintptr_t>(image) % 16 == 0) ? 1 : 0;
-  const SegGeometry g = seg_geometry(h, w);
-  const int warps = g.nstrips * g.nruns;
+  int vec = w % 4 == 0 ? 1 : 0;
+  for (int f = 0; f < nframes; f++)
+    if (reinterpret_cast<uintptr_t>(F.image[f]) % 16 != 0)
+      vec = 0;
+  const SegGeometry g = seg_geometry(h, w, nframes, run_rows, seg_slots<K>());
+  const long long warps = (long long)nframes * g.nstrips * g.nruns;
+  const size_t mask_bytes = b.words * sizeof(uint32_t);
   uint8_t *scr1 = reinterpret_cast<uint8_t *>(b.scr1);
   uint8_t *fin = reinterpret_cast<uint8_t *>(b.bits);
-  seg_stage01<K><<<(warps + kSegWarps - 1) / kSegWarps, kSegWarps * 32, sizeof(S), stream>>>(
-      image, h, w, vec, g.nstrips, g.nruns, g.run_rows, P, T, scr1, fin, b.cand, b.cand_cap,
-      b.counters, b.wide);
-  stream_wide<K><<<2 * 152, 256, 0, stream>>>(image, h, w, g.run_rows, P, scr1, fin, b.cand,
-                                               b.cand_cap, b.counters, b.wide);
-  seg_stage2<K><<<8 * 152, 256, 0, stream>>>(image, h, w, P, b.scr1, b.bits, b.cand,
-                                              b.cand_cap, b.counters, b.staging, b.capacity);
-  uint32_t nwords = (uint32_t)(((size_t)w + 31) / 32 * h);
-  int width = w;
-  uint32_t cand_cap = b.cand_cap, capacity = b.capacity;
-  const uint32_t *bits_c = b.bits;
-  const uint32_t *counters_c = b.counters;
-  const sf_signal_pixel *staging_c = b.staging;
-  void *args[] = {&width,    &bits_c,    &nwords,    (void *)&b.prefix, (void *)&b.block_sums,
-                  &counters_c, &cand_cap, &staging_c, &capacity,         (void *)&b.out,
-                  (void *)&b.count_out};
-  e = cudaLaunchCooperativeKernel((void *)order_coop, dim3(order_blocks()), dim3(kOrderThreads),
-                                  args, 0, stream);
-  if (e != cudaSuccess)
-    return e;
+  const int sms = device_sms();
+  seg_stage01<K><<<(unsigned)((warps + kSegWarps - 1) / kSegWarps), kSegWarps * 32, sizeof(S),
+                   stream>>>(F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, P, T, scr1,
+                             fin, mask_bytes, b.counters, b.wide);
+  stream_wide<K><<<2 * sms, 256, 0, stream>>>(F, h, w, g.run_rows, P, scr1, fin, mask_bytes,
+                                               b.counters, b.wide);
+  if (marks)
+    cudaEventRecord(marks->stage01, stream);
+  const dim3 og((unsigned)order_bpf(nframes), (unsigned)nframes);
+  mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
+  mask_list<<<og, kScanT, 0, stream>>>(b.bits, b.words, w, b.block_sums, b.cand, b.cand_cap,
+                                       b.counters);
+  const unsigned s2x = (unsigned)std::max(1, (8 * sms + nframes - 1) / nframes);
+  seg_stage2<K><<<dim3(s2x, nframes), 256, 0, stream>>>(F, h, w, vec, P, b.scr1, b.bits, b.words,
+                                                        b.cand, b.cand_cap, b.counters, b.res);
+  if (marks)
+    cudaEventRecord(marks->stage2, stream);
+  pass_sums<<<og, kScanT, 0, stream>>>(b.res, b.cand_cap, b.counters, b.block_sums);
+  pass_scatter<<<og, kScanT, 0, stream>>>(F, b.cand, b.cand_cap, b.res, b.counters, b.block_sums,
+                                          b.out, b.out_stride, b.capacity, b.count_out);
+  if (b.prefix) {
+    mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
+    mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.prefix);
+  }
+  if (marks)
+    cudaEventRecord(marks->order, stream);
   return cudaGetLastError();
 }
 
-cudaError_t launch_stream(const uint32_t *image, int h, int w, const LaunchParams &P,
-                          const StreamBuffers &b, cudaStream_t stream) {
-  cudaError_t e = cudaMemsetAsync(b.counters, 0, kCtrCount * sizeof(uint32_t), stream);
+cudaError_t launch_stream(const FramePtrs &F, int nframes, int h, int w, const LaunchParams &P,
+                          const StreamBuffers &b, int run_rows, cudaStream_t stream,
+                          const StreamMarks *marks) {
+  if (nframes < 1 || nframes > kMaxBatch)
+    return cudaErrorInvalidValue;
+  if (marks)
+    cudaEventRecord(marks->start, stream);
+  cudaError_t e =
+      cudaMemsetAsync(b.counters, 0, counter_words(nframes) * sizeof(uint32_t), stream);
   if (e != cudaSuccess)
     return e;
   switch (P.half) {
   case 2:
-    return launch_stream_k<2>(image, h, w, P, b, stream);
+    return launch_stream_k<2>(F, nframes, h, w, P, b, run_rows, stream, marks);
   case 3:
-    return launch_stream_k<3>(image, h, w, P, b, stream);
+    return launch_stream_k<3>(F, nframes, h, w, P, b, run_rows, stream, marks);
   case 4:
-    return launch_stream_k<4>(image, h, w, P, b, stream);
+    return launch_stream_k<4>(F, nframes, h, w, P, b, run_rows, stream, marks);
   default:
     return cudaErrorInvalidValue;
   }

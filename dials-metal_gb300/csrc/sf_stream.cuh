@@ -1,84 +1,92 @@
-// Internal interface of the streaming threshold (sf_stream.cu).
+// Internal interface of the streaming threshold (sf_stream.cu): 32-bit
+// frames, dispersion_extended, gain 1 and integral sigmas, one frame or a
+// batch of same-shaped frames per launch sequence.
 //
-// The float decision of the dispersion test. With exact n, S (integers) and
-// Q~ = the float sum of the window's p^2 (13 roundings of non-negative terms
-// at most, so Q~ = Q (1 + e), |e| <= 13 u, u = 2^-24), the reference's test
-// at gain 1 and integral sigma_b is A > RN(X) with A = nQ - S(S + n - 1)
-// exact and X = S sigma_b r_n (the reference's double r_n). Writing
-// c = n - 1 + sigma_b r_n, A - X = nQ - S(S + c). Tables per n give floats
-// nf_hi >= n (1 + 2^-14), nf_lo <= n (1 - 2^-14) and c_lo <= c <= c_hi.
-//   RN(nf_hi Q~) <= RN(S~ RN(S~ + c_lo))     =>  nQ <= S(S + c): not signal
-//   RN(nf_lo Q~) >= RN(RN(1.0001 RN(S~ RN(S~ + c_hi))) + 2)
-//                                            =>  nQ >= S(S + c) + 1: signal
-// (the 2^-14 and 1.0001 margins exceed the few-u float errors by orders of
-// magnitude). Anything else is decided exactly. The packed sums (count above
-// a 27-, 26- or 25-bit sum for K = 2, 3, 4) hold while every valid pixel is
-// below 2^bits / n_max, which also keeps nQ < 2^53 and S^2 < 2^52, where the
-// reference's double left side is exactly A.
+// The stage-0 decision from exact 32-bit window sums. With gain 1 and an
+// integral sigma_b the reference's test (src/spots/dext.cc:99-109) is
+// A > RN(X), A = nQ - S(S + n - 1) exact in double and X = S sigma_b r_n
+// (r_n the reference's double sqrt(2 (n - 1))). Writing c = n - 1 +
+// sigma_b r_n, A - X = nQ - S(S + c). Per window count n the host gives two
+// integers in 2^-8 units, clo <= 2^8 c <= chi (from the 2^-20 brackets of
+// r_n), and nk = 2^8 n (0 when n cannot be tested):
+//   2^8 n Q <= S (2^8 S + clo)           =>  A <= X: not signal
+//   2^8 n Q >= S (2^8 S + chi) + 2^9     =>  A >= X + 2 > RN(X): signal
+// both exact in 64-bit integers. The thin band between goes to the exact
+// decision of sf_common.cuh. The packed sums (the window's masked-pixel count
+// above a 27-, 26- or 25-bit sum for K = 2, 3, 4) and the 32-bit sum of
+// squares hold while every valid pixel is below narrow_max; a run holding a
+// larger valid pixel is handed to a 64-bit path.
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "sf_common.cuh"
 
 namespace sf {
 
-// Counter words at the start of the stream workspace.
-enum {
-  kCtrTotal = 0,  // signal pixels found
-  kCtrCand,       // candidates found
-  kCtrWide,       // runs handed to the 64-bit path
-  kCtrCount = 8
+// Frames one launch sequence takes.
+constexpr int kMaxBatch = 64;
+
+struct FramePtrs {
+  const uint32_t *image[kMaxBatch];
 };
 
-// Strips of 240 output columns (one warp each) by runs of rows: as many runs
-// as fill the GPU once (3 blocks of 4 warps on each of 152 SMs), each at least
-// 16 rows.
+// Counter words: the batch's own first, then kCtrCount per frame.
+enum {
+  kCtrWide = 0,   // batch: runs handed to the 64-bit path
+  kCtrBatch = 4,  // first frame's counters
+  kCtrCand = 0,   // frame: candidates (set bits of the candidate mask)
+  kCtrCount = 4
+};
+inline size_t counter_words(int nframes) { return kCtrBatch + (size_t)nframes * kCtrCount; }
+
+// Strips of 240 output columns (one warp each) by runs of run_rows rows.
 struct SegGeometry {
   int nstrips, nruns, run_rows;
 };
-inline SegGeometry seg_geometry(int h, int w) {
-  SegGeometry g;
-  g.nstrips = (w + 239) / 240;
-  const int target = 1800;
-  int nruns = (target + g.nstrips - 1) / g.nstrips;
-  g.run_rows = (h + nruns - 1) / nruns;
-  if (g.run_rows < 16)
-    g.run_rows = 16;
-  g.nruns = (h + g.run_rows - 1) / g.run_rows;
-  return g;
-}
+// run_rows 0 picks runs that fill `slots` warps once.
+SegGeometry seg_geometry(int h, int w, int nframes, int run_rows, int slots);
+constexpr int kMinRunRows = 16;
 
 struct StreamTables {
   uint32_t narrow_max;  // valid pixels at or above this take the 64-bit path
-  float nf_hi[kMaxN0 + 1], nf_lo[kMaxN0 + 1], c_lo[kMaxN0 + 1], c_hi[kMaxN0 + 1];
+  uint32_t nk[kMaxN0 + 1], clo[kMaxN0 + 1], chi[kMaxN0 + 1];
 };
 
 struct StreamBuffers {
-  uint32_t *bits;         // final strong mask (output)
-  uint32_t *scr1;         // eroded mask
-  uint32_t *prefix;       // per-word exclusive popcount prefix (maybe output)
-  uint32_t *cand;         // candidate pixel indices
+  uint32_t *bits;          // final strong masks (output), frame f at bits + f * words
+  uint32_t *scr1;          // eroded masks, same layout
+  uint32_t *prefix;        // per-word list positions (output) or null
+  size_t words;            // mask words per frame
+  uint32_t *cand;          // ascending candidate indices, frame f at cand + f * cand_cap
+  uint2 *res;              // stage-2 result per candidate, same layout
   uint32_t cand_cap;
-  uint32_t *counters;     // kCtrCount words
-  uint4 *wide;            // handed-over runs
-  uint32_t *block_sums;   // per-block sums of the ordering kernel
-  sf_signal_pixel *staging;
-  sf_signal_pixel *out;   // ascending list (output)
+  uint32_t *counters;      // counter_words(nframes)
+  uint4 *wide;             // handed-over runs, two uint4 each
+  uint32_t *block_sums;    // per-block sums of the scan kernels
   uint32_t capacity;
-  uint32_t *count_out;    // the caller's count word
+  sf_signal_pixel *out;    // ascending lists (output), frame f at out + f * out_stride
+  size_t out_stride;
+  uint32_t *count_out;     // one count per frame
 };
 
-inline int stream_units(int h, int w) {
-  const SegGeometry g = seg_geometry(h, w);
-  return g.nstrips * g.nruns;
-}
-
+// Wide-list entries a batch may need (every run hands over at most once).
+size_t stream_wide_entries(int h, int w, int nframes);
+// Blocks of the ordering kernel (the size of block_sums).
+int stream_order_blocks();
 
 void make_stream_tables(const LaunchParams &P, StreamTables *T);
 
-cudaError_t launch_stream(const uint32_t *image, int h, int w, const LaunchParams &P,
-                          const StreamBuffers &b, cudaStream_t stream);
+// Events recorded on the stream between the kernel groups when profiling.
+struct StreamMarks {
+  cudaEvent_t start, stage01, stage2, order;
+};
+
+// run_rows 0: the default geometry. marks may be null.
+cudaError_t launch_stream(const FramePtrs &frames, int nframes, int h, int w,
+                          const LaunchParams &P, const StreamBuffers &b, int run_rows,
+                          cudaStream_t stream, const StreamMarks *marks = nullptr);
 
 } // namespace sf

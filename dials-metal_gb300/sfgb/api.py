@@ -102,6 +102,12 @@ def lib() -> ctypes.CDLL:
             getattr(L, name).argtypes = [vp, sz, sz, ctypes.POINTER(ThresholdParams), vp,
                                          sz, u32p, u32p, u32p, vp, sz, vp]
             getattr(L, name).restype = ctypes.c_int
+        L.sf_batch_workspace_bytes.argtypes = [sz, sz, sz, sz]
+        L.sf_batch_workspace_bytes.restype = sz
+        for name in ("sf_threshold_u32_batch_device", "sf_threshold_u16_batch_device"):
+            getattr(L, name).argtypes = [vp, sz, sz, sz, ctypes.POINTER(ThresholdParams), vp,
+                                         sz, u32p, u32p, u32p, vp, sz, vp]
+            getattr(L, name).restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -233,6 +239,86 @@ class DeviceThreshold:
     def mask(self) -> np.ndarray:
         """The strong-pixel mask as booleans (h, w) (host copy)."""
         words = self.bits.cpu().numpy().view(np.uint32).reshape(self.h, self.words_per_row)
+        bits = np.unpackbits(words.view(np.uint8).reshape(self.h, -1), axis=1,
+                             bitorder="little")
+        return bits[:, : self.w].astype(bool)
+
+
+MAX_BATCH = 64
+
+
+class DeviceBatch:
+    """Batched device threshold (sf_threshold_*_batch_device): up to
+    MAX_BATCH same-shaped frames already in HBM per call, one launch
+    sequence, each frame's list, mask and count as a single-frame call gives.
+    """
+
+    def __init__(self, height: int, width: int, max_frames: int,
+                 capacity: int | None = None, params: Params | None = None,
+                 word_prefix: bool = False):
+        import torch
+        if not 1 <= max_frames <= MAX_BATCH:
+            raise ValueError(f"1 to {MAX_BATCH} frames per batch")
+        self.h, self.w, self.n = height, width, max_frames
+        self.capacity = capacity if capacity is not None else max(1, height * width // 4)
+        self.params = (params or Params()).c()
+        dev = torch.device("cuda")
+        self.words_per_row = (width + 31) // 32
+        self.words = self.words_per_row * height
+        self.out = torch.empty((max_frames, self.capacity * 16), dtype=torch.uint8, device=dev)
+        self.bits = torch.empty((max_frames, self.words), dtype=torch.int32, device=dev)
+        self.counts = torch.zeros(max_frames, dtype=torch.int32, device=dev)
+        self.word_prefix = (torch.empty((max_frames, self.words), dtype=torch.int32,
+                                        device=dev) if word_prefix else None)
+        nbytes = lib().sf_batch_workspace_bytes(max_frames, height, width, self.capacity)
+        if nbytes == 0:
+            raise ValueError("frame shape or batch size rejected")
+        self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        self._ptrs = (ctypes.c_void_p * MAX_BATCH)()
+        self.last = 0
+
+    def __call__(self, frames, stream=None) -> None:
+        """frames: a sequence of contiguous (h, w) CUDA tensors, or one
+        (n, h, w) tensor; all 32-bit or all 16-bit."""
+        import torch
+        frames = list(frames)
+        if not 1 <= len(frames) <= self.n:
+            raise ValueError(f"1 to {self.n} frames")
+        dt = frames[0].dtype
+        for f in frames:
+            if f.device.type != "cuda" or not f.is_contiguous() or f.dtype != dt:
+                raise ValueError("contiguous CUDA tensors of one dtype")
+            if tuple(f.shape) != (self.h, self.w):
+                raise ValueError("frame shape differs from this batch's")
+        for j, f in enumerate(frames):
+            self._ptrs[j] = f.data_ptr()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        L = lib()
+        if dt in (torch.int32, torch.uint32):
+            fn = L.sf_threshold_u32_batch_device
+        elif dt in (torch.int16, torch.uint16):
+            fn = L.sf_threshold_u16_batch_device
+        else:
+            raise TypeError("frames are 16- or 32-bit")
+        rc = fn(ctypes.cast(self._ptrs, ctypes.c_void_p), len(frames), self.h, self.w,
+                ctypes.byref(self.params), self.out.data_ptr(), self.capacity,
+                self.bits.data_ptr(), self.counts.data_ptr(),
+                self.word_prefix.data_ptr() if self.word_prefix is not None else None,
+                self.workspace.data_ptr(), self.workspace.numel(), s.cuda_stream)
+        _check(rc, "batched device threshold")
+        self.last = len(frames)
+
+    def result(self, j: int) -> np.ndarray:
+        """Synchronise and return frame j's signal list (host copy)."""
+        import torch
+        torch.cuda.current_stream().synchronize()
+        n = int(self.counts[j].item()) & 0xffffffff
+        if n > self.capacity:
+            raise OverflowError_(f"{n} signal pixels, capacity {self.capacity}")
+        return self.out[j, : n * 16].cpu().numpy().view(SIGNAL_DTYPE).copy()
+
+    def mask(self, j: int) -> np.ndarray:
+        words = self.bits[j].cpu().numpy().view(np.uint32).reshape(self.h, self.words_per_row)
         bits = np.unpackbits(words.view(np.uint8).reshape(self.h, -1), axis=1,
                              bitorder="little")
         return bits[:, : self.w].astype(bool)

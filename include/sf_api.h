@@ -101,9 +101,12 @@ int sf_find_u16_params(const uint16_t *image, size_t height, size_t width,
 
 /* Replaces gpu::profile_stages / gpu::last_stage_times
  * (src/spots/dext_gpu.hh:89-127). Times in milliseconds for the calling
- * thread's last profiled frame: upload, the fused threshold (reported as
- * `fused`), copy (list read-back). stage0/1/2 and sort stay 0: the stages
- * run as one kernel and the list arrives sorted. */
+ * thread's last profiled call (host frame, device frame or batch, all its
+ * frames): upload (host-frame calls), `fused` (the whole threshold), copy
+ * (list read-back). On the 32-bit dispersion_extended path also stage0
+ * (stage 0 and the erosion, one kernel: the reference's stage0 + stage1),
+ * stage2 and sort (ordering the list); stage1 stays 0. A device call's
+ * times are read when sf_last_stage_times is called, which waits for it. */
 typedef struct {
   double upload, stage0, stage1, stage2, fused, copy, sort;
 } sf_stage_times;
@@ -138,6 +141,36 @@ int sf_threshold_u16_device(const uint16_t *d_image, size_t height,
                             uint32_t *d_bits, uint32_t *d_count,
                             uint32_t *d_word_prefix, void *d_workspace,
                             size_t workspace_bytes, void *stream);
+
+/*
+ * Batched device threshold (no reference counterpart; the reference's -j
+ * workers run one frame per call, src/apps/find_spots.cc:760-833): up to
+ * SF_MAX_BATCH same-shaped frames in one launch sequence, with the results
+ * of each frame equal to a single-frame call on it.
+ *   d_images     host array of n_frames device pointers (16-byte aligned
+ *                frames read as 128-bit rows; others work, slower)
+ *   d_out        n_frames * capacity records: frame j's list at j * capacity
+ *   d_bits       n_frames * ceil(width/32) * height words, frame after frame
+ *   d_counts     n_frames uint32 counts
+ *   d_word_prefix optional (NULL): n_frames * the words of one mask
+ *   d_workspace  sf_batch_workspace_bytes(n_frames, height, width, capacity)
+ * sf_batch_workspace_bytes returns 0 for a shape or batch size it refuses.
+ */
+#define SF_MAX_BATCH 64
+size_t sf_batch_workspace_bytes(size_t n_frames, size_t height, size_t width,
+                                size_t capacity);
+int sf_threshold_u32_batch_device(const uint32_t *const *d_images, size_t n_frames,
+                                  size_t height, size_t width,
+                                  const sf_threshold_params *params, sf_signal_pixel *d_out,
+                                  size_t capacity, uint32_t *d_bits, uint32_t *d_counts,
+                                  uint32_t *d_word_prefix, void *d_workspace,
+                                  size_t workspace_bytes, void *stream);
+int sf_threshold_u16_batch_device(const uint16_t *const *d_images, size_t n_frames,
+                                  size_t height, size_t width,
+                                  const sf_threshold_params *params, sf_signal_pixel *d_out,
+                                  size_t capacity, uint32_t *d_bits, uint32_t *d_counts,
+                                  uint32_t *d_word_prefix, void *d_workspace,
+                                  size_t workspace_bytes, void *stream);
 
 /* ---- 3-D spot labelling (src/spots/dials_spots.hh) ---- */
 
