@@ -53,12 +53,13 @@ constexpr int kDecShift = 8;
 // prefetched), takes its 8 row sums of 2K+1 columns in registers (masked
 // count and sum packed as m << PS | S, exact; p^2 exact in 32 bits), and
 // carries 8 column sums down in registers; the row sum leaving the window
-// comes back from a small per-lane ring in shared memory. A lane whose 8 + 2K
-// pixels are all valid and small (nearly all of them) packs nothing: its
-// masked count is 0. Each new stage-0 row gives 8 decisions (sf_stream.cuh)
-// from two 64-bit bounds per window without a branch (windows with masked
-// pixels read their constants from a small table); the rare windows between
-// the bounds are decided exactly, out of line. The decisions are kept as
+// comes back from a small per-lane ring in shared memory. Each new stage-0
+// row gives 8 decisions (sf_stream.cuh) from two 64-bit bounds per window,
+// with the constants for the window's masked count from a small table; the
+// rare windows between the bounds are decided exactly, out of line. The
+// common path has no divergent branch: on this SIMT machine a rarely taken
+// per-lane branch still costs the whole warp its schedule, so masked pixels
+// are folded in by selects rather than a separate path. The decisions are kept as
 // 8-bit chunks in a 64-bit history; the erosion ANDs
 // 2E+1 chunks vertically, then across columns with the neighbouring lanes'
 // chunks (two shuffles). Lanes 0 and 31 are halo: they feed their
@@ -129,7 +130,6 @@ struct SegRun {
   int X, cx, ra, rb, p0, warp, lane;
   bool writer;
   uint32_t inside8;
-  uint32_t nk0, clo0, chi0;  // decision constants of full windows
 };
 
 // The exact decision for the thin band neither bound settles. Out of line:
@@ -169,38 +169,34 @@ __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const ui
   constexpr int NP = 8 + 2 * K;
   const uint32_t narrow = T.narrow_max;
 
-  // The pixels the row sums use, as masked-count << PS | value and value^2.
-  uint32_t m4[4];
+  // The pixels the row sums use, as masked-count << PS | value and value^2,
+  // without a branch: u = v + 2 sends the masked sentinels to 0 and 1, a
+  // masked pixel packs as a count bit alone, and its square (2^PS)^2 wraps
+  // to 0. A valid pixel at or above narrow_max hands the run over.
+  uint32_t ns[16], q[16], valid8 = 0;
+  bool wide;
+  {
+    uint32_t u[16];
 #pragma unroll
-  for (int j = 0; j < 4; j++) {
-    uint32_t a = 0;
+    for (int i = o; i < o + NP; i++)
+      u[i] = raw[i] + 2u;
+    uint32_t m4[4];
 #pragma unroll
-    for (int i = o + j; i < o + NP; i += 4)
-      a = max(a, raw[i]);
-    m4[j] = a;
-  }
-  const uint32_t mx = max(max(m4[0], m4[1]), max(m4[2], m4[3]));
-  uint32_t ns[16], q[16], valid8;
-  bool wide = false;
-  if (mx < narrow) {
-    // All valid and small (nearly every lane): no masked pixel to count.
+    for (int j = 0; j < 4; j++) {
+      uint32_t a = 0;
 #pragma unroll
-    for (int i = o; i < o + NP; i++) {
-      ns[i] = raw[i];
-      q[i] = raw[i] * raw[i];
+      for (int i = o + j; i < o + NP; i += 4)
+        a = max(a, u[i]);
+      m4[j] = a;
     }
-    valid8 = 0xFFu;
-  } else {
-    valid8 = 0;
+    wide = max(max(m4[0], m4[1]), max(m4[2], m4[3])) >= narrow + 2u;
 #pragma unroll
     for (int i = o; i < o + NP; i++) {
-      const uint32_t v = raw[i];
-      const bool small = v < narrow;
-      wide |= !small && v < 0xFFFFFFFEu;
-      ns[i] = small ? v : (1u << G::PS);
-      q[i] = small ? v * v : 0u;
-      if (i >= 4 && i < 12)
-        valid8 |= (v < 0xFFFFFFFEu ? 1u : 0u) << (i - 4);
+      const bool ok = u[i] >= 2u;
+      ns[i] = ok ? raw[i] : (1u << G::PS);
+      q[i] = ns[i] * ns[i];
+      if (i >= 4 && i < 12 && ok)
+        valid8 |= 1u << (i - 4);
     }
   }
   if (__any_sync(0xffffffffu, wide)) {
@@ -258,29 +254,20 @@ __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const ui
   if (!kSteady && p < r.p0 + 2 * K)
     return true;  // the column sums are not yet full windows (warp-uniform)
 
-  // Stage-0 row p - K: eight decisions, maybe/sure bits without branches;
-  // masked pixels are set.
+  // Stage-0 row p - K: eight decisions, maybe/sure bits without a branch
+  // (the constants by masked count come from a small table; nearly every
+  // lane reads the same entry); masked pixels are set.
   const uint32_t vrow = (uint32_t)(st.hval >> (8 * K)) & 0xFFu;
   uint32_t maybe8 = 0, sure8 = 0;
-  const uint32_t any_masked = (st.vns[0] | st.vns[1] | st.vns[2] | st.vns[3] | st.vns[4] |
-                               st.vns[5] | st.vns[6] | st.vns[7]) >> G::PS;
-  if (any_masked == 0) {
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-      bool mb, su;
-      seg_bounds(st.vns[c], st.vq[c], r.nk0, r.clo0, r.chi0, &mb, &su);
-      maybe8 |= mb ? 1u << c : 0u;
-      sure8 |= su ? 1u << c : 0u;
-    }
-  } else {
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-      const uint4 t = s.tab[st.vns[c] >> G::PS];
-      bool mb, su;
-      seg_bounds(st.vns[c] & G::MASK, st.vq[c], t.x, t.y, t.z, &mb, &su);
-      maybe8 |= mb ? 1u << c : 0u;
-      sure8 |= su ? 1u << c : 0u;
-    }
+  for (int c = 0; c < 8; c++) {
+    // The masked count is at most N0 by construction; the clamp keeps the
+    // table read in bounds whatever the sums hold.
+    const uint4 t = s.tab[min(st.vns[c] >> G::PS, (uint32_t)G::N0)];
+    bool mb, su;
+    seg_bounds(st.vns[c] & G::MASK, st.vq[c], t.x, t.y, t.z, &mb, &su);
+    maybe8 |= mb ? 1u << c : 0u;
+    sure8 |= su ? 1u << c : 0u;
   }
   uint32_t s8 = (~vrow | sure8) & 0xFFu;
   const uint32_t amb8 = maybe8 & ~sure8 & vrow;
@@ -289,7 +276,8 @@ __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const ui
     for (int c = 0; c < 8; c++) {
       const uint32_t x = st.vns[c];
       if (((amb8 >> c) & 1u) &&
-          seg_exact((uint32_t)G::N0 - (x >> G::PS), x & G::MASK, st.vq[c], P))
+          seg_exact((uint32_t)G::N0 - min(x >> G::PS, (uint32_t)G::N0), x & G::MASK,
+                    st.vq[c], P))
         s8 |= 1u << c;
     }
   }
@@ -362,9 +350,6 @@ seg_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
   r.writer = lane >= 1 && lane <= 30 && r.cx < r.bytes_per_row * 8;
   // Bits of this lane's columns that lie inside the frame.
   r.inside8 = r.cx >= width ? 0u : (r.cx + 8 <= width ? 0xFFu : ((1u << (width - r.cx)) - 1u));
-  r.nk0 = T.nk[G::N0];
-  r.clo0 = T.clo[G::N0];
-  r.chi0 = T.chi[G::N0];
   const bool interior = vec && r.cx - 4 >= 0 && r.cx + 12 <= width;
 
 #pragma unroll
