@@ -128,7 +128,7 @@ int make_launch_params(const sf_threshold_params *in, LaunchParams *P) {
 // frames, dispersion_extended, gain 1 and integral sigmas; one frame or a
 // batch) and the tile path (everything else, one frame at a time).
 struct WorkspaceLayout {
-  size_t staging, cand, res, scr1, wide, counters, block_sums, tile_base, row_total, total;
+  size_t staging, cand, res, scr1, amb, wide, counters, block_sums, tile_base, row_total, total;
   size_t cand_cap, words;
 };
 
@@ -148,6 +148,7 @@ static WorkspaceLayout layout(size_t h, size_t w, size_t capacity, size_t nframe
   L.cand = take(nframes * L.cand_cap * sizeof(uint32_t));
   L.res = take(nframes * L.cand_cap * sizeof(uint2));
   L.scr1 = take(nframes * L.words * sizeof(uint32_t));
+  L.amb = take(nframes * L.words * sizeof(uint32_t));
   L.wide = take(stream_wide_entries((int)h, (int)w, (int)nframes) * 2 * sizeof(uint4));
   L.counters = take(counter_words((int)nframes) * sizeof(uint32_t));
   L.block_sums = take((size_t)std::max(kScanBlocks, stream_order_blocks()) * sizeof(uint32_t));
@@ -197,6 +198,7 @@ static int threshold_frames(const T *const *d_images, size_t n, size_t h, size_t
     b.bits = d_bits;
     b.words = L.words;
     b.scr1 = reinterpret_cast<uint32_t *>(ws + L.scr1);
+    b.amb = reinterpret_cast<uint32_t *>(ws + L.amb);
     b.prefix = d_word_prefix;
     b.cand = reinterpret_cast<uint32_t *>(ws + L.cand);
     b.res = reinterpret_cast<uint2 *>(ws + L.res);

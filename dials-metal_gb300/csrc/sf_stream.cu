@@ -25,6 +25,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <mutex>
 
@@ -123,7 +124,7 @@ __device__ __forceinline__ void seg_load(const uint32_t *__restrict__ image, int
 // What one warp's run writes to, resolved once per warp.
 struct SegRun {
   const uint32_t *image;
-  uint8_t *scr1_bytes, *final_bytes;
+  uint8_t *scr1_bytes, *final_bytes, *amb_bytes;
   uint32_t *wide_ctr;
   uint4 *wide_list;
   int frame, height, width, bytes_per_row;
@@ -131,13 +132,6 @@ struct SegRun {
   bool writer;
   uint32_t inside8;
 };
-
-// The exact decision for the thin band neither bound settles. Out of line:
-// the common path neither carries nor issues it.
-static __device__ __noinline__ bool seg_exact(uint32_t n, uint32_t S, uint32_t Q,
-                                              const LaunchParams &P) {
-  return stage0_u32(n, (unsigned long long)S, (unsigned long long)Q, P, P.root_lo, P.root_hi);
-}
 
 // Everything a lane carries from row to row.
 template <int K> struct SegState {
@@ -158,12 +152,14 @@ __device__ __forceinline__ void seg_bounds(uint32_t S, uint32_t Q, uint32_t nk, 
 
 // One pixel row p for this lane. Steady rows (every row past a run's first
 // PRO) output an eroded row; the first PRO rows only fill the windows and the
-// decision history. Returns false when the warp must hand the rest of its run
-// to the 64-bit path.
+// decision history. Nothing here branches on the data: a row holding a pixel
+// too large for the 32-bit sums returns true (the warp hands the rest of its
+// run to the 64-bit path when it is done; what it writes past that row is
+// rewritten there), and the windows between the two bounds are taken as
+// signal here and recorded in the ambiguous mask for amb_fix.
 template <int K, bool kSteady>
 __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const uint32_t raw[16],
-                                        int p, const SegRun &r, const LaunchParams &P,
-                                        const StreamTables &T) {
+                                        int p, const SegRun &r, const StreamTables &T) {
   using G = SegG<K>;
   constexpr int o = 4 - K;               // first of the 8 + 2K pixels used
   constexpr int NP = 8 + 2 * K;
@@ -172,7 +168,7 @@ __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const ui
   // The pixels the row sums use, as masked-count << PS | value and value^2,
   // without a branch: u = v + 2 sends the masked sentinels to 0 and 1, a
   // masked pixel packs as a count bit alone, and its square (2^PS)^2 wraps
-  // to 0. A valid pixel at or above narrow_max hands the run over.
+  // to 0. A valid pixel at or above narrow_max ends the narrow sums.
   uint32_t ns[16], q[16], valid8 = 0;
   bool wide;
   {
@@ -199,18 +195,7 @@ __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const ui
         valid8 |= 1u << (i - 4);
     }
   }
-  if (__any_sync(0xffffffffu, wide)) {
-    if (r.lane == 0) {
-      const uint32_t k = atomicAdd(r.wide_ctr, 1u);
-      // Up to the end of the row's last mask word: the columns past the
-      // frame are written as zeros there, as the lanes here would have.
-      const int xb = max(0, r.X + 8), xe = min(r.bytes_per_row * 8, r.X + 8 + kSegOut);
-      r.wide_list[2 * k] =
-          make_uint4((uint32_t)xb, (uint32_t)xe, (uint32_t)max(r.ra, p - G::R1), (uint32_t)r.rb);
-      r.wide_list[2 * k + 1] = make_uint4((uint32_t)r.frame, 0u, 0u, 0u);
-    }
-    return false;
-  }
+  const bool wide_row = __any_sync(0xffffffffu, wide);
   st.hval = (st.hval << 8) | valid8;
 
   // Row sums of 2K + 1 columns for the 8 columns, as two sliding chains.
@@ -252,7 +237,7 @@ __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const ui
     st.slot = st.slot + 1 == G::W0 ? 0 : st.slot + 1;
   }
   if (!kSteady && p < r.p0 + 2 * K)
-    return true;  // the column sums are not yet full windows (warp-uniform)
+    return wide_row;  // the column sums are not yet full windows (warp-uniform)
 
   // Stage-0 row p - K: eight decisions, maybe/sure bits without a branch
   // (the constants by masked count come from a small table; nearly every
@@ -261,29 +246,22 @@ __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const ui
   uint32_t maybe8 = 0, sure8 = 0;
 #pragma unroll
   for (int c = 0; c < 8; c++) {
-    // The masked count is at most N0 by construction; the clamp keeps the
-    // table read in bounds whatever the sums hold.
+    // The masked count is at most N0 while the sums are exact; past a
+    // too-large pixel they are not, and the clamp keeps the read in bounds.
     const uint4 t = s.tab[min(st.vns[c] >> G::PS, (uint32_t)G::N0)];
     bool mb, su;
     seg_bounds(st.vns[c] & G::MASK, st.vq[c], t.x, t.y, t.z, &mb, &su);
     maybe8 |= mb ? 1u << c : 0u;
     sure8 |= su ? 1u << c : 0u;
   }
-  uint32_t s8 = (~vrow | sure8) & 0xFFu;
   const uint32_t amb8 = maybe8 & ~sure8 & vrow;
-  if (amb8) {  // the thin band: exact, out of line (rare)
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-      const uint32_t x = st.vns[c];
-      if (((amb8 >> c) & 1u) &&
-          seg_exact((uint32_t)G::N0 - min(x >> G::PS, (uint32_t)G::N0), x & G::MASK,
-                    st.vq[c], P))
-        s8 |= 1u << c;
-    }
-  }
+  const uint32_t s8 = (~vrow | sure8 | amb8) & 0xFFu;
+  const int d = p - K;  // the decision row; each run records its own rows'
+  if (r.writer && d >= r.ra && d < r.rb)
+    r.amb_bytes[(size_t)d * r.bytes_per_row + (r.cx >> 3)] = (uint8_t)amb8;
   st.hs0 = (st.hs0 << 8) | s8;
   if (!kSteady)
-    return true;  // the erosion needs 2E more decision rows
+    return wide_row;  // the erosion needs 2E more decision rows
 
   // Erosion of row p - R1: vertical AND of 2E + 1 chunks, then across columns
   // with the neighbours' chunks.
@@ -308,7 +286,7 @@ __device__ __forceinline__ bool seg_row(SegSmem<K> &s, SegState<K> &st, const ui
     r.scr1_bytes[at] = (uint8_t)scr1;
     r.final_bytes[at] = (uint8_t)(scr1 & ~masked8);
   }
-  return true;
+  return wide_row;
 }
 
 template <int K>
@@ -316,8 +294,8 @@ __global__ void __launch_bounds__(kSegWarps * 32, SegG<K>::OCC)
 seg_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int width, int vec,
             int nstrips, int nruns, int run_rows, const __grid_constant__ LaunchParams P,
             const __grid_constant__ StreamTables T, uint8_t *__restrict__ scr1_bytes,
-            uint8_t *__restrict__ final_bytes, size_t mask_bytes, uint32_t *__restrict__ counters,
-            uint4 *__restrict__ wide_list) {
+            uint8_t *__restrict__ final_bytes, uint8_t *__restrict__ amb_bytes, size_t mask_bytes,
+            uint32_t *__restrict__ counters, uint4 *__restrict__ wide_list) {
   using G = SegG<K>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SegSmem<K> &s = *reinterpret_cast<SegSmem<K> *>(smem_raw);
@@ -338,6 +316,7 @@ seg_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
   r.bytes_per_row = ((width + 31) >> 5) * 4;
   r.scr1_bytes = scr1_bytes + (size_t)f * mask_bytes;
   r.final_bytes = final_bytes + (size_t)f * mask_bytes;
+  r.amb_bytes = amb_bytes + (size_t)f * mask_bytes;
   r.wide_ctr = counters + kCtrWide;
   r.wide_list = wide_list;
   r.X = kSegOut * sx - 8;
@@ -370,28 +349,41 @@ seg_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
   // then every row outputs one eroded row (two per pass, the loads of the
   // next row prefetched into the other buffer).
   const int p1 = r.rb + G::R1;
-  bool go = true;
-  for (int p = r.p0; go && p < r.p0 + G::PRO; p++) {
+  int first_wide = INT_MAX;
+  for (int p = r.p0; p < r.p0 + G::PRO; p++) {
     uint32_t v[16];
     seg_load(r.image, height, width, interior, r.cx, p, v);
-    go = seg_row<K, false>(s, st, v, p, r, P, T);
+    if (seg_row<K, false>(s, st, v, p, r, T))
+      first_wide = min(first_wide, p);
   }
-  if (go) {
+  {
     uint32_t A[16], B[16];
     int p = r.p0 + G::PRO;
     seg_load(r.image, height, width, interior, r.cx, p, A);
     for (; p < p1; p += 2) {
       if (p + 1 < p1)
         seg_load(r.image, height, width, interior, r.cx, p + 1, B);
-      if (!seg_row<K, true>(s, st, A, p, r, P, T))
-        break;
+      if (seg_row<K, true>(s, st, A, p, r, T))
+        first_wide = min(first_wide, p);
       if (p + 1 >= p1)
         break;
       if (p + 2 < p1)
         seg_load(r.image, height, width, interior, r.cx, p + 2, A);
-      if (!seg_row<K, true>(s, st, B, p + 1, r, P, T))
-        break;
+      if (seg_row<K, true>(s, st, B, p + 1, r, T))
+        first_wide = min(first_wide, p + 1);
     }
+  }
+  if (first_wide != INT_MAX && lane == 0) {
+    // From the first row with a too-large pixel on, the 64-bit path redoes
+    // the eroded rows [yb, rb) (their windows reach that row) and clears the
+    // ambiguous records of the decision rows [dz, rb) written from bad sums.
+    const uint32_t k = atomicAdd(r.wide_ctr, 1u);
+    // Up to the end of the row's last mask word: the columns past the frame
+    // are written as zeros there, as the lanes here would have.
+    const int xb = max(0, r.X + 8), xe = min(r.bytes_per_row * 8, r.X + 8 + kSegOut);
+    const int yb = max(r.ra, first_wide - G::R1), dz = max(r.ra, first_wide - K);
+    r.wide_list[2 * k] = make_uint4((uint32_t)xb, (uint32_t)xe, (uint32_t)yb, (uint32_t)r.rb);
+    r.wide_list[2 * k + 1] = make_uint4((uint32_t)r.frame, (uint32_t)dz, 0u, 0u);
   }
 }
 
@@ -404,8 +396,8 @@ template <int K>
 __global__ void __launch_bounds__(256)
 stream_wide(const __grid_constant__ FramePtrs F, int height, int width, int run_rows,
             const __grid_constant__ LaunchParams P, uint8_t *__restrict__ scr1_all,
-            uint8_t *__restrict__ final_all, size_t mask_bytes, uint32_t *__restrict__ counters,
-            const uint4 *__restrict__ wide_list) {
+            uint8_t *__restrict__ final_all, uint8_t *__restrict__ amb_all, size_t mask_bytes,
+            uint32_t *__restrict__ counters, const uint4 *__restrict__ wide_list) {
   constexpr int E = K - 1, R1 = 2 * K - 1;
   constexpr int TS = 32, IW = TS + 2 * R1, S0 = IW - 2 * K;
   __shared__ uint32_t pix[IW][IW];
@@ -425,7 +417,8 @@ stream_wide(const __grid_constant__ FramePtrs F, int height, int width, int run_
   for (uint32_t item = blockIdx.x; item < nwide * TPS * TPR; item += gridDim.x) {
     const uint32_t k = item / (TPS * TPR);
     const uint4 w = wide_list[2 * k];
-    const int f = (int)wide_list[2 * k + 1].x;
+    const int f = (int)wide_list[2 * k + 1].x, dz = (int)wide_list[2 * k + 1].y;
+    uint8_t *amb_bytes = amb_all + (size_t)f * mask_bytes;
     const uint32_t *image = F.image[f];
     uint8_t *scr1_bytes = scr1_all + (size_t)f * mask_bytes;
     uint8_t *final_bytes = final_all + (size_t)f * mask_bytes;
@@ -495,6 +488,77 @@ stream_wide(const __grid_constant__ FramePtrs F, int height, int width, int run_
         if (bx < xe && (bx >> 3) < bytes_per_row) {
           scr1_bytes[(size_t)gy * bytes_per_row + (bx >> 3)] = (uint8_t)(word >> (8 * lane));
           final_bytes[(size_t)gy * bytes_per_row + (bx >> 3)] = (uint8_t)(cm >> (8 * lane));
+          if (gy >= dz)
+            amb_bytes[(size_t)gy * bytes_per_row + (bx >> 3)] = 0;
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The windows between the two bounds (the ambiguous mask): each is decided
+// exactly from its 64-bit sums (src/spots/dext.cc:99-109, sf_common.cuh). The
+// first pass took each as signal; where it is not, its (2E+1)^2 neighbourhood
+// cannot survive the erosion (an AND of the stage-0 bits), so every valid
+// pixel there leaves the eroded and candidate masks. A clearing is true of
+// the frame whatever else was decided, so the order of the fixes, and any
+// ambiguous record left by rows the 64-bit path rewrote, do not matter.
+// ---------------------------------------------------------------------------
+template <int K>
+__global__ void __launch_bounds__(256)
+amb_fix(const __grid_constant__ FramePtrs F, int height, int width,
+        const __grid_constant__ LaunchParams P, const uint32_t *__restrict__ amb_all,
+        uint32_t *__restrict__ scr1_all, uint32_t *__restrict__ final_all, size_t words) {
+  constexpr int E = K - 1;
+  const int f = blockIdx.y;
+  const uint32_t *image = F.image[f];
+  const uint32_t *amb = amb_all + (size_t)f * words;
+  uint32_t *scr1 = scr1_all + (size_t)f * words;
+  uint32_t *fin = final_all + (size_t)f * words;
+  const uint32_t wpr = ((uint32_t)width + 31u) >> 5;
+  // One thread per mask word: the scan runs at memory speed, and the rare
+  // set bits are handled where they are found.
+  const size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w < words) {
+    uint32_t bits = amb[w];
+    const int y = (int)(w / wpr);
+    const int x0 = (int)(w - (size_t)y * wpr) * 32;
+    while (bits) {
+      const int x = x0 + __ffs(bits) - 1;
+      bits &= bits - 1u;
+      uint32_t n = 0;
+      unsigned long long S = 0, Q = 0;
+      for (int dy = -K; dy <= K; dy++) {
+        const int yy = y + dy;
+        if (yy < 0 || yy >= height)
+          continue;
+        for (int dx = -K; dx <= K; dx++) {
+          const int xx = x + dx;
+          if (xx < 0 || xx >= width)
+            continue;
+          const uint32_t v = __ldg(image + (size_t)yy * width + xx);
+          if (v < 0xFFFFFFFEu) {
+            n++;
+            S += v;
+            Q += (unsigned long long)v * v;
+          }
+        }
+      }
+      if (stage0_u32(n, S, Q, P, P.root_lo, P.root_hi))
+        continue;
+      for (int dy = -E; dy <= E; dy++) {
+        const int yy = y + dy;
+        if (yy < 0 || yy >= height)
+          continue;
+        for (int dx = -E; dx <= E; dx++) {
+          const int xx = x + dx;
+          if (xx < 0 || xx >= width || __ldg(image + (size_t)yy * width + xx) >= 0xFFFFFFFEu)
+            continue;
+          const size_t at = (size_t)yy * wpr + (xx >> 5);
+          const uint32_t keep = ~(1u << (xx & 31));
+          atomicAnd(scr1 + at, keep);
+          atomicAnd(fin + at, keep);
         }
       }
     }
@@ -506,16 +570,20 @@ stream_wide(const __grid_constant__ FramePtrs F, int height, int width, int run_
 // the first pass wrote it), ascending, from two scans over the mask words.
 // Every kernel below runs on a (block, frame) grid.
 // ---------------------------------------------------------------------------
-constexpr int kScanT = 1024;
+constexpr int kScanT = 256;                    // threads of a scan block
+constexpr int kScanPer = 8;                    // consecutive items per thread
+constexpr int kScanChunk = kScanT * kScanPer;  // items per block pass
 
-__device__ __forceinline__ void chunk_of(size_t n, uint32_t *lo, uint32_t *hi) {
-  const size_t chunk = (n + gridDim.x - 1) / gridDim.x;
-  *lo = (uint32_t)min(n, (size_t)blockIdx.x * chunk);
-  *hi = (uint32_t)min(n, (size_t)*lo + chunk);
+// This block's share [lo, hi) of a frame's n items, in whole passes.
+__device__ __forceinline__ void chunk_of(size_t n, size_t *lo, size_t *hi) {
+  size_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  chunk = (chunk + kScanChunk - 1) / kScanChunk * kScanChunk;
+  *lo = min(n, (size_t)blockIdx.x * chunk);
+  *hi = min(n, *lo + chunk);
 }
 
-// Sum of the block's predecessors' counts in its frame, and (block 0) the
-// frame's total.
+// Sum of the block's predecessors' counts in its frame, and the frame's
+// total.
 __device__ __forceinline__ uint32_t block_base(const uint32_t *__restrict__ block_sums,
                                                uint32_t *total) {
   __shared__ uint32_t s_base, s_total;
@@ -541,19 +609,58 @@ __device__ __forceinline__ uint32_t block_base(const uint32_t *__restrict__ bloc
   return s_base;
 }
 
-// Popcounts of the block's share of a frame's mask words.
-__global__ void __launch_bounds__(kScanT)
-mask_sums(const uint32_t *__restrict__ bits_all, size_t words, uint32_t *__restrict__ block_sums) {
-  const uint32_t *bits = bits_all + (size_t)blockIdx.y * words;
-  uint32_t lo, hi;
-  chunk_of(words, &lo, &hi);
+// The block's count over [lo, hi): kScanPer consecutive items per thread.
+template <class Count>
+__device__ __forceinline__ void scan_count(size_t lo, size_t hi, Count count,
+                                           uint32_t *__restrict__ block_sums) {
   uint32_t acc = 0;
-  for (uint32_t w = lo + threadIdx.x; w < hi; w += blockDim.x)
-    acc += __popc(bits[w]);
+  for (size_t base = lo; base < hi; base += kScanChunk) {
+    const size_t i0 = base + (size_t)threadIdx.x * kScanPer;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++)
+      acc += i0 + k < hi ? count(i0 + k) : 0u;
+  }
   uint32_t total;
   (void)block_exclusive_scan(acc, &total);
   if (threadIdx.x == 0)
     block_sums[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = total;
+}
+
+// Every item of [lo, hi) with its count's exclusive prefix (offset by
+// carry): emit(i, item, position) for items that count.
+template <typename V, class Load, class Count, class Emit>
+__device__ __forceinline__ void scan_emit(size_t lo, size_t hi, uint32_t carry, Load load,
+                                          Count count, Emit emit) {
+  for (size_t base = lo; base < hi; base += kScanChunk) {
+    const size_t i0 = base + (size_t)threadIdx.x * kScanPer;
+    V v[kScanPer];
+    uint32_t c[kScanPer], tot = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+      const bool in = i0 + k < hi;
+      v[k] = in ? load(i0 + k) : V();
+      c[k] = in ? count(v[k]) : 0u;
+      tot += c[k];
+    }
+    uint32_t t;
+    uint32_t pos = carry + block_exclusive_scan(tot, &t);
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+      if (c[k])
+        emit(i0 + k, v[k], pos);
+      pos += c[k];
+    }
+    carry += t;
+  }
+}
+
+// Popcounts of the block's share of a frame's mask words.
+__global__ void __launch_bounds__(kScanT)
+mask_sums(const uint32_t *__restrict__ bits_all, size_t words, uint32_t *__restrict__ block_sums) {
+  const uint32_t *bits = bits_all + (size_t)blockIdx.y * words;
+  size_t lo, hi;
+  chunk_of(words, &lo, &hi);
+  scan_count(lo, hi, [&](size_t w) { return (uint32_t)__popc(bits[w]); }, block_sums);
 }
 
 // The pixel index of every set bit of the block's share, in order.
@@ -565,30 +672,26 @@ mask_list(const uint32_t *__restrict__ bits_all, size_t words, int width,
   const uint32_t *bits = bits_all + (size_t)f * words;
   uint32_t *cand = cand_all + (size_t)f * cand_cap;
   uint32_t total;
-  uint32_t carry = block_base(block_sums, &total);
+  const uint32_t carry = block_base(block_sums, &total);
   if (blockIdx.x == 0 && threadIdx.x == 0)
     counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand] = total;
   const uint32_t wpr = ((uint32_t)width + 31u) >> 5;
-  uint32_t lo, hi;
+  size_t lo, hi;
   chunk_of(words, &lo, &hi);
-  for (uint32_t base = lo; base < hi; base += blockDim.x) {
-    const uint32_t w = base + threadIdx.x;
-    uint32_t word = w < hi ? bits[w] : 0u;
-    uint32_t t;
-    uint32_t pos = carry + block_exclusive_scan(__popc(word), &t);
-    if (word) {
-      const uint32_t row = w / wpr;
-      const uint32_t first = row * (uint32_t)width + (w - row * wpr) * 32u;
-      while (word) {
-        const int b = __ffs(word) - 1;
-        word &= word - 1u;
-        if (pos < cand_cap)
-          cand[pos] = first + (uint32_t)b;
-        pos++;
-      }
-    }
-    carry += t;
-  }
+  scan_emit<uint32_t>(
+      lo, hi, carry, [&](size_t w) { return bits[w]; },
+      [](uint32_t word) { return (uint32_t)__popc(word); },
+      [&](size_t w, uint32_t word, uint32_t pos) {
+        const uint32_t row = (uint32_t)w / wpr;
+        const uint32_t first = row * (uint32_t)width + ((uint32_t)w - row * wpr) * 32u;
+        while (word) {
+          const int b = __ffs(word) - 1;
+          word &= word - 1u;
+          if (pos < cand_cap)
+            cand[pos] = first + (uint32_t)b;
+          pos++;
+        }
+      });
 }
 
 // ---------------------------------------------------------------------------
@@ -601,7 +704,9 @@ mask_list(const uint32_t *__restrict__ bits_all, size_t words, int width,
 // res[i] (the background's bits; the population, and the pass bit at 16),
 // and a candidate that fails is cleared from the final mask.
 // ---------------------------------------------------------------------------
-template <int K>
+// k32: every valid pixel of the frame is below 2^24 (no run needed the 64-bit
+// path), so a window's background sum (at most 169 of them) fits 32 bits.
+template <int K, bool k32>
 __device__ __forceinline__ void s2_window(const uint32_t *__restrict__ image,
                                           const uint32_t *__restrict__ scr1_words, int height,
                                           int width, int wpr, int vec, int sub, int y, int x,
@@ -644,9 +749,17 @@ __device__ __forceinline__ void s2_window(const uint32_t *__restrict__ image,
                               t[k][3].x, t[k][3].y, t[k][3].z, t[k][3].w};
       // Not in the eroded mask, so valid (masked pixels are in it).
       n += __popc(bg);
+      if (k32) {
+        uint32_t s32 = 0;
 #pragma unroll
-      for (int d = 0; d < 16; d++)
-        S += ((bg >> d) & 1u) ? v[d] : 0u;
+        for (int d = 0; d < 16; d++)
+          s32 += ((bg >> d) & 1u) ? v[d] : 0u;
+        S += s32;
+      } else {
+#pragma unroll
+        for (int d = 0; d < 16; d++)
+          S += ((bg >> d) & 1u) ? v[d] : 0u;
+      }
     }
   } else {
     const int xlo = max(0, x - K2), xhi = min(width - 1, x + K2);
@@ -689,6 +802,8 @@ seg_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   uint2 *res = res_all + (size_t)f * cand_cap;
   const int wpr = (width + 31) >> 5;
   const uint32_t nc = min(counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand], cand_cap);
+  // No run of the batch met a valid pixel at or above the narrow bound.
+  const bool narrow = counters[kCtrWide] == 0;
   const int lane = threadIdx.x & 31, sub = lane & 3;
   const uint32_t per_pass = (gridDim.x * blockDim.x) >> 2;
   for (uint32_t base = (blockIdx.x * blockDim.x) >> 2; base < nc; base += per_pass) {
@@ -702,7 +817,10 @@ seg_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
       y = (int)(idx / (uint32_t)width);
       x = (int)(idx - (uint32_t)y * (uint32_t)width);
       p = __ldg(image + idx);
-      s2_window<K>(image, scr1_words, height, width, wpr, vec, sub, y, x, &n, &S);
+      if (narrow)
+        s2_window<K, true>(image, scr1_words, height, width, wpr, vec, sub, y, x, &n, &S);
+      else
+        s2_window<K, false>(image, scr1_words, height, width, wpr, vec, sub, y, x, &n, &S);
     }
     n += __shfl_xor_sync(0xffffffffu, n, 1);
     S += __shfl_xor_sync(0xffffffffu, S, 1);
@@ -729,15 +847,9 @@ pass_sums(const uint2 *__restrict__ res_all, uint32_t cand_cap,
   const int f = blockIdx.y;
   const uint2 *res = res_all + (size_t)f * cand_cap;
   const uint32_t nc = min(counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand], cand_cap);
-  uint32_t lo, hi;
+  size_t lo, hi;
   chunk_of(nc, &lo, &hi);
-  uint32_t acc = 0;
-  for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-    acc += (res[i].y >> 16) & 1u;
-  uint32_t total;
-  (void)block_exclusive_scan(acc, &total);
-  if (threadIdx.x == 0)
-    block_sums[(size_t)f * gridDim.x + blockIdx.x] = total;
+  scan_count(lo, hi, [&](size_t i) { return (res[i].y >> 16) & 1u; }, block_sums);
 }
 
 __global__ void __launch_bounds__(kScanT)
@@ -754,31 +866,28 @@ pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ c
   const uint32_t ncand = counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand];
   const uint32_t nc = min(ncand, cand_cap);
   uint32_t total;
-  uint32_t carry = block_base(block_sums, &total);
+  const uint32_t carry = block_base(block_sums, &total);
   if (blockIdx.x == 0 && threadIdx.x == 0)
     // The signal found; all ones if the candidate list overflowed, as for a
     // count above capacity (the list is then incomplete).
     count_out[f] = ncand > cand_cap ? 0xFFFFFFFFu : total;
-  uint32_t lo, hi;
+  size_t lo, hi;
   chunk_of(nc, &lo, &hi);
-  for (uint32_t base = lo; base < hi; base += blockDim.x) {
-    const uint32_t i = base + threadIdx.x;
-    const uint2 r = i < hi ? res[i] : make_uint2(0u, 0u);
-    const uint32_t pass = (r.y >> 16) & 1u;
-    uint32_t t;
-    const uint32_t pos = carry + block_exclusive_scan(pass, &t);
-    if (pass && pos < capacity) {
-      const uint32_t idx = cand[i];
-      sf_signal_pixel rec;
-      rec.index = idx;
-      rec.value = __ldg(image + idx);
-      rec.background = __uint_as_float(r.x);
-      rec.population = (uint16_t)(r.y & 0xFFFFu);
-      rec.reserved = 0;
-      out[pos] = rec;
-    }
-    carry += t;
-  }
+  scan_emit<uint2>(
+      lo, hi, carry, [&](size_t i) { return res[i]; },
+      [](uint2 r) { return (r.y >> 16) & 1u; },
+      [&](size_t i, uint2 r, uint32_t pos) {
+        if (pos >= capacity)
+          return;
+        const uint32_t idx = cand[i];
+        sf_signal_pixel rec;
+        rec.index = idx;
+        rec.value = __ldg(image + idx);
+        rec.background = __uint_as_float(r.x);
+        rec.population = (uint16_t)(r.y & 0xFFFFu);
+        rec.reserved = 0;
+        out[pos] = rec;
+      });
 }
 
 // Optional: per final-mask word, the list position of its first pixel.
@@ -790,15 +899,24 @@ mask_prefix(const uint32_t *__restrict__ bits_all, size_t words,
   uint32_t *prefix = prefix_all + (size_t)f * words;
   uint32_t total;
   uint32_t carry = block_base(block_sums, &total);
-  uint32_t lo, hi;
+  size_t lo, hi;
   chunk_of(words, &lo, &hi);
-  for (uint32_t base = lo; base < hi; base += blockDim.x) {
-    const uint32_t w = base + threadIdx.x;
-    const uint32_t c = w < hi ? __popc(bits[w]) : 0u;
+  for (size_t base = lo; base < hi; base += kScanChunk) {
+    const size_t i0 = base + (size_t)threadIdx.x * kScanPer;
+    uint32_t c[kScanPer], tot = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+      c[k] = i0 + k < hi ? (uint32_t)__popc(bits[i0 + k]) : 0u;
+      tot += c[k];
+    }
     uint32_t t;
-    const uint32_t e = block_exclusive_scan(c, &t);
-    if (w < hi)
-      prefix[w] = carry + e;
+    uint32_t pos = carry + block_exclusive_scan(tot, &t);
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+      if (i0 + k < hi)
+        prefix[i0 + k] = pos;
+      pos += c[k];
+    }
     carry += t;
   }
 }
@@ -820,12 +938,13 @@ static int device_sms() {
   return cached;
 }
 
-// Blocks of the ordering kernels: about two per SM over the batch, never
-// more than kOrderMaxBlocks in all.
-constexpr int kOrderMaxBlocks = 1024;
-static int order_bpf(int nframes) {
-  const int want = (2 * device_sms() + nframes - 1) / nframes;
-  return std::max(1, std::min(want, kOrderMaxBlocks / nframes));
+// Blocks per frame of the scan kernels: one per 2048 mask words (a scan
+// block walks its share in two passes), at least one, never more than
+// kOrderMaxBlocks over the batch.
+constexpr int kOrderMaxBlocks = 8192;
+static int order_bpf(int nframes, size_t words) {
+  const long long want = (long long)((words + 2047) / 2048);
+  return (int)std::max(1ll, std::min(want, (long long)(kOrderMaxBlocks / nframes)));
 }
 
 int stream_order_blocks() { return kOrderMaxBlocks; }
@@ -915,14 +1034,17 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
   uint8_t *scr1 = reinterpret_cast<uint8_t *>(b.scr1);
   uint8_t *fin = reinterpret_cast<uint8_t *>(b.bits);
   const int sms = device_sms();
+  uint8_t *amb = reinterpret_cast<uint8_t *>(b.amb);
   seg_stage01<K><<<(unsigned)((warps + kSegWarps - 1) / kSegWarps), kSegWarps * 32, sizeof(S),
                    stream>>>(F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, P, T, scr1,
-                             fin, mask_bytes, b.counters, b.wide);
-  stream_wide<K><<<2 * sms, 256, 0, stream>>>(F, h, w, g.run_rows, P, scr1, fin, mask_bytes,
+                             fin, amb, mask_bytes, b.counters, b.wide);
+  stream_wide<K><<<2 * sms, 256, 0, stream>>>(F, h, w, g.run_rows, P, scr1, fin, amb, mask_bytes,
                                                b.counters, b.wide);
+  amb_fix<K><<<dim3((unsigned)((b.words + 255) / 256), nframes), 256, 0, stream>>>(
+      F, h, w, P, b.amb, b.scr1, b.bits, b.words);
   if (marks)
     cudaEventRecord(marks->stage01, stream);
-  const dim3 og((unsigned)order_bpf(nframes), (unsigned)nframes);
+  const dim3 og((unsigned)order_bpf(nframes, b.words), (unsigned)nframes);
   mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
   mask_list<<<og, kScanT, 0, stream>>>(b.bits, b.words, w, b.block_sums, b.cand, b.cand_cap,
                                        b.counters);

@@ -58,6 +58,7 @@ struct StreamTables {
 struct StreamBuffers {
   uint32_t *bits;          // final strong masks (output), frame f at bits + f * words
   uint32_t *scr1;          // eroded masks, same layout
+  uint32_t *amb;           // ambiguous stage-0 windows, same layout
   uint32_t *prefix;        // per-word list positions (output) or null
   size_t words;            // mask words per frame
   uint32_t *cand;          // ascending candidate indices, frame f at cand + f * cand_cap

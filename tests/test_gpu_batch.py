@@ -118,3 +118,28 @@ def test_batch_16m_frames(api):
     b = _run(api, frames, capacity=frames[0].size // 4)
     for j, f in enumerate(frames):
         _same(b.result(j), O.dext(f), f"16M frame {j}")
+
+
+@pytest.mark.parametrize("kernel", [2, 3, 4])
+def test_batch_near_threshold_windows(api, kernel):
+    # Negative-binomial backgrounds whose dispersion index sits at the
+    # stage-0 threshold (about 1 + sigma_b sqrt(2 / (n - 1))): many windows
+    # fall between the two integer bounds and are decided by the exact pass,
+    # which then clears the neighbourhoods of those that are not signal.
+    rng = np.random.default_rng(40 + kernel)
+    n = (2 * kernel + 1) ** 2
+    index = 1.0 + 6.0 * np.sqrt(2.0 / (n - 1))
+    frames = []
+    for j in range(4):
+        mean = 2.0 + j
+        p = 1.0 / index
+        r = mean * p / (1.0 - p)
+        f = rng.negative_binomial(r, p, size=(190, 260)).astype(np.uint32)
+        f[rng.random(f.shape) < 0.002] = 0xFFFFFFFF
+        frames.append(f)
+    params = dict(kernel_x=kernel, kernel_y=kernel)
+    b = _run(api, frames, params=api.Params(**params))
+    for j, f in enumerate(frames):
+        want, mask = O.dext(f, O.Params(**params), with_mask=True)
+        _same(b.result(j), want, f"kernel {kernel} frame {j}")
+        assert np.array_equal(b.mask(j), mask.astype(bool))
