@@ -159,8 +159,9 @@ def cpu_baseline(frames, seconds_budget: float = 20.0, threads: int | None = Non
     t0 = time.perf_counter()
     oracle.dext(frames[0])  # warm (and measure one frame single-threaded)
     one = time.perf_counter() - t0
-    n = max(threads, min(len(frames) * 4, int(seconds_budget * threads / max(one, 1e-3))))
-    n = max(1, min(n, 4 * threads))
+    # About seconds_budget of wall time on all threads.
+    n = int(seconds_budget * threads / max(one, 1e-3))
+    n = max(threads, min(n, 16 * threads))
     lab = oracle.Labeller(H, W)
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
@@ -221,17 +222,18 @@ def run_ours(args):
     frames = make_pool(pool_n, seed_offset=rank)
     pool = torch.stack([torch.from_numpy(f.view(np.int32)) for f in frames]).to(dev)
     stream = torch.cuda.Stream(device=dev)
-    batch = api.DeviceBatch(H, W, B)
+    views = [pool[j % pool_n] for j in range(B)]
 
-    def step(i0: int):
-        views = [pool[(i0 + j) % pool_n] for j in range(B)]
-        batch(views, stream=stream)
-
+    # The batched form: a plan tuned on these frames, its launch sequence
+    # replayed as a CUDA graph (the same frame buffers every step).
+    plan = api.Plan(H, W, B)
     with torch.cuda.stream(stream):
+        run_rows = plan.tune(views, stream=stream)
         for w in range(args.warmup):
-            step(w * B)
+            plan(views, stream=stream)
     stream.synchronize()
-    n_signal = int(batch.counts[:B].double().mean().item())
+    counts = np.array([len(plan.result(j)) for j in range(B)])
+    n_signal = int(counts.mean())
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
@@ -246,7 +248,7 @@ def run_ours(args):
         start.record(stream)
         for s in range(args.steps):
             ev[s][0].record(stream)
-            step((args.warmup + s) * B)
+            plan(views, stream=stream)
             ev[s][1].record(stream)
         end.record(stream)
     torch.cuda.synchronize(dev)
@@ -258,6 +260,7 @@ def run_ours(args):
     frames_done = sum_over_ranks(args.steps * B, world, dev)
     value = frames_done / (elapsed_ms / 1e3)
     launch_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    graphs = plan.graphs
 
     # Roofline of the threshold launch sequence: algorithmic bytes per frame
     # (the frame read once, the bitmask written, the signal list written).
@@ -280,6 +283,56 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     per_frame = n_single / (a.elapsed_time(b) / 1e3)
     del single
+
+    # 3-D labelling of the batch's lists on the device (reported beside the
+    # threshold; its bytes are O(signal), outside the threshold roofline).
+    label = None
+    if not args.no_label:
+        from sfgb import labeller
+        lab = labeller.DeviceLabeller(H, W)
+        lists_ptr = api.lib().sf_plan_lists(plan._p)
+        counts_ptr = api.lib().sf_plan_counts(plan._p)
+        nb = 0
+        with torch.cuda.stream(stream):
+            plan(views, stream=stream)
+            lab.add_device(list(range(nb, nb + B)), lists_ptr, plan.capacity, counts_ptr,
+                           stream.cuda_stream)
+            nb += B
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            for s in range(args.steps):
+                lab.add_device(list(range(nb, nb + B)), lists_ptr, plan.capacity, counts_ptr,
+                               stream.cuda_stream)
+                nb += B
+            t1 = time.perf_counter()
+            res = lab.finish()
+        label_ms = (t1 - t0) * 1e3 / (args.steps * B)
+        label = {"ms_per_frame": label_ms, "frames_per_s": 1e3 / label_ms,
+                 "threshold_and_label_frames_per_s": 1.0 / (1.0 / value + label_ms / 1e3),
+                 "spots": int(len(res.spots)),
+                 "path": "sf_label_add_device on the plan's lists, 16 frames per call, "
+                         "consecutive frame numbers (the pool repeats)"}
+
+    # The host link's own speed: pinned frames copied to the device.
+    h2d_gbs = None
+    if not args.no_e2e:
+        hbuf = torch.empty((4, H * W), dtype=torch.int32).pin_memory()
+        dbuf = torch.empty((4, H * W), dtype=torch.int32, device=dev)
+        streams = [torch.cuda.Stream(device=dev) for _ in range(2)]
+        for _ in range(2):
+            for k in range(4):
+                with torch.cuda.stream(streams[k % 2]):
+                    dbuf[k].copy_(hbuf[k], non_blocking=True)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        reps = 8
+        for _ in range(reps):
+            for k in range(4):
+                with torch.cuda.stream(streams[k % 2]):
+                    dbuf[k].copy_(hbuf[k], non_blocking=True)
+        torch.cuda.synchronize(dev)
+        h2d_gbs = reps * 4 * H * W * 4 / (time.perf_counter() - t0) / 1e9
+        del hbuf, dbuf
 
     # End to end through the C ABI host-frame call (gpu::find drop-in), from
     # several host threads as mxi_find's -j workers call it.
@@ -332,7 +385,13 @@ def run_ours(args):
                "d2h_bytes_per_step": int(d2h / args.steps),
                "path": f"sf_find_u32 (C ABI, gpu::find<uint32_t> drop-in) from {T} host "
                        "threads, pinned host frames; per frame the copy in, the threshold "
-                       "and the signal list's read-back"}
+                       "and the signal list's read-back",
+               "h2d_peak_gbs": h2d_gbs,
+               "achieved_h2d_gbs": None,
+               "frac_of_h2d_peak": None}
+        e2e["achieved_h2d_gbs"] = e2e["value"] * H * W * 4 / 1e9
+        if h2d_gbs:
+            e2e["frac_of_h2d_peak"] = e2e["achieved_h2d_gbs"] / h2d_gbs
         for ptr in host + outs:
             L.sf_host_free(ptr)
 
@@ -357,17 +416,19 @@ def run_ours(args):
                                 f"{B} frames per launch sequence",
                        "signal_pixels_per_frame": n_signal,
                        "plain_per_frame_frames_per_s": per_frame,
-                       "batched_over_plain": value / per_frame},
+                       "batched_over_plain": value / per_frame,
+                       "tuned_run_rows": run_rows, "cuda_graphs": graphs},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind,
                          "kernel": "threshold launch sequence of a batch (seg_stage01, "
-                                   "stream_wide, seg_stage2, order_sums, order_prefix, "
-                                   "order_scatter), CUDA events around each batch",
+                                   "stream_wide, amb_fix, mask_sums, mask_list, seg_stage2, "
+                                   "pass_sums, pass_scatter) replayed as one CUDA graph, "
+                                   "CUDA events around each batch",
                          "algorithmic_bytes_per_launch": algo_bytes,
                          "launch_ms": launch_ms, "traffic": args.traffic},
-            "cpu_baseline": base, "e2e": e2e, "clocks": clock,
-            "gpu_launches": 6 * args.steps,
+            "cpu_baseline": base, "e2e": e2e, "labelling": label, "clocks": clock,
+            "gpu_launches": 8 * args.steps,
         }
         print(json.dumps(line))
     if world > 1:
@@ -387,6 +448,7 @@ def main(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-threads", type=int, default=4)
+    ap.add_argument("--no-label", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per threshold launch from an ncu capture")
     args = ap.parse_args(argv)

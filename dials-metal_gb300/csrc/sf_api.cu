@@ -11,6 +11,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "sf_api.h"
 #include "sf_common.cuh"
@@ -64,6 +65,9 @@ struct DeviceMarks {
   }
 };
 thread_local DeviceMarks t_marks;
+// Set while a plan captures its launch sequence into a graph: no profiling
+// events are recorded into it.
+thread_local bool t_capturing = false;
 
 int fail(cudaError_t e, const char *what) {
   t_last_error = std::string("CUDA: ") + what + ": " + cudaGetErrorString(e);
@@ -210,14 +214,14 @@ static int threshold_frames(const T *const *d_images, size_t n, size_t h, size_t
     b.out = d_out;
     b.out_stride = capacity;
     b.count_out = d_counts;
-    const StreamMarks *marks = g_profiling ? t_marks.arm() : nullptr;
+    const StreamMarks *marks = g_profiling && !t_capturing ? t_marks.arm() : nullptr;
     t_marks.staged = true;
     cudaError_t e = launch_stream(F, (int)n, (int)h, (int)w, P, b, run_rows, stream, marks);
     if (e != cudaSuccess)
       return fail(e, "launching the threshold");
     return SF_OK;
   }
-  const StreamMarks *marks = g_profiling ? t_marks.arm() : nullptr;
+  const StreamMarks *marks = g_profiling && !t_capturing ? t_marks.arm() : nullptr;
   t_marks.staged = false;
   if (marks)
     cudaEventRecord(marks->start, stream);
@@ -685,3 +689,237 @@ extern "C" int sf_threshold_u32_device_noalloc(
                                     kNoAllocScratchBytes,
                                     static_cast<cudaStream_t>(stream));
 }
+
+// ---------------------------------------------------------------------------
+// Batch plans: one frame shape, its outputs and workspace, a run length tuned
+// on real frames, and the launch sequence captured as CUDA graphs, replayed
+// whenever the same frame buffers come again (a detector loop cycles a fixed
+// set of them).
+// ---------------------------------------------------------------------------
+
+namespace sf {
+
+constexpr size_t kPlanMaxGraphs = 16;
+
+struct Plan {
+  size_t h = 0, w = 0, max_frames = 0, capacity = 0, words = 0;
+  sf_threshold_params params{};
+  int run_rows = 0;  // 0: the default geometry
+  void *ws = nullptr;
+  size_t ws_bytes = 0;
+  sf_signal_pixel *lists = nullptr;
+  uint32_t *masks = nullptr, *counts = nullptr;
+  cudaStream_t capture = nullptr;
+  struct Graph {
+    std::vector<const uint32_t *> frames;
+    cudaGraphExec_t exec = nullptr;
+  };
+  std::vector<Graph> graphs;  // most recently made last
+  bool warm = false;
+
+  ~Plan() {
+    drop_graphs();
+    if (capture)
+      cudaStreamDestroy(capture);
+    cudaFree(ws);
+    cudaFree(lists);
+    cudaFree(masks);
+    cudaFree(counts);
+  }
+  void drop_graphs() {
+    for (Graph &g : graphs)
+      cudaGraphExecDestroy(g.exec);
+    graphs.clear();
+  }
+  int launch(const uint32_t *const *images, size_t n, cudaStream_t s) {
+    return threshold_frames<uint32_t>(images, n, h, w, &params, lists, capacity, masks, counts,
+                                      nullptr, ws, ws_bytes, run_rows, s);
+  }
+};
+
+static int plan_run(Plan &pl, const uint32_t *const *images, size_t n, cudaStream_t s) {
+  if (!images || n == 0 || n > pl.max_frames)
+    return SF_EBADARG;
+  if (!pl.warm) {
+    // The first launch runs directly: one-time set-up (kernel attributes,
+    // occupancy queries) stays outside any capture.
+    const int rc = pl.launch(images, n, s);
+    pl.warm = rc == SF_OK;
+    return rc;
+  }
+  for (size_t i = 0; i < pl.graphs.size(); i++) {
+    Plan::Graph &g = pl.graphs[i];
+    if (g.frames.size() == n && std::equal(g.frames.begin(), g.frames.end(), images)) {
+      const cudaError_t e = cudaGraphLaunch(g.exec, s);
+      return e == cudaSuccess ? SF_OK : fail(e, "cudaGraphLaunch");
+    }
+  }
+  cudaError_t e;
+  if ((e = cudaStreamBeginCapture(pl.capture, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+    return fail(e, "cudaStreamBeginCapture");
+  t_capturing = true;
+  const int rc = pl.launch(images, n, pl.capture);
+  t_capturing = false;
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(pl.capture, &graph);
+  if (rc != SF_OK) {
+    if (graph)
+      cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess)
+    return fail(e, "cudaStreamEndCapture");
+  Plan::Graph g;
+  g.frames.assign(images, images + n);
+  e = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess)
+    return fail(e, "cudaGraphInstantiate");
+  if (pl.graphs.size() == kPlanMaxGraphs) {
+    cudaGraphExecDestroy(pl.graphs.front().exec);
+    pl.graphs.erase(pl.graphs.begin());
+  }
+  pl.graphs.push_back(std::move(g));
+  e = cudaGraphLaunch(pl.graphs.back().exec, s);
+  return e == cudaSuccess ? SF_OK : fail(e, "cudaGraphLaunch");
+}
+
+} // namespace sf
+
+struct sf_plan {
+  sf::Plan impl;
+};
+
+extern "C" {
+
+sf_plan *sf_plan_create(size_t height, size_t width, size_t max_frames, size_t capacity,
+                        const sf_threshold_params *params) {
+  using namespace sf;
+  if (!shape_ok(height, width) || max_frames == 0 || max_frames > (size_t)kMaxBatch ||
+      capacity == 0 || capacity > 0xffffffffu) {
+    t_last_error = "plan: bad shape, batch size or capacity";
+    return nullptr;
+  }
+  LaunchParams P;
+  if (make_launch_params(params, &P) != SF_OK) {
+    t_last_error = "plan: threshold parameters refused";
+    return nullptr;
+  }
+  sf_plan *pl = new sf_plan();
+  Plan &p = pl->impl;
+  p.h = height;
+  p.w = width;
+  p.max_frames = max_frames;
+  p.capacity = capacity;
+  p.words = (width + 31) / 32 * height;
+  if (params)
+    p.params = *params;
+  else
+    sf_default_params(&p.params);
+  p.ws_bytes = sf_batch_workspace_bytes(max_frames, height, width, capacity);
+  cudaError_t e;
+  if ((e = cudaMalloc(&p.ws, p.ws_bytes)) != cudaSuccess ||
+      (e = cudaMalloc(&p.lists, max_frames * capacity * sizeof(sf_signal_pixel))) !=
+          cudaSuccess ||
+      (e = cudaMalloc(&p.masks, max_frames * p.words * sizeof(uint32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&p.counts, max_frames * sizeof(uint32_t))) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&p.capture, cudaStreamNonBlocking)) != cudaSuccess) {
+    fail(e, "plan: device buffers");
+    delete pl;
+    return nullptr;
+  }
+  return pl;
+}
+
+void sf_plan_destroy(sf_plan *plan) {
+  if (!plan)
+    return;
+  cudaDeviceSynchronize();
+  delete plan;
+}
+
+int sf_plan_run(sf_plan *plan, const uint32_t *const *d_images, size_t n_frames, void *stream) {
+  if (!plan)
+    return SF_EBADARG;
+  return sf::plan_run(plan->impl, d_images, n_frames, static_cast<cudaStream_t>(stream));
+}
+
+int sf_plan_tune(sf_plan *plan, const uint32_t *const *d_images, size_t n_frames, void *stream) {
+  using namespace sf;
+  if (!plan || !d_images || n_frames == 0 || n_frames > plan->impl.max_frames)
+    return SF_EBADARG;
+  Plan &p = plan->impl;
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  LaunchParams P;
+  int rc = make_launch_params(&p.params, &P);
+  if (rc != SF_OK)
+    return rc;
+  if (P.algorithm != SF_DISPERSION_EXTENDED || !P.int_ok)
+    return SF_OK;  // the tile path has nothing to tune
+  const int base = stream_default_run_rows(P, (int)p.h, (int)p.w, (int)n_frames);
+  std::vector<int> cands = {base, base / 2, base / 3, base / 4, 2 * base, 64, 128, 256, 512};
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best_ms = 1e30f;
+  int best = base;
+  for (int rr : cands) {
+    if (rr < kMinRunRows || rr > (int)p.h)
+      continue;
+    p.run_rows = rr;
+    float ms[3];
+    for (int it = 0; it < 4; it++) {
+      cudaEventRecord(a, s);
+      if ((rc = p.launch(d_images, n_frames, s)) != SF_OK)
+        break;
+      cudaEventRecord(b, s);
+      cudaEventSynchronize(b);
+      if (it)
+        cudaEventElapsedTime(&ms[it - 1], a, b);
+    }
+    if (rc != SF_OK)
+      break;
+    std::sort(ms, ms + 3);
+    if (ms[1] < best_ms) {
+      best_ms = ms[1];
+      best = rr;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  p.run_rows = best;
+  p.drop_graphs();
+  p.warm = true;
+  return rc;
+}
+
+int sf_plan_run_rows(const sf_plan *plan) { return plan ? plan->impl.run_rows : 0; }
+size_t sf_plan_graphs(const sf_plan *plan) { return plan ? plan->impl.graphs.size() : 0; }
+sf_signal_pixel *sf_plan_lists(const sf_plan *plan) { return plan ? plan->impl.lists : nullptr; }
+uint32_t *sf_plan_counts(const sf_plan *plan) { return plan ? plan->impl.counts : nullptr; }
+uint32_t *sf_plan_masks(const sf_plan *plan) { return plan ? plan->impl.masks : nullptr; }
+
+int sf_plan_result(sf_plan *plan, size_t j, sf_signal_pixel *out, size_t capacity,
+                   size_t *found) {
+  using namespace sf;
+  if (found)
+    *found = 0;
+  if (!plan || !found || j >= plan->impl.max_frames || (!out && capacity))
+    return SF_EBADARG;
+  Plan &p = plan->impl;
+  cudaError_t e;
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess)
+    return fail(e, "cudaDeviceSynchronize");
+  uint32_t n = 0;
+  if ((e = cudaMemcpy(&n, p.counts + j, sizeof(n), cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return fail(e, "reading a plan's count");
+  *found = n;
+  if (n > p.capacity || n > capacity)
+    return SF_EOVERFLOW;
+  if (n && (e = cudaMemcpy(out, p.lists + j * p.capacity, n * sizeof(sf_signal_pixel),
+                           cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return fail(e, "reading a plan's list");
+  return SF_OK;
+}
+
+} // extern "C"

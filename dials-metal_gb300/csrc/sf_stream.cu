@@ -1065,6 +1065,11 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
   return cudaGetLastError();
 }
 
+int stream_default_run_rows(const LaunchParams &P, int h, int w, int nframes) {
+  const int slots = P.half == 2 ? seg_slots<2>() : P.half == 3 ? seg_slots<3>() : seg_slots<4>();
+  return seg_geometry(h, w, nframes, 0, slots).run_rows;
+}
+
 cudaError_t launch_stream(const FramePtrs &F, int nframes, int h, int w, const LaunchParams &P,
                           const StreamBuffers &b, int run_rows, cudaStream_t stream,
                           const StreamMarks *marks) {

@@ -80,6 +80,9 @@ int stream_order_blocks();
 
 void make_stream_tables(const LaunchParams &P, StreamTables *T);
 
+// The run length the default geometry picks for a batch (the tuner's start).
+int stream_default_run_rows(const LaunchParams &P, int h, int w, int nframes);
+
 // Events recorded on the stream between the kernel groups when profiling.
 struct StreamMarks {
   cudaEvent_t start, stage01, stage2, order;

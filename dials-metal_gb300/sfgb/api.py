@@ -108,6 +108,21 @@ def lib() -> ctypes.CDLL:
             getattr(L, name).argtypes = [vp, sz, sz, sz, ctypes.POINTER(ThresholdParams), vp,
                                          sz, u32p, u32p, u32p, vp, sz, vp]
             getattr(L, name).restype = ctypes.c_int
+        L.sf_plan_create.argtypes = [sz, sz, sz, sz, ctypes.POINTER(ThresholdParams)]
+        L.sf_plan_create.restype = vp
+        L.sf_plan_destroy.argtypes = [vp]
+        for name in ("sf_plan_run", "sf_plan_tune"):
+            getattr(L, name).argtypes = [vp, vp, sz, vp]
+            getattr(L, name).restype = ctypes.c_int
+        L.sf_plan_run_rows.argtypes = [vp]
+        L.sf_plan_run_rows.restype = ctypes.c_int
+        L.sf_plan_graphs.argtypes = [vp]
+        L.sf_plan_graphs.restype = sz
+        for name in ("sf_plan_lists", "sf_plan_counts", "sf_plan_masks"):
+            getattr(L, name).argtypes = [vp]
+            getattr(L, name).restype = vp
+        L.sf_plan_result.argtypes = [vp, sz, vp, sz, ctypes.POINTER(sz)]
+        L.sf_plan_result.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -322,3 +337,69 @@ class DeviceBatch:
         bits = np.unpackbits(words.view(np.uint8).reshape(self.h, -1), axis=1,
                              bitorder="little")
         return bits[:, : self.w].astype(bool)
+
+
+class Plan:
+    """A batch plan (sf_plan_*): tuned run length and CUDA-graph replay of
+    the batched threshold for one frame shape; outputs stay on the device."""
+
+    def __init__(self, height: int, width: int, max_frames: int,
+                 capacity: int | None = None, params: Params | None = None):
+        self.h, self.w, self.n = height, width, max_frames
+        self.capacity = capacity if capacity is not None else max(1, height * width // 4)
+        self.words = (width + 31) // 32 * height
+        p = (params or Params()).c()
+        self._p = lib().sf_plan_create(height, width, max_frames, self.capacity,
+                                       ctypes.byref(p))
+        if not self._p:
+            raise SpotFinderError("plan: " + last_error())
+        self._ptrs = (ctypes.c_void_p * MAX_BATCH)()
+
+    def close(self):
+        if self._p:
+            lib().sf_plan_destroy(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _set(self, frames):
+        frames = list(frames)
+        if not 1 <= len(frames) <= self.n:
+            raise ValueError(f"1 to {self.n} frames")
+        for j, f in enumerate(frames):
+            if tuple(f.shape) != (self.h, self.w) or not f.is_contiguous():
+                raise ValueError("contiguous frames of the plan's shape")
+            self._ptrs[j] = f.data_ptr()
+        return len(frames)
+
+    def __call__(self, frames, stream=None) -> None:
+        import torch
+        n = self._set(frames)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        _check(lib().sf_plan_run(self._p, ctypes.cast(self._ptrs, ctypes.c_void_p), n,
+                                 s.cuda_stream), "plan run")
+
+    def tune(self, frames, stream=None) -> int:
+        import torch
+        n = self._set(frames)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        _check(lib().sf_plan_tune(self._p, ctypes.cast(self._ptrs, ctypes.c_void_p), n,
+                                  s.cuda_stream), "plan tune")
+        return lib().sf_plan_run_rows(self._p)
+
+    @property
+    def graphs(self) -> int:
+        return int(lib().sf_plan_graphs(self._p))
+
+    def result(self, j: int) -> np.ndarray:
+        """Wait for the plan's work and return frame j's list (host copy)."""
+        out = np.empty(self.capacity, SIGNAL_DTYPE)
+        found = ctypes.c_size_t(0)
+        rc = lib().sf_plan_result(self._p, j, out.ctypes.data, self.capacity,
+                                  ctypes.byref(found))
+        _check(rc, "plan result")
+        return out[: found.value].copy()

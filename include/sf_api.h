@@ -172,6 +172,35 @@ int sf_threshold_u16_batch_device(const uint16_t *const *d_images, size_t n_fram
                                   uint32_t *d_word_prefix, void *d_workspace,
                                   size_t workspace_bytes, void *stream);
 
+/*
+ * Batch plans (no reference counterpart): one frame shape with its device
+ * outputs and workspace. sf_plan_run enqueues the batched threshold of
+ * n_frames <= max_frames device frames (as sf_threshold_u32_batch_device);
+ * after the first run the launch sequence is captured as a CUDA graph and
+ * replayed whenever the same frame pointers come again (up to 16 pointer
+ * sets are kept). sf_plan_tune times the strip run lengths on the given
+ * frames and keeps the fastest; the results are the same for any run
+ * length. Outputs (device pointers, valid until sf_plan_destroy): frame j's
+ * list at sf_plan_lists(p) + j * capacity, its count at sf_plan_counts(p)[j],
+ * its mask at sf_plan_masks(p) + j * ceil(width/32) * height. NULL on failure
+ * (the reason in sf_last_error()).
+ */
+typedef struct sf_plan sf_plan;
+sf_plan *sf_plan_create(size_t height, size_t width, size_t max_frames, size_t capacity,
+                        const sf_threshold_params *params);
+void sf_plan_destroy(sf_plan *plan);
+int sf_plan_run(sf_plan *plan, const uint32_t *const *d_images, size_t n_frames, void *stream);
+int sf_plan_tune(sf_plan *plan, const uint32_t *const *d_images, size_t n_frames, void *stream);
+int sf_plan_run_rows(const sf_plan *plan);
+size_t sf_plan_graphs(const sf_plan *plan);
+sf_signal_pixel *sf_plan_lists(const sf_plan *plan);
+uint32_t *sf_plan_counts(const sf_plan *plan);
+uint32_t *sf_plan_masks(const sf_plan *plan);
+/* Waits for the plan's work and copies frame j's list to the host: 0, or -2
+ * with *found the count when it exceeds the plan's or this capacity. */
+int sf_plan_result(sf_plan *plan, size_t j, sf_signal_pixel *out, size_t capacity,
+                   size_t *found);
+
 /* ---- 3-D spot labelling (src/spots/dials_spots.hh) ---- */
 
 /* dials_spots::Pixel (src/spots/dials_spots.hh:50-54): a signal pixel of an
