@@ -489,47 +489,150 @@ __device__ void bitonic_sort(uint32_t *s, int m, int t, int nt, bool warp_only) 
   }
 }
 
+// The first-pass sums of the reference's emit() (dials_spots.cc:240-276) in
+// integers. Every term of its double accumulations is an integer (the value,
+// its square) or a half-integer (the value times a pixel centre c + 0.5), so
+// while each sum stays below 2^53 (2^52 for the half-integers) every partial
+// sum is exact in double and the doubles equal these integers, whatever the
+// order. W[ax] holds twice the weighted sum. `exact` is false when a bound
+// could fail; the double sequence then runs instead.
+struct FirstPass {
+  unsigned long long S, Q2, W[3];
+  int32_t bb[6];  // x0, x1, y0, y1, z0, z1
+  // The brightest pixel, ties to the first in member order; none (all ones)
+  // until a value above 0, where the reference's peak stays at (0, 0, 0).
+  uint32_t peak_v, peak_k;
+  bool exact;
+};
+
+__device__ __forceinline__ void fp_init(FirstPass &f) {
+  f.S = f.Q2 = f.W[0] = f.W[1] = f.W[2] = 0;
+  f.bb[0] = f.bb[2] = f.bb[4] = INT_MAX;
+  f.bb[1] = f.bb[3] = f.bb[5] = INT_MIN;
+  f.peak_v = 0;
+  f.peak_k = 0xFFFFFFFFu;
+  f.exact = true;
+}
+
+__device__ __forceinline__ void fp_add(FirstPass &f, uint32_t k, uint32_t v, int32_t x,
+                                       int32_t y, int32_t z) {
+  // v < 2^26 keeps v^2 < 2^52; coordinates below 2^20 keep v (2c + 1) < 2^53;
+  // negative frames would make partial sums exceed the total.
+  f.exact = f.exact && v < (1u << 26) && z >= 0 && x < (1 << 20) && y < (1 << 20) &&
+            z < (1 << 20);
+  const unsigned long long vv = v;
+  f.S += vv;
+  f.Q2 += vv * vv;
+  f.W[0] += vv * (unsigned long long)(2 * x + 1);
+  f.W[1] += vv * (unsigned long long)(2 * y + 1);
+  f.W[2] += vv * (unsigned long long)(2 * (long long)z + 1);
+  f.bb[0] = min(f.bb[0], x), f.bb[1] = max(f.bb[1], x + 1);
+  f.bb[2] = min(f.bb[2], y), f.bb[3] = max(f.bb[3], y + 1);
+  f.bb[4] = min(f.bb[4], z), f.bb[5] = max(f.bb[5], z + 1);
+  if (v > 0 && (v > f.peak_v || (v == f.peak_v && k < f.peak_k))) {
+    f.peak_v = v;
+    f.peak_k = k;
+  }
+}
+
+__device__ __forceinline__ void fp_merge(FirstPass &f, const FirstPass &g) {
+  f.S += g.S;
+  f.Q2 += g.Q2;
+  for (int a = 0; a < 3; a++)
+    f.W[a] += g.W[a];
+  for (int a = 0; a < 6; a += 2) {
+    f.bb[a] = min(f.bb[a], g.bb[a]);
+    f.bb[a + 1] = max(f.bb[a + 1], g.bb[a + 1]);
+  }
+  if (g.peak_k != 0xFFFFFFFFu &&
+      (g.peak_v > f.peak_v || (g.peak_v == f.peak_v && g.peak_k < f.peak_k))) {
+    f.peak_v = g.peak_v;
+    f.peak_k = g.peak_k;
+  }
+  f.exact = f.exact && g.exact;
+}
+
+__device__ __forceinline__ bool fp_finish(FirstPass &f) {
+  const unsigned long long lim = 1ull << 53;
+  f.exact = f.exact && f.S < lim && f.Q2 < lim && f.W[0] < lim && f.W[1] < lim && f.W[2] < lim;
+  return f.exact;
+}
+
+// The member's pixel: (x, y, z) and value.
+__device__ __forceinline__ void member(const uint32_t q, const int32_t *frame,
+                                       const uint32_t *index, const uint32_t *value,
+                                       uint32_t width, int32_t *x, int32_t *y, int32_t *z,
+                                       uint32_t *v) {
+  const uint32_t idx = index[q];
+  *x = (int32_t)(idx % width);
+  *y = (int32_t)(idx / width);
+  *z = frame[q];
+  *v = value[q];
+}
+
 // The reference's emit() (dials_spots.cc:240-353) over members sorted into
-// (frame, index) order, sequentially in double: the same operations in the
-// same order. Returns false if the peak-centroid filter rejects it.
+// (frame, index) order: the first pass from exact integers when they are
+// exact (else the double sequence), then the variance pass sequentially in
+// double, the same operations in the same order as the reference. The
+// variance pass is skipped when only acceptance is wanted. Returns false if
+// the peak-centroid filter rejects the spot.
 __device__ bool emit_spot(const uint32_t *mem, uint32_t n, const int32_t *frame,
                           const uint32_t *index, const uint32_t *value, uint32_t width,
-                          double max_separation, sf_spot *spot) {
-  double sum = 0.0, sum_sq = 0.0;
-  double weighted[3] = {0.0, 0.0, 0.0};
-  int32_t x0 = 0, x1 = 0, y0 = 0, y1 = 0, z0 = 0, z1 = 0;
-  uint32_t peak_value = 0;
-  double peak[3] = {0.0, 0.0, 0.0};
-  for (uint32_t k = 0; k < n; k++) {
-    const uint32_t q = mem[k];
-    const uint32_t idx = index[q];
-    const int32_t x = (int32_t)(idx % width), y = (int32_t)(idx / width), z = frame[q];
-    if (k == 0) {
-      x0 = x, x1 = x + 1, y0 = y, y1 = y + 1, z0 = z, z1 = z + 1;
-    } else {
-      x0 = x < x0 ? x : x0;
-      x1 = x + 1 > x1 ? x + 1 : x1;
-      y0 = y < y0 ? y : y0;
-      y1 = y + 1 > y1 ? y + 1 : y1;
-      z0 = z < z0 ? z : z0;
-      z1 = z + 1 > z1 ? z + 1 : z1;
+                          double max_separation, sf_spot *spot, bool variance = true,
+                          const FirstPass *given = nullptr) {
+  FirstPass f;
+  if (given) {
+    f = *given;
+  } else {
+    fp_init(f);
+    for (uint32_t k = 0; k < n; k++) {
+      int32_t x, y, z;
+      uint32_t v;
+      member(mem[k], frame, index, value, width, &x, &y, &z, &v);
+      fp_add(f, k, v, x, y, z);
     }
-    const uint32_t v = value[q];
-    const double val = (double)v;
-    const double pos[3] = {__dadd_rn((double)x, 0.5), __dadd_rn((double)y, 0.5),
-                           __dadd_rn((double)z, 0.5)};
-    sum = __dadd_rn(sum, val);
-    sum_sq = __dadd_rn(sum_sq, __dmul_rn(val, val));
+    fp_finish(f);
+  }
+  double sum, sum_sq, weighted[3], peak[3];
+  if (f.exact) {
+    sum = (double)f.S;
+    sum_sq = (double)f.Q2;
     for (int ax = 0; ax < 3; ax++)
-      weighted[ax] = __dadd_rn(weighted[ax], __dmul_rn(val, pos[ax]));
-    if (v > peak_value) {
-      peak_value = v;
-      peak[0] = pos[0], peak[1] = pos[1], peak[2] = pos[2];
+      weighted[ax] = __dmul_rn((double)f.W[ax], 0.5);  // exact: W < 2^53
+    peak[0] = peak[1] = peak[2] = 0.0;
+    if (f.peak_k != 0xFFFFFFFFu) {
+      int32_t px, py, pz;
+      uint32_t pv;
+      member(mem[f.peak_k], frame, index, value, width, &px, &py, &pz, &pv);
+      peak[0] = __dadd_rn((double)px, 0.5);
+      peak[1] = __dadd_rn((double)py, 0.5);
+      peak[2] = __dadd_rn((double)pz, 0.5);
+    }
+  } else {
+    sum = sum_sq = 0.0;
+    weighted[0] = weighted[1] = weighted[2] = 0.0;
+    peak[0] = peak[1] = peak[2] = 0.0;
+    uint32_t peak_value = 0;
+    for (uint32_t k = 0; k < n; k++) {
+      int32_t x, y, z;
+      uint32_t v;
+      member(mem[k], frame, index, value, width, &x, &y, &z, &v);
+      const double val = (double)v;
+      const double pos[3] = {__dadd_rn((double)x, 0.5), __dadd_rn((double)y, 0.5),
+                             __dadd_rn((double)z, 0.5)};
+      sum = __dadd_rn(sum, val);
+      sum_sq = __dadd_rn(sum_sq, __dmul_rn(val, val));
+      for (int ax = 0; ax < 3; ax++)
+        weighted[ax] = __dadd_rn(weighted[ax], __dmul_rn(val, pos[ax]));
+      if (v > peak_value) {
+        peak_value = v;
+        peak[0] = pos[0], peak[1] = pos[1], peak[2] = pos[2];
+      }
     }
   }
   sf_spot s;
-  s.bbox[0] = x0, s.bbox[1] = x1, s.bbox[2] = y0, s.bbox[3] = y1, s.bbox[4] = z0,
-  s.bbox[5] = z1;
+  for (int a = 0; a < 6; a++)
+    s.bbox[a] = f.bb[a];
   s.intensity = sum;
   s.intensity_variance = sum;
   s.n_signal = n;
@@ -539,28 +642,30 @@ __device__ bool emit_spot(const uint32_t *mem, uint32_t n, const int32_t *frame,
   if (sum > 0.0) {
     for (int ax = 0; ax < 3; ax++)
       s.position[ax] = __ddiv_rn(weighted[ax], sum);
-    double delta_sq[3] = {0.0, 0.0, 0.0};
-    for (uint32_t k = 0; k < n; k++) {
-      const uint32_t q = mem[k];
-      const uint32_t idx = index[q];
-      const double val = (double)value[q];
-      const double pos[3] = {__dadd_rn((double)(idx % width), 0.5),
-                             __dadd_rn((double)(idx / width), 0.5),
-                             __dadd_rn((double)frame[q], 0.5)};
-      for (int ax = 0; ax < 3; ax++) {
-        const double d = __dsub_rn(pos[ax], s.position[ax]);
-        delta_sq[ax] = __dadd_rn(delta_sq[ax], __dmul_rn(__dmul_rn(val, d), d));
+    if (variance) {
+      double delta_sq[3] = {0.0, 0.0, 0.0};
+      for (uint32_t k = 0; k < n; k++) {
+        int32_t x, y, z;
+        uint32_t v;
+        member(mem[k], frame, index, value, width, &x, &y, &z, &v);
+        const double val = (double)v;
+        const double pos[3] = {__dadd_rn((double)x, 0.5), __dadd_rn((double)y, 0.5),
+                               __dadd_rn((double)z, 0.5)};
+        for (int ax = 0; ax < 3; ax++) {
+          const double d = __dsub_rn(pos[ax], s.position[ax]);
+          delta_sq[ax] = __dadd_rn(delta_sq[ax], __dmul_rn(__dmul_rn(val, d), d));
+        }
       }
-    }
-    const double ss = __dmul_rn(sum, sum);
-    if (ss > sum_sq) {
-      for (int ax = 0; ax < 3; ax++) {
-        const double var = __ddiv_rn(__dmul_rn(delta_sq[ax], sum), __dsub_rn(ss, sum_sq));
-        s.variance[ax] = __dadd_rn(__ddiv_rn(var, sum), pixel_variance);
+      const double ss = __dmul_rn(sum, sum);
+      if (ss > sum_sq) {
+        for (int ax = 0; ax < 3; ax++) {
+          const double var = __ddiv_rn(__dmul_rn(delta_sq[ax], sum), __dsub_rn(ss, sum_sq));
+          s.variance[ax] = __dadd_rn(__ddiv_rn(var, sum), pixel_variance);
+        }
+      } else {
+        for (int ax = 0; ax < 3; ax++)
+          s.variance[ax] = pixel_variance;
       }
-    } else {
-      for (int ax = 0; ax < 3; ax++)
-        s.variance[ax] = pixel_variance;
     }
     if (s.bbox[5] == s.bbox[4] + 1)
       s.position[2] = __dadd_rn((double)s.bbox[4], 0.5);
@@ -610,10 +715,35 @@ k_sort_accept(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ c
       bitonic_sort(s, (int)n, lane, 32, true);
       for (uint32_t i = lane; i < n; i += 32)
         m[i] = s[i];
+      // The first pass across the warp, exact in integers.
+      FirstPass f;
+      fp_init(f);
+      for (uint32_t i = lane; i < n; i += 32) {
+        int32_t x, y, z;
+        uint32_t v;
+        member(s[i], frame, index, value, a.width, &x, &y, &z, &v);
+        fp_add(f, i, v, x, y, z);
+      }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        FirstPass g;
+        g.S = __shfl_xor_sync(0xffffffffu, f.S, o);
+        g.Q2 = __shfl_xor_sync(0xffffffffu, f.Q2, o);
+        for (int ax = 0; ax < 3; ax++)
+          g.W[ax] = __shfl_xor_sync(0xffffffffu, f.W[ax], o);
+        for (int b = 0; b < 6; b++)
+          g.bb[b] = __shfl_xor_sync(0xffffffffu, f.bb[b], o);
+        g.peak_v = __shfl_xor_sync(0xffffffffu, f.peak_v, o);
+        g.peak_k = __shfl_xor_sync(0xffffffffu, f.peak_k, o);
+        g.exact = __shfl_xor_sync(0xffffffffu, f.exact ? 1 : 0, o) != 0;
+        fp_merge(f, g);
+      }
       __syncwarp();
       if (lane == 0) {
+        fp_finish(f);
         sf_spot spot;
-        const bool ok = emit_spot(s, n, frame, index, value, a.width, a.max_separation, &spot);
+        const bool ok = emit_spot(s, n, frame, index, value, a.width, a.max_separation, &spot,
+                                  false, f.exact ? &f : nullptr);
         acc[c] = ok ? 1u : 0u;
         acc_n[c] = ok ? n : 0u;
         separated += ok ? 0u : 1u;
@@ -643,7 +773,8 @@ k_sort_accept(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ c
       for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
         m[i] = s_sort[i];
       if (threadIdx.x == 0) {
-        s_ok = emit_spot(s_sort, n, frame, index, value, a.width, a.max_separation, &s_spot)
+        s_ok = emit_spot(s_sort, n, frame, index, value, a.width, a.max_separation, &s_spot,
+                         false)
                    ? 1u : 0u;
         acc[c] = s_ok;
         acc_n[c] = s_ok ? n : 0u;
@@ -657,7 +788,12 @@ k_sort_accept(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ c
 }
 
 // Accepted spots and their pixels into the batch outputs (dials_spots.cc:
-// 355-359): spot k's pixels at acc_off[k] in member order.
+// 355-359): spot k's pixels at acc_off[k] in member order. Four lanes to a
+// candidate: the first pass split four ways (exact integers), then each of
+// three lanes runs one axis of the variance pass -- a sequence of rounded
+// double additions in member order, as the reference -- and lane 0 writes
+// the spot. Where the integers could be inexact lane 0 runs the whole
+// reference sequence alone.
 __global__ void __launch_bounds__(kThreads)
 k_write(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ cand_n,
         const uint32_t *__restrict__ cand_off, const uint32_t *__restrict__ members,
@@ -668,31 +804,111 @@ k_write(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ cand_n,
   if (st->error)
     return;
   const uint32_t ncand = st->n_cand;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nwarps = blockDim.x >> 5;
-  for (uint32_t c = blockIdx.x * nwarps + warp; c < ncand; c += gridDim.x * nwarps) {
-    if (!acc[c])
-      continue;
-    const uint32_t n = cand_n[c];
-    const uint32_t si = acc_idx[c], po = acc_off[c];
-    if (si >= spots_cap || (size_t)po + n > pixels_cap) {
-      if (lane == 0)
-        atomicOr(&st->error, kErrOutFull);
-      continue;
+  const int lane = threadIdx.x & 31, sub = lane & 3;
+  const uint32_t per_pass = (gridDim.x * blockDim.x) >> 2;
+  for (uint32_t base = (blockIdx.x * blockDim.x) >> 2; base < ncand; base += per_pass) {
+    const uint32_t c = base + (threadIdx.x >> 2);
+    bool live = c < ncand && acc[c];
+    uint32_t n = 0, si = 0, po = 0;
+    const uint32_t *m = nullptr;
+    if (live) {
+      n = cand_n[c];
+      si = acc_idx[c];
+      po = acc_off[c];
+      m = members + cand_off[c];
+      if (si >= spots_cap || (size_t)po + n > pixels_cap) {
+        if (sub == 0)
+          atomicOr(&st->error, kErrOutFull);
+        live = false;
+      }
     }
-    const uint32_t *m = members + cand_off[c];
-    for (uint32_t k = lane; k < n; k += 32) {
-      const uint32_t q = m[k];
-      sf_pixel px;
-      px.frame = frame[q];
-      px.index = index[q];
-      px.value = value[q];
-      pixels[po + k] = px;
+    FirstPass f;
+    fp_init(f);
+    if (live)
+      for (uint32_t k = sub; k < n; k += 4) {
+        const uint32_t q = m[k];
+        int32_t x, y, z;
+        uint32_t v;
+        member(q, frame, index, value, a.width, &x, &y, &z, &v);
+        fp_add(f, k, v, x, y, z);
+        sf_pixel px;
+        px.frame = z;
+        px.index = index[q];
+        px.value = v;
+        pixels[po + k] = px;
+      }
+#pragma unroll
+    for (int o = 1; o <= 2; o <<= 1) {
+      FirstPass g;
+      g.S = __shfl_xor_sync(0xffffffffu, f.S, o);
+      g.Q2 = __shfl_xor_sync(0xffffffffu, f.Q2, o);
+      for (int ax = 0; ax < 3; ax++)
+        g.W[ax] = __shfl_xor_sync(0xffffffffu, f.W[ax], o);
+      for (int bb = 0; bb < 6; bb++)
+        g.bb[bb] = __shfl_xor_sync(0xffffffffu, f.bb[bb], o);
+      g.peak_v = __shfl_xor_sync(0xffffffffu, f.peak_v, o);
+      g.peak_k = __shfl_xor_sync(0xffffffffu, f.peak_k, o);
+      g.exact = __shfl_xor_sync(0xffffffffu, f.exact ? 1 : 0, o) != 0;
+      fp_merge(f, g);
     }
-    if (lane == 0) {
-      sf_spot spot;
-      emit_spot(m, n, frame, index, value, a.width, a.max_separation, &spot);
-      spot.first = po; // batch-local; the host adds the run's offset
+    fp_finish(f);
+    double var_ax = 0.0;
+    sf_spot spot;
+    if (live && f.exact) {
+      // This lane's axis of the variance pass (lanes 0, 1, 2).
+      const double sum = (double)f.S, sum_sq = (double)f.Q2;
+      double pos_c[3];
+      for (int ax = 0; ax < 3; ax++)
+        pos_c[ax] = __ddiv_rn(__dmul_rn((double)f.W[ax], 0.5), sum);
+      if (sub < 3 && sum > 0.0) {
+        double delta_sq = 0.0;
+        const double centre = pos_c[sub];
+        for (uint32_t k = 0; k < n; k++) {
+          const uint32_t q = m[k];
+          int32_t x, y, z;
+          uint32_t v;
+          member(q, frame, index, value, a.width, &x, &y, &z, &v);
+          const int32_t coord = sub == 0 ? x : sub == 1 ? y : z;
+          const double d = __dsub_rn(__dadd_rn((double)coord, 0.5), centre);
+          delta_sq = __dadd_rn(delta_sq, __dmul_rn(__dmul_rn((double)v, d), d));
+        }
+        const double ss = __dmul_rn(sum, sum);
+        var_ax = ss > sum_sq
+                     ? __dadd_rn(__ddiv_rn(__ddiv_rn(__dmul_rn(delta_sq, sum),
+                                                     __dsub_rn(ss, sum_sq)),
+                                           sum),
+                                 1.0 / 12.0)
+                     : 1.0 / 12.0;
+      }
+      for (int b6 = 0; b6 < 6; b6++)
+        spot.bbox[b6] = f.bb[b6];
+      spot.intensity = sum;
+      spot.intensity_variance = sum;
+      spot.n_signal = n;
+      if (sum > 0.0) {
+        spot.position[0] = pos_c[0];
+        spot.position[1] = pos_c[1];
+        spot.position[2] = spot.bbox[5] == spot.bbox[4] + 1
+                               ? __dadd_rn((double)spot.bbox[4], 0.5) : pos_c[2];
+      } else {
+        spot.position[0] = __ddiv_rn((double)(spot.bbox[1] + spot.bbox[0]), 2.0);
+        spot.position[1] = __ddiv_rn((double)(spot.bbox[3] + spot.bbox[2]), 2.0);
+        spot.position[2] = __ddiv_rn((double)(spot.bbox[5] + spot.bbox[4]), 2.0);
+      }
+    }
+    // Lane 0 of each group gathers the three axes' variances.
+    const double v1 = __shfl_down_sync(0xffffffffu, var_ax, 1);
+    const double v2 = __shfl_down_sync(0xffffffffu, var_ax, 2);
+    if (live && sub == 0) {
+      if (f.exact) {
+        const bool spread = (double)f.S > 0.0;
+        spot.variance[0] = spread ? var_ax : 0.0;
+        spot.variance[1] = spread ? v1 : 0.0;
+        spot.variance[2] = spread ? v2 : 0.0;
+      } else {
+        emit_spot(m, n, frame, index, value, a.width, a.max_separation, &spot);
+      }
+      spot.first = po;  // batch-local; the host adds the run's offset
       spots[si] = spot;
     }
   }
@@ -742,6 +958,44 @@ template <typename T> static cudaError_t dalloc(T **p, size_t n) {
   return cudaMalloc(reinterpret_cast<void **>(p), (n ? n : 1) * sizeof(T));
 }
 
+// A host array in page-locked memory, grown by doubling: the batches' spots
+// and pixels come back by direct DMA rather than through a pageable bounce.
+template <typename T> struct PinnedVec {
+  T *p = nullptr;
+  size_t n = 0, cap = 0;
+  PinnedVec() = default;
+  PinnedVec(const PinnedVec &) = delete;
+  PinnedVec &operator=(const PinnedVec &) = delete;
+  ~PinnedVec() {
+    if (p)
+      cudaFreeHost(p);
+  }
+  size_t size() const { return n; }
+  bool empty() const { return n == 0; }
+  T *data() { return p; }
+  const T *data() const { return p; }
+  T &operator[](size_t i) { return p[i]; }
+  cudaError_t resize(size_t m) {
+    if (m > cap) {
+      size_t c = cap ? cap : 1024;
+      while (c < m)
+        c *= 2;
+      T *q = nullptr;
+      const cudaError_t e = cudaMallocHost(&q, c * sizeof(T));
+      if (e != cudaSuccess)
+        return e;
+      if (n)
+        std::memcpy(q, p, n * sizeof(T));
+      if (p)
+        cudaFreeHost(p);
+      p = q;
+      cap = c;
+    }
+    n = m;
+    return cudaSuccess;
+  }
+};
+
 struct Labeller {
   size_t height = 0, width = 0, capacity = 0, spots_cap = 0;
   sf_label_options opt;
@@ -771,8 +1025,8 @@ struct Labeller {
   sf_signal_pixel *d_list = nullptr;
   size_t d_list_cap = 0;
   uint32_t *d_counts = nullptr;
-  std::vector<sf_spot> spots;
-  std::vector<sf_pixel> pixels;
+  PinnedVec<sf_spot> spots;
+  PinnedVec<sf_pixel> pixels;
   sf_counts counts{};
   uint32_t live = 0;
   std::string error;
@@ -960,8 +1214,9 @@ struct Labeller {
     }
     const uint32_t na = host_st->n_accept, npx = host_st->n_accept_pixels;
     const size_t s0 = spots.size(), p0 = pixels.size();
-    spots.resize(s0 + na);
-    pixels.resize(p0 + npx);
+    if ((e = spots.resize(s0 + na)) != cudaSuccess ||
+        (e = pixels.resize(p0 + npx)) != cudaSuccess)
+      return fail(e, "cudaMallocHost for the labeller's results");
     if (na &&
         (e = cudaMemcpyAsync(spots.data() + s0, d_spots, na * sizeof(sf_spot),
                              cudaMemcpyDeviceToHost, s)) != cudaSuccess)
