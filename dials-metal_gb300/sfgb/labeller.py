@@ -97,15 +97,7 @@ class DeviceLabeller:
         return self.result()
 
     def result(self) -> LabelResult:
-        L = _lib()
-        ns, npx = L.sf_label_n_spots(self._h), L.sf_label_n_pixels(self._h)
-        spots = np.zeros(ns, SPOT_DTYPE)
-        pixels = np.zeros(npx, PIXEL_DTYPE)
-        self._check(L.sf_label_spots(self._h, spots.ctypes.data, ns), "spots")
-        self._check(L.sf_label_pixels(self._h, pixels.ctypes.data, npx), "pixels")
-        c = np.zeros(6, np.uint64)
-        L.sf_label_counts(self._h, c.ctypes.data)
-        return LabelResult(spots, pixels, dict(zip(COUNT_NAMES, map(int, c))))
+        return result_of(self._h)
 
     @property
     def live(self) -> int:
@@ -118,3 +110,18 @@ class DeviceLabeller:
 
     def __del__(self):
         self.close()
+
+
+def result_of(handle) -> LabelResult:
+    """The spots, kept pixels and counts a labeller handle holds so far."""
+    L = _lib()
+    ns, npx = L.sf_label_n_spots(handle), L.sf_label_n_pixels(handle)
+    spots = np.zeros(ns, SPOT_DTYPE)
+    pixels = np.zeros(npx, PIXEL_DTYPE)
+    for rc, what in ((L.sf_label_spots(handle, spots.ctypes.data, ns), "spots"),
+                     (L.sf_label_pixels(handle, pixels.ctypes.data, npx), "pixels")):
+        if rc != 0:
+            raise RuntimeError(f"{what}: {api.last_error()} ({rc})")
+    c = np.zeros(6, np.uint64)
+    L.sf_label_counts(handle, c.ctypes.data)
+    return LabelResult(spots, pixels, dict(zip(COUNT_NAMES, map(int, c))))

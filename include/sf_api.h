@@ -32,6 +32,7 @@ extern "C" {
 #define SF_EOVERFLOW (-2)
 #define SF_ECUDA (-3)
 #define SF_EUNSUPPORTED (-4)
+#define SF_EBUSY (-5) /* the served form's device-memory budget is taken */
 
 /* src/spots/signal_pixel.hh:20-28: one surviving pixel, 16 bytes. */
 typedef struct {
@@ -306,6 +307,54 @@ int sf_threshold_u32_device_noalloc(const uint32_t *d_image, size_t height,
                                     sf_signal_pixel *d_out, size_t capacity,
                                     uint32_t *d_bits, uint32_t *d_count,
                                     uint32_t *d_word_prefix, void *stream);
+
+/*
+ * The served form (no reference counterpart; the reference's mxi_find reads
+ * one sweep from disk): a request loop for frames arriving from several
+ * detector streams at once. Each open sweep keeps its frame ring and its 3-D
+ * labeller resident on the device; sweeps are admitted against a device
+ * memory budget (sf_server_open_sweep returns SF_EBUSY when it is taken:
+ * retry once another sweep closes). Frames are submitted in ascending order
+ * per sweep from host memory (page-locked, e.g. sf_host_alloc, for a fast
+ * copy) that must stay untouched until the frame is reported done. A worker
+ * thread copies them in, thresholds whatever is ready across sweeps of one
+ * shape and parameter set in one launch (up to max_batch frames) and labels
+ * each sweep's frames in order; sf_server_poll returns the finished frames
+ * with their submit-to-labelled latency. After sf_server_finish_sweep the
+ * sweep's spots are read from its labeller (sf_server_labeller, sf_label_*).
+ * A frame's results do not depend on the other sweeps in the mix.
+ */
+typedef struct {
+  size_t hbm_budget;       /* device bytes for sweeps; 0: 80% of the free memory */
+  size_t max_batch;        /* frames per threshold launch, 1..SF_MAX_BATCH (16) */
+  size_t ring;             /* device frame slots per sweep, >= max_batch (32) */
+  size_t capacity_divisor; /* signal-list capacity = pixels / this (16) */
+} sf_server_options;
+
+typedef struct {
+  int64_t sweep, frame;
+  uint32_t n_signal;       /* signal pixels of the frame */
+  int status;              /* 0, or the error code of its sweep */
+  double latency_ms;       /* from sf_server_submit to labelled */
+} sf_frame_done;
+
+typedef struct sf_server sf_server;
+void sf_default_server_options(sf_server_options *options);
+sf_server *sf_server_open(const sf_server_options *options);
+void sf_server_close(sf_server *server);
+size_t sf_server_sweep_bytes(const sf_server *server, size_t height, size_t width,
+                             const sf_label_options *label);
+size_t sf_server_used_bytes(const sf_server *server);
+int sf_server_open_sweep(sf_server *server, size_t height, size_t width,
+                         const sf_threshold_params *params, const sf_label_options *label,
+                         int64_t *sweep);
+int sf_server_submit(sf_server *server, int64_t sweep, int64_t frame,
+                     const uint32_t *host_frame);
+/* Up to max finished frames; waits up to wait_ms for the first one. */
+size_t sf_server_poll(sf_server *server, sf_frame_done *out, size_t max, int wait_ms);
+int sf_server_finish_sweep(sf_server *server, int64_t sweep);
+sf_labeller *sf_server_labeller(sf_server *server, int64_t sweep);
+int sf_server_close_sweep(sf_server *server, int64_t sweep);
 
 #ifdef __cplusplus
 }

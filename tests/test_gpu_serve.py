@@ -1,0 +1,120 @@
+"""The served form (sf_server_*): sweeps submitted frame by frame from several
+streams at once give, sweep for sweep, the spots the reference's labeller
+gives for that sweep alone (golden fixture and oracle), whatever they are
+mixed with; admission is by the device-memory budget."""
+import os
+import threading
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def serve():
+    from sfgb import api, serve as s
+    if not api.available():
+        pytest.fail("no usable GB300: " + api.unavailable_reason())
+    return s
+
+
+def _oracle_sweep(frames, numbers):
+    lab = O.Labeller(frames[0].shape[0], frames[0].shape[1])
+    for f, n in zip(frames, numbers):
+        lab.add(n, O.dext(f))
+    return lab.finish()
+
+
+def _synth(h, w, n, seed):
+    from sfgb import synth
+    sw = synth.Sweep(synth.preset("plain_1m", height=h, width=w, n_frames=n,
+                                  spots_per_frame=h * w / 1500.0, seed=seed,
+                                  row_band_start=h // 3, row_band_len=3,
+                                  col_band_start=w // 4, col_band_len=2, n_hot=5))
+    return [sw.frame(i) for i in range(n)]
+
+
+def test_one_sweep_matches_golden(serve):
+    g = np.load(os.path.join(GOLDEN, "sweep_small.npz"))
+    frames = [np.ascontiguousarray(f) for f in g["frames"]]
+    srv = serve.Server(max_batch=4, ring=8)
+    sid = srv.open_sweep(*frames[0].shape)
+    for i, f in enumerate(frames):
+        srv.submit(sid, i, f)
+    res = srv.finish_sweep(sid)
+    done = []
+    while len(done) < len(frames):
+        done += srv.poll(wait_ms=100)
+    assert O.spot_fields_equal(res.spots, g["spots_3d"])
+    assert res.pixels.tobytes() == g["pixels_3d"].tobytes()
+    by_frame = {d["frame"]: d for d in done}
+    for i in range(len(frames)):
+        assert by_frame[i]["status"] == 0
+        assert by_frame[i]["n_signal"] == len(g[f"signal_{i}"])
+        assert by_frame[i]["latency_ms"] > 0
+    srv.close_sweep(sid)
+    srv.close()
+
+
+def test_same_alone_and_in_the_mix(serve):
+    sweeps = {
+        "a": (_synth(300, 350, 14, 1), list(range(14))),
+        "b": (_synth(300, 350, 11, 2), [3 + i + (4 if i > 5 else 0) for i in range(11)]),
+        "c": (_synth(200, 260, 17, 3), list(range(17))),
+    }
+    want = {k: _oracle_sweep(*v) for k, v in sweeps.items()}
+    srv = serve.Server(max_batch=5, ring=6)
+    ids = {k: srv.open_sweep(*v[0][0].shape) for k, v in sweeps.items()}
+
+    def feed(k):
+        frames, numbers = sweeps[k]
+        for f, n in zip(frames, numbers):
+            srv.submit(ids[k], n, f)
+
+    threads = [threading.Thread(target=feed, args=(k,)) for k in sweeps]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    got = {k: srv.finish_sweep(ids[k]) for k in sweeps}
+    for k in sweeps:
+        assert O.spot_fields_equal(got[k].spots, want[k].spots), k
+        assert got[k].pixels.tobytes() == want[k].pixels.tobytes(), k
+        assert got[k].counts == want[k].counts, k
+        srv.close_sweep(ids[k])
+    srv.close()
+
+
+def test_admission_by_budget(serve):
+    probe = serve.Server(hbm_budget=1 << 40, max_batch=4, ring=8)
+    probe.close_sweep(probe.open_sweep(256, 320))
+    probe_sweep = probe.open_sweep(256, 320)
+    one = probe.used_bytes  # a sweep and its shape group
+    probe.close_sweep(probe_sweep)
+    probe.close()
+    srv = serve.Server(hbm_budget=int(one * 1.3), max_batch=4, ring=8)
+    a = srv.open_sweep(256, 320)
+    with pytest.raises(serve.Busy):
+        srv.open_sweep(256, 320)
+    srv.close_sweep(a)
+    b = srv.open_sweep(256, 320)
+    assert srv.used_bytes > 0
+    srv.close_sweep(b)
+    srv.close()
+
+
+def test_out_of_order_refused(serve):
+    srv = serve.Server(max_batch=2, ring=2)
+    sid = srv.open_sweep(64, 64)
+    f = np.zeros((64, 64), np.uint32)
+    srv.submit(sid, 5, f)
+    with pytest.raises(ValueError):
+        srv.submit(sid, 5, f)
+    with pytest.raises(ValueError):
+        srv.submit(sid, 4, f)
+    srv.finish_sweep(sid)
+    srv.close()
