@@ -1,19 +1,21 @@
 // The served form (include/sf_api.h, sf_server_*): a request loop for frames
 // that arrive from several detector streams at once.
 //
-// Every open sweep keeps its state on the device: a ring of frame slots and
-// its 3-D labeller (the open components and their pixels, dials_spots.cc).
-// Sweeps are admitted against a device-memory budget. One worker thread runs
-// the loop:
-//   1. submitted host frames go to free slots of their sweep, copied on a
-//      copy stream while the GPU computes;
-//   2. frames already on the device form a batch (continuous batching: what
-//      is ready now, across sweeps of one frame shape and parameter set, up
-//      to max_batch) and one threshold launch sequence handles it on the
-//      compute stream, into one of two output sets;
-//   3. meanwhile the previous batch is labelled, each sweep's frames in
-//      frame order, on a label stream; when that finishes its frames are done
-//      (latency: submit to labelled) and their slots are free again.
+// Every open sweep keeps its state on the device: a ring of frame slots, the
+// signal list of each slot's frame, and its 3-D labeller (the open components
+// and their pixels, dials_spots.cc). Sweeps are admitted against a
+// device-memory budget. Two kinds of thread run the loop:
+//   the worker   copies submitted host frames into the next free slots of
+//                their sweep on a copy stream, and as soon as frames are on
+//                the device forms a batch (continuous batching: whatever is
+//                ready across the sweeps of one frame shape and parameter
+//                set, up to max_batch), thresholds it in one launch sequence
+//                on the compute stream and copies each frame's list into its
+//                sweep's slot; it never waits for labelling;
+//   one labeller per sweep
+//                labels that sweep's frames in frame order on its own stream
+//                as their lists become ready; then its frames are done
+//                (latency: submit to labelled) and their slots free.
 // A frame's result does not depend on what shares its batch: every frame is
 // thresholded alone within a batch and each sweep's labeller sees only its
 // own frames, in order.
@@ -42,12 +44,50 @@ double now_s() {
       .count();
 }
 
+// Each frame's list from a batch's outputs into its sweep's slot.
+struct CopyArgs {
+  sf_signal_pixel *dst[SF_MAX_BATCH];
+  uint32_t *dst_count[SF_MAX_BATCH];
+};
+
+__global__ void k_copy_lists(const sf_signal_pixel *__restrict__ src,
+                             const uint32_t *__restrict__ counts, size_t capacity,
+                             const __grid_constant__ CopyArgs a) {
+  const int j = blockIdx.y;
+  const uint32_t c = counts[j];
+  const size_t n = c < capacity ? c : capacity;
+  const uint4 *s = reinterpret_cast<const uint4 *>(src + (size_t)j * capacity);
+  uint4 *d = reinterpret_cast<uint4 *>(a.dst[j]);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    d[i] = s[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    *a.dst_count[j] = c;  // an overflowing count stays, and the labeller refuses it
+}
+static_assert(sizeof(sf_signal_pixel) == sizeof(uint4), "records move as 16 bytes");
+
+struct Event {
+  cudaEvent_t e = nullptr;
+  Event() { cudaEventCreateWithFlags(&e, cudaEventDisableTiming); }
+  ~Event() {
+    if (e)
+      cudaEventDestroy(e);
+  }
+};
+
 struct SrvFrame {
   int64_t sweep = 0, number = 0;
   const uint32_t *host = nullptr;
   double t_submit = 0.0;
   int slot = -1;
-  cudaEvent_t up = nullptr;  // upload done
+  std::shared_ptr<Event> up;  // upload done
+};
+
+// A run of one sweep's frames in consecutive slots, ready once `ready` fires.
+struct LabelTask {
+  std::vector<SrvFrame> frames;
+  int first_slot = 0;
+  std::shared_ptr<Event> ready;
 };
 
 // Frames of one shape and parameter set share launches and outputs.
@@ -56,20 +96,15 @@ struct SrvGroup {
   sf_threshold_params params{};
   void *ws = nullptr;
   size_t ws_bytes = 0;
-  sf_signal_pixel *out[2] = {nullptr, nullptr};
-  uint32_t *counts[2] = {nullptr, nullptr}, *bits[2] = {nullptr, nullptr};
-  uint32_t *host_counts = nullptr;  // pinned, max_batch
-  int next = 0, users = 0;
+  sf_signal_pixel *out = nullptr;
+  uint32_t *counts = nullptr, *bits = nullptr;
+  int users = 0;
   size_t bytes = 0;
   ~SrvGroup() {
     cudaFree(ws);
-    for (int i = 0; i < 2; i++) {
-      cudaFree(out[i]);
-      cudaFree(counts[i]);
-      cudaFree(bits[i]);
-    }
-    if (host_counts)
-      cudaFreeHost(host_counts);
+    cudaFree(out);
+    cudaFree(counts);
+    cudaFree(bits);
   }
 };
 
@@ -77,79 +112,47 @@ struct SrvSweep {
   int64_t id = 0;
   SrvGroup *group = nullptr;
   sf_labeller *lab = nullptr;
-  size_t bytes = 0;
-  std::vector<uint32_t *> slots;
-  std::vector<int> free_slots;
-  std::deque<SrvFrame> pending;   // submitted, waiting for a slot
-  std::deque<SrvFrame> uploaded;  // on the device, waiting for a batch
-  size_t in_flight = 0;           // submitted and not yet done
+  size_t bytes = 0, ring = 0;
+  std::vector<uint32_t *> slots;        // frames
+  sf_signal_pixel *lists = nullptr;     // ring * capacity records
+  uint32_t *counts = nullptr;           // ring
+  uint32_t *host_counts = nullptr;      // pinned, ring
+  int head = 0;                         // next slot to fill (slots free in order)
+  size_t nfree = 0;
+  std::deque<SrvFrame> pending;         // submitted, waiting for a slot
+  std::deque<SrvFrame> uploaded;        // on the device, waiting for a batch
+  std::deque<LabelTask> tasks;          // lists ready (or soon), waiting to be labelled
+  size_t in_flight = 0;                 // submitted and not yet done
   int64_t last_number = LLONG_MIN;
   bool finishing = false, finished = false;
   int status = 0;
+  std::string error;  // the first failure's message
+  std::condition_variable cv;
+  std::thread thread;
+  cudaStream_t stream = nullptr;
+
+  void set_error(int rc, const char *why = nullptr) {
+    if (status == 0) {
+      status = rc;
+      const char *m = why ? why : sf_last_error();
+      error = m ? m : "";
+    }
+  }
   ~SrvSweep() {
+    if (thread.joinable())
+      thread.join();
     if (lab)
       sf_label_close(lab);
     for (uint32_t *p : slots)
       cudaFree(p);
+    cudaFree(lists);
+    cudaFree(counts);
+    if (host_counts)
+      cudaFreeHost(host_counts);
+    if (stream)
+      cudaStreamDestroy(stream);
   }
 };
-
-struct SrvBatch {
-  SrvGroup *g = nullptr;
-  int buf = 0;
-  std::vector<SrvFrame> frames;  // grouped by sweep, in frame order
-  cudaEvent_t done = nullptr;
-};
-
-} // namespace
-
-struct sf_server {
-  sf_server_options opt{};
-  int device = 0;
-  std::mutex m;
-  std::condition_variable cv_work, cv_done;
-  std::map<int64_t, std::unique_ptr<SrvSweep>> sweeps;
-  std::vector<std::unique_ptr<SrvGroup>> groups;
-  std::deque<sf_frame_done> done;
-  std::vector<cudaEvent_t> event_pool;
-  std::thread worker;
-  bool stop = false;
-  int64_t next_id = 1;
-  size_t used = 0;
-  cudaStream_t copy_s = nullptr, comp_s = nullptr, label_s = nullptr;
-  std::string error;
-
-  cudaEvent_t get_event() {
-    if (!event_pool.empty()) {
-      cudaEvent_t e = event_pool.back();
-      event_pool.pop_back();
-      return e;
-    }
-    cudaEvent_t e = nullptr;
-    cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
-    return e;
-  }
-  void put_event(cudaEvent_t e) {
-    if (e)
-      event_pool.push_back(e);
-  }
-
-  bool work_ready() {
-    for (auto &kv : sweeps) {
-      SrvSweep &s = *kv.second;
-      if ((!s.pending.empty() && !s.free_slots.empty()) || !s.uploaded.empty())
-        return true;
-      if (s.finishing && !s.finished && s.in_flight == 0)
-        return true;
-    }
-    return false;
-  }
-
-  void run();
-  void label_batch(SrvBatch &b);
-};
-
-namespace {
 
 size_t labeller_capacity(size_t h, size_t w) {
   return std::min<size_t>((size_t)1 << 22, std::max<size_t>(h * w / 2, 1024));
@@ -166,7 +169,7 @@ size_t labeller_bytes(size_t capacity, size_t min_spot_size) {
 size_t group_bytes(size_t h, size_t w, size_t capacity, size_t max_batch) {
   const size_t words = (w + 31) / 32 * h;
   return sf_batch_workspace_bytes(max_batch, h, w, capacity) +
-         2 * max_batch * (capacity * sizeof(sf_signal_pixel) + words * 4 + 4);
+         max_batch * (capacity * sizeof(sf_signal_pixel) + words * 4 + 4);
 }
 
 bool same_params(const sf_threshold_params &a, const sf_threshold_params &b) {
@@ -177,99 +180,171 @@ bool same_params(const sf_threshold_params &a, const sf_threshold_params &b) {
 
 } // namespace
 
-void sf_server::label_batch(SrvBatch &b) {
-  // The batch's threshold is done (the label stream waits for it); each
-  // sweep's run of frames goes to its labeller in order.
-  cudaStreamWaitEvent(label_s, b.done, 0);
-  SrvGroup &g = *b.g;
-  const size_t n = b.frames.size();
-  cudaMemcpyAsync(g.host_counts, g.counts[b.buf], n * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                  label_s);
-  std::vector<int> status(n, 0);
-  size_t j = 0;
-  while (j < n) {
-    size_t k = j;
-    while (k < n && b.frames[k].sweep == b.frames[j].sweep)
-      k++;
-    SrvSweep *s = nullptr;
+struct sf_server {
+  sf_server_options opt{};
+  int device = 0;
+  std::mutex m;
+  std::condition_variable cv_work, cv_done;
+  std::map<int64_t, std::unique_ptr<SrvSweep>> sweeps;
+  std::vector<std::unique_ptr<SrvGroup>> groups;
+  std::deque<sf_frame_done> done;
+  std::thread worker;
+  bool stop = false;
+  int64_t next_id = 1;
+  size_t used = 0;
+  // Uploads rotate over several copy streams: one stream's copies run one
+  // at a time, and the host link needs a few in flight to reach its speed.
+  static constexpr int kCopyStreams = 4;
+  cudaStream_t copy_s[kCopyStreams] = {}, comp_s = nullptr;
+  int next_copy = 0;
+  sf_server_stats stats{};
+
+  bool work_ready() {
+    for (auto &kv : sweeps) {
+      SrvSweep &s = *kv.second;
+      if ((!s.pending.empty() && s.nfree > 0) || !s.uploaded.empty())
+        return true;
+    }
+    return false;
+  }
+
+  void run();
+  void label_loop(SrvSweep *s);
+};
+
+void sf_server::label_loop(SrvSweep *s) {
+  cudaSetDevice(device);
+  const size_t cap = s->group->capacity;
+  while (true) {
+    LabelTask t;
     {
-      std::lock_guard<std::mutex> lock(m);
-      auto it = sweeps.find(b.frames[j].sweep);
-      s = it == sweeps.end() ? nullptr : it->second.get();
+      std::unique_lock<std::mutex> lock(m);
+      s->cv.wait(lock, [&] {
+        return stop || !s->tasks.empty() || (s->finishing && s->in_flight == 0);
+      });
+      // A short wait for more of the sweep's frames when the call would be
+      // small: a label call has a fixed cost of some forty launches.
+      auto queued = [&] {
+        size_t n = 0;
+        for (const LabelTask &u : s->tasks)
+          n += u.frames.size();
+        return n;
+      };
+      if (!stop && !s->finishing && queued() < opt.max_batch)
+        s->cv.wait_for(lock, std::chrono::microseconds(opt.coalesce_us), [&] {
+          return stop || s->finishing || queued() >= opt.max_batch;
+        });
+      if (s->tasks.empty()) {
+        if (s->finishing && s->in_flight == 0 && !s->finished) {
+          const int status = s->status;
+          lock.unlock();
+          const int rc = status == 0 ? sf_label_finish(s->lab) : status;
+          lock.lock();
+          if (rc != SF_OK)
+            s->set_error(rc);
+          s->finished = true;
+          cv_done.notify_all();
+        }
+        if (stop || s->finished)
+          return;
+        continue;
+      }
+      // Every waiting run that continues in the next slots joins this call,
+      // up to max_batch frames (what the labeller's live pool is sized for):
+      // one call's fixed cost for many frames.
+      t = std::move(s->tasks.front());
+      s->tasks.pop_front();
+      cudaStreamWaitEvent(s->stream, t.ready->e, 0);
+      while (!s->tasks.empty() &&
+             s->tasks.front().first_slot == t.first_slot + (int)t.frames.size() &&
+             t.frames.size() + s->tasks.front().frames.size() <= opt.max_batch) {
+        LabelTask &u = s->tasks.front();
+        cudaStreamWaitEvent(s->stream, u.ready->e, 0);
+        for (SrvFrame &f : u.frames)
+          t.frames.push_back(f);
+        s->tasks.pop_front();
+      }
     }
-    int rc = SF_EBADARG;
-    if (s && s->status == 0) {
+    const size_t k = t.frames.size();
+    cudaMemcpyAsync(s->host_counts + t.first_slot, s->counts + t.first_slot,
+                    k * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream);
+    int rc = s->status;
+    const double t_call = now_s();
+    if (rc == SF_OK) {
       std::vector<int64_t> numbers;
-      for (size_t i = j; i < k; i++)
-        numbers.push_back(b.frames[i].number);
-      rc = sf_label_add_device(s->lab, numbers.data(), numbers.size(),
-                               g.out[b.buf] + j * g.capacity, g.capacity, g.counts[b.buf] + j,
-                               label_s);
-      if (rc != SF_OK)
-        s->status = rc;
-    } else if (s) {
-      rc = s->status;
+      for (const SrvFrame &f : t.frames)
+        numbers.push_back(f.number);
+      rc = sf_label_add_device(s->lab, numbers.data(), k, s->lists + (size_t)t.first_slot * cap,
+                               cap, s->counts + t.first_slot, s->stream);
     }
-    for (size_t i = j; i < k; i++)
-      status[i] = rc;
-    j = k;
-  }
-  cudaStreamSynchronize(label_s);
-  const double t = now_s();
-  std::lock_guard<std::mutex> lock(m);
-  for (size_t i = 0; i < n; i++) {
-    SrvFrame &f = b.frames[i];
-    sf_frame_done d;
-    d.sweep = f.sweep;
-    d.frame = f.number;
-    d.n_signal = g.host_counts[i];
-    d.latency_ms = (t - f.t_submit) * 1e3;
-    d.status = status[i];
-    done.push_back(d);
-    auto it = sweeps.find(f.sweep);
-    if (it != sweeps.end()) {
-      it->second->free_slots.push_back(f.slot);
-      it->second->in_flight--;
+    cudaStreamSynchronize(s->stream);
+    const double now = now_s();
+    std::lock_guard<std::mutex> lock(m);
+    stats.label_calls++;
+    stats.label_frames += k;
+    stats.label_seconds += now - t_call;
+    if (rc != SF_OK)
+      s->set_error(rc);
+    for (size_t i = 0; i < k; i++) {
+      sf_frame_done d;
+      d.sweep = s->id;
+      d.frame = t.frames[i].number;
+      d.n_signal = s->host_counts[t.first_slot + i];
+      d.status = rc;
+      d.latency_ms = (now - t.frames[i].t_submit) * 1e3;
+      done.push_back(d);
     }
-    put_event(f.up);
+    s->nfree += k;
+    s->in_flight -= k;
+    cv_done.notify_all();
+    cv_work.notify_all();
   }
-  put_event(b.done);
-  cv_done.notify_all();
-  cv_work.notify_all();
 }
 
 void sf_server::run() {
   cudaSetDevice(device);
-  std::unique_ptr<SrvBatch> prev;
   while (true) {
-    std::unique_ptr<SrvBatch> cur;
-    std::vector<SrvSweep *> to_finish;
+    std::vector<SrvFrame> batch;
+    SrvGroup *g = nullptr;
     {
       std::unique_lock<std::mutex> lock(m);
-      cv_work.wait(lock, [&] { return stop || work_ready() || prev; });
-      if (stop && !work_ready() && !prev)
-        break;
-      // 1. Uploads into free slots, oldest submissions first.
+      cv_work.wait(lock, [&] { return stop || work_ready(); });
+      if (stop)
+        return;
+      // A short wait for a fuller batch when few frames are ready.
+      auto ready = [&] {
+        size_t n = 0;
+        for (auto &kv : sweeps)
+          n += kv.second->uploaded.size() + std::min(kv.second->pending.size(), kv.second->nfree);
+        return n;
+      };
+      if (ready() < opt.max_batch)
+        cv_work.wait_for(lock, std::chrono::microseconds(opt.coalesce_us),
+                         [&] { return stop || ready() >= opt.max_batch; });
+      // 1. Uploads into the sweeps' next slots, in submission order.
       for (auto &kv : sweeps) {
         SrvSweep &s = *kv.second;
-        while (!s.pending.empty() && !s.free_slots.empty()) {
+        while (!s.pending.empty() && s.nfree > 0) {
           SrvFrame f = s.pending.front();
           s.pending.pop_front();
-          f.slot = s.free_slots.back();
-          s.free_slots.pop_back();
-          f.up = get_event();
+          f.slot = s.head;
+          s.head = (s.head + 1) % (int)s.ring;
+          s.nfree--;
+          f.up = std::make_shared<Event>();
           const size_t bytes = s.group->h * s.group->w * sizeof(uint32_t);
+          const cudaStream_t cs = copy_s[next_copy];
+          next_copy = (next_copy + 1) % kCopyStreams;
           cudaError_t e = cudaMemcpyAsync(s.slots[f.slot], f.host, bytes,
-                                          cudaMemcpyHostToDevice, copy_s);
+                                          cudaMemcpyHostToDevice, cs);
           if (e == cudaSuccess)
-            e = cudaEventRecord(f.up, copy_s);
-          if (e != cudaSuccess && s.status == 0)
-            s.status = SF_ECUDA;
+            e = cudaEventRecord(f.up->e, cs);
+          if (e != cudaSuccess)
+            s.set_error(SF_ECUDA, "copying a frame to the device");
           s.uploaded.push_back(f);
         }
       }
       // 2. A batch: the shape group of the oldest frame on the device, every
-      // ready frame of its sweeps up to max_batch, grouped by sweep.
+      // ready frame of its sweeps up to max_batch, grouped by sweep in order.
       SrvSweep *first = nullptr;
       for (auto &kv : sweeps) {
         SrvSweep &s = *kv.second;
@@ -277,58 +352,65 @@ void sf_server::run() {
             (!first || s.uploaded.front().t_submit < first->uploaded.front().t_submit))
           first = &s;
       }
-      if (first) {
-        cur.reset(new SrvBatch);
-        cur->g = first->group;
-        for (auto &kv : sweeps) {
-          SrvSweep &s = *kv.second;
-          if (s.group != cur->g)
-            continue;
-          while (!s.uploaded.empty() && cur->frames.size() < opt.max_batch) {
-            cur->frames.push_back(s.uploaded.front());
-            s.uploaded.pop_front();
-          }
-        }
-        cur->buf = cur->g->next;
-        cur->g->next ^= 1;
-        cur->done = get_event();
-      }
+      if (!first)
+        continue;
+      g = first->group;
       for (auto &kv : sweeps) {
         SrvSweep &s = *kv.second;
-        if (s.finishing && !s.finished && s.in_flight == 0)
-          to_finish.push_back(&s);
+        if (s.group != g)
+          continue;
+        while (!s.uploaded.empty() && batch.size() < opt.max_batch) {
+          batch.push_back(s.uploaded.front());
+          s.uploaded.pop_front();
+        }
       }
     }
-    if (cur) {
-      SrvGroup &g = *cur->g;
-      std::vector<const uint32_t *> images;
-      for (SrvFrame &f : cur->frames) {
-        cudaStreamWaitEvent(comp_s, f.up, 0);
-        std::lock_guard<std::mutex> lock(m);
-        images.push_back(sweeps[f.sweep]->slots[f.slot]);
-      }
-      const int rc = sf_threshold_u32_batch_device(
-          images.data(), images.size(), g.h, g.w, &g.params, g.out[cur->buf], g.capacity,
-          g.bits[cur->buf], g.counts[cur->buf], nullptr, g.ws, g.ws_bytes, comp_s);
-      cudaEventRecord(cur->done, comp_s);
-      if (rc != SF_OK) {
-        std::lock_guard<std::mutex> lock(m);
-        for (SrvFrame &f : cur->frames)
-          if (sweeps[f.sweep]->status == 0)
-            sweeps[f.sweep]->status = rc;
-      }
-    }
-    // 3. The previous batch is labelled while this one is thresholded.
-    if (prev)
-      label_batch(*prev);
-    prev = std::move(cur);
-    for (SrvSweep *s : to_finish) {
-      const int rc = s->status == 0 ? sf_label_finish(s->lab) : s->status;
+    // 3. Threshold the batch, then each list into its sweep's slot.
+    const double t_launch = now_s();
+    std::vector<const uint32_t *> images;
+    CopyArgs ca;
+    {
       std::lock_guard<std::mutex> lock(m);
-      if (rc != SF_OK && s->status == 0)
-        s->status = rc;
-      s->finished = true;
-      cv_done.notify_all();
+      for (size_t j = 0; j < batch.size(); j++) {
+        SrvSweep &s = *sweeps[batch[j].sweep];
+        images.push_back(s.slots[batch[j].slot]);
+        ca.dst[j] = s.lists + (size_t)batch[j].slot * g->capacity;
+        ca.dst_count[j] = s.counts + batch[j].slot;
+      }
+    }
+    for (SrvFrame &f : batch)
+      cudaStreamWaitEvent(comp_s, f.up->e, 0);
+    const int rc = sf_threshold_u32_batch_device(images.data(), images.size(), g->h, g->w,
+                                                 &g->params, g->out, g->capacity, g->bits,
+                                                 g->counts, nullptr, g->ws, g->ws_bytes,
+                                                 comp_s);
+    if (rc == SF_OK)
+      k_copy_lists<<<dim3(8, (unsigned)batch.size()), 256, 0, comp_s>>>(g->out, g->counts,
+                                                                       g->capacity, ca);
+    auto ready = std::make_shared<Event>();
+    cudaEventRecord(ready->e, comp_s);
+    // 4. Each sweep's run of frames goes to its labeller, split where its
+    // slots wrap (a label call takes evenly spaced lists).
+    std::lock_guard<std::mutex> lock(m);
+    stats.batches++;
+    stats.batch_frames += batch.size();
+    stats.launch_seconds += now_s() - t_launch;
+    size_t j = 0;
+    while (j < batch.size()) {
+      SrvSweep &s = *sweeps[batch[j].sweep];
+      if (rc != SF_OK)
+        s.set_error(rc);
+      LabelTask t;
+      t.first_slot = batch[j].slot;
+      t.ready = ready;
+      while (j < batch.size() && batch[j].sweep == s.id &&
+             batch[j].slot == t.first_slot + (int)t.frames.size()) {
+        batch[j].up.reset();
+        t.frames.push_back(batch[j]);
+        j++;
+      }
+      s.tasks.push_back(std::move(t));
+      s.cv.notify_all();
     }
   }
 }
@@ -342,6 +424,7 @@ void sf_default_server_options(sf_server_options *o) {
   o->max_batch = 16;
   o->ring = 32;
   o->capacity_divisor = 16;
+  o->coalesce_us = 1000;
 }
 
 sf_server *sf_server_open(const sf_server_options *options) {
@@ -361,9 +444,10 @@ sf_server *sf_server_open(const sf_server_options *options) {
     cudaMemGetInfo(&fb, &tb);
     sv->opt.hbm_budget = fb / 10 * 8;
   }
-  if (cudaStreamCreateWithFlags(&sv->copy_s, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&sv->comp_s, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&sv->label_s, cudaStreamNonBlocking) != cudaSuccess) {
+  bool ok = cudaStreamCreateWithFlags(&sv->comp_s, cudaStreamNonBlocking) == cudaSuccess;
+  for (cudaStream_t &cs : sv->copy_s)
+    ok = ok && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess;
+  if (!ok) {
     delete sv;
     return nullptr;
   }
@@ -377,18 +461,21 @@ void sf_server_close(sf_server *sv) {
   {
     std::lock_guard<std::mutex> lock(sv->m);
     sv->stop = true;
+    for (auto &kv : sv->sweeps)
+      kv.second->cv.notify_all();
   }
   sv->cv_work.notify_all();
   if (sv->worker.joinable())
     sv->worker.join();
+  for (auto &kv : sv->sweeps)
+    if (kv.second->thread.joinable())
+      kv.second->thread.join();
   cudaDeviceSynchronize();
   sv->sweeps.clear();
   sv->groups.clear();
-  for (cudaEvent_t e : sv->event_pool)
-    cudaEventDestroy(e);
-  cudaStreamDestroy(sv->copy_s);
+  for (cudaStream_t cs : sv->copy_s)
+    cudaStreamDestroy(cs);
   cudaStreamDestroy(sv->comp_s);
-  cudaStreamDestroy(sv->label_s);
   delete sv;
 }
 
@@ -397,7 +484,9 @@ size_t sf_server_sweep_bytes(const sf_server *sv, size_t height, size_t width,
   if (!sv || height == 0 || width == 0)
     return 0;
   const size_t min_size = label ? label->min_spot_size : 3;
-  return sv->opt.ring * height * width * sizeof(uint32_t) +
+  const size_t capacity = std::max<size_t>(1, height * width / sv->opt.capacity_divisor);
+  return sv->opt.ring * (height * width * sizeof(uint32_t) + capacity * sizeof(sf_signal_pixel) +
+                         sizeof(uint32_t)) +
          labeller_bytes(labeller_capacity(height, width), min_size);
 }
 
@@ -417,7 +506,7 @@ int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,
   for (auto &gr : sv->groups)
     if (gr->h == height && gr->w == width && same_params(gr->params, p))
       g = gr.get();
-  size_t need = sf_server_sweep_bytes(sv, height, width, label);
+  const size_t need = sf_server_sweep_bytes(sv, height, width, label);
   const size_t gb = g ? 0 : group_bytes(height, width, capacity, sv->opt.max_batch);
   if (sv->used + need + gb > sv->opt.hbm_budget)
     return SF_EBUSY;
@@ -434,21 +523,18 @@ int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,
     G.bytes = gb;
     G.ws_bytes = sf_batch_workspace_bytes(sv->opt.max_batch, height, width, capacity);
     const size_t words = (width + 31) / 32 * height;
-    if ((e = cudaMalloc(&G.ws, G.ws_bytes)) == cudaSuccess)
-      for (int i = 0; i < 2 && e == cudaSuccess; i++) {
-        e = cudaMalloc(&G.out[i], sv->opt.max_batch * capacity * sizeof(sf_signal_pixel));
-        if (e == cudaSuccess)
-          e = cudaMalloc(&G.counts[i], sv->opt.max_batch * sizeof(uint32_t));
-        if (e == cudaSuccess)
-          e = cudaMalloc(&G.bits[i], sv->opt.max_batch * words * sizeof(uint32_t));
-      }
-    if (e == cudaSuccess)
-      e = cudaMallocHost(&G.host_counts, sv->opt.max_batch * sizeof(uint32_t));
+    if ((e = cudaMalloc(&G.ws, G.ws_bytes)) == cudaSuccess &&
+        (e = cudaMalloc(&G.out, sv->opt.max_batch * capacity * sizeof(sf_signal_pixel))) ==
+            cudaSuccess &&
+        (e = cudaMalloc(&G.counts, sv->opt.max_batch * sizeof(uint32_t))) == cudaSuccess)
+      e = cudaMalloc(&G.bits, sv->opt.max_batch * words * sizeof(uint32_t));
     if (e != cudaSuccess)
       return SF_ECUDA;
   }
   std::unique_ptr<SrvSweep> s(new SrvSweep);
   s->bytes = need;
+  s->ring = sv->opt.ring;
+  s->nfree = s->ring;
   sf_label_options lo;
   if (label)
     lo = *label;
@@ -457,13 +543,17 @@ int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,
   s->lab = sf_label_open(height, width, &lo, labeller_capacity(height, width));
   if (!s->lab)
     return SF_EBADARG;
-  for (size_t i = 0; i < sv->opt.ring; i++) {
+  for (size_t i = 0; i < s->ring; i++) {
     uint32_t *slot = nullptr;
     if ((e = cudaMalloc(&slot, height * width * sizeof(uint32_t))) != cudaSuccess)
       return SF_ECUDA;
     s->slots.push_back(slot);
-    s->free_slots.push_back((int)(sv->opt.ring - 1 - i));
   }
+  if ((e = cudaMalloc(&s->lists, s->ring * capacity * sizeof(sf_signal_pixel))) != cudaSuccess ||
+      (e = cudaMalloc(&s->counts, s->ring * sizeof(uint32_t))) != cudaSuccess ||
+      (e = cudaMallocHost(&s->host_counts, s->ring * sizeof(uint32_t))) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return SF_ECUDA;
   lock.lock();
   if (fresh) {
     g = fresh.get();
@@ -475,7 +565,9 @@ int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,
   s->id = sv->next_id++;
   sv->used += need;
   *sweep = s->id;
+  SrvSweep *raw = s.get();
   sv->sweeps[s->id] = std::move(s);
+  raw->thread = std::thread([sv, raw] { sv->label_loop(raw); });
   return SF_OK;
 }
 
@@ -519,6 +611,19 @@ size_t sf_server_poll(sf_server *sv, sf_frame_done *out, size_t max, int wait_ms
   return n;
 }
 
+static int wait_finished(sf_server *sv, std::unique_lock<std::mutex> &lock, SrvSweep *s) {
+  s->finishing = true;
+  s->cv.notify_all();
+  sv->cv_work.notify_all();
+  // Bounded: a sweep whose frames never complete reports an error rather
+  // than holding the caller.
+  if (!sv->cv_done.wait_for(lock, std::chrono::seconds(120), [&] { return s->finished; })) {
+    s->set_error(SF_ECUDA, "finishing a sweep timed out");
+    return SF_ECUDA;
+  }
+  return s->status;
+}
+
 int sf_server_finish_sweep(sf_server *sv, int64_t sweep) {
   if (!sv)
     return SF_EBADARG;
@@ -526,11 +631,7 @@ int sf_server_finish_sweep(sf_server *sv, int64_t sweep) {
   auto it = sv->sweeps.find(sweep);
   if (it == sv->sweeps.end())
     return SF_EBADARG;
-  SrvSweep *s = it->second.get();
-  s->finishing = true;
-  sv->cv_work.notify_all();
-  sv->cv_done.wait(lock, [&] { return s->finished; });
-  return s->status;
+  return wait_finished(sv, lock, it->second.get());
 }
 
 sf_labeller *sf_server_labeller(sf_server *sv, int64_t sweep) {
@@ -541,6 +642,14 @@ sf_labeller *sf_server_labeller(sf_server *sv, int64_t sweep) {
   return it == sv->sweeps.end() ? nullptr : it->second->lab;
 }
 
+const char *sf_server_sweep_error(sf_server *sv, int64_t sweep) {
+  if (!sv)
+    return "";
+  std::lock_guard<std::mutex> lock(sv->m);
+  auto it = sv->sweeps.find(sweep);
+  return it == sv->sweeps.end() ? "" : it->second->error.c_str();
+}
+
 int sf_server_close_sweep(sf_server *sv, int64_t sweep) {
   if (!sv)
     return SF_EBADARG;
@@ -549,25 +658,34 @@ int sf_server_close_sweep(sf_server *sv, int64_t sweep) {
   if (it == sv->sweeps.end())
     return SF_EBADARG;
   SrvSweep *s = it->second.get();
-  if (!s->finished) {
-    s->finishing = true;
-    sv->cv_work.notify_all();
-    sv->cv_done.wait(lock, [&] { return s->finished; });
-  }
-  SrvGroup *g = s->group;
-  sv->used -= s->bytes;
+  if (!s->finished && wait_finished(sv, lock, s) == SF_ECUDA && !s->finished)
+    return SF_ECUDA;
+  std::unique_ptr<SrvSweep> gone = std::move(it->second);
   sv->sweeps.erase(it);
+  SrvGroup *g = gone->group;
+  sv->used -= gone->bytes;
+  std::unique_ptr<SrvGroup> gone_group;
   if (--g->users == 0) {
     sv->used -= g->bytes;
     for (auto gi = sv->groups.begin(); gi != sv->groups.end(); ++gi)
       if (gi->get() == g) {
+        gone_group = std::move(*gi);
         sv->groups.erase(gi);
         break;
       }
   }
+  lock.unlock();
+  gone.reset();  // joins its (finished) label thread, frees its memory
   return SF_OK;
 }
 
 size_t sf_server_used_bytes(const sf_server *sv) { return sv ? sv->used : 0; }
+
+void sf_server_get_stats(sf_server *sv, sf_server_stats *out) {
+  if (!sv || !out)
+    return;
+  std::lock_guard<std::mutex> lock(sv->m);
+  *out = sv->stats;
+}
 
 } // extern "C"

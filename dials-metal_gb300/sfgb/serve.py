@@ -17,13 +17,20 @@ SF_EBUSY = -5
 
 class ServerOptions(ctypes.Structure):
     _fields_ = [("hbm_budget", ctypes.c_size_t), ("max_batch", ctypes.c_size_t),
-                ("ring", ctypes.c_size_t), ("capacity_divisor", ctypes.c_size_t)]
+                ("ring", ctypes.c_size_t), ("capacity_divisor", ctypes.c_size_t),
+                ("coalesce_us", ctypes.c_size_t)]
 
 
 class FrameDone(ctypes.Structure):
     _fields_ = [("sweep", ctypes.c_int64), ("frame", ctypes.c_int64),
                 ("n_signal", ctypes.c_uint32), ("status", ctypes.c_int),
                 ("latency_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("batches", ctypes.c_uint64), ("batch_frames", ctypes.c_uint64),
+                ("label_calls", ctypes.c_uint64), ("label_frames", ctypes.c_uint64),
+                ("launch_seconds", ctypes.c_double), ("label_seconds", ctypes.c_double)]
 
 
 class Busy(RuntimeError):
@@ -59,15 +66,18 @@ def _lib():
             getattr(L, name).restype = ctypes.c_int
         L.sf_server_labeller.argtypes = [vp, ctypes.c_int64]
         L.sf_server_labeller.restype = vp
+        L.sf_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+        L.sf_server_sweep_error.argtypes = [vp, ctypes.c_int64]
+        L.sf_server_sweep_error.restype = ctypes.c_char_p
         _bound = True
     return L
 
 
 class Server:
     def __init__(self, hbm_budget: int = 0, max_batch: int = 16, ring: int = 32,
-                 capacity_divisor: int = 16):
+                 capacity_divisor: int = 16, coalesce_us: int = 1000):
         L = _lib()
-        o = ServerOptions(hbm_budget, max_batch, ring, capacity_divisor)
+        o = ServerOptions(hbm_budget, max_batch, ring, capacity_divisor, coalesce_us)
         self._s = L.sf_server_open(ctypes.byref(o))
         if not self._s:
             raise api.SpotFinderError("server refused its options: " + api.last_error())
@@ -105,7 +115,11 @@ class Server:
                 self._keep[(sweep, frame)] = image
         else:
             ptr = int(image)
-        api._check(_lib().sf_server_submit(self._s, sweep, frame, ptr), "submit")
+        rc = _lib().sf_server_submit(self._s, sweep, frame, ptr)
+        if rc == api.SF_EBADARG:
+            raise ValueError("submit: frames go in ascending order to an open sweep")
+        if rc != 0:
+            raise api.SpotFinderError(f"submit ({rc}): {self.sweep_error(sweep)}")
 
     def poll(self, max_n: int = 4096, wait_ms: int = 0) -> list:
         buf = (FrameDone * max_n)()
@@ -119,10 +133,19 @@ class Server:
                             "status": d.status, "latency_ms": d.latency_ms})
         return out
 
+    def stats(self) -> dict:
+        st = ServerStats()
+        _lib().sf_server_get_stats(self._s, ctypes.byref(st))
+        return {n: getattr(st, n) for n, _ in ServerStats._fields_}
+
+    def sweep_error(self, sweep: int) -> str:
+        return (_lib().sf_server_sweep_error(self._s, sweep) or b"").decode()
+
     def finish_sweep(self, sweep: int) -> labeller.LabelResult:
         L = _lib()
         rc = L.sf_server_finish_sweep(self._s, sweep)
-        api._check(rc, "finish sweep")
+        if rc != 0:
+            raise api.SpotFinderError(f"finish sweep ({rc}): {self.sweep_error(sweep)}")
         return labeller.result_of(L.sf_server_labeller(self._s, sweep))
 
     def close_sweep(self, sweep: int) -> None:

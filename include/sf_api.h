@@ -329,6 +329,7 @@ typedef struct {
   size_t max_batch;        /* frames per threshold launch, 1..SF_MAX_BATCH (16) */
   size_t ring;             /* device frame slots per sweep, >= max_batch (32) */
   size_t capacity_divisor; /* signal-list capacity = pixels / this (16) */
+  size_t coalesce_us;      /* wait up to this long to fill a launch or a label call (1000) */
 } sf_server_options;
 
 typedef struct {
@@ -338,6 +339,14 @@ typedef struct {
   double latency_ms;       /* from sf_server_submit to labelled */
 } sf_frame_done;
 
+/* Counters since sf_server_open: threshold launches and the frames in them,
+ * label calls and their frames, host seconds spent launching batches and in
+ * label calls (summed over the sweeps' labellers). */
+typedef struct {
+  uint64_t batches, batch_frames, label_calls, label_frames;
+  double launch_seconds, label_seconds;
+} sf_server_stats;
+
 typedef struct sf_server sf_server;
 void sf_default_server_options(sf_server_options *options);
 sf_server *sf_server_open(const sf_server_options *options);
@@ -345,6 +354,7 @@ void sf_server_close(sf_server *server);
 size_t sf_server_sweep_bytes(const sf_server *server, size_t height, size_t width,
                              const sf_label_options *label);
 size_t sf_server_used_bytes(const sf_server *server);
+void sf_server_get_stats(sf_server *server, sf_server_stats *out);
 int sf_server_open_sweep(sf_server *server, size_t height, size_t width,
                          const sf_threshold_params *params, const sf_label_options *label,
                          int64_t *sweep);
@@ -354,6 +364,8 @@ int sf_server_submit(sf_server *server, int64_t sweep, int64_t frame,
 size_t sf_server_poll(sf_server *server, sf_frame_done *out, size_t max, int wait_ms);
 int sf_server_finish_sweep(sf_server *server, int64_t sweep);
 sf_labeller *sf_server_labeller(sf_server *server, int64_t sweep);
+/* The message of a sweep's first failure ("" if none). */
+const char *sf_server_sweep_error(sf_server *server, int64_t sweep);
 int sf_server_close_sweep(sf_server *server, int64_t sweep);
 
 #ifdef __cplusplus
