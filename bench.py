@@ -44,6 +44,13 @@ WORKLOAD = ("eiger_16m: 4362x4148 uint32 (EIGER2 16M tiling, module gaps masked)
 H, W = 4362, 4148
 
 
+# DRAM bytes (read + write) that one 16M frame of the eiger_16m workload costs
+# across the threshold's kernels, from an ncu capture of a single-frame launch
+# sequence (seg_stage01 73.6 MB, seg_stage2 15.2 MB, pass_scatter 5.2 MB, the
+# mask scans and amb_fix 8.3 MB); the algorithmic bytes are 76.5 MB.
+DRAM_BYTES_PER_FRAME = 102.3e6
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -509,6 +516,14 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     if rank == 0:
+        if args.traffic is not None:
+            traffic, traffic_source = args.traffic, "given on the command line"
+        else:
+            traffic = DRAM_BYTES_PER_FRAME * B
+            traffic_source = (
+                "ncu dram__bytes_read.sum + dram__bytes_write.sum over the 8 kernels of one "
+                f"single-frame launch sequence of this workload ({DRAM_BYTES_PER_FRAME / 1e6:.1f} MB),"
+                f" times the {B} frames of a launch (each frame's work is independent)")
         line = {
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -533,7 +548,8 @@ def run_ours(args):
                                    "pass_sums, pass_scatter) replayed as one CUDA graph, "
                                    "CUDA events around each batch",
                          "algorithmic_bytes_per_launch": algo_bytes,
-                         "launch_ms": launch_ms, "traffic": args.traffic},
+                         "launch_ms": launch_ms, "traffic": traffic,
+                         "traffic_source": traffic_source},
             "cpu_baseline": base, "e2e": e2e, "labelling": label, "served": served_line,
             "clocks": clock,
             "gpu_launches": 8 * args.steps,
