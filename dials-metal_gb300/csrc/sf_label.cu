@@ -66,7 +66,13 @@ struct LabelStatus {
   unsigned long long counts[6];
 };
 
+// One call's arguments. They live in device memory (copied in before every
+// call) so that a captured launch sequence can be replayed with new ones.
 struct BatchArgs {
+  const sf_signal_pixel *lists;  // frame j's list at lists + j * stride
+  const uint32_t *counts;        // frame j's count
+  unsigned long long stride;
+  unsigned long long pixel_base;  // kept pixels stored before this call
   int nb;
   int finishing;        // close everything (finish(), dials_spots.cc:147-151)
   int two_d;
@@ -131,10 +137,13 @@ __device__ __forceinline__ uint32_t lower_bound(const uint32_t *v, uint32_t lo, 
 // Kernels of one batch, in launch order.
 // ---------------------------------------------------------------------------
 
-__global__ void k_offsets(LabelStatus *st, const uint32_t *__restrict__ counts,
-                          size_t stride, const BatchArgs a, uint32_t capacity) {
+__global__ void k_offsets(LabelStatus *st, const BatchArgs *__restrict__ ap,
+                          uint32_t capacity) {
   if (threadIdx.x != 0 || st->error)
     return;
+  const BatchArgs &a = *ap;
+  const uint32_t *counts = a.counts;
+  const size_t stride = a.stride;
   uint32_t off = 0;
   for (int j = 0; j < a.nb; j++) {
     st->frame_off[j] = off;
@@ -156,11 +165,13 @@ __global__ void k_offsets(LabelStatus *st, const uint32_t *__restrict__ counts,
   st->counts[kCntSignal] += off;
 }
 
-__global__ void k_append(LabelStatus *st, const sf_signal_pixel *__restrict__ lists,
-                         size_t stride, const BatchArgs a, int32_t *frame,
+__global__ void k_append(LabelStatus *st, const BatchArgs *__restrict__ ap, int32_t *frame,
                          uint32_t *index, uint32_t *value, uint32_t *parent) {
   if (st->error)
     return;
+  const BatchArgs &a = *ap;
+  const sf_signal_pixel *__restrict__ lists = a.lists;
+  const size_t stride = a.stride;
   const int j = blockIdx.y;
   const uint32_t n = st->frame_off[j + 1] - st->frame_off[j];
   const uint32_t base = st->n_live + st->frame_off[j];
@@ -178,11 +189,13 @@ __global__ void k_append(LabelStatus *st, const sf_signal_pixel *__restrict__ li
 
 // dials_spots.cc:106-137: left (same row), above (same frame), and the same
 // index on the previous frame when it is the one before.
-__global__ void k_link(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ index,
-                       uint32_t *parent) {
+__global__ void k_link(LabelStatus *st, const BatchArgs *__restrict__ ap,
+                       const uint32_t *__restrict__ index, uint32_t *parent) {
+  const BatchArgs &a = *ap;
   if (st->error)
     return;
   const int j = blockIdx.y;
+  const uint32_t width = a.width;
   const uint32_t start = st->n_live + st->frame_off[j];
   const uint32_t end = st->n_live + st->frame_off[j + 1];
   uint32_t plo = 0, phi = 0;
@@ -193,10 +206,10 @@ __global__ void k_link(LabelStatus *st, const BatchArgs a, const uint32_t *__res
   for (uint32_t p = start + blockIdx.x * blockDim.x + threadIdx.x; p < end;
        p += gridDim.x * blockDim.x) {
     const uint32_t idx = index[p];
-    if (p > start && idx % a.width != 0 && index[p - 1] == idx - 1)
+    if (p > start && idx % width != 0 && index[p - 1] == idx - 1)
       uf_unite(parent, p, p - 1, st);
-    if (idx >= a.width) {
-      const uint32_t t = idx - a.width;
+    if (idx >= width) {
+      const uint32_t t = idx - width;
       const uint32_t q = lower_bound(index, start, p, t);
       if (q < p && index[q] == t)
         uf_unite(parent, p, q, st);
@@ -260,10 +273,11 @@ __device__ __forceinline__ uint32_t bucket_of(const BatchArgs &a, int32_t z) {
   return 1u + (uint32_t)lo;
 }
 
-__global__ void k_closing_flags(LabelStatus *st, const BatchArgs a,
+__global__ void k_closing_flags(LabelStatus *st, const BatchArgs *__restrict__ ap,
                                 const uint32_t *__restrict__ root,
                                 const int32_t *__restrict__ zlast, uint32_t *flag,
                                 uint32_t *open) {
+  const BatchArgs &a = *ap;
   if (st->error)
     return;
   const uint32_t n = st->n_total;
@@ -276,11 +290,12 @@ __global__ void k_closing_flags(LabelStatus *st, const BatchArgs a,
   }
 }
 
-__global__ void k_closing_list(LabelStatus *st, const BatchArgs a,
+__global__ void k_closing_list(LabelStatus *st, const BatchArgs *__restrict__ ap,
                                const uint32_t *__restrict__ flag,
                                const uint32_t *__restrict__ pos,
                                const int32_t *__restrict__ zlast, uint32_t *clist,
                                uint32_t *cbucket) {
+  const BatchArgs &a = *ap;
   if (st->error)
     return;
   const uint32_t n = st->n_total;
@@ -388,9 +403,10 @@ k_bucket_scatter(LabelStatus *st, const uint32_t *__restrict__ clist,
 
 // Size filters (dials_spots.cc:224-231) over the closing components in
 // emission order.
-__global__ void k_size_filter(LabelStatus *st, const BatchArgs a,
+__global__ void k_size_filter(LabelStatus *st, const BatchArgs *__restrict__ ap,
                               const uint32_t *__restrict__ order,
                               const uint32_t *__restrict__ csize, uint32_t *cflag) {
+  const BatchArgs &a = *ap;
   if (st->error)
     return;
   const uint32_t n = st->n_closing;
@@ -691,10 +707,12 @@ __device__ bool emit_spot(const uint32_t *mem, uint32_t n, const int32_t *frame,
 // order, write them back, run emit() and record acceptance.
 template <bool BLOCK>
 __global__ void __launch_bounds__(kThreads)
-k_sort_accept(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ cand_n,
+k_sort_accept(LabelStatus *st, const BatchArgs *__restrict__ ap,
+              const uint32_t *__restrict__ cand_n,
               const uint32_t *__restrict__ cand_off, uint32_t *members,
               const int32_t *__restrict__ frame, const uint32_t *__restrict__ index,
               const uint32_t *__restrict__ value, uint32_t *acc, uint32_t *acc_n) {
+  const BatchArgs &a = *ap;
   if (st->error)
     return;
   extern __shared__ __align__(16) uint32_t s_sort[];
@@ -795,12 +813,14 @@ k_sort_accept(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ c
 // the spot. Where the integers could be inexact lane 0 runs the whole
 // reference sequence alone.
 __global__ void __launch_bounds__(kThreads)
-k_write(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ cand_n,
+k_write(LabelStatus *st, const BatchArgs *__restrict__ ap,
+        const uint32_t *__restrict__ cand_n,
         const uint32_t *__restrict__ cand_off, const uint32_t *__restrict__ members,
         const int32_t *__restrict__ frame, const uint32_t *__restrict__ index,
         const uint32_t *__restrict__ value, const uint32_t *__restrict__ acc,
         const uint32_t *__restrict__ acc_idx, const uint32_t *__restrict__ acc_off,
         sf_spot *spots, size_t spots_cap, sf_pixel *pixels, size_t pixels_cap) {
+  const BatchArgs &a = *ap;
   if (st->error)
     return;
   const uint32_t ncand = st->n_cand;
@@ -908,7 +928,7 @@ k_write(LabelStatus *st, const BatchArgs a, const uint32_t *__restrict__ cand_n,
       } else {
         emit_spot(m, n, frame, index, value, a.width, a.max_separation, &spot);
       }
-      spot.first = po;  // batch-local; the host adds the run's offset
+      spot.first = a.pixel_base + po;
       spots[si] = spot;
     }
   }
@@ -935,7 +955,8 @@ __global__ void k_compact(LabelStatus *st, const uint32_t *__restrict__ open,
   }
 }
 
-__global__ void k_end_batch(LabelStatus *st, const BatchArgs a) {
+__global__ void k_end_batch(LabelStatus *st, const BatchArgs *__restrict__ ap) {
+  const BatchArgs &a = *ap;
   if (threadIdx.x != 0 || st->error)
     return;
   st->counts[kCntAccepted] += st->n_accept;
@@ -958,41 +979,79 @@ template <typename T> static cudaError_t dalloc(T **p, size_t n) {
   return cudaMalloc(reinterpret_cast<void **>(p), (n ? n : 1) * sizeof(T));
 }
 
-// A host array in page-locked memory, grown by doubling: the batches' spots
-// and pixels come back by direct DMA rather than through a pageable bounce.
-template <typename T> struct PinnedVec {
-  T *p = nullptr;
+// The run's spots and kept pixels, append-only in device memory, in chunks
+// that never move (1 MiB first, doubling to 256 MiB): a batch's outputs are
+// appended by device-to-device copies on its stream, and nothing is copied to
+// the host until a caller asks. Growing a host array instead meant pinning
+// and copying ever larger buffers on the labelling thread.
+template <typename T> struct DeviceStore {
+  struct Chunk {
+    T *p;
+    size_t cap;
+  };
+  std::vector<Chunk> chunks;
   size_t n = 0, cap = 0;
-  PinnedVec() = default;
-  PinnedVec(const PinnedVec &) = delete;
-  PinnedVec &operator=(const PinnedVec &) = delete;
-  ~PinnedVec() {
-    if (p)
-      cudaFreeHost(p);
+  DeviceStore() = default;
+  DeviceStore(const DeviceStore &) = delete;
+  DeviceStore &operator=(const DeviceStore &) = delete;
+  ~DeviceStore() {
+    for (const Chunk &c : chunks)
+      cudaFree(c.p);
   }
   size_t size() const { return n; }
-  bool empty() const { return n == 0; }
-  T *data() { return p; }
-  const T *data() const { return p; }
-  T &operator[](size_t i) { return p[i]; }
-  cudaError_t resize(size_t m) {
-    if (m > cap) {
-      size_t c = cap ? cap : 1024;
-      while (c < m)
-        c *= 2;
+  // Room for m more elements.
+  cudaError_t reserve_more(size_t m) {
+    constexpr size_t kFirst = (size_t(1) << 20) / sizeof(T) + 1;
+    constexpr size_t kMax = (size_t(256) << 20) / sizeof(T);
+    while (cap < n + m) {
+      size_t c = chunks.empty() ? kFirst : std::min(chunks.back().cap * 2, kMax);
+      c = std::max(c, std::min(n + m - cap, kMax));
       T *q = nullptr;
-      const cudaError_t e = cudaMallocHost(&q, c * sizeof(T));
+      const cudaError_t e = cudaMalloc(&q, c * sizeof(T));
       if (e != cudaSuccess)
         return e;
-      if (n)
-        std::memcpy(q, p, n * sizeof(T));
-      if (p)
-        cudaFreeHost(p);
-      p = q;
-      cap = c;
+      chunks.push_back({q, c});
+      cap += c;
     }
-    n = m;
     return cudaSuccess;
+  }
+  // Visit [from, from + m) as pieces (chunk pointer, element offset in the run,
+  // length).
+  template <typename F> cudaError_t pieces(size_t from, size_t m, F f) const {
+    size_t base = 0;
+    for (const Chunk &c : chunks) {
+      if (m == 0)
+        break;
+      if (from < base + c.cap) {
+        const size_t off = from - base, take = std::min(c.cap - off, m);
+        const cudaError_t e = f(c.p + off, from, take);
+        if (e != cudaSuccess)
+          return e;
+        from += take;
+        m -= take;
+      }
+      base += c.cap;
+    }
+    return cudaSuccess;
+  }
+  cudaError_t append(const T *src, size_t m, cudaStream_t s) {
+    cudaError_t e = reserve_more(m);
+    if (e != cudaSuccess || m == 0)
+      return e;
+    const size_t at = n;
+    e = pieces(at, m, [&](T *dst, size_t pos, size_t len) {
+      return cudaMemcpyAsync(dst, src + (pos - at), len * sizeof(T), cudaMemcpyDeviceToDevice, s);
+    });
+    if (e == cudaSuccess)
+      n += m;
+    return e;
+  }
+  // Everything stored, into host memory, on stream s (synchronised).
+  cudaError_t read(T *out, cudaStream_t s) const {
+    cudaError_t e = pieces(0, n, [&](T *src, size_t pos, size_t len) {
+      return cudaMemcpyAsync(out + pos, src, len * sizeof(T), cudaMemcpyDeviceToHost, s);
+    });
+    return e == cudaSuccess ? cudaStreamSynchronize(s) : e;
   }
 };
 
@@ -1018,6 +1077,11 @@ struct Labeller {
   int32_t *zlast = nullptr;
   LabelStatus *st = nullptr;
   LabelStatus *host_st = nullptr;
+  BatchArgs *d_args = nullptr, *h_args = nullptr;
+  // Captured launch sequences by (live pool, frames in the batch).
+  cudaGraphExec_t graphs[2][kLabelMaxBatch + 1] = {};
+  bool seen[2][kLabelMaxBatch + 1] = {};
+  bool use_graphs = true;
   // Batch outputs, copied to the host vectors after every batch.
   sf_spot *d_spots = nullptr;
   sf_pixel *d_pixels = nullptr;
@@ -1025,8 +1089,12 @@ struct Labeller {
   sf_signal_pixel *d_list = nullptr;
   size_t d_list_cap = 0;
   uint32_t *d_counts = nullptr;
-  PinnedVec<sf_spot> spots;
-  PinnedVec<sf_pixel> pixels;
+  DeviceStore<sf_spot> spots;
+  DeviceStore<sf_pixel> pixels;
+  // Recorded after each call's appends: the next call (on whatever stream)
+  // and the readers wait for it before touching the batch outputs or the
+  // stores.
+  cudaEvent_t appended = nullptr;
   sf_counts counts{};
   uint32_t live = 0;
   std::string error;
@@ -1047,13 +1115,22 @@ struct Labeller {
                         members, acc, acc_n, acc_idx, acc_off, hist, block_sums, d_counts};
     for (uint32_t *b : bufs)
       cudaFree(b);
+    for (auto &row : graphs)
+      for (cudaGraphExec_t g : row)
+        if (g)
+          cudaGraphExecDestroy(g);
     cudaFree(zlast);
     cudaFree(st);
+    cudaFree(d_args);
+    if (h_args)
+      cudaFreeHost(h_args);
     cudaFree(d_spots);
     cudaFree(d_pixels);
     cudaFree(d_list);
     if (host_st)
       cudaFreeHost(host_st);
+    if (appended)
+      cudaEventDestroy(appended);
   }
 
   int init() {
@@ -1102,6 +1179,12 @@ struct Labeller {
       return fail(e, "cudaMalloc for the labeller status");
     if ((e = cudaMallocHost(&host_st, sizeof(LabelStatus))) != cudaSuccess)
       return fail(e, "cudaMallocHost for the labeller status");
+    if ((e = cudaEventCreateWithFlags(&appended, cudaEventDisableTiming)) != cudaSuccess)
+      return fail(e, "cudaEventCreate");
+    if ((e = cudaMalloc(&d_args, sizeof(BatchArgs))) != cudaSuccess)
+      return fail(e, "cudaMalloc for the labeller's arguments");
+    if ((e = cudaMallocHost(&h_args, sizeof(BatchArgs))) != cudaSuccess)
+      return fail(e, "cudaMallocHost for the labeller's arguments");
     if ((e = cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking)) != cudaSuccess)
       return fail(e, "cudaStreamCreate");
     if ((e = cudaMemsetAsync(st, 0, sizeof(LabelStatus), own_stream)) != cudaSuccess)
@@ -1111,12 +1194,105 @@ struct Labeller {
     return SF_OK;
   }
 
-  // Enqueue one batch: frames[j]'s list at lists + j * stride, count counts[j].
+  // The launch sequence of one batch of nb frames on stream s, reading the
+  // call's arguments from d_args; pool c is the live pool, 1 - c the next.
+  cudaError_t enqueue(int nb, int c, cudaStream_t s) {
+    const int o = 1 - c;
+    const BatchArgs *ap = d_args;
+    const dim3 g2(kGrid / 4 > 0 ? kGrid / 4 : 1, nb);
+    cudaError_t e;
+    k_offsets<<<1, 32, 0, s>>>(st, ap, (uint32_t)capacity);
+    k_append<<<g2, kThreads, 0, s>>>(st, ap, frame[c], index[c], value[c], parent[c]);
+    k_link<<<g2, kThreads, 0, s>>>(st, ap, index[c], parent[c]);
+    k_flatten<<<kGrid, kThreads, 0, s>>>(st, parent[c], root, zlast, csize, candid);
+    k_comp_stats<<<kGrid, kThreads, 0, s>>>(st, root, frame[c], zlast, csize);
+    k_closing_flags<<<kGrid, kThreads, 0, s>>>(st, ap, root, zlast, flag, open);
+    const uint32_t *err = &st->error;
+    if ((e = exclusive_scan(flag, posa, &st->n_total, &st->n_closing, block_sums, err, s)) !=
+        cudaSuccess)
+      return e;
+    k_closing_list<<<kGrid, kThreads, 0, s>>>(st, ap, flag, posa, zlast, clist, cbucket);
+    k_bucket_hist<<<kGrid, kThreads, 0, s>>>(st, cbucket, hist);
+    k_bucket_offsets<<<1, 128, 0, s>>>(st, hist);
+    k_bucket_scatter<<<kGrid, kThreads, 0, s>>>(st, clist, cbucket, hist, order);
+    k_size_filter<<<kGrid, kThreads, 0, s>>>(st, ap, order, csize, cflag);
+    if ((e = exclusive_scan(cflag, cpos, &st->n_closing, &st->n_cand, block_sums, err, s)) !=
+        cudaSuccess)
+      return e;
+    k_cand_list<<<kGrid, kThreads, 0, s>>>(st, order, csize, cflag, cpos, cand_root, cand_n,
+                                           candid, cursor);
+    if ((e = exclusive_scan(cand_n, cand_off, &st->n_cand, &st->n_cand_pixels, block_sums,
+                            err, s)) != cudaSuccess)
+      return e;
+    k_gather<<<kGrid, kThreads, 0, s>>>(st, root, candid, cand_off, cursor, members);
+    k_sort_accept<false><<<kGrid, kThreads, (kThreads / 32) * kWarpSortMax * 4, s>>>(
+        st, ap, cand_n, cand_off, members, frame[c], index[c], value[c], acc, acc_n);
+    k_sort_accept<true><<<kGrid / 2, kThreads, kBlockSortMax * 4, s>>>(
+        st, ap, cand_n, cand_off, members, frame[c], index[c], value[c], acc, acc_n);
+    if ((e = exclusive_scan(acc, acc_idx, &st->n_cand, &st->n_accept, block_sums, err, s)) !=
+        cudaSuccess)
+      return e;
+    if ((e = exclusive_scan(acc_n, acc_off, &st->n_cand, &st->n_accept_pixels, block_sums,
+                            err, s)) != cudaSuccess)
+      return e;
+    k_write<<<kGrid, kThreads, 0, s>>>(st, ap, cand_n, cand_off, members, frame[c], index[c],
+                                       value[c], acc, acc_idx, acc_off, d_spots, spots_cap,
+                                       d_pixels, capacity);
+    if ((e = exclusive_scan(open, posb, &st->n_total, &st->n_open, block_sums, err, s)) !=
+        cudaSuccess)
+      return e;
+    k_compact<<<kGrid, kThreads, 0, s>>>(st, open, posb, root, frame[c], index[c], value[c],
+                                         frame[o], index[o], value[o], parent[o]);
+    k_end_batch<<<1, 32, 0, s>>>(st, ap);
+    return cudaGetLastError();
+  }
+
+  // The sequence for (nb, c) as a CUDA graph, captured on the labeller's own
+  // stream the second time that shape is met (the first runs directly, so
+  // every kernel is loaded before a capture), then replayed on any stream.
+  // Null if capture is not possible (the caller's stream is itself being
+  // captured, or the capture failed): the sequence then runs directly.
+  cudaGraphExec_t graph_for(int nb, int c, cudaStream_t s) {
+    cudaGraphExec_t &g = graphs[c][nb];
+    if (g || !use_graphs)
+      return g;
+    if (!seen[c][nb]) {
+      seen[c][nb] = true;
+      return nullptr;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (s != cudaStreamLegacy && cudaStreamIsCapturing(s, &cs) == cudaSuccess &&
+        cs != cudaStreamCaptureStatusNone)
+      return nullptr;
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(own_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    const cudaError_t e = enqueue(nb, c, own_stream);
+    const cudaError_t e2 = cudaStreamEndCapture(own_stream, &graph);
+    if (e == cudaSuccess && e2 == cudaSuccess && graph &&
+        cudaGraphInstantiate(&g, graph, 0) != cudaSuccess)
+      g = nullptr;
+    if (graph)
+      cudaGraphDestroy(graph);
+    if (!g) {
+      use_graphs = false;  // do not try again
+      cudaGetLastError();
+    }
+    return g;
+  }
+
+  // One batch: frames[j]'s list at lists + j * stride, count counts[j].
   int run_batch(const int64_t *frames, int nb, const sf_signal_pixel *lists,
                 size_t stride, const uint32_t *counts_dev, bool finishing,
                 cudaStream_t s) {
-    BatchArgs a;
+    BatchArgs &a = *h_args;
     std::memset(&a, 0, sizeof(a));
+    a.lists = lists;
+    a.counts = counts_dev;
+    a.stride = stride;
+    a.pixel_base = pixels.size();
     a.nb = nb;
     a.finishing = finishing ? 1 : 0;
     a.two_d = opt.two_d ? 1 : 0;
@@ -1138,54 +1314,19 @@ struct Labeller {
       a.frames[0] = (int32_t)(last_frame + 1);
       a.link_prev[0] = 0;
     }
-    const int c = cur, o = 1 - cur;
-    const dim3 g2(kGrid / 4 > 0 ? kGrid / 4 : 1, a.nb);
+    // h_args is reused by the next call only after collect() has waited for
+    // this one, so the copy has read it by then.
     cudaError_t e;
-    k_offsets<<<1, 32, 0, s>>>(st, counts_dev, stride, a, (uint32_t)capacity);
-    k_append<<<g2, kThreads, 0, s>>>(st, lists, stride, a, frame[c], index[c], value[c],
-                                     parent[c]);
-    k_link<<<g2, kThreads, 0, s>>>(st, a, index[c], parent[c]);
-    k_flatten<<<kGrid, kThreads, 0, s>>>(st, parent[c], root, zlast, csize, candid);
-    k_comp_stats<<<kGrid, kThreads, 0, s>>>(st, root, frame[c], zlast, csize);
-    k_closing_flags<<<kGrid, kThreads, 0, s>>>(st, a, root, zlast, flag, open);
-    const uint32_t *err = &st->error;
-    if ((e = exclusive_scan(flag, posa, &st->n_total, &st->n_closing, block_sums, err, s)) !=
+    if ((e = cudaStreamWaitEvent(s, appended, 0)) != cudaSuccess)
+      return fail(e, "cudaStreamWaitEvent");
+    if ((e = cudaMemcpyAsync(d_args, h_args, sizeof(BatchArgs), cudaMemcpyHostToDevice, s)) !=
         cudaSuccess)
-      return fail(e, "labeller scan");
-    k_closing_list<<<kGrid, kThreads, 0, s>>>(st, a, flag, posa, zlast, clist, cbucket);
-    k_bucket_hist<<<kGrid, kThreads, 0, s>>>(st, cbucket, hist);
-    k_bucket_offsets<<<1, 128, 0, s>>>(st, hist);
-    k_bucket_scatter<<<kGrid, kThreads, 0, s>>>(st, clist, cbucket, hist, order);
-    k_size_filter<<<kGrid, kThreads, 0, s>>>(st, a, order, csize, cflag);
-    if ((e = exclusive_scan(cflag, cpos, &st->n_closing, &st->n_cand, block_sums, err, s)) !=
-        cudaSuccess)
-      return fail(e, "labeller scan");
-    k_cand_list<<<kGrid, kThreads, 0, s>>>(st, order, csize, cflag, cpos, cand_root, cand_n,
-                                           candid, cursor);
-    if ((e = exclusive_scan(cand_n, cand_off, &st->n_cand, &st->n_cand_pixels, block_sums,
-                            err, s)) != cudaSuccess)
-      return fail(e, "labeller scan");
-    k_gather<<<kGrid, kThreads, 0, s>>>(st, root, candid, cand_off, cursor, members);
-    k_sort_accept<false><<<kGrid, kThreads, (kThreads / 32) * kWarpSortMax * 4, s>>>(
-        st, a, cand_n, cand_off, members, frame[c], index[c], value[c], acc, acc_n);
-    k_sort_accept<true><<<kGrid / 2, kThreads, kBlockSortMax * 4, s>>>(
-        st, a, cand_n, cand_off, members, frame[c], index[c], value[c], acc, acc_n);
-    if ((e = exclusive_scan(acc, acc_idx, &st->n_cand, &st->n_accept, block_sums, err, s)) !=
-        cudaSuccess)
-      return fail(e, "labeller scan");
-    if ((e = exclusive_scan(acc_n, acc_off, &st->n_cand, &st->n_accept_pixels, block_sums,
-                            err, s)) != cudaSuccess)
-      return fail(e, "labeller scan");
-    k_write<<<kGrid, kThreads, 0, s>>>(st, a, cand_n, cand_off, members, frame[c], index[c],
-                                       value[c], acc, acc_idx, acc_off, d_spots, spots_cap,
-                                       d_pixels, capacity);
-    if ((e = exclusive_scan(open, posb, &st->n_total, &st->n_open, block_sums, err, s)) !=
-        cudaSuccess)
-      return fail(e, "labeller scan");
-    k_compact<<<kGrid, kThreads, 0, s>>>(st, open, posb, root, frame[c], index[c], value[c],
-                                         frame[o], index[o], value[o], parent[o]);
-    k_end_batch<<<1, 32, 0, s>>>(st, a);
-    if ((e = cudaGetLastError()) != cudaSuccess)
+      return fail(e, "copying the labeller's arguments");
+    if (cudaGraphExec_t g = graph_for(a.nb, cur, s))
+      e = cudaGraphLaunch(g, s);
+    else
+      e = enqueue(a.nb, cur, s);
+    if (e != cudaSuccess)
       return fail(e, "launching the labeller");
     return collect(s, nb > 0 ? frames[nb - 1] : last_frame, nb > 0);
   }
@@ -1213,22 +1354,11 @@ struct Labeller {
       return SF_EOVERFLOW;
     }
     const uint32_t na = host_st->n_accept, npx = host_st->n_accept_pixels;
-    const size_t s0 = spots.size(), p0 = pixels.size();
-    if ((e = spots.resize(s0 + na)) != cudaSuccess ||
-        (e = pixels.resize(p0 + npx)) != cudaSuccess)
-      return fail(e, "cudaMallocHost for the labeller's results");
-    if (na &&
-        (e = cudaMemcpyAsync(spots.data() + s0, d_spots, na * sizeof(sf_spot),
-                             cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-      return fail(e, "reading spots back");
-    if (npx &&
-        (e = cudaMemcpyAsync(pixels.data() + p0, d_pixels, npx * sizeof(sf_pixel),
-                             cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-      return fail(e, "reading spot pixels back");
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess)
-      return fail(e, "cudaStreamSynchronize");
-    for (size_t i = s0; i < spots.size(); i++)
-      spots[i].first += p0;
+    if ((e = spots.append(d_spots, na, s)) != cudaSuccess ||
+        (e = pixels.append(d_pixels, npx, s)) != cudaSuccess)
+      return fail(e, "storing the labeller's results");
+    if ((e = cudaEventRecord(appended, s)) != cudaSuccess)
+      return fail(e, "cudaEventRecord");
     const unsigned long long *c = host_st->counts;
     counts.signal_pixels = c[kCntSignal];
     counts.groups = c[kCntGroups];
@@ -1253,6 +1383,19 @@ using namespace sf;
 struct sf_labeller {
   Labeller impl;
 };
+
+// The stored results to the host, after the last call's appends.
+template <typename T>
+static int read_store(const Labeller &L, const DeviceStore<T> &v, T *out, size_t capacity,
+                      const char *what) {
+  if (capacity < v.size())
+    return SF_EOVERFLOW;
+  cudaError_t e;
+  if ((e = cudaStreamWaitEvent(L.own_stream, L.appended, 0)) != cudaSuccess ||
+      (e = v.read(out, L.own_stream)) != cudaSuccess)
+    return fail(e, what);
+  return SF_OK;
+}
 
 extern "C" {
 
@@ -1389,23 +1532,13 @@ size_t sf_label_live(const sf_labeller *l) { return l ? l->impl.live : 0; }
 int sf_label_spots(const sf_labeller *l, sf_spot *out, size_t capacity) {
   if (!l || (!out && capacity))
     return SF_EBADARG;
-  const auto &v = l->impl.spots;
-  if (capacity < v.size())
-    return SF_EOVERFLOW;
-  if (!v.empty())
-    std::memcpy(out, v.data(), v.size() * sizeof(sf_spot));
-  return SF_OK;
+  return read_store(l->impl, l->impl.spots, out, capacity, "reading spots back");
 }
 
 int sf_label_pixels(const sf_labeller *l, sf_pixel *out, size_t capacity) {
   if (!l || (!out && capacity))
     return SF_EBADARG;
-  const auto &v = l->impl.pixels;
-  if (capacity < v.size())
-    return SF_EOVERFLOW;
-  if (!v.empty())
-    std::memcpy(out, v.data(), v.size() * sizeof(sf_pixel));
-  return SF_OK;
+  return read_store(l->impl, l->impl.pixels, out, capacity, "reading spot pixels back");
 }
 
 void sf_label_counts(const sf_labeller *l, sf_counts *out) {

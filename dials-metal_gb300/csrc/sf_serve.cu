@@ -39,6 +39,18 @@
 
 namespace {
 
+// The labellers' streams run at the device's highest priority: a label call
+// is a chain of small kernels, each of which would otherwise wait behind a
+// whole threshold batch's blocks for an SM, which sets every frame's latency.
+int label_priority() {
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return greatest;
+}
+
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
       .count();
@@ -552,7 +564,8 @@ int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,
   if ((e = cudaMalloc(&s->lists, s->ring * capacity * sizeof(sf_signal_pixel))) != cudaSuccess ||
       (e = cudaMalloc(&s->counts, s->ring * sizeof(uint32_t))) != cudaSuccess ||
       (e = cudaMallocHost(&s->host_counts, s->ring * sizeof(uint32_t))) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
+      (e = cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, label_priority())) !=
+          cudaSuccess)
     return SF_ECUDA;
   lock.lock();
   if (fresh) {

@@ -141,12 +141,19 @@ class Server:
     def sweep_error(self, sweep: int) -> str:
         return (_lib().sf_server_sweep_error(self._s, sweep) or b"").decode()
 
-    def finish_sweep(self, sweep: int) -> labeller.LabelResult:
+    def finish_sweep(self, sweep: int, read: bool = True):
+        """Wait for the sweep's frames, close its open spots and (read=True)
+        return its spots, kept pixels and counts."""
         L = _lib()
         rc = L.sf_server_finish_sweep(self._s, sweep)
         if rc != 0:
             raise api.SpotFinderError(f"finish sweep ({rc}): {self.sweep_error(sweep)}")
-        return labeller.result_of(L.sf_server_labeller(self._s, sweep))
+        return labeller.result_of(L.sf_server_labeller(self._s, sweep)) if read else None
+
+    def n_spots(self, sweep: int) -> int:
+        """Spots the sweep has produced so far (nothing is copied)."""
+        L = _lib()
+        return int(L.sf_label_n_spots(L.sf_server_labeller(self._s, sweep)))
 
     def close_sweep(self, sweep: int) -> None:
         api._check(_lib().sf_server_close_sweep(self._s, sweep), "close sweep")

@@ -273,8 +273,10 @@ int sf_label_add_device(sf_labeller *labeller, const int64_t *frames,
 int sf_label_finish(sf_labeller *labeller);
 
 /* Replace Labeller::spots(), pixels(), counts(), live()
- * (src/spots/dials_spots.hh:119-125). The copies return -2 if capacity is
- * short. */
+ * (src/spots/dials_spots.hh:119-125). The spots and kept pixels are held in
+ * device memory as they are produced; sf_label_spots / sf_label_pixels copy
+ * them to the caller's buffer (waiting for the last add), and return -2 if
+ * capacity is short. */
 size_t sf_label_n_spots(const sf_labeller *labeller);
 size_t sf_label_n_pixels(const sf_labeller *labeller);
 int sf_label_spots(const sf_labeller *labeller, sf_spot *out, size_t capacity);
