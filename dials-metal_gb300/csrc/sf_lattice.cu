@@ -1,0 +1,798 @@
+// Stage 0 and the erosion of the streaming threshold for the reference's own
+// window (kernel 3,3: 7 x 7 stage-0 windows, erosion by 2), in two kernels:
+//
+//   lat_stage01  stage 0 on a lattice of every third row and every third
+//                column only, and the erosion of that lattice: an upper bound
+//                of the eroded mask, written as the eroded and candidate masks
+//   lat_verify   the exact stage 0 and erosion on the 8 x 28 tiles that hold
+//                a candidate of the bound; the candidates that fail leave both
+//                masks, which are then the reference's
+//
+// Why the bound holds. The erosion (src/spots/dext.cc:117-142) keeps a valid
+// pixel only if every in-frame pixel of its 5 x 5 neighbourhood is signal or
+// masked after stage 0. ANDing over only the lattice pixels of the
+// neighbourhood can keep more pixels, never fewer. Every 5 x 5 neighbourhood
+// holds 1 to 4 lattice pixels, and next to a masked band or the frame's edge
+// a valid pixel still sees a 3 x 3 block of in-frame valid pixels, so a
+// lattice pixel; the bound passes about 1.7 times the exact candidates, all in
+// and around spots.
+//
+// The lattice decisions are an upper bound too: a window counts as signal
+// when the lower of the two integer bounds of sf_stream.cuh says it may be,
+// and when its sums may not be exact. Valid pixels are summed saturated at
+// kLatCap (2^15 - 1), so every packed sum is exact for the saturated values;
+// a window whose saturated sum S is below kLatCap - 1 holds no saturated
+// pixel, its sum of squares is at most S^2 < 2^30, and its decision is that
+// of the reference. A window with a larger S is taken as signal, and the tile
+// check decides it exactly.
+//
+// The tile check decides only the stage-0 windows within 2 of a candidate
+// (the only ones whose decision can clear one), about a fifth of a tile's,
+// spread over the warp's lanes. Its 18 x 38 pixels cover the stage-2 window
+// (11 x 11) of every candidate of the tile, so it is also where a frame is
+// marked for the 64-bit stage 2: a tile holding a valid pixel at or above
+// narrow_max marks its frame.
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "sf_common.cuh"
+#include "sf_stream.cuh"
+
+namespace sf {
+namespace {
+
+constexpr int kLatK = 3;                    // stage-0 half-width
+constexpr int kLatN0 = 49;                  // pixels of a stage-0 window
+constexpr int kLatCols = 12;                // columns a lane owns
+constexpr int kLatOutLanes = 30;            // lanes 0-29 write, lane 30 feeds lane 29
+constexpr int kLatOut = kLatCols * kLatOutLanes;  // 360 output columns a warp
+constexpr int kLatWarps = 4;                // warps a block
+constexpr int kLatOcc = 5;                  // blocks an SM the kernel is built for
+constexpr uint32_t kLatPS = 26;             // masked count above a 26-bit sum
+constexpr uint32_t kLatMask = (1u << kLatPS) - 1u;
+constexpr uint32_t kLatCap = 32767;         // valid pixels saturate here
+constexpr int kDec = 8;                     // fixed-point bits of clo / chi
+
+static_assert(kLatOut % 24 == 0, "lane pairs write whole bytes");
+static_assert(kLatN0 * kLatCap < (1u << kLatPS), "saturated sums stay below the count field");
+
+// The 12 bound bits of a lane from the lattice bits b0-b4 at its columns
+// -1, 2, 5, 8 and 11 (b4 is the next lane's b0): column c keeps the lattice
+// columns within 2 of it.
+__host__ __device__ constexpr uint32_t lat_bound12(uint32_t b) {
+  const uint32_t b0 = b & 1u, b1 = (b >> 1) & 1u, b2 = (b >> 2) & 1u, b3 = (b >> 3) & 1u,
+                 b4 = (b >> 4) & 1u;
+  const uint32_t a = b0 & b1, d = b1 & b2, e = b2 & b3, g = b3 & b4;
+  return a * 0x003u | b1 << 2 | d * 0x018u | b2 << 5 | e * 0x0C0u | b3 << 8 | g * 0x600u |
+         b4 << 11;
+}
+
+__device__ __forceinline__ void lat_load(const uint32_t *__restrict__ image, int height, int width,
+                                         bool interior, int cx, int p, uint32_t v[16]) {
+  if (p < 0 || p >= height) {
+#pragma unroll
+    for (int i = 0; i < 16; i++)
+      v[i] = 0xFFFFFFFFu;
+    return;
+  }
+  const uint32_t *row = image + (size_t)p * width + (cx - 4);
+  if (interior) {
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+      const uint4 t = __ldg(reinterpret_cast<const uint4 *>(row) + f);
+      v[4 * f] = t.x, v[4 * f + 1] = t.y, v[4 * f + 2] = t.z, v[4 * f + 3] = t.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      const int gx = cx - 4 + i;
+      v[i] = (gx >= 0 && gx < width) ? __ldg(row + i) : 0xFFFFFFFFu;
+    }
+  }
+}
+
+// One pixel row of a lane: the 16 pixels of columns -4 .. 11 packed (masked
+// as a lone count bit whose square wraps to 0, valid saturated at kLatCap),
+// the row sums of 7 columns at the lattice columns -1, 2, 5, 8, and the
+// masked bits of the lane's own 12 columns.
+__device__ __forceinline__ void lat_row(const uint32_t v[16], uint32_t hn[4], uint32_t hq[4],
+                                        uint32_t *m12, uint32_t *mh) {
+  uint32_t ns[16], q[16];
+#pragma unroll
+  for (int i = 0; i < 16; i++) {
+    ns[i] = v[i] >= 0xFFFFFFFEu ? (1u << kLatPS) : min(v[i], kLatCap);
+    q[i] = ns[i] * ns[i];
+  }
+  // Triples of columns [3a - 4, 3a - 2], then the 7-column windows.
+  uint32_t gn[5], gq[5];
+#pragma unroll
+  for (int a = 0; a < 5; a++) {
+    gn[a] = ns[3 * a] + ns[3 * a + 1] + ns[3 * a + 2];
+    gq[a] = q[3 * a] + q[3 * a + 1] + q[3 * a + 2];
+  }
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    hn[a] = gn[a] + gn[a + 1] + ns[3 * a + 6];
+    hq[a] = gq[a] + gq[a + 1] + q[3 * a + 6];
+  }
+  // A valid packed pixel is below 2^15, so shifting it right by 26 - c
+  // (c <= 11) leaves nothing: the shifted words add up to the masked bits.
+  uint32_t m = 0;
+#pragma unroll
+  for (int c = 0; c < kLatCols; c++)
+    m += ns[4 + c] >> (kLatPS - c);
+  *m12 = m;
+  *mh = ns[3] >> kLatPS;  // column -1, the first lattice column
+}
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// The ring variant (kRing: 4 | width and 16-byte aligned frames) stages each
+// warp's pixel rows in shared memory by cp.async, kRingSlots - 1 rows ahead:
+// a row is the 95 16-byte pieces from column X - 4 (X the strip's first
+// output column) that the lanes read, 12 columns a lane apart. The other
+// variant loads each lane's 16 columns straight from the frame, a row ahead.
+constexpr int kRingSlots = 4;
+constexpr int kRingPieces = 95;            // 16-byte pieces fetched a row
+constexpr int kRingStride = 388;           // words a slot: what lane 31 reads
+constexpr size_t kRingBytes = (size_t)kLatWarps * kRingSlots * kRingStride * sizeof(uint32_t);
+
+template <int kOcc, bool kRing>
+__global__ void __launch_bounds__(kLatWarps * 32, kOcc)
+lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int width, int vec,
+            int nstrips, int nruns, int run_rows, const __grid_constant__ StreamTables T,
+            uint8_t *__restrict__ scr1_bytes, uint8_t *__restrict__ final_bytes,
+            size_t mask_bytes) {
+  extern __shared__ __align__(16) uint32_t lat_ring[];
+  // Lower-bound constants by masked count m (window count 49 - m).
+  __shared__ uint2 tab[kLatN0 + 1];
+  __shared__ uint16_t lut[32];
+  for (int m = threadIdx.x; m <= kLatN0; m += blockDim.x)
+    tab[m] = make_uint2(T.nk[kLatN0 - m], T.clo[kLatN0 - m]);
+  if (threadIdx.x < 32)
+    lut[threadIdx.x] = (uint16_t)lat_bound12(threadIdx.x);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gw = blockIdx.x * kLatWarps + warp;
+  const int sx = gw % nstrips, t0 = gw / nstrips;
+  const int ry = t0 % nruns, f = t0 / nruns;
+  if (f >= nframes)
+    return;  // whole warp
+  const uint32_t *image = F.image[f];
+  const int bytes_per_row = ((width + 31) >> 5) * 4;
+  uint8_t *scr1 = scr1_bytes + (size_t)f * mask_bytes;
+  uint8_t *fin = final_bytes + (size_t)f * mask_bytes;
+  const int cx = kLatOut * sx + kLatCols * lane;
+  const bool interior = vec && cx - 4 >= 0 && cx + 12 <= width;
+  // This lane's first mask byte (lane pairs share three bytes), and the bits
+  // of its columns inside the frame.
+  const int pair_byte = (kLatOut * sx + 24 * (lane >> 1)) >> 3;
+  const bool writer = lane < kLatOutLanes;
+  const uint32_t inside12 =
+      cx >= width ? 0u : (cx + kLatCols <= width ? 0xFFFu : ((1u << (width - cx)) - 1u));
+  const int ra = ry * run_rows;
+  const int rb = min(height, ra + run_rows);
+  const int ja = ra / 3;
+  const int ntrip = (rb - ra + 2) / 3;
+
+  // U = h(last row of triple t-2) + T(t-1) per lattice column; hl = the
+  // last row of the previous triple.
+  uint32_t Un[4], Uq[4], hln[4], hlq[4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+    Un[a] = Uq[a] = hln[a] = hlq[a] = 0u;
+  uint32_t mprev[3] = {0u, 0u, 0u}, bprev = 0u, cmprev = 0u;
+
+  // Pixel rows [pbeg, pend) of the run.
+  const int pbeg = 3 * (ja - 2), pend = 3 * (ja + ntrip + 1);
+  uint32_t *ring = lat_ring + (size_t)warp * kRingSlots * kRingStride;
+  // The ring's pieces of this lane: column offsets and whether each lies in
+  // the frame.
+  const int X = kLatOut * sx;
+  int pc[3];
+  bool pin[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const int k = lane + 32 * i, x = X - 4 + 4 * k;
+    pc[i] = x;
+    pin[i] = k < kRingPieces && x >= 0 && x + 4 <= width;
+  }
+  auto fetch = [&](int p) {
+    uint32_t *dst = ring + ((p - pbeg) % kRingSlots) * kRingStride;
+    const bool rowin = p >= 0 && p < height && p < pend;
+    const uint32_t *src = image + (size_t)(rowin ? p : 0) * width;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const int k = lane + 32 * i;
+      if (rowin && pin[i])
+        cp_async16(dst + 4 * k, src + pc[i]);
+      else if (k < kRingPieces)
+        *reinterpret_cast<uint4 *>(dst + 4 * k) = make_uint4(~0u, ~0u, ~0u, ~0u);
+    }
+  };
+  if (kRing) {
+    // The words past the fetched pieces (read by lane 31 only) stay masked.
+    for (int i = 4 * kRingPieces + lane; i < kRingSlots * kRingStride; i += 32)
+      if (i % kRingStride >= 4 * kRingPieces)
+        ring[i] = ~0u;
+#pragma unroll
+    for (int i = 0; i < kRingSlots - 1; i++) {
+      fetch(pbeg + i);
+      cp_async_commit();
+    }
+  }
+
+  uint32_t v[16];
+  if (!kRing)
+    lat_load(image, height, width, interior, cx, pbeg, v);
+  for (int t = 0; t < ntrip + 3; t++) {
+    const int p0 = 3 * (ja - 2 + t);
+    uint32_t Tn[4], Tq[4], mcur[3], cm = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const int p = p0 + k;
+      uint32_t nxt[16];
+      if (kRing) {
+        // Row p + kRingSlots - 1 goes out; row p has landed.
+        __syncwarp();
+        fetch(p + kRingSlots - 1);
+        cp_async_commit();
+        cp_async_wait<kRingSlots - 1>();
+        __syncwarp();
+        const uint4 *src =
+            reinterpret_cast<const uint4 *>(ring + ((p - pbeg) % kRingSlots) * kRingStride) +
+            3 * lane;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const uint4 x = src[i];
+          v[4 * i] = x.x, v[4 * i + 1] = x.y, v[4 * i + 2] = x.z, v[4 * i + 3] = x.w;
+        }
+      } else if (k < 2 || t + 1 < ntrip + 3) {
+        // The next row's loads go out before this row's arithmetic.
+        lat_load(image, height, width, interior, cx, p + 1, nxt);
+      }
+      uint32_t hn[4], hq[4], mh;
+      lat_row(v, hn, hq, &mcur[k], &mh);
+      if (!kRing) {
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+          v[i] = nxt[i];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        Tn[a] = k == 0 ? hn[a] : Tn[a] + hn[a];
+        Tq[a] = k == 0 ? hq[a] : Tq[a] + hq[a];
+      }
+      if (k == 2) {
+        // Masked centres of this row's lattice columns -1, 2, 5, 8: the
+        // lattice row the next triple decides.
+        const uint32_t m12 = mcur[2];
+        cm = mh | ((m12 >> 1) & 2u) | ((m12 >> 3) & 4u) | ((m12 >> 5) & 8u);
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+          // Window rows p0 - 4 .. p0 + 2, centred on the previous triple's
+          // last row (a lattice row).
+          const uint32_t Wn = Un[a] + Tn[a], Wq = Uq[a] + Tq[a];
+          Un[a] = hln[a] + Tn[a];
+          Uq[a] = hlq[a] + Tq[a];
+          hln[a] = hn[a];
+          hlq[a] = hq[a];
+          Tn[a] = Wn;
+          Tq[a] = Wq;
+        }
+      }
+    }
+    if (t < 2) {
+      cmprev = cm;
+#pragma unroll
+      for (int k = 0; k < 3; k++)
+        mprev[k] = mcur[k];
+      continue;  // warp-uniform: the windows are not yet whole
+    }
+    // Lattice row p0 - 1: four decisions by the lower bound (sf_stream.cuh),
+    // windows whose sums may be inexact taken as signal, masked centres set.
+    uint32_t b4 = cmprev;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      const uint32_t W = Tn[a];
+      const uint2 c = tab[W >> kLatPS];
+      const uint32_t S = W & kLatMask;
+      const unsigned long long L = (unsigned long long)Tq[a] * c.x;
+      const unsigned long long R = (unsigned long long)S * ((S << kDec) + c.y);
+      const bool unc = S >= kLatCap - 1u;
+      b4 |= (L > R || unc) ? 1u << a : 0u;
+    }
+    const uint32_t b5 = b4 | (__shfl_down_sync(0xffffffffu, b4, 1) & 1u) << 4;
+    if (t >= 3) {
+      // The previous triple's rows p0 - 3 .. p0 - 1: the first two see the
+      // lattice rows p0 - 4 and p0 - 1, the last only p0 - 1.
+      const uint32_t bd01 = lut[bprev & b5], bd2 = lut[b5];
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const int r = p0 - 3 + k;
+        const uint32_t bd = k < 2 ? bd01 : bd2;
+        const uint32_t mk = mprev[k];
+        const uint32_t c12 = bd & ~mk & inside12, s12 = (bd | mk) & inside12;
+        // Lane pairs: the even lane writes the pair's first two bytes, the
+        // odd lane the third.
+        const uint32_t mine = c12 | s12 << 16;
+        const uint32_t odd = __shfl_down_sync(0xffffffffu, mine, 1);
+        if (writer && r < rb) {
+          const size_t at = (size_t)r * bytes_per_row;
+          if ((lane & 1) == 0) {
+            if (pair_byte < bytes_per_row) {
+              fin[at + pair_byte] = (uint8_t)c12;
+              scr1[at + pair_byte] = (uint8_t)s12;
+            }
+            if (pair_byte + 1 < bytes_per_row) {
+              fin[at + pair_byte + 1] = (uint8_t)((c12 >> 8) | (odd & 0xFu) << 4);
+              scr1[at + pair_byte + 1] = (uint8_t)((s12 >> 8) | ((odd >> 16) & 0xFu) << 4);
+            }
+          } else if (pair_byte + 2 < bytes_per_row) {
+            fin[at + pair_byte + 2] = (uint8_t)(c12 >> 4);
+            scr1[at + pair_byte + 2] = (uint8_t)(s12 >> 4);
+          }
+        }
+      }
+    }
+    bprev = b5;
+    cmprev = cm;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+      mprev[k] = mcur[k];
+  }
+  if (kRing)
+    cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
+// The exact check of the bound's candidates, on tiles of 8 rows x 28 columns.
+//
+//   lat_tiles   lists the tiles that hold a candidate (any order)
+//   lat_verify  one warp per listed tile, persistent: the tile's 12 x 32
+//               stage-0 windows (rows r0 - 2 .., columns c0 - 2 .., lane =
+//               column) from its 18 x 38 pixels, the erosion of its 8 x 28
+//               pixels, and the candidates that fail cleared from both masks
+//
+// A warp copies the next tile's pixels into shared memory (cp.async, 16-byte
+// pieces where the frame allows) while it checks the current one, so the
+// loads' latency is hidden behind the arithmetic. Column sums of 7 rows go to
+// shared memory; then only the stage-0 windows within 2 of a candidate (the
+// only ones that can clear one, about a fifth of the tile's) are decided,
+// spread over the lanes: the two bounds of sf_stream.cuh, and the reference's
+// sequence between them (sf_common.cuh). Tiles share mask words, so the
+// clearing is an atomic AND; each candidate belongs to one tile, so the order
+// does not matter. A tile's 18 x 38 pixels cover the stage-2 window (11 x 11)
+// of each of its candidates, so a tile holding a valid pixel at or above
+// narrow_max marks its frame for the 64-bit stage 2.
+// ---------------------------------------------------------------------------
+constexpr int kVerRows = 8;                  // output rows of a tile
+constexpr int kVerTW = 28;                   // output columns of a tile
+constexpr int kVerPR = kVerRows + 10;        // pixel rows
+constexpr int kVerDR = kVerRows + 4;         // stage-0 rows
+constexpr int kVerPC = 38;                   // pixel columns
+constexpr int kVerPW = 44;                   // staged columns: 11 16-byte pieces
+constexpr int kVerWarps = 4;
+constexpr int kVerOcc = 5;                   // blocks an SM the kernel is built for
+
+__host__ __device__ inline int ver_ntx(int w) { return (w + kVerTW - 1) / kVerTW; }
+__host__ __device__ inline int ver_nty(int h) { return (h + kVerRows - 1) / kVerRows; }
+
+struct VerWarp {
+  uint32_t pix[2][kVerPR][kVerPW];  // staged pixels, two tiles
+  uint32_t cw[2][kVerRows][2];      // the tile's candidate words, two tiles
+  uint2 vs[kVerDR][kVerPC + 2];     // column sums of 7 rows
+  uint32_t msk[kVerPC + 2];         // masked pixels by row, a word a column
+  uint32_t dec[kVerDR], need[kVerDR], pre[kVerDR];
+};
+
+// The reference's decision for one window from exact sums, out of line: the
+// callers reach it only between the two bounds.
+__device__ __noinline__ bool lat_exact(uint32_t n, uint32_t S, uint32_t Q, const LaunchParams &P) {
+  return stage0_u32(n, S, Q, P, P.root_lo, P.root_hi);
+}
+
+// The stage-0 bit (signal or masked; off the frame counts as set) of pixel
+// (y, x) from the frame with 64-bit sums, for tiles holding a pixel too large
+// for the 32-bit ones.
+__device__ __noinline__ bool lat_wide(const uint32_t *__restrict__ image, int height, int width,
+                                      int y, int x, const LaunchParams &P) {
+  if (y < 0 || y >= height || x < 0 || x >= width ||
+      __ldg(image + (size_t)y * width + x) >= 0xFFFFFFFEu)
+    return true;
+  uint32_t n = 0;
+  unsigned long long S = 0, Q = 0;
+  for (int dy = -kLatK; dy <= kLatK; dy++) {
+    const int yy = y + dy;
+    if (yy < 0 || yy >= height)
+      continue;
+    for (int dx = -kLatK; dx <= kLatK; dx++) {
+      const int xx = x + dx;
+      if (xx < 0 || xx >= width)
+        continue;
+      const uint32_t v = __ldg(image + (size_t)yy * width + xx);
+      if (v < 0xFFFFFFFEu) {
+        n++;
+        S += v;
+        Q += (unsigned long long)v * v;
+      }
+    }
+  }
+  return stage0_u32(n, S, Q, P, P.root_lo, P.root_hi);
+}
+
+// One warp per 32 consecutive tiles of a tile row: 32 tiles of 28 columns
+// span 28 mask words (29 with the last tile's straddle), so lane l ORs word
+// 28 g + l over the tile row's 8 rows and each lane tests its tile from two
+// lanes' ORs.
+__global__ void __launch_bounds__(256)
+lat_tiles(int height, int width, const uint32_t *__restrict__ final_all, size_t words,
+          uint32_t *__restrict__ list, uint32_t *__restrict__ counters) {
+  const int f = blockIdx.y, lane = threadIdx.x & 31;
+  const uint32_t *fin = final_all + (size_t)f * words;
+  const int wpr = (width + 31) >> 5, ntx = ver_ntx(width), nty = ver_nty(height);
+  const int ngx = (ntx + 31) / 32;
+  const uint32_t ntiles = (uint32_t)ntx * (uint32_t)nty;
+  const long long groups = (long long)nty * ngx;
+  for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < groups;
+       g += ((long long)gridDim.x * blockDim.x) >> 5) {
+    const int ty = (int)(g / ngx), gx = (int)(g - (long long)ty * ngx);
+    const int wd = 28 * gx + lane, r0 = ty * kVerRows;
+    uint32_t acc = 0;
+    if (lane < 29 && wd < wpr) {
+#pragma unroll
+      for (int o = 0; o < kVerRows; o++)
+        if (r0 + o < height)
+          acc |= fin[(size_t)(r0 + o) * wpr + wd];
+    }
+    const int lw = (kVerTW * lane) >> 5, sh = (kVerTW * lane) & 31;
+    const uint32_t lo = __shfl_sync(0xffffffffu, acc, lw);
+    const uint32_t hi = __shfl_sync(0xffffffffu, acc, lw + 1);
+    const int tx = 32 * gx + lane;
+    const bool any = tx < ntx && ((uint32_t)(((unsigned long long)hi << 32 | lo) >> sh) &
+                                  ((1u << kVerTW) - 1u)) != 0u;
+    const unsigned bal = __ballot_sync(0xffffffffu, any);
+    if (bal) {
+      uint32_t base = 0;
+      if (lane == 0)
+        base = atomicAdd(counters + kCtrTiles, (uint32_t)__popc(bal));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (any)
+        list[base + __popc(bal & ((1u << lane) - 1u))] =
+            (uint32_t)f * ntiles + (uint32_t)ty * ntx + tx;
+    }
+  }
+}
+
+// Copies listed tile e's pixels and candidate words into buffer s (pieces
+// off the frame are written as masked pixels / zero words).
+__device__ __forceinline__ void ver_stage(VerWarp &sm, int s, uint32_t e, const FramePtrs &F,
+                                          int height, int width, int vec, uint32_t ntiles,
+                                          int ntx, const uint32_t *__restrict__ final_all,
+                                          size_t words, int lane) {
+  const int f = (int)(e / ntiles);
+  const uint32_t t = e - (uint32_t)f * ntiles;
+  const int ty = (int)(t / (uint32_t)ntx), tx = (int)(t - (uint32_t)ty * ntx);
+  const int r0 = ty * kVerRows, c0 = tx * kVerTW;
+  const int xs = (c0 - 5) & ~3;
+  const uint32_t *image = F.image[f];
+  if (vec) {
+    // With 4 | width and a 16-byte aligned frame, every piece lies wholly
+    // inside the frame or wholly outside it.
+    for (int k = lane; k < kVerPR * (kVerPW / 4); k += 32) {
+      const int r = k / (kVerPW / 4), ch = k - r * (kVerPW / 4);
+      const int y = r0 - 5 + r, x = xs + 4 * ch;
+      uint32_t *dst = &sm.pix[s][r][4 * ch];
+      if (y >= 0 && y < height && x >= 0 && x + 4 <= width)
+        cp_async16(dst, image + (size_t)y * width + x);
+      else
+        *reinterpret_cast<uint4 *>(dst) = make_uint4(~0u, ~0u, ~0u, ~0u);
+    }
+  } else {
+    for (int k = lane; k < kVerPR * kVerPW; k += 32) {
+      const int r = k / kVerPW, c = k - r * kVerPW;
+      const int y = r0 - 5 + r, x = xs + c;
+      uint32_t *dst = &sm.pix[s][r][c];
+      if (y >= 0 && y < height && x >= 0 && x < width)
+        cp_async4(dst, image + (size_t)y * width + x);
+      else
+        *dst = ~0u;
+    }
+  }
+  if (lane < 2 * kVerRows) {
+    const int o = lane >> 1, wdx = (c0 >> 5) + (lane & 1);
+    const int wpr = (width + 31) >> 5;
+    uint32_t *dst = &sm.cw[s][o][lane & 1];
+    if (r0 + o < height && wdx < wpr)
+      cp_async4(dst, final_all + (size_t)f * words + (size_t)(r0 + o) * wpr + wdx);
+    else
+      *dst = 0u;
+  }
+}
+
+template <int kOcc>
+__global__ void __launch_bounds__(kVerWarps * 32, kOcc)
+lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
+           const __grid_constant__ LaunchParams P, const __grid_constant__ StreamTables T,
+           uint32_t *__restrict__ scr1_all, uint32_t *__restrict__ final_all, size_t words,
+           const uint32_t *__restrict__ list, uint32_t *__restrict__ counters) {
+  extern __shared__ __align__(16) unsigned char ver_smem[];
+  uint4 *tab = reinterpret_cast<uint4 *>(ver_smem);
+  VerWarp *warps = reinterpret_cast<VerWarp *>(ver_smem + sizeof(uint4) * 64);
+  for (int m = threadIdx.x; m <= kLatN0; m += blockDim.x)
+    tab[m] = make_uint4(T.nk[kLatN0 - m], T.clo[kLatN0 - m], T.chi[kLatN0 - m], 0u);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  VerWarp &sm = warps[warp];
+  const int wpr = (width + 31) >> 5;
+  const int ntx = ver_ntx(width);
+  const uint32_t ntiles = (uint32_t)ntx * (uint32_t)ver_nty(height);
+  const uint32_t narrow2 = T.narrow_max + 2u;
+  const uint32_t count = counters[kCtrTiles];
+  const uint32_t nw = gridDim.x * kVerWarps;
+  uint32_t k = blockIdx.x * kVerWarps + warp;
+  if (k < count)
+    ver_stage(sm, 0, list[k], F, height, width, vec, ntiles, ntx, final_all, words, lane);
+  cp_async_commit();
+  for (int s = 0; k < count; k += nw, s ^= 1) {
+    const uint32_t e = list[k];
+    if (k + nw < count)
+      ver_stage(sm, s ^ 1, list[k + nw], F, height, width, vec, ntiles, ntx, final_all, words,
+                lane);
+    cp_async_commit();
+    cp_async_wait<1>();  // this tile's pieces have landed
+    __syncwarp();
+    const int f = (int)(e / ntiles);
+    const uint32_t t = e - (uint32_t)f * ntiles;
+    const int ty = (int)(t / (uint32_t)ntx), tx = (int)(t - (uint32_t)ty * ntx);
+    const int r0 = ty * kVerRows, c0 = tx * kVerTW;
+    const int off = (c0 - 5) - ((c0 - 5) & ~3);
+    const int w0 = c0 >> 5, sh = c0 & 31;
+    uint32_t cj[kVerRows];
+#pragma unroll
+    for (int o = 0; o < kVerRows; o++) {
+      const unsigned long long x =
+          (unsigned long long)sm.cw[s][o][0] | (unsigned long long)sm.cw[s][o][1] << 32;
+      cj[o] = (uint32_t)(x >> sh) & ((1u << kVerTW) - 1u);
+    }
+    // Columns B (pixel columns 32-37, stage-0 columns 26-31) matter only
+    // when a candidate lies in the tile's last 6 columns.
+    uint32_t late = 0;
+#pragma unroll
+    for (int o = 0; o < kVerRows; o++)
+      late |= cj[o] >> 22;
+    const int npass = late ? 2 : 1;
+    // Pixel columns off + lane (A) and off + 32 + lane (B, lanes 0-5): the
+    // masked pixels by row, the largest valid one, and the column sums of 7
+    // rows for the 12 stage-0 rows (exact in 32 bits unless the tile holds a
+    // valid pixel at or above narrow_max, which the check below catches).
+    uint32_t mx = 0;
+#pragma unroll
+    for (int pass = 0; pass < 2; pass++) {
+      if (pass == npass)
+        break;  // warp-uniform
+      if (pass == 1 && lane >= kVerPC - 32)
+        break;
+      const int col = off + 32 * pass + lane;
+      uint32_t ns[kVerPR], q[kVerPR], mk = 0;
+#pragma unroll
+      for (int r = 0; r < kVerPR; r++) {
+        const uint32_t v = sm.pix[s][r][col];
+        const bool masked = v >= 0xFFFFFFFEu;
+        mx = max(mx, v + 2u);
+        mk |= (masked ? 1u : 0u) << r;
+        ns[r] = masked ? (1u << kLatPS) : v;
+        q[r] = ns[r] * ns[r];
+      }
+      sm.msk[32 * pass + lane] = mk;
+      uint32_t cn = 0, cq = 0;
+#pragma unroll
+      for (int r = 0; r < 2 * kLatK; r++) {
+        cn += ns[r];
+        cq += q[r];
+      }
+#pragma unroll
+      for (int d = 0; d < kVerDR; d++) {
+        cn += ns[d + 2 * kLatK];
+        cq += q[d + 2 * kLatK];
+        sm.vs[d][32 * pass + lane] = make_uint2(cn, cq);
+        cn -= ns[d];
+        cq -= q[d];
+      }
+    }
+    __syncwarp();
+    const bool wide = __any_sync(0xffffffffu, mx >= narrow2);
+    if (wide && lane == 0)
+      counters[kCtrBatch + (size_t)f * kCtrCount + kCtrWideFrame] = 1u;
+    // The stage-0 positions within 2 of a candidate, lane d for stage-0 row d
+    // (row r0 - 2 + d, bit = column c0 - 2 + bit), and how many come before
+    // each row (a scan over lanes 0-11).
+    uint32_t need = 0;
+#pragma unroll
+    for (int o = 0; o < kVerRows; o++)
+      need |= (o >= lane - 4 && o <= lane) ? cj[o] : 0u;
+    {
+      const uint32_t x2 = need | need << 1;
+      need = lane < kVerDR ? (x2 | x2 << 2 | need << 4) : 0u;
+    }
+    int incl = __popc(need);
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      incl += lane >= o ? y : 0;
+    }
+    if (lane < kVerDR) {
+      sm.need[lane] = need;
+      sm.pre[lane] = (uint32_t)(incl - __popc(need));
+      sm.dec[lane] = 0xFFFFFFFFu;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, kVerDR - 1);
+    int pre[kVerDR];
+#pragma unroll
+    for (int d = 1; d < kVerDR; d++)
+      pre[d] = __shfl_sync(0xffffffffu, incl, d - 1);
+    __syncwarp();
+    // The needed positions, spread over the lanes in order: each clears its
+    // bit of the stage-0 rows when its window is not signal and its centre
+    // is not masked.
+    const uint32_t *image = F.image[f];
+    for (int q = lane; q < total; q += 32) {
+      int d = 0;
+#pragma unroll
+      for (int e2 = 1; e2 < kVerDR; e2++)
+        d += q >= pre[e2] ? 1 : 0;
+      const int col = (int)__fns(sm.need[d], 0u, q - (int)sm.pre[d] + 1);
+      if ((sm.msk[col + kLatK] >> (d + kLatK)) & 1u)
+        continue;  // masked centre (or off the frame): set
+      bool sig;
+      if (wide) {
+        sig = lat_wide(image, height, width, r0 - 2 + d, c0 - 2 + col, P);
+      } else {
+        uint32_t Wn = 0, Wq = 0;
+#pragma unroll
+        for (int u = 0; u <= 2 * kLatK; u++) {
+          const uint2 x = sm.vs[d][col + u];
+          Wn += x.x;
+          Wq += x.y;
+        }
+        const uint32_t m = Wn >> kLatPS, S = Wn & kLatMask;
+        const uint4 c = tab[m];
+        const unsigned long long L = (unsigned long long)Wq * c.x;
+        const bool maybe = L > (unsigned long long)S * ((S << kDec) + c.y);
+        const bool sure = L >= (unsigned long long)S * ((S << kDec) + c.z) + (2ull << kDec);
+        sig = sure;
+        if (maybe && !sure)
+          sig = lat_exact((uint32_t)kLatN0 - m, S, Wq, P);
+      }
+      if (!sig)
+        atomicAnd(&sm.dec[d], ~(1u << col));
+    }
+    __syncwarp();
+    uint32_t D[kVerDR];
+#pragma unroll
+    for (int d = 0; d < kVerDR; d++)
+      D[d] = sm.dec[d];
+    __syncwarp();  // the next tile rewrites the shared rows
+    // The exact erosion of the tile's rows; the candidates that fail leave
+    // both masks.
+    uint32_t *scr1 = scr1_all + (size_t)f * words;
+    uint32_t *fin = final_all + (size_t)f * words;
+#pragma unroll
+    for (int o = 0; o < kVerRows; o++) {
+      uint32_t V = 0xFFFFFFFFu;
+#pragma unroll
+      for (int u = 0; u < 5; u++)
+        V &= D[o + u];
+      uint32_t H = V;
+#pragma unroll
+      for (int u = 1; u < 5; u++)
+        H &= V >> u;
+      const uint32_t clear = cj[o] & ~H;
+      if (clear && lane < 2) {
+        const unsigned long long c64 = (unsigned long long)clear << sh;
+        const uint32_t part = (uint32_t)(c64 >> (32 * lane));
+        if (part && w0 + lane < wpr) {
+          const size_t at = (size_t)(r0 + o) * wpr + w0 + lane;
+          atomicAnd(scr1 + at, ~part);
+          atomicAnd(fin + at, ~part);
+        }
+      }
+    }
+  }
+  cp_async_wait<0>();
+}
+
+constexpr size_t ver_smem_bytes() { return sizeof(uint4) * 64 + sizeof(VerWarp) * kVerWarps; }
+
+int lat_slots() {
+  static int slots = 0;
+  if (!slots) {
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lat_stage01<kLatOcc, true>,
+                                                  kLatWarps * 32, kRingBytes);
+    slots = std::max(1, per) * kLatWarps * device_sms();
+  }
+  return slots;
+}
+
+} // namespace
+
+size_t lattice_tiles(int h, int w) { return (size_t)ver_ntx(w) * (size_t)ver_nty(h); }
+
+LatticeGeometry lattice_geometry(int h, int w, int nframes, int run_rows) {
+  LatticeGeometry g;
+  // Whole mask rows: the last strip reaches the end of the row's last word.
+  const int cols = (w + 31) / 32 * 32;
+  g.nstrips = (cols + kLatOut - 1) / kLatOut;
+  if (run_rows <= 0) {
+    const long long per = (long long)nframes * g.nstrips;
+    const long long nruns = std::max(1ll, (long long)lat_slots() / per);
+    run_rows = (int)((h + nruns - 1) / nruns);
+  }
+  run_rows = std::max(run_rows, kMinRunRows);
+  g.run_rows = (run_rows + 2) / 3 * 3;  // whole triples of rows
+  g.nruns = (h + g.run_rows - 1) / g.run_rows;
+  return g;
+}
+
+cudaError_t launch_lattice(const FramePtrs &F, int nframes, int h, int w, int vec,
+                           const LaunchParams &P, const StreamTables &T, const StreamBuffers &b,
+                           int run_rows, cudaStream_t stream) {
+  if (P.half != kLatK)
+    return cudaErrorInvalidValue;
+  const LatticeGeometry g = lattice_geometry(h, w, nframes, run_rows);
+  const long long warps = (long long)nframes * g.nstrips * g.nruns;
+  const size_t mask_bytes = b.words * sizeof(uint32_t);
+  const unsigned lb = (unsigned)((warps + kLatWarps - 1) / kLatWarps);
+  if (vec)
+    lat_stage01<kLatOcc, true><<<lb, kLatWarps * 32, kRingBytes, stream>>>(
+        F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, T,
+        reinterpret_cast<uint8_t *>(b.scr1), reinterpret_cast<uint8_t *>(b.bits), mask_bytes);
+  else
+    lat_stage01<kLatOcc, false><<<lb, kLatWarps * 32, 0, stream>>>(
+        F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, T,
+        reinterpret_cast<uint8_t *>(b.scr1), reinterpret_cast<uint8_t *>(b.bits), mask_bytes);
+  static std::once_flag configured;
+  static cudaError_t config_error = cudaSuccess;
+  static int ver_blocks = 0;
+  std::call_once(configured, [] {
+    config_error = cudaFuncSetAttribute(lat_verify<kVerOcc>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)ver_smem_bytes());
+    int per = 0;
+    if (config_error == cudaSuccess)
+      config_error = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per, lat_verify<kVerOcc>, kVerWarps * 32, ver_smem_bytes());
+    ver_blocks = std::max(1, per);
+  });
+  if (config_error != cudaSuccess)
+    return config_error;
+  // The tile list lives in the buffer the ambiguous mask takes in the other
+  // streaming path.
+  const long long tgroups = (long long)ver_nty(h) * ((ver_ntx(w) + 31) / 32);
+  const unsigned tb = (unsigned)std::min<long long>(
+      std::max(1, 8 * device_sms() / std::max(1, nframes)), (tgroups + 7) / 8);
+  lat_tiles<<<dim3(tb, nframes), 256, 0, stream>>>(h, w, b.bits, b.words, b.amb, b.counters);
+  lat_verify<kVerOcc><<<ver_blocks * device_sms(), kVerWarps * 32, ver_smem_bytes(), stream>>>(
+      F, h, w, vec, P, T, b.scr1, b.bits, b.words, b.amb, b.counters);
+  return cudaGetLastError();
+}
+
+} // namespace sf

@@ -803,7 +803,8 @@ seg_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   const int wpr = (width + 31) >> 5;
   const uint32_t nc = min(counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand], cand_cap);
   // No run of the batch met a valid pixel at or above the narrow bound.
-  const bool narrow = counters[kCtrWide] == 0;
+  const bool narrow = counters[kCtrWide] == 0 &&
+                     counters[kCtrBatch + (size_t)f * kCtrCount + kCtrWideFrame] == 0;
   const int lane = threadIdx.x & 31, sub = lane & 3;
   const uint32_t per_pass = (gridDim.x * blockDim.x) >> 2;
   for (uint32_t base = (blockIdx.x * blockDim.x) >> 2; base < nc; base += per_pass) {
@@ -925,7 +926,7 @@ mask_prefix(const uint32_t *__restrict__ bits_all, size_t words,
 // Host side.
 // ---------------------------------------------------------------------------
 
-static int device_sms() {
+int device_sms() {
   static int cached = 0;
   if (cached)
     return cached;
@@ -1028,20 +1029,27 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
   for (int f = 0; f < nframes; f++)
     if (reinterpret_cast<uintptr_t>(F.image[f]) % 16 != 0)
       vec = 0;
-  const SegGeometry g = seg_geometry(h, w, nframes, run_rows, seg_slots<K>());
-  const long long warps = (long long)nframes * g.nstrips * g.nruns;
-  const size_t mask_bytes = b.words * sizeof(uint32_t);
-  uint8_t *scr1 = reinterpret_cast<uint8_t *>(b.scr1);
-  uint8_t *fin = reinterpret_cast<uint8_t *>(b.bits);
   const int sms = device_sms();
-  uint8_t *amb = reinterpret_cast<uint8_t *>(b.amb);
-  seg_stage01<K><<<(unsigned)((warps + kSegWarps - 1) / kSegWarps), kSegWarps * 32, sizeof(S),
-                   stream>>>(F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, P, T, scr1,
-                             fin, amb, mask_bytes, b.counters, b.wide);
-  stream_wide<K><<<2 * sms, 256, 0, stream>>>(F, h, w, g.run_rows, P, scr1, fin, amb, mask_bytes,
-                                               b.counters, b.wide);
-  amb_fix<K><<<dim3((unsigned)((b.words + 255) / 256), nframes), 256, 0, stream>>>(
-      F, h, w, P, b.amb, b.scr1, b.bits, b.words);
+  if (K == 3) {
+    // The reference's window: the lattice bound and its exact check.
+    const cudaError_t e = launch_lattice(F, nframes, h, w, vec, P, T, b, run_rows, stream);
+    if (e != cudaSuccess)
+      return e;
+  } else {
+    const SegGeometry g = seg_geometry(h, w, nframes, run_rows, seg_slots<K>());
+    const long long warps = (long long)nframes * g.nstrips * g.nruns;
+    const size_t mask_bytes = b.words * sizeof(uint32_t);
+    uint8_t *scr1 = reinterpret_cast<uint8_t *>(b.scr1);
+    uint8_t *fin = reinterpret_cast<uint8_t *>(b.bits);
+    uint8_t *amb = reinterpret_cast<uint8_t *>(b.amb);
+    seg_stage01<K><<<(unsigned)((warps + kSegWarps - 1) / kSegWarps), kSegWarps * 32, sizeof(S),
+                     stream>>>(F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, P, T, scr1,
+                               fin, amb, mask_bytes, b.counters, b.wide);
+    stream_wide<K><<<2 * sms, 256, 0, stream>>>(F, h, w, g.run_rows, P, scr1, fin, amb,
+                                                 mask_bytes, b.counters, b.wide);
+    amb_fix<K><<<dim3((unsigned)((b.words + 255) / 256), nframes), 256, 0, stream>>>(
+        F, h, w, P, b.amb, b.scr1, b.bits, b.words);
+  }
   if (marks)
     cudaEventRecord(marks->stage01, stream);
   const dim3 og((unsigned)order_bpf(nframes, b.words), (unsigned)nframes);
@@ -1066,7 +1074,9 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
 }
 
 int stream_default_run_rows(const LaunchParams &P, int h, int w, int nframes) {
-  const int slots = P.half == 2 ? seg_slots<2>() : P.half == 3 ? seg_slots<3>() : seg_slots<4>();
+  if (P.half == 3)
+    return lattice_geometry(h, w, nframes, 0).run_rows;
+  const int slots = P.half == 2 ? seg_slots<2>() : seg_slots<4>();
   return seg_geometry(h, w, nframes, 0, slots).run_rows;
 }
 

@@ -26,6 +26,9 @@
 
 namespace sf {
 
+// The current device's SM count (152 until a device answers).
+int device_sms();
+
 // Frames one launch sequence takes.
 constexpr int kMaxBatch = 64;
 
@@ -36,8 +39,10 @@ struct FramePtrs {
 // Counter words: the batch's own first, then kCtrCount per frame.
 enum {
   kCtrWide = 0,   // batch: runs handed to the 64-bit path
+  kCtrTiles = 1,  // batch: tiles listed for the exact check (kernel 3,3)
   kCtrBatch = 4,  // first frame's counters
   kCtrCand = 0,   // frame: candidates (set bits of the candidate mask)
+  kCtrWideFrame = 1,  // frame: a valid pixel may be too large for 32-bit stage-2 sums
   kCtrCount = 4
 };
 inline size_t counter_words(int nframes) { return kCtrBatch + (size_t)nframes * kCtrCount; }
@@ -58,7 +63,7 @@ struct StreamTables {
 struct StreamBuffers {
   uint32_t *bits;          // final strong masks (output), frame f at bits + f * words
   uint32_t *scr1;          // eroded masks, same layout
-  uint32_t *amb;           // ambiguous stage-0 windows, same layout
+  uint32_t *amb;           // ambiguous stage-0 windows, same layout (kernel 3,3: the tile list)
   uint32_t *prefix;        // per-word list positions (output) or null
   size_t words;            // mask words per frame
   uint32_t *cand;          // ascending candidate indices, frame f at cand + f * cand_cap
@@ -87,6 +92,23 @@ int stream_default_run_rows(const LaunchParams &P, int h, int w, int nframes);
 struct StreamMarks {
   cudaEvent_t start, stage01, stage2, order;
 };
+
+// The lattice pass for kernel 3,3 (sf_lattice.cu): strips of 360 output
+// columns (one warp each) by runs of run_rows rows, a multiple of 3.
+struct LatticeGeometry {
+  int nstrips, nruns, run_rows;
+};
+// run_rows 0 picks runs that fill the resident warps once.
+LatticeGeometry lattice_geometry(int h, int w, int nframes, int run_rows);
+// Tiles of the exact check a frame has; the tile list takes one word each
+// (in StreamBuffers::amb, which must hold max(words, lattice_tiles) a frame).
+size_t lattice_tiles(int h, int w);
+// Stage 0 and the erosion for kernel 3,3: the lattice bound, then the exact
+// check of its candidates; writes b.scr1 and b.bits as the first pass of
+// launch_stream does (vec: the frames allow 16-byte loads).
+cudaError_t launch_lattice(const FramePtrs &frames, int nframes, int h, int w, int vec,
+                           const LaunchParams &P, const StreamTables &T, const StreamBuffers &b,
+                           int run_rows, cudaStream_t stream);
 
 // run_rows 0: the default geometry. marks may be null.
 cudaError_t launch_stream(const FramePtrs &frames, int nframes, int h, int w,
