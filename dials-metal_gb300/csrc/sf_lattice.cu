@@ -548,14 +548,18 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   const uint32_t count = counters[kCtrTiles];
   const uint32_t nw = gridDim.x * kVerWarps;
   uint32_t k = blockIdx.x * kVerWarps + warp;
+  // List entries are read a tile before they are staged, and staged a tile
+  // before they are checked.
+  uint32_t e = k < count ? list[k] : 0u;
+  uint32_t e1 = k + nw < count ? list[k + nw] : 0u;
   if (k < count)
-    ver_stage(sm, 0, list[k], F, height, width, vec, ntiles, ntx, final_all, words, lane);
+    ver_stage(sm, 0, e, F, height, width, vec, ntiles, ntx, final_all, words, lane);
   cp_async_commit();
-  for (int s = 0; k < count; k += nw, s ^= 1) {
-    const uint32_t e = list[k];
+  uint32_t e2 = 0u;
+  for (int s = 0; k < count; k += nw, s ^= 1, e = e1, e1 = e2) {
+    e2 = k + 2 * nw < count ? list[k + 2 * nw] : 0u;
     if (k + nw < count)
-      ver_stage(sm, s ^ 1, list[k + nw], F, height, width, vec, ntiles, ntx, final_all, words,
-                lane);
+      ver_stage(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, final_all, words, lane);
     cp_async_commit();
     cp_async_wait<1>();  // this tile's pieces have landed
     __syncwarp();
@@ -719,6 +723,239 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   cp_async_wait<0>();
 }
 
+// ---------------------------------------------------------------------------
+// Stage 2 (src/spots/dext.cc:151-222) on the listed tiles, after the exact
+// check: a candidate's background is the valid pixels of its clipped 11 x 11
+// window outside the eroded mask, and the tile's 18 x 38 pixels hold every
+// window of its candidates. A warp stages them with the eroded-mask words
+// over them (cp.async, the next tile's while it works on this one), takes
+// column sums of 11 rows once per tile, then per candidate adds 11 of them
+// and runs the reference's test (sf_common.cuh). The result goes to the
+// candidate's place in the ascending candidate list, from the per-word list
+// positions of the candidate mask (mask_prefix); the mask itself is left as
+// it is until every position is taken (pass_sums clears the failures).
+// ---------------------------------------------------------------------------
+struct S2Warp {
+  uint32_t pix[2][kVerPR][kVerPW];  // staged pixels, two tiles
+  uint32_t ew[2][kVerPR][3];        // eroded-mask words over the staged columns
+  uint32_t cw[2][kVerRows][2];      // candidate-mask words of the tile's rows
+  uint32_t pw[2][kVerRows][2];      // their list positions
+  uint2 cs[kVerRows][kVerPC + 2];   // {count, sum} of 11 rows of background
+};
+
+__device__ __forceinline__ void s2_stage(S2Warp &sm, int s, uint32_t e, const FramePtrs &F,
+                                         int height, int width, int vec, uint32_t ntiles, int ntx,
+                                         const uint32_t *__restrict__ scr1_all,
+                                         const uint32_t *__restrict__ final_all,
+                                         const uint32_t *__restrict__ prefix_all, size_t words,
+                                         int lane) {
+  const int f = (int)(e / ntiles);
+  const uint32_t t = e - (uint32_t)f * ntiles;
+  const int ty = (int)(t / (uint32_t)ntx), tx = (int)(t - (uint32_t)ty * ntx);
+  const int r0 = ty * kVerRows, c0 = tx * kVerTW;
+  const int xs = (c0 - 5) & ~3;
+  const uint32_t *image = F.image[f];
+  if (vec) {
+    for (int k = lane; k < kVerPR * (kVerPW / 4); k += 32) {
+      const int r = k / (kVerPW / 4), ch = k - r * (kVerPW / 4);
+      const int y = r0 - 5 + r, x = xs + 4 * ch;
+      uint32_t *dst = &sm.pix[s][r][4 * ch];
+      if (y >= 0 && y < height && x >= 0 && x + 4 <= width)
+        cp_async16(dst, image + (size_t)y * width + x);
+      else
+        *reinterpret_cast<uint4 *>(dst) = make_uint4(~0u, ~0u, ~0u, ~0u);
+    }
+  } else {
+    for (int k = lane; k < kVerPR * kVerPW; k += 32) {
+      const int r = k / kVerPW, c = k - r * kVerPW;
+      const int y = r0 - 5 + r, x = xs + c;
+      uint32_t *dst = &sm.pix[s][r][c];
+      if (y >= 0 && y < height && x >= 0 && x < width)
+        cp_async4(dst, image + (size_t)y * width + x);
+      else
+        *dst = ~0u;
+    }
+  }
+  const int wpr = (width + 31) >> 5;
+  const uint32_t *scr1 = scr1_all + (size_t)f * words;
+  for (int k = lane; k < kVerPR * 3; k += 32) {
+    const int r = k / 3, j = k - 3 * r;
+    const int y = r0 - 5 + r, wd = (xs >> 5) + j;
+    uint32_t *dst = &sm.ew[s][r][j];
+    if (y >= 0 && y < height && wd >= 0 && wd < wpr)
+      cp_async4(dst, scr1 + (size_t)y * wpr + wd);
+    else
+      *dst = 0u;
+  }
+  if (lane < 2 * kVerRows) {
+    const int o = lane >> 1, wdx = (c0 >> 5) + (lane & 1);
+    const bool in = r0 + o < height && wdx < wpr;
+    const size_t at = (size_t)f * words + (size_t)(r0 + o) * wpr + wdx;
+    if (in) {
+      cp_async4(&sm.cw[s][o][lane & 1], final_all + at);
+      cp_async4(&sm.pw[s][o][lane & 1], prefix_all + at);
+    } else {
+      sm.cw[s][o][lane & 1] = 0u;
+      sm.pw[s][o][lane & 1] = 0u;
+    }
+  }
+}
+
+template <int kOcc>
+__global__ void __launch_bounds__(kVerWarps * 32, kOcc)
+lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
+           const __grid_constant__ LaunchParams P, const uint32_t *__restrict__ scr1_all,
+           const uint32_t *__restrict__ final_all, const uint32_t *__restrict__ prefix_all,
+           size_t words, const uint32_t *__restrict__ list, const uint32_t *__restrict__ counters,
+           uint32_t *__restrict__ cand_all, uint2 *__restrict__ res_all, uint32_t cand_cap) {
+  extern __shared__ __align__(16) unsigned char s2_smem[];
+  S2Warp &sm = reinterpret_cast<S2Warp *>(s2_smem)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int ntx = ver_ntx(width);
+  const uint32_t ntiles = (uint32_t)ntx * (uint32_t)ver_nty(height);
+  const uint32_t count = counters[kCtrTiles];
+  const uint32_t nw = gridDim.x * kVerWarps;
+  uint32_t k = blockIdx.x * kVerWarps + (threadIdx.x >> 5);
+  uint32_t e = k < count ? list[k] : 0u;
+  uint32_t e1 = k + nw < count ? list[k + nw] : 0u;
+  if (k < count)
+    s2_stage(sm, 0, e, F, height, width, vec, ntiles, ntx, scr1_all, final_all, prefix_all,
+             words, lane);
+  cp_async_commit();
+  uint32_t e2 = 0u;
+  for (int s = 0; k < count; k += nw, s ^= 1, e = e1, e1 = e2) {
+    e2 = k + 2 * nw < count ? list[k + 2 * nw] : 0u;
+    if (k + nw < count)
+      s2_stage(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, scr1_all, final_all,
+               prefix_all, words, lane);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncwarp();
+    const int f = (int)(e / ntiles);
+    const uint32_t t = e - (uint32_t)f * ntiles;
+    const int ty = (int)(t / (uint32_t)ntx), tx = (int)(t - (uint32_t)ty * ntx);
+    const int r0 = ty * kVerRows, c0 = tx * kVerTW;
+    const int xs = (c0 - 5) & ~3, off = (c0 - 5) - xs;
+    const int w0 = c0 >> 5, sh = c0 & 31;
+    uint32_t cj[kVerRows], late = 0;
+    int incl = 0;
+#pragma unroll
+    for (int o = 0; o < kVerRows; o++) {
+      const unsigned long long x =
+          (unsigned long long)sm.cw[s][o][0] | (unsigned long long)sm.cw[s][o][1] << 32;
+      cj[o] = (uint32_t)(x >> sh) & ((1u << kVerTW) - 1u);
+      late |= cj[o] >> 22;
+      incl += __popc(cj[o]);
+    }
+    const int total = incl;  // the tile's candidates (the same in every lane)
+    if (total == 0) {
+      __syncwarp();
+      continue;  // every candidate of the tile failed the exact check
+    }
+    // Background by column: A = staged column off + lane, B = off + 32 + lane
+    // (needed only for candidates in the tile's last 6 columns). Valid
+    // pixels below 2^24 keep the sums of 121 of them within 32 bits; a tile
+    // holding a larger one sums each window in 64 bits instead.
+    uint32_t mx = 0;
+    const int npass = late ? 2 : 1;
+#pragma unroll
+    for (int pass = 0; pass < 2; pass++) {
+      if (pass == npass)
+        break;
+      if (pass == 1 && lane >= kVerPC - 32)
+        break;
+      const int j = off + 32 * pass + lane;
+      const int x = xs + j, wi = (x >> 5) - (xs >> 5), b = x & 31;
+      uint32_t bn[kVerPR], bs[kVerPR];
+#pragma unroll
+      for (int r = 0; r < kVerPR; r++) {
+        const uint32_t v = sm.pix[s][r][j];
+        const bool eroded = (sm.ew[s][r][wi] >> b) & 1u;
+        const bool bg = v < 0xFFFFFFFEu && !eroded;
+        mx = max(mx, v + 2u);
+        bn[r] = bg ? 1u : 0u;
+        bs[r] = bg ? v : 0u;
+      }
+      uint32_t cn = 0, cs = 0;
+#pragma unroll
+      for (int r = 0; r < 10; r++) {
+        cn += bn[r];
+        cs += bs[r];
+      }
+#pragma unroll
+      for (int o = 0; o < kVerRows; o++) {
+        cn += bn[o + 10];
+        cs += bs[o + 10];
+        sm.cs[o][32 * pass + lane] = make_uint2(cn, cs);
+        cn -= bn[o];
+        cs -= bs[o];
+      }
+    }
+    const bool wide = __any_sync(0xffffffffu, mx >= (1u << 24) + 2u);
+    __syncwarp();
+    // The tile's candidates, spread over the lanes in order.
+    int pre[kVerRows];
+    {
+      int run = 0;
+#pragma unroll
+      for (int o = 0; o < kVerRows; o++) {
+        pre[o] = run;
+        run += __popc(cj[o]);
+      }
+    }
+    uint32_t *cand = cand_all + (size_t)f * cand_cap;
+    uint2 *res = res_all + (size_t)f * cand_cap;
+    for (int q = lane; q < total; q += 32) {
+      int o = 0;
+#pragma unroll
+      for (int e2 = 1; e2 < kVerRows; e2++)
+        o += q >= pre[e2] ? 1 : 0;
+      uint32_t bits = 0;
+#pragma unroll
+      for (int e2 = 0; e2 < kVerRows; e2++)
+        bits = e2 == o ? cj[e2] : bits;
+      const int tcol = (int)__fns(bits, 0u, q - pre[o] + 1);
+      uint32_t n = 0;
+      unsigned long long S = 0;
+      if (!wide) {
+        uint32_t s32 = 0;
+#pragma unroll
+        for (int u = 0; u < 11; u++) {
+          const uint2 c = sm.cs[o][tcol + u];
+          n += c.x;
+          s32 += c.y;
+        }
+        S = s32;
+      } else {
+        for (int r = o; r < o + 11; r++)
+          for (int u = 0; u < 11; u++) {
+            const int j = off + tcol + u, x = xs + j;
+            const uint32_t v = sm.pix[s][r][j];
+            const bool eroded = (sm.ew[s][r][(x >> 5) - (xs >> 5)] >> (x & 31)) & 1u;
+            if (v < 0xFFFFFFFEu && !eroded) {
+              n++;
+              S += v;
+            }
+          }
+      }
+      const uint32_t p = sm.pix[s][o + 5][off + tcol + 5];
+      float bg = 0.0f;
+      // dext.cc:205: only pixels above the global threshold are tested.
+      const bool sig = (uint64_t)p >= P.p_min && stage2_u32(p, n, S, P, &bg);
+      const int x = c0 + tcol, jw = (x >> 5) - w0, bit = x & 31;
+      const uint32_t i = sm.pw[s][o][jw] + (uint32_t)__popc(sm.cw[s][o][jw] & ((1u << bit) - 1u));
+      if (i < cand_cap) {
+        cand[i] = (uint32_t)(r0 + o) * (uint32_t)width + (uint32_t)x;
+        res[i] = make_uint2(__float_as_uint(bg), n | (sig ? 1u << 16 : 0u));
+      }
+    }
+    __syncwarp();  // the next tile rewrites the shared sums
+  }
+  cp_async_wait<0>();
+}
+
+constexpr size_t s2_smem_bytes() { return sizeof(S2Warp) * kVerWarps; }
+
 constexpr size_t ver_smem_bytes() { return sizeof(uint4) * 64 + sizeof(VerWarp) * kVerWarps; }
 
 int lat_slots() {
@@ -735,6 +972,32 @@ int lat_slots() {
 } // namespace
 
 size_t lattice_tiles(int h, int w) { return (size_t)ver_ntx(w) * (size_t)ver_nty(h); }
+
+cudaError_t launch_lattice_stage2(const FramePtrs &F, int nframes, int h, int w, int vec,
+                                  const LaunchParams &P, const StreamBuffers &b,
+                                  cudaStream_t stream) {
+  static std::once_flag configured;
+  static cudaError_t config_error = cudaSuccess;
+  static int blocks = 0;
+  std::call_once(configured, [] {
+    config_error = cudaFuncSetAttribute(lat_stage2<kVerOcc>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)s2_smem_bytes());
+    int per = 0;
+    if (config_error == cudaSuccess)
+      config_error = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per, lat_stage2<kVerOcc>, kVerWarps * 32, s2_smem_bytes());
+    blocks = std::max(1, per);
+  });
+  if (config_error != cudaSuccess)
+    return config_error;
+  const uint32_t *prefix = b.amb;
+  const uint32_t *list = b.amb + (size_t)nframes * b.words;
+  lat_stage2<kVerOcc><<<blocks * device_sms(), kVerWarps * 32, s2_smem_bytes(), stream>>>(
+      F, h, w, vec, P, b.scr1, b.bits, prefix, b.words, list, b.counters, b.cand, b.res,
+      b.cand_cap);
+  return cudaGetLastError();
+}
 
 LatticeGeometry lattice_geometry(int h, int w, int nframes, int run_rows) {
   LatticeGeometry g;
@@ -784,14 +1047,16 @@ cudaError_t launch_lattice(const FramePtrs &F, int nframes, int h, int w, int ve
   });
   if (config_error != cudaSuccess)
     return config_error;
-  // The tile list lives in the buffer the ambiguous mask takes in the other
-  // streaming path.
+  // The ambiguous-mask buffer of the other streaming path holds, here, the
+  // candidate mask's per-word list positions (stage 2) and then the tile
+  // list.
   const long long tgroups = (long long)ver_nty(h) * ((ver_ntx(w) + 31) / 32);
   const unsigned tb = (unsigned)std::min<long long>(
       std::max(1, 8 * device_sms() / std::max(1, nframes)), (tgroups + 7) / 8);
-  lat_tiles<<<dim3(tb, nframes), 256, 0, stream>>>(h, w, b.bits, b.words, b.amb, b.counters);
+  uint32_t *list = b.amb + (size_t)nframes * b.words;
+  lat_tiles<<<dim3(tb, nframes), 256, 0, stream>>>(h, w, b.bits, b.words, list, b.counters);
   lat_verify<kVerOcc><<<ver_blocks * device_sms(), kVerWarps * 32, ver_smem_bytes(), stream>>>(
-      F, h, w, vec, P, T, b.scr1, b.bits, b.words, b.amb, b.counters);
+      F, h, w, vec, P, T, b.scr1, b.bits, b.words, list, b.counters);
   return cudaGetLastError();
 }
 

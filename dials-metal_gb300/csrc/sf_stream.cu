@@ -844,13 +844,27 @@ seg_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kScanT)
 pass_sums(const uint2 *__restrict__ res_all, uint32_t cand_cap,
-          const uint32_t *__restrict__ counters, uint32_t *__restrict__ block_sums) {
+          const uint32_t *__restrict__ counters, uint32_t *__restrict__ block_sums,
+          const uint32_t *__restrict__ cand_all, uint32_t *__restrict__ final_all, size_t words,
+          int width) {
   const int f = blockIdx.y;
   const uint2 *res = res_all + (size_t)f * cand_cap;
   const uint32_t nc = min(counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand], cand_cap);
+  // final_all given: the candidates that failed stage 2 leave the final mask
+  // here (their stage 2 left it alone).
+  const uint32_t *cand = cand_all + (size_t)f * cand_cap;
+  uint32_t *fin = final_all ? final_all + (size_t)f * words : nullptr;
+  const uint32_t wpr = ((uint32_t)width + 31u) >> 5;
   size_t lo, hi;
   chunk_of(nc, &lo, &hi);
-  scan_count(lo, hi, [&](size_t i) { return (res[i].y >> 16) & 1u; }, block_sums);
+  scan_count(lo, hi, [&](size_t i) {
+    const uint32_t pass = (res[i].y >> 16) & 1u;
+    if (fin && !pass) {
+      const uint32_t idx = cand[i], y = idx / (uint32_t)width, x = idx - y * (uint32_t)width;
+      atomicAnd(fin + (size_t)y * wpr + (x >> 5), ~(1u << (x & 31)));
+    }
+    return pass;
+  }, block_sums);
 }
 
 __global__ void __launch_bounds__(kScanT)
@@ -894,12 +908,15 @@ pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ c
 // Optional: per final-mask word, the list position of its first pixel.
 __global__ void __launch_bounds__(kScanT)
 mask_prefix(const uint32_t *__restrict__ bits_all, size_t words,
-            const uint32_t *__restrict__ block_sums, uint32_t *__restrict__ prefix_all) {
+            const uint32_t *__restrict__ block_sums, uint32_t *__restrict__ prefix_all,
+            uint32_t *__restrict__ counters) {
   const int f = blockIdx.y;
   const uint32_t *bits = bits_all + (size_t)f * words;
   uint32_t *prefix = prefix_all + (size_t)f * words;
   uint32_t total;
   uint32_t carry = block_base(block_sums, &total);
+  if (counters && blockIdx.x == 0 && threadIdx.x == 0)
+    counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand] = total;  // the candidates
   size_t lo, hi;
   chunk_of(words, &lo, &hi);
   for (size_t base = lo; base < hi; base += kScanChunk) {
@@ -1054,19 +1071,29 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
     cudaEventRecord(marks->stage01, stream);
   const dim3 og((unsigned)order_bpf(nframes, b.words), (unsigned)nframes);
   mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
-  mask_list<<<og, kScanT, 0, stream>>>(b.bits, b.words, w, b.block_sums, b.cand, b.cand_cap,
-                                       b.counters);
-  const unsigned s2x = (unsigned)std::max(1, (8 * sms + nframes - 1) / nframes);
-  seg_stage2<K><<<dim3(s2x, nframes), 256, 0, stream>>>(F, h, w, vec, P, b.scr1, b.bits, b.words,
-                                                        b.cand, b.cand_cap, b.counters, b.res);
+  if (K == 3) {
+    // Stage 2 on the exact check's tiles, into the list positions.
+    mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.amb, b.counters);
+    const cudaError_t e = launch_lattice_stage2(F, nframes, h, w, vec, P, b, stream);
+    if (e != cudaSuccess)
+      return e;
+  } else {
+    mask_list<<<og, kScanT, 0, stream>>>(b.bits, b.words, w, b.block_sums, b.cand, b.cand_cap,
+                                         b.counters);
+    const unsigned s2x = (unsigned)std::max(1, (8 * sms + nframes - 1) / nframes);
+    seg_stage2<K><<<dim3(s2x, nframes), 256, 0, stream>>>(F, h, w, vec, P, b.scr1, b.bits,
+                                                          b.words, b.cand, b.cand_cap, b.counters,
+                                                          b.res);
+  }
   if (marks)
     cudaEventRecord(marks->stage2, stream);
-  pass_sums<<<og, kScanT, 0, stream>>>(b.res, b.cand_cap, b.counters, b.block_sums);
+  pass_sums<<<og, kScanT, 0, stream>>>(b.res, b.cand_cap, b.counters, b.block_sums, b.cand,
+                                       K == 3 ? b.bits : nullptr, b.words, w);
   pass_scatter<<<og, kScanT, 0, stream>>>(F, b.cand, b.cand_cap, b.res, b.counters, b.block_sums,
                                           b.out, b.out_stride, b.capacity, b.count_out);
   if (b.prefix) {
     mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
-    mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.prefix);
+    mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.prefix, nullptr);
   }
   if (marks)
     cudaEventRecord(marks->order, stream);

@@ -63,7 +63,7 @@ struct StreamTables {
 struct StreamBuffers {
   uint32_t *bits;          // final strong masks (output), frame f at bits + f * words
   uint32_t *scr1;          // eroded masks, same layout
-  uint32_t *amb;           // ambiguous stage-0 windows, same layout (kernel 3,3: the tile list)
+  uint32_t *amb;           // ambiguous stage-0 windows, same layout (kernel 3,3: see lattice_tiles)
   uint32_t *prefix;        // per-word list positions (output) or null
   size_t words;            // mask words per frame
   uint32_t *cand;          // ascending candidate indices, frame f at cand + f * cand_cap
@@ -100,9 +100,15 @@ struct LatticeGeometry {
 };
 // run_rows 0 picks runs that fill the resident warps once.
 LatticeGeometry lattice_geometry(int h, int w, int nframes, int run_rows);
-// Tiles of the exact check a frame has; the tile list takes one word each
-// (in StreamBuffers::amb, which must hold max(words, lattice_tiles) a frame).
+// Tiles of the exact check a frame has. For kernel 3,3 StreamBuffers::amb
+// holds words + lattice_tiles words a frame: the candidate mask's per-word
+// list positions, then the tile list.
 size_t lattice_tiles(int h, int w);
+// Stage 2 for kernel 3,3 on the listed tiles, after launch_lattice and
+// mask_prefix into b.amb: the candidate list and the results (b.cand, b.res).
+cudaError_t launch_lattice_stage2(const FramePtrs &frames, int nframes, int h, int w, int vec,
+                                  const LaunchParams &P, const StreamBuffers &b,
+                                  cudaStream_t stream);
 // Stage 0 and the erosion for kernel 3,3: the lattice bound, then the exact
 // check of its candidates; writes b.scr1 and b.bits as the first pass of
 // launch_stream does (vec: the frames allow 16-byte loads).
