@@ -51,7 +51,7 @@ constexpr int kLatCols = 12;                // columns a lane owns
 constexpr int kLatOutLanes = 30;            // lanes 0-29 write, lane 30 feeds lane 29
 constexpr int kLatOut = kLatCols * kLatOutLanes;  // 360 output columns a warp
 constexpr int kLatWarps = 4;                // warps a block
-constexpr int kLatOcc = 5;                  // blocks an SM the kernel is built for
+constexpr int kLatOcc = 6;                  // blocks an SM the kernel is built for
 constexpr uint32_t kLatPS = 26;             // masked count above a 26-bit sum
 constexpr uint32_t kLatMask = (1u << kLatPS) - 1u;
 constexpr uint32_t kLatCap = 32767;         // valid pixels saturate here
@@ -203,28 +203,27 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
   // Pixel rows [pbeg, pend) of the run.
   const int pbeg = 3 * (ja - 2), pend = 3 * (ja + ntrip + 1);
   uint32_t *ring = lat_ring + (size_t)warp * kRingSlots * kRingStride;
-  // The ring's pieces of this lane: column offsets and whether each lies in
-  // the frame.
+  // The ring's pieces of this lane: l, l + 32, l + 64 (a warp's copy
+  // instruction covers 512 contiguous bytes), and whether each lies in the
+  // frame.
   const int X = kLatOut * sx;
-  int pc[3];
-  bool pin[3];
+  const int x0 = X - 4 + 4 * lane;
+  bool pin[3], pok[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    const int k = lane + 32 * i, x = X - 4 + 4 * k;
-    pc[i] = x;
-    pin[i] = k < kRingPieces && x >= 0 && x + 4 <= width;
+    pok[i] = lane + 32 * i < kRingPieces;
+    pin[i] = pok[i] && x0 + 128 * i >= 0 && x0 + 128 * i + 4 <= width;
   }
   auto fetch = [&](int p) {
-    uint32_t *dst = ring + ((p - pbeg) % kRingSlots) * kRingStride;
+    uint32_t *dst = ring + ((p - pbeg) % kRingSlots) * kRingStride + 4 * lane;
     const bool rowin = p >= 0 && p < height && p < pend;
-    const uint32_t *src = image + (size_t)(rowin ? p : 0) * width;
+    const uint32_t *src = image + (size_t)(rowin ? p : 0) * width + x0;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      const int k = lane + 32 * i;
       if (rowin && pin[i])
-        cp_async16(dst + 4 * k, src + pc[i]);
-      else if (k < kRingPieces)
-        *reinterpret_cast<uint4 *>(dst + 4 * k) = make_uint4(~0u, ~0u, ~0u, ~0u);
+        cp_async16(dst + 128 * i, src + 128 * i);
+      else if (pok[i])
+        *reinterpret_cast<uint4 *>(dst + 128 * i) = make_uint4(~0u, ~0u, ~0u, ~0u);
     }
   };
   if (kRing) {
@@ -312,7 +311,7 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
 #pragma unroll
     for (int a = 0; a < 4; a++) {
       const uint32_t W = Tn[a];
-      const uint2 c = tab[W >> kLatPS];
+      const uint2 c = tab[min(W >> kLatPS, (uint32_t)kLatN0)];  // 49 pixels: m <= 49
       const uint32_t S = W & kLatMask;
       const unsigned long long L = (unsigned long long)Tq[a] * c.x;
       const unsigned long long R = (unsigned long long)S * ((S << kDec) + c.y);
@@ -400,7 +399,6 @@ struct VerWarp {
   uint32_t cw[2][kVerRows][2];      // the tile's candidate words, two tiles
   uint2 vs[kVerDR][kVerPC + 2];     // column sums of 7 rows
   uint32_t msk[kVerPC + 2];         // masked pixels by row, a word a column
-  uint32_t dec[kVerDR], need[kVerDR], pre[kVerDR];
 };
 
 // The reference's decision for one window from exact sums, out of line: the
@@ -625,9 +623,10 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
     const bool wide = __any_sync(0xffffffffu, mx >= narrow2);
     if (wide && lane == 0)
       counters[kCtrBatch + (size_t)f * kCtrCount + kCtrWideFrame] = 1u;
-    // The stage-0 positions within 2 of a candidate, lane d for stage-0 row d
-    // (row r0 - 2 + d, bit = column c0 - 2 + bit), and how many come before
-    // each row (a scan over lanes 0-11).
+    // The stage-0 positions within 2 of a candidate: lane d first forms row
+    // d's (row r0 - 2 + d, bit = column c0 - 2 + bit), then every lane takes
+    // its own column's rows of them, less those whose centre is masked (set
+    // whatever the window).
     uint32_t need = 0;
 #pragma unroll
     for (int o = 0; o < kVerRows; o++)
@@ -636,47 +635,33 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
       const uint32_t x2 = need | need << 1;
       need = lane < kVerDR ? (x2 | x2 << 2 | need << 4) : 0u;
     }
-    int incl = __popc(need);
+    uint32_t rows = 0;
 #pragma unroll
-    for (int o = 1; o < 16; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      incl += lane >= o ? y : 0;
-    }
-    if (lane < kVerDR) {
-      sm.need[lane] = need;
-      sm.pre[lane] = (uint32_t)(incl - __popc(need));
-      sm.dec[lane] = 0xFFFFFFFFu;
-    }
-    const int total = __shfl_sync(0xffffffffu, incl, kVerDR - 1);
-    int pre[kVerDR];
-#pragma unroll
-    for (int d = 1; d < kVerDR; d++)
-      pre[d] = __shfl_sync(0xffffffffu, incl, d - 1);
-    __syncwarp();
-    // The needed positions, spread over the lanes in order: each clears its
-    // bit of the stage-0 rows when its window is not signal and its centre
-    // is not masked.
+    for (int d = 0; d < kVerDR; d++)
+      rows |= ((__shfl_sync(0xffffffffu, need, d) >> lane) & 1u) << d;
+    rows &= ~(sm.msk[lane + kLatK] >> kLatK);
+    // Each lane decides its column's needed windows (lane = column, so no
+    // two lanes share a result bit): a row's bit clears when its window is
+    // not signal.
     const uint32_t *image = F.image[f];
-    for (int q = lane; q < total; q += 32) {
-      int d = 0;
-#pragma unroll
-      for (int e2 = 1; e2 < kVerDR; e2++)
-        d += q >= pre[e2] ? 1 : 0;
-      const int col = (int)__fns(sm.need[d], 0u, q - (int)sm.pre[d] + 1);
-      if ((sm.msk[col + kLatK] >> (d + kLatK)) & 1u)
-        continue;  // masked centre (or off the frame): set
+    uint32_t keep = 0xFFFFFFFFu;  // bit d: row d's window here is signal (or not needed)
+    while (rows) {
+      const int d = __ffs(rows) - 1;
+      rows &= rows - 1u;
       bool sig;
       if (wide) {
-        sig = lat_wide(image, height, width, r0 - 2 + d, c0 - 2 + col, P);
+        sig = lat_wide(image, height, width, r0 - 2 + d, c0 - 2 + lane, P);
       } else {
         uint32_t Wn = 0, Wq = 0;
 #pragma unroll
         for (int u = 0; u <= 2 * kLatK; u++) {
-          const uint2 x = sm.vs[d][col + u];
+          const uint2 x = sm.vs[d][lane + u];
           Wn += x.x;
           Wq += x.y;
         }
-        const uint32_t m = Wn >> kLatPS, S = Wn & kLatMask;
+        // A window holds 49 pixels, so m <= 49; the clamp keeps the table
+        // and the exact decision's per-count tables in bounds regardless.
+        const uint32_t m = min(Wn >> kLatPS, (uint32_t)kLatN0), S = Wn & kLatMask;
         const uint4 c = tab[m];
         const unsigned long long L = (unsigned long long)Wq * c.x;
         const bool maybe = L > (unsigned long long)S * ((S << kDec) + c.y);
@@ -686,13 +671,12 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
           sig = lat_exact((uint32_t)kLatN0 - m, S, Wq, P);
       }
       if (!sig)
-        atomicAnd(&sm.dec[d], ~(1u << col));
+        keep &= ~(1u << d);
     }
-    __syncwarp();
     uint32_t D[kVerDR];
 #pragma unroll
     for (int d = 0; d < kVerDR; d++)
-      D[d] = sm.dec[d];
+      D[d] = __ballot_sync(0xffffffffu, (keep >> d) & 1u);
     __syncwarp();  // the next tile rewrites the shared rows
     // The exact erosion of the tile's rows; the candidates that fail leave
     // both masks.
