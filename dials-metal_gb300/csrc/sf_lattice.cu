@@ -525,6 +525,23 @@ __device__ __forceinline__ void ver_stage(VerWarp &sm, int s, uint32_t e, const 
   }
 }
 
+// The packed sums of the stage-0 window of row d, column `col` of a tile
+// (seven column sums of seven rows; a window holds 49 pixels, so its masked
+// count m <= 49 -- callers clamp it anyway, which keeps the per-count tables
+// in bounds whatever the sums).
+__device__ __forceinline__ void ver_window(const VerWarp &sm, int d, int col, uint32_t *Wn,
+                                           uint32_t *Wq) {
+  uint32_t n = 0, q = 0;
+#pragma unroll
+  for (int u = 0; u <= 2 * kLatK; u++) {
+    const uint2 x = sm.vs[d][col + u];
+    n += x.x;
+    q += x.y;
+  }
+  *Wn = n;
+  *Wq = q;
+}
+
 template <int kOcc>
 __global__ void __launch_bounds__(kVerWarps * 32, kOcc)
 lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
@@ -645,33 +662,40 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
     // not signal.
     const uint32_t *image = F.image[f];
     uint32_t keep = 0xFFFFFFFFu;  // bit d: row d's window here is signal (or not needed)
-    while (rows) {
-      const int d = __ffs(rows) - 1;
-      rows &= rows - 1u;
-      bool sig;
-      if (wide) {
-        sig = lat_wide(image, height, width, r0 - 2 + d, c0 - 2 + lane, P);
-      } else {
-        uint32_t Wn = 0, Wq = 0;
-#pragma unroll
-        for (int u = 0; u <= 2 * kLatK; u++) {
-          const uint2 x = sm.vs[d][lane + u];
-          Wn += x.x;
-          Wq += x.y;
-        }
-        // A window holds 49 pixels, so m <= 49; the clamp keeps the table
-        // and the exact decision's per-count tables in bounds regardless.
+    if (wide) {
+      // 64-bit sums from the frame (rare).
+      while (rows) {
+        const int d = __ffs(rows) - 1;
+        rows &= rows - 1u;
+        if (!lat_wide(image, height, width, r0 - 2 + d, c0 - 2 + lane, P))
+          keep &= ~(1u << d);
+      }
+    } else {
+      // The two bounds first; the windows between them (rare) are decided by
+      // the reference's sequence afterwards, out of the loop.
+      uint32_t amb = 0;
+      while (rows) {
+        const int d = __ffs(rows) - 1;
+        rows &= rows - 1u;
+        uint32_t Wn, Wq;
+        ver_window(sm, d, lane, &Wn, &Wq);
         const uint32_t m = min(Wn >> kLatPS, (uint32_t)kLatN0), S = Wn & kLatMask;
         const uint4 c = tab[m];
         const unsigned long long L = (unsigned long long)Wq * c.x;
         const bool maybe = L > (unsigned long long)S * ((S << kDec) + c.y);
         const bool sure = L >= (unsigned long long)S * ((S << kDec) + c.z) + (2ull << kDec);
-        sig = sure;
-        if (maybe && !sure)
-          sig = lat_exact((uint32_t)kLatN0 - m, S, Wq, P);
+        keep &= maybe ? ~0u : ~(1u << d);
+        amb |= (maybe && !sure) ? 1u << d : 0u;
       }
-      if (!sig)
-        keep &= ~(1u << d);
+      while (amb) {
+        const int d = __ffs(amb) - 1;
+        amb &= amb - 1u;
+        uint32_t Wn, Wq;
+        ver_window(sm, d, lane, &Wn, &Wq);
+        const uint32_t m = min(Wn >> kLatPS, (uint32_t)kLatN0);
+        if (!lat_exact((uint32_t)kLatN0 - m, Wn & kLatMask, Wq, P))
+          keep &= ~(1u << d);
+      }
     }
     uint32_t D[kVerDR];
 #pragma unroll
