@@ -45,10 +45,11 @@ H, W = 4362, 4148
 
 
 # DRAM bytes (read + write) that one 16M frame of the eiger_16m workload costs
-# across the threshold's kernels, from an ncu capture of a single-frame launch
-# sequence (seg_stage01 73.6 MB, seg_stage2 15.2 MB, pass_scatter 5.2 MB, the
-# mask scans and amb_fix 8.3 MB); the algorithmic bytes are 76.5 MB.
-DRAM_BYTES_PER_FRAME = 102.3e6
+# across the threshold's kernels in a timed 16-frame launch, from an ncu
+# capture of this bench without cache flushes between kernels (2,763.9 MB for
+# the launch: lat_stage01 1,387 MB, lat_verify 532 MB, lat_stage2 656 MB, the
+# scans and the list 189 MB); the algorithmic bytes are 76.5 MB a frame.
+DRAM_BYTES_PER_FRAME = 172.7e6
 
 
 def dist_env():
@@ -535,9 +536,9 @@ def run_ours(args):
         else:
             traffic = DRAM_BYTES_PER_FRAME * B
             traffic_source = (
-                "ncu dram__bytes_read.sum + dram__bytes_write.sum over the 8 kernels of one "
-                f"single-frame launch sequence of this workload ({DRAM_BYTES_PER_FRAME / 1e6:.1f} MB),"
-                f" times the {B} frames of a launch (each frame's work is independent)")
+                "ncu dram__bytes_read.sum + dram__bytes_write.sum over the 8 kernels of a timed "
+                "16-frame launch of this workload, no cache flush between kernels "
+                f"({DRAM_BYTES_PER_FRAME / 1e6:.1f} MB a frame), times the {B} frames of a launch")
         line = {
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -557,8 +558,8 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind,
-                         "kernel": "threshold launch sequence of a batch (seg_stage01, "
-                                   "stream_wide, amb_fix, mask_sums, mask_list, seg_stage2, "
+                         "kernel": "threshold launch sequence of a batch (lat_stage01, "
+                                   "lat_tiles, lat_verify, mask_sums, mask_prefix, lat_stage2, "
                                    "pass_sums, pass_scatter) replayed as one CUDA graph, "
                                    "CUDA events around each batch",
                          "algorithmic_bytes_per_launch": algo_bytes,
