@@ -58,6 +58,34 @@ constexpr uint32_t kLatCap = 32767;         // valid pixels saturate here
 constexpr int kDec = 8;                     // fixed-point bits of clo / chi
 
 static_assert(kLatOut % 24 == 0, "lane pairs write whole bytes");
+
+// Division of 32-bit numerators by a divisor fixed for a launch (tile
+// counts), by one multiply-high and shifts: the round-up method of
+// Granlund & Montgomery, "Division by invariant integers using
+// multiplication" (PLDI 1994), with its add-and-shift step for multipliers of
+// 33 bits. Exact for every numerator and divisor below 2^32.
+struct FastDiv {
+  uint32_t d, m, s1, s2;
+};
+
+FastDiv make_fastdiv(uint32_t d) {
+  int l = 0;
+  while ((1ull << l) < d)
+    l++;
+  FastDiv f;
+  f.d = d;
+  f.m = (uint32_t)(((((unsigned long long)1 << l) - d) << 32) / d + 1);
+  f.s1 = l < 1 ? (uint32_t)l : 1u;
+  f.s2 = l > 1 ? (uint32_t)(l - 1) : 0u;
+  return f;
+}
+
+__device__ __forceinline__ uint32_t fast_div(uint32_t n, const FastDiv &f) {
+  const uint32_t t = __umulhi(n, f.m);
+  return (t + ((n - t) >> f.s1)) >> f.s2;
+}
+
+
 static_assert(kLatN0 * kLatCap < (1u << kLatPS), "saturated sums stay below the count field");
 
 // The 12 bound bits of a lane from the lattice bits b0-b4 at its columns
@@ -442,16 +470,17 @@ __device__ __noinline__ bool lat_wide(const uint32_t *__restrict__ image, int he
 // lanes' ORs.
 __global__ void __launch_bounds__(256)
 lat_tiles(int height, int width, const uint32_t *__restrict__ final_all, size_t words,
-          uint32_t *__restrict__ list, uint32_t *__restrict__ counters) {
+          uint32_t *__restrict__ list, uint32_t *__restrict__ counters, FastDiv by_ngx) {
   const int f = blockIdx.y, lane = threadIdx.x & 31;
   const uint32_t *fin = final_all + (size_t)f * words;
   const int wpr = (width + 31) >> 5, ntx = ver_ntx(width), nty = ver_nty(height);
   const int ngx = (ntx + 31) / 32;
   const uint32_t ntiles = (uint32_t)ntx * (uint32_t)nty;
-  const long long groups = (long long)nty * ngx;
-  for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < groups;
-       g += ((long long)gridDim.x * blockDim.x) >> 5) {
-    const int ty = (int)(g / ngx), gx = (int)(g - (long long)ty * ngx);
+  const uint32_t groups = (uint32_t)nty * (uint32_t)ngx;
+  for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < groups;
+       g += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t ty32 = fast_div(g, by_ngx);
+    const int ty = (int)ty32, gx = (int)(g - ty32 * (uint32_t)ngx);
     const int wd = 28 * gx + lane, r0 = ty * kVerRows;
     uint32_t acc = 0;
     if (lane < 29 && wd < wpr) {
@@ -483,11 +512,12 @@ lat_tiles(int height, int width, const uint32_t *__restrict__ final_all, size_t 
 // off the frame are written as masked pixels / zero words).
 __device__ __forceinline__ void ver_stage(VerWarp &sm, int s, uint32_t e, const FramePtrs &F,
                                           int height, int width, int vec, uint32_t ntiles,
-                                          int ntx, const uint32_t *__restrict__ final_all,
+                                          int ntx, const FastDiv &by_ntiles,
+                                          const FastDiv &by_ntx,
+                                          const uint32_t *__restrict__ final_all,
                                           size_t words, int lane) {
-  const int f = (int)(e / ntiles);
-  const uint32_t t = e - (uint32_t)f * ntiles;
-  const int ty = (int)(t / (uint32_t)ntx), tx = (int)(t - (uint32_t)ty * ntx);
+  const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
+  const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
   const int r0 = ty * kVerRows, c0 = tx * kVerTW;
   const int xs = (c0 - 5) & ~3;
   const uint32_t *image = F.image[f];
@@ -547,7 +577,8 @@ __global__ void __launch_bounds__(kVerWarps * 32, kOcc)
 lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
            const __grid_constant__ LaunchParams P, const __grid_constant__ StreamTables T,
            uint32_t *__restrict__ scr1_all, uint32_t *__restrict__ final_all, size_t words,
-           const uint32_t *__restrict__ list, uint32_t *__restrict__ counters) {
+           const uint32_t *__restrict__ list, uint32_t *__restrict__ counters, FastDiv by_ntiles,
+           FastDiv by_ntx) {
   extern __shared__ __align__(16) unsigned char ver_smem[];
   uint4 *tab = reinterpret_cast<uint4 *>(ver_smem);
   VerWarp *warps = reinterpret_cast<VerWarp *>(ver_smem + sizeof(uint4) * 64);
@@ -568,19 +599,20 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   uint32_t e = k < count ? list[k] : 0u;
   uint32_t e1 = k + nw < count ? list[k + nw] : 0u;
   if (k < count)
-    ver_stage(sm, 0, e, F, height, width, vec, ntiles, ntx, final_all, words, lane);
+    ver_stage(sm, 0, e, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, final_all,
+              words, lane);
   cp_async_commit();
   uint32_t e2 = 0u;
   for (int s = 0; k < count; k += nw, s ^= 1, e = e1, e1 = e2) {
     e2 = k + 2 * nw < count ? list[k + 2 * nw] : 0u;
     if (k + nw < count)
-      ver_stage(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, final_all, words, lane);
+      ver_stage(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx,
+                final_all, words, lane);
     cp_async_commit();
     cp_async_wait<1>();  // this tile's pieces have landed
     __syncwarp();
-    const int f = (int)(e / ntiles);
-    const uint32_t t = e - (uint32_t)f * ntiles;
-    const int ty = (int)(t / (uint32_t)ntx), tx = (int)(t - (uint32_t)ty * ntx);
+    const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
+    const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
     const int r0 = ty * kVerRows, c0 = tx * kVerTW;
     const int off = (c0 - 5) - ((c0 - 5) & ~3);
     const int w0 = c0 >> 5, sh = c0 & 31;
@@ -753,13 +785,13 @@ struct S2Warp {
 
 __device__ __forceinline__ void s2_stage(S2Warp &sm, int s, uint32_t e, const FramePtrs &F,
                                          int height, int width, int vec, uint32_t ntiles, int ntx,
+                                         const FastDiv &by_ntiles, const FastDiv &by_ntx,
                                          const uint32_t *__restrict__ scr1_all,
                                          const uint32_t *__restrict__ final_all,
                                          const uint32_t *__restrict__ prefix_all, size_t words,
                                          int lane) {
-  const int f = (int)(e / ntiles);
-  const uint32_t t = e - (uint32_t)f * ntiles;
-  const int ty = (int)(t / (uint32_t)ntx), tx = (int)(t - (uint32_t)ty * ntx);
+  const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
+  const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
   const int r0 = ty * kVerRows, c0 = tx * kVerTW;
   const int xs = (c0 - 5) & ~3;
   const uint32_t *image = F.image[f];
@@ -815,7 +847,8 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
            const __grid_constant__ LaunchParams P, const uint32_t *__restrict__ scr1_all,
            const uint32_t *__restrict__ final_all, const uint32_t *__restrict__ prefix_all,
            size_t words, const uint32_t *__restrict__ list, const uint32_t *__restrict__ counters,
-           uint32_t *__restrict__ cand_all, uint2 *__restrict__ res_all, uint32_t cand_cap) {
+           uint32_t *__restrict__ cand_all, uint2 *__restrict__ res_all, uint32_t cand_cap,
+           FastDiv by_ntiles, FastDiv by_ntx) {
   extern __shared__ __align__(16) unsigned char s2_smem[];
   S2Warp &sm = reinterpret_cast<S2Warp *>(s2_smem)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
@@ -827,21 +860,20 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   uint32_t e = k < count ? list[k] : 0u;
   uint32_t e1 = k + nw < count ? list[k + nw] : 0u;
   if (k < count)
-    s2_stage(sm, 0, e, F, height, width, vec, ntiles, ntx, scr1_all, final_all, prefix_all,
-             words, lane);
+    s2_stage(sm, 0, e, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
+             final_all, prefix_all, words, lane);
   cp_async_commit();
   uint32_t e2 = 0u;
   for (int s = 0; k < count; k += nw, s ^= 1, e = e1, e1 = e2) {
     e2 = k + 2 * nw < count ? list[k + 2 * nw] : 0u;
     if (k + nw < count)
-      s2_stage(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, scr1_all, final_all,
-               prefix_all, words, lane);
+      s2_stage(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
+               final_all, prefix_all, words, lane);
     cp_async_commit();
     cp_async_wait<1>();
     __syncwarp();
-    const int f = (int)(e / ntiles);
-    const uint32_t t = e - (uint32_t)f * ntiles;
-    const int ty = (int)(t / (uint32_t)ntx), tx = (int)(t - (uint32_t)ty * ntx);
+    const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
+    const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
     const int r0 = ty * kVerRows, c0 = tx * kVerTW;
     const int xs = (c0 - 5) & ~3, off = (c0 - 5) - xs;
     const int w0 = c0 >> 5, sh = c0 & 31;
@@ -1003,7 +1035,7 @@ cudaError_t launch_lattice_stage2(const FramePtrs &F, int nframes, int h, int w,
   const uint32_t *list = b.amb + (size_t)nframes * b.words;
   lat_stage2<kVerOcc><<<blocks * device_sms(), kVerWarps * 32, s2_smem_bytes(), stream>>>(
       F, h, w, vec, P, b.scr1, b.bits, prefix, b.words, list, b.counters, b.cand, b.res,
-      b.cand_cap);
+      b.cand_cap, make_fastdiv((uint32_t)lattice_tiles(h, w)), make_fastdiv((uint32_t)ver_ntx(w)));
   return cudaGetLastError();
 }
 
@@ -1062,9 +1094,13 @@ cudaError_t launch_lattice(const FramePtrs &F, int nframes, int h, int w, int ve
   const unsigned tb = (unsigned)std::min<long long>(
       std::max(1, 8 * device_sms() / std::max(1, nframes)), (tgroups + 7) / 8);
   uint32_t *list = b.amb + (size_t)nframes * b.words;
-  lat_tiles<<<dim3(tb, nframes), 256, 0, stream>>>(h, w, b.bits, b.words, list, b.counters);
+  const FastDiv by_ngx = make_fastdiv((uint32_t)((ver_ntx(w) + 31) / 32));
+  const FastDiv by_ntiles = make_fastdiv((uint32_t)lattice_tiles(h, w));
+  const FastDiv by_ntx = make_fastdiv((uint32_t)ver_ntx(w));
+  lat_tiles<<<dim3(tb, nframes), 256, 0, stream>>>(h, w, b.bits, b.words, list, b.counters,
+                                                   by_ngx);
   lat_verify<kVerOcc><<<ver_blocks * device_sms(), kVerWarps * 32, ver_smem_bytes(), stream>>>(
-      F, h, w, vec, P, T, b.scr1, b.bits, b.words, list, b.counters);
+      F, h, w, vec, P, T, b.scr1, b.bits, b.words, list, b.counters, by_ntiles, by_ntx);
   return cudaGetLastError();
 }
 
