@@ -152,7 +152,7 @@ static WorkspaceLayout layout(size_t h, size_t w, size_t capacity, size_t nframe
   L.cand = take(nframes * L.cand_cap * sizeof(uint32_t));
   L.res = take(nframes * L.cand_cap * sizeof(uint2));
   L.scr1 = take(nframes * L.words * sizeof(uint32_t));
-  L.amb = take(nframes * (L.words + lattice_tiles((int)h, (int)w)) * sizeof(uint32_t));
+  L.amb = take(nframes * (L.words + 2 * lattice_tiles((int)h, (int)w)) * sizeof(uint32_t));
   L.wide = take(stream_wide_entries((int)h, (int)w, (int)nframes) * 2 * sizeof(uint4));
   L.counters = take(counter_words((int)nframes) * sizeof(uint32_t));
   L.block_sums = take((size_t)std::max(kScanBlocks, stream_order_blocks()) * sizeof(uint32_t));

@@ -68,6 +68,9 @@ struct FastDiv {
   uint32_t d, m, s1, s2;
 };
 
+// Marks a tile of stage 2's list whose candidates all failed the exact check.
+constexpr uint32_t kNoTile = 0xFFFFFFFFu;
+
 FastDiv make_fastdiv(uint32_t d) {
   int l = 0;
   while ((1ull << l) < d)
@@ -464,47 +467,72 @@ __device__ __noinline__ bool lat_wide(const uint32_t *__restrict__ image, int he
   return stage0_u32(n, S, Q, P, P.root_lo, P.root_hi);
 }
 
-// One warp per 32 consecutive tiles of a tile row: 32 tiles of 28 columns
-// span 28 mask words (29 with the last tile's straddle), so lane l ORs word
-// 28 g + l over the tile row's 8 rows and each lane tests its tile from two
-// lanes' ORs.
+// Tiles of a tile row come in groups of 32 consecutive ones: 32 tiles of 28
+// columns span 28 mask words (29 with the last tile's straddle), so lane l
+// ORs word 28 g + l over the tile row's 8 rows and each lane tests its tile
+// from two lanes' ORs. A warp takes a run of kTileRun groups (of any frames),
+// keeps their ballots, and takes its list space with one atomic: the
+// counter is shared by the whole launch, so fewer atomics contend less.
+constexpr int kTileRun = 16;
+
 __global__ void __launch_bounds__(256)
-lat_tiles(int height, int width, const uint32_t *__restrict__ final_all, size_t words,
-          uint32_t *__restrict__ list, uint32_t *__restrict__ counters, FastDiv by_ngx) {
-  const int f = blockIdx.y, lane = threadIdx.x & 31;
-  const uint32_t *fin = final_all + (size_t)f * words;
+lat_tiles(int nframes, int height, int width, const uint32_t *__restrict__ final_all,
+          size_t words, uint32_t *__restrict__ list, uint32_t *__restrict__ counters,
+          FastDiv by_ngx, FastDiv by_fgroups) {
+  const int lane = threadIdx.x & 31;
   const int wpr = (width + 31) >> 5, ntx = ver_ntx(width), nty = ver_nty(height);
   const int ngx = (ntx + 31) / 32;
   const uint32_t ntiles = (uint32_t)ntx * (uint32_t)nty;
-  const uint32_t groups = (uint32_t)nty * (uint32_t)ngx;
-  for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < groups;
-       g += (gridDim.x * blockDim.x) >> 5) {
-    const uint32_t ty32 = fast_div(g, by_ngx);
-    const int ty = (int)ty32, gx = (int)(g - ty32 * (uint32_t)ngx);
-    const int wd = 28 * gx + lane, r0 = ty * kVerRows;
-    uint32_t acc = 0;
-    if (lane < 29 && wd < wpr) {
+  const uint32_t fgroups = (uint32_t)nty * (uint32_t)ngx;  // groups a frame
+  const uint32_t total = fgroups * (uint32_t)nframes;
+  const uint32_t g0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kTileRun;
+  if (g0 >= total)
+    return;  // whole warp
+  unsigned bal[kTileRun];
+  uint32_t mine = 0, n = 0;
 #pragma unroll
-      for (int o = 0; o < kVerRows; o++)
-        if (r0 + o < height)
-          acc |= fin[(size_t)(r0 + o) * wpr + wd];
+  for (int i = 0; i < kTileRun; i++) {
+    const uint32_t g = g0 + i;
+    bool any = false;
+    if (g < total) {  // warp-uniform
+      const uint32_t f = fast_div(g, by_fgroups), gf = g - f * fgroups;
+      const uint32_t ty = fast_div(gf, by_ngx), gx = gf - ty * (uint32_t)ngx;
+      const uint32_t *fin = final_all + (size_t)f * words;
+      const int wd = 28 * (int)gx + lane, r0 = (int)ty * kVerRows;
+      uint32_t acc = 0;
+      if (lane < 29 && wd < wpr) {
+#pragma unroll
+        for (int o = 0; o < kVerRows; o++)
+          if (r0 + o < height)
+            acc |= fin[(size_t)(r0 + o) * wpr + wd];
+      }
+      const int lw = (kVerTW * lane) >> 5, sh = (kVerTW * lane) & 31;
+      const uint32_t lo = __shfl_sync(0xffffffffu, acc, lw);
+      const uint32_t hi = __shfl_sync(0xffffffffu, acc, lw + 1);
+      const int tx = 32 * (int)gx + lane;
+      any = tx < ntx && ((uint32_t)(((unsigned long long)hi << 32 | lo) >> sh) &
+                         ((1u << kVerTW) - 1u)) != 0u;
     }
-    const int lw = (kVerTW * lane) >> 5, sh = (kVerTW * lane) & 31;
-    const uint32_t lo = __shfl_sync(0xffffffffu, acc, lw);
-    const uint32_t hi = __shfl_sync(0xffffffffu, acc, lw + 1);
-    const int tx = 32 * gx + lane;
-    const bool any = tx < ntx && ((uint32_t)(((unsigned long long)hi << 32 | lo) >> sh) &
-                                  ((1u << kVerTW) - 1u)) != 0u;
-    const unsigned bal = __ballot_sync(0xffffffffu, any);
-    if (bal) {
-      uint32_t base = 0;
-      if (lane == 0)
-        base = atomicAdd(counters + kCtrTiles, (uint32_t)__popc(bal));
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (any)
-        list[base + __popc(bal & ((1u << lane) - 1u))] =
-            (uint32_t)f * ntiles + (uint32_t)ty * ntx + tx;
+    bal[i] = __ballot_sync(0xffffffffu, any);
+    mine |= any ? 1u << i : 0u;
+    n += (uint32_t)__popc(bal[i]);
+  }
+  if (n == 0)
+    return;  // whole warp
+  uint32_t base = 0;
+  if (lane == 0)
+    base = atomicAdd(counters + kCtrTiles, n);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+  for (int i = 0; i < kTileRun; i++) {
+    if ((mine >> i) & 1u) {
+      const uint32_t g = g0 + i;
+      const uint32_t f = fast_div(g, by_fgroups), gf = g - f * fgroups;
+      const uint32_t ty = fast_div(gf, by_ngx), gx = gf - ty * (uint32_t)ngx;
+      list[base + __popc(bal[i] & below)] = f * ntiles + ty * (uint32_t)ntx + 32 * gx + lane;
     }
+    base += (uint32_t)__popc(bal[i]);
   }
 }
 
@@ -578,7 +606,7 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
            const __grid_constant__ LaunchParams P, const __grid_constant__ StreamTables T,
            uint32_t *__restrict__ scr1_all, uint32_t *__restrict__ final_all, size_t words,
            const uint32_t *__restrict__ list, uint32_t *__restrict__ counters, FastDiv by_ntiles,
-           FastDiv by_ntx) {
+           FastDiv by_ntx, uint32_t *__restrict__ list2) {
   extern __shared__ __align__(16) unsigned char ver_smem[];
   uint4 *tab = reinterpret_cast<uint4 *>(ver_smem);
   VerWarp *warps = reinterpret_cast<VerWarp *>(ver_smem + sizeof(uint4) * 64);
@@ -735,9 +763,10 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
       D[d] = __ballot_sync(0xffffffffu, (keep >> d) & 1u);
     __syncwarp();  // the next tile rewrites the shared rows
     // The exact erosion of the tile's rows; the candidates that fail leave
-    // both masks.
+    // both masks, and a tile with a candidate left goes on stage 2's list.
     uint32_t *scr1 = scr1_all + (size_t)f * words;
     uint32_t *fin = final_all + (size_t)f * words;
+    uint32_t left = 0;
 #pragma unroll
     for (int o = 0; o < kVerRows; o++) {
       uint32_t V = 0xFFFFFFFFu;
@@ -748,6 +777,7 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
 #pragma unroll
       for (int u = 1; u < 5; u++)
         H &= V >> u;
+      left |= cj[o] & H;
       const uint32_t clear = cj[o] & ~H;
       if (clear && lane < 2) {
         const unsigned long long c64 = (unsigned long long)clear << sh;
@@ -759,6 +789,8 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
         }
       }
     }
+    if (lane == 0)
+      list2[k] = left ? e : kNoTile;  // same place as in the tile list: no atomics
   }
   cp_async_wait<0>();
 }
@@ -854,19 +886,30 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   const int lane = threadIdx.x & 31;
   const int ntx = ver_ntx(width);
   const uint32_t ntiles = (uint32_t)ntx * (uint32_t)ver_nty(height);
+  // The exact check's tile list with the tiles left without a candidate
+  // marked kNoTile; a warp takes every nw-th entry and stages the next one it
+  // will check while it checks the current one.
   const uint32_t count = counters[kCtrTiles];
   const uint32_t nw = gridDim.x * kVerWarps;
-  uint32_t k = blockIdx.x * kVerWarps + (threadIdx.x >> 5);
-  uint32_t e = k < count ? list[k] : 0u;
-  uint32_t e1 = k + nw < count ? list[k + nw] : 0u;
+  auto next_live = [&](uint32_t from, uint32_t *at) {
+    uint32_t x = kNoTile;
+    for (; from < count; from += nw) {
+      x = list[from];
+      if (x != kNoTile)
+        break;
+    }
+    *at = from;
+    return from < count ? x : kNoTile;
+  };
+  uint32_t k, k1;
+  uint32_t e = next_live(blockIdx.x * kVerWarps + (threadIdx.x >> 5), &k);
+  uint32_t e1 = next_live(k + nw, &k1);
   if (k < count)
     s2_stage(sm, 0, e, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
              final_all, prefix_all, words, lane);
   cp_async_commit();
-  uint32_t e2 = 0u;
-  for (int s = 0; k < count; k += nw, s ^= 1, e = e1, e1 = e2) {
-    e2 = k + 2 * nw < count ? list[k + 2 * nw] : 0u;
-    if (k + nw < count)
+  for (int s = 0; k < count; s ^= 1) {
+    if (k1 < count)
       s2_stage(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
                final_all, prefix_all, words, lane);
     cp_async_commit();
@@ -890,7 +933,10 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
     const int total = incl;  // the tile's candidates (the same in every lane)
     if (total == 0) {
       __syncwarp();
-      continue;  // every candidate of the tile failed the exact check
+      k = k1;
+      e = e1;
+      e1 = next_live(k1 + nw, &k1);
+      continue;
     }
     // Background by column: A = staged column off + lane, B = off + 32 + lane
     // (needed only for candidates in the tile's last 6 columns). Valid
@@ -990,6 +1036,9 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
       }
     }
     __syncwarp();  // the next tile rewrites the shared sums
+    k = k1;
+    e = e1;
+    e1 = next_live(k1 + nw, &k1);
   }
   cp_async_wait<0>();
 }
@@ -1031,8 +1080,9 @@ cudaError_t launch_lattice_stage2(const FramePtrs &F, int nframes, int h, int w,
   });
   if (config_error != cudaSuccess)
     return config_error;
+  // The tiles the exact check left a candidate in (its second list).
   const uint32_t *prefix = b.amb;
-  const uint32_t *list = b.amb + (size_t)nframes * b.words;
+  const uint32_t *list = b.amb + (size_t)nframes * (b.words + lattice_tiles(h, w));
   lat_stage2<kVerOcc><<<blocks * device_sms(), kVerWarps * 32, s2_smem_bytes(), stream>>>(
       F, h, w, vec, P, b.scr1, b.bits, prefix, b.words, list, b.counters, b.cand, b.res,
       b.cand_cap, make_fastdiv((uint32_t)lattice_tiles(h, w)), make_fastdiv((uint32_t)ver_ntx(w)));
@@ -1088,19 +1138,21 @@ cudaError_t launch_lattice(const FramePtrs &F, int nframes, int h, int w, int ve
   if (config_error != cudaSuccess)
     return config_error;
   // The ambiguous-mask buffer of the other streaming path holds, here, the
-  // candidate mask's per-word list positions (stage 2) and then the tile
-  // list.
+  // candidate mask's per-word list positions (stage 2), the tile list and the
+  // list of tiles the exact check leaves a candidate in.
   const long long tgroups = (long long)ver_nty(h) * ((ver_ntx(w) + 31) / 32);
-  const unsigned tb = (unsigned)std::min<long long>(
-      std::max(1, 8 * device_sms() / std::max(1, nframes)), (tgroups + 7) / 8);
+  const long long twarps = (tgroups * nframes + kTileRun - 1) / kTileRun;
+  const unsigned tb = (unsigned)((twarps + 7) / 8);
   uint32_t *list = b.amb + (size_t)nframes * b.words;
   const FastDiv by_ngx = make_fastdiv((uint32_t)((ver_ntx(w) + 31) / 32));
+  const FastDiv by_fgroups = make_fastdiv((uint32_t)tgroups);
   const FastDiv by_ntiles = make_fastdiv((uint32_t)lattice_tiles(h, w));
   const FastDiv by_ntx = make_fastdiv((uint32_t)ver_ntx(w));
-  lat_tiles<<<dim3(tb, nframes), 256, 0, stream>>>(h, w, b.bits, b.words, list, b.counters,
-                                                   by_ngx);
+  lat_tiles<<<tb, 256, 0, stream>>>(nframes, h, w, b.bits, b.words, list, b.counters, by_ngx,
+                                    by_fgroups);
   lat_verify<kVerOcc><<<ver_blocks * device_sms(), kVerWarps * 32, ver_smem_bytes(), stream>>>(
-      F, h, w, vec, P, T, b.scr1, b.bits, b.words, list, b.counters, by_ntiles, by_ntx);
+      F, h, w, vec, P, T, b.scr1, b.bits, b.words, list, b.counters, by_ntiles, by_ntx,
+      list + (size_t)nframes * lattice_tiles(h, w));
   return cudaGetLastError();
 }
 

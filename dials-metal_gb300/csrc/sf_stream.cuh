@@ -40,6 +40,7 @@ struct FramePtrs {
 enum {
   kCtrWide = 0,   // batch: runs handed to the 64-bit path
   kCtrTiles = 1,  // batch: tiles listed for the exact check (kernel 3,3)
+  kCtrTiles2 = 2, // batch: tiles with a candidate left after it (stage 2's list)
   kCtrBatch = 4,  // first frame's counters
   kCtrCand = 0,   // frame: candidates (set bits of the candidate mask)
   kCtrWideFrame = 1,  // frame: a valid pixel may be too large for 32-bit stage-2 sums
@@ -101,8 +102,8 @@ struct LatticeGeometry {
 // run_rows 0 picks runs that fill the resident warps once.
 LatticeGeometry lattice_geometry(int h, int w, int nframes, int run_rows);
 // Tiles of the exact check a frame has. For kernel 3,3 StreamBuffers::amb
-// holds words + lattice_tiles words a frame: the candidate mask's per-word
-// list positions, then the tile list.
+// holds words + 2 lattice_tiles words a frame: the candidate mask's per-word
+// list positions, the tile list, and the list of tiles left for stage 2.
 size_t lattice_tiles(int h, int w);
 // Stage 2 for kernel 3,3 on the listed tiles, after launch_lattice and
 // mask_prefix into b.amb: the candidate list and the results (b.cand, b.res).
