@@ -1397,6 +1397,24 @@ static int read_store(const Labeller &L, const DeviceStore<T> &v, T *out, size_t
   return SF_OK;
 }
 
+namespace sf {
+
+size_t label_width(const sf_labeller *l) { return l ? l->impl.width : 0; }
+
+int label_gather_pixels(const sf_labeller *l, sf_pixel *d_out, cudaStream_t *stream) {
+  const Labeller &L = l->impl;
+  *stream = L.own_stream;
+  cudaError_t e = cudaStreamWaitEvent(L.own_stream, L.appended, 0);
+  if (e == cudaSuccess)
+    e = L.pixels.pieces(0, L.pixels.size(), [&](sf_pixel *src, size_t pos, size_t len) {
+      return cudaMemcpyAsync(d_out + pos, src, len * sizeof(sf_pixel), cudaMemcpyDeviceToDevice,
+                             L.own_stream);
+    });
+  return e == cudaSuccess ? SF_OK : fail(e, "gathering the spot pixels");
+}
+
+} // namespace sf
+
 extern "C" {
 
 void sf_default_label_options(sf_label_options *o) {

@@ -29,6 +29,16 @@ class LabelOptions(ctypes.Structure):
                 ("max_separation", ctypes.c_double), ("two_d", ctypes.c_int)]
 
 
+class ReflOptions(ctypes.Structure):
+    """refl::Options (src/spots/refl.hh:53-64)."""
+    _fields_ = [("panel", ctypes.c_size_t), ("id", ctypes.c_int),
+                ("identifier", ctypes.c_char_p), ("shoeboxes", ctypes.c_int)]
+
+
+def _refl_options(shoeboxes: bool, identifier: str, id: int, panel: int) -> ReflOptions:
+    return ReflOptions(panel, id, identifier.encode() if identifier else None, int(shoeboxes))
+
+
 _bound = False
 
 
@@ -55,6 +65,11 @@ def _lib():
         L.sf_label_pixels.argtypes = [vp, vp, sz]
         L.sf_label_pixels.restype = ctypes.c_int
         L.sf_label_counts.argtypes = [vp, vp]
+        L.sf_refl_write.argtypes = [ctypes.c_char_p, vp, sz, vp, sz, sz,
+                                    ctypes.POINTER(ReflOptions)]
+        L.sf_refl_write.restype = ctypes.c_int
+        L.sf_label_write_refl.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ReflOptions)]
+        L.sf_label_write_refl.restype = ctypes.c_int
         _bound = True
     return L
 
@@ -103,6 +118,14 @@ class DeviceLabeller:
     def live(self) -> int:
         return _lib().sf_label_live(self._h)
 
+    def write_refl(self, path: str, shoeboxes: bool = True, identifier: str = "",
+                   id: int = 0, panel: int = 0) -> None:
+        """refl::write of the spots so far (src/spots/refl.hh:72-74), the
+        shoebox column built on the device."""
+        o = _refl_options(shoeboxes, identifier, id, panel)
+        self._check(_lib().sf_label_write_refl(self._h, path.encode(), ctypes.byref(o)),
+                    f"writing {path}")
+
     def close(self):
         if getattr(self, "_h", None):
             _lib().sf_label_close(self._h)
@@ -125,3 +148,17 @@ def result_of(handle) -> LabelResult:
     c = np.zeros(6, np.uint64)
     L.sf_label_counts(handle, c.ctypes.data)
     return LabelResult(spots, pixels, dict(zip(COUNT_NAMES, map(int, c))))
+
+
+def write_refl(path: str, spots: np.ndarray, pixels: np.ndarray, width: int,
+               shoeboxes: bool = True, identifier: str = "", id: int = 0,
+               panel: int = 0) -> None:
+    """refl::write (src/spots/refl.hh:72-74) of host spot and pixel arrays;
+    needs no GPU."""
+    spots = np.ascontiguousarray(spots, SPOT_DTYPE)
+    pixels = np.ascontiguousarray(pixels, PIXEL_DTYPE)
+    o = _refl_options(shoeboxes, identifier, id, panel)
+    rc = _lib().sf_refl_write(path.encode(), spots.ctypes.data, len(spots), pixels.ctypes.data,
+                              len(pixels), width, ctypes.byref(o))
+    if rc != 0:
+        raise RuntimeError(f"writing {path}: {api.last_error()} ({rc})")

@@ -285,6 +285,37 @@ int sf_label_pixels(const sf_labeller *labeller, sf_pixel *out,
 void sf_label_counts(const sf_labeller *labeller, sf_counts *out);
 size_t sf_label_live(const sf_labeller *labeller);
 
+/* ---- The reflection table (src/spots/refl.hh) ---- */
+
+/* refl::Options (src/spots/refl.hh:53-64). identifier NULL or "" writes an
+ * empty identifier map. */
+typedef struct {
+  size_t panel;            /* 0 */
+  int id;                  /* 0 */
+  const char *identifier;  /* NULL */
+  int shoeboxes;           /* 1 */
+} sf_refl_options;
+
+void sf_default_refl_options(sf_refl_options *options);
+
+/* Replaces refl::write (src/spots/refl.hh:72-74, refl.cc:223-351): the DIALS
+ * .refl of spots (with their kept pixels, for the shoeboxes) in host memory,
+ * byte for byte the reference's file. Needs no GPU. -1 for no path, a zero
+ * width, spots whose pixels or boxes are not in the arrays, or a file that
+ * cannot be written (reason in sf_last_error()); -4 when the shoebox column
+ * would exceed msgpack's 4 GB binary (the reference throws for both). */
+int sf_refl_write(const char *path, const sf_spot *spots, size_t n_spots,
+                  const sf_pixel *pixels, size_t n_pixels, size_t width,
+                  const sf_refl_options *options);
+
+/* refl::write of a device labeller's spots: the same file as sf_refl_write
+ * on sf_label_spots / sf_label_pixels, with the shoebox column built in
+ * device memory from the labeller's device-resident pixels and copied out
+ * once (after the labeller's last add). No reference counterpart as an entry
+ * point: the reference writes from host vectors. -3 on a CUDA failure. */
+int sf_label_write_refl(const sf_labeller *labeller, const char *path,
+                        const sf_refl_options *options);
+
 /*
  * sf_threshold_u32_device as above, for callers that cannot allocate device
  * memory: a plugin inside a host application whose own allocator owns all

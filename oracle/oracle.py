@@ -135,6 +135,9 @@ def ref() -> ctypes.CDLL:
         R.ref_label_counts.argtypes = [vp, vp]
         R.ref_label_write_refl.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
         R.ref_label_write_refl.restype = ctypes.c_int
+        R.ref_label_write_refl_opts.argtypes = [vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_char_p, ctypes.c_size_t]
+        R.ref_label_write_refl_opts.restype = ctypes.c_int
         R.ref_label_close.argtypes = [vp]
         _ref = R
     return _ref
@@ -286,8 +289,12 @@ class RefLabeller:
         R.ref_label_counts(self._h, _ptr(c))
         return LabelResult(spots, pixels, dict(zip(COUNT_NAMES, map(int, c))))
 
-    def write_refl(self, path: str, shoeboxes: bool = True) -> None:
-        if ref().ref_label_write_refl(self._h, path.encode(), int(shoeboxes)) != 0:
+    def write_refl(self, path: str, shoeboxes: bool = True, identifier: str = "",
+                   id: int = 0, panel: int = 0) -> None:
+        """The reference's refl::write (src/spots/refl.cc:223-351) of the
+        spots so far."""
+        if ref().ref_label_write_refl_opts(self._h, path.encode(), int(shoeboxes), id,
+                                           identifier.encode(), panel) != 0:
             raise RuntimeError("reference refl::write failed")
 
     def __del__(self):

@@ -166,6 +166,23 @@ void ref_label_counts(void *handle, std::uint64_t out[6]) {
   out[5] = c.accepted;
 }
 
+int ref_label_write_refl_opts(void *handle, const char *path, int shoeboxes, int id,
+                              const char *identifier, size_t panel) {
+  RefLabeller *l = static_cast<RefLabeller *>(handle);
+  refl::Options o;
+  o.shoeboxes = shoeboxes != 0;
+  o.id = id;
+  o.identifier = identifier ? identifier : "";
+  o.panel = panel;
+  try {
+    refl::write(path, l->labeller.spots(), l->labeller.pixels(), l->width, o);
+  } catch (const std::exception &e) {
+    l->error = e.what();
+    return -1;
+  }
+  return 0;
+}
+
 int ref_label_write_refl(void *handle, const char *path, int shoeboxes) {
   RefLabeller *l = static_cast<RefLabeller *>(handle);
   refl::Options o;

@@ -19,6 +19,12 @@ Fixtures:
                           counts in 3-D and 2-D, and with frame 7 missing (a gap)
   refl_small.refl         refl::write of the 3-D spot table of sweep_small,
                           shoeboxes on (byte-exact writer fixture)
+  refl_small_opts.refl    the same table without shoeboxes, with id 3, panel 1
+                          and an experiment identifier
+  refl_small_2d.refl      refl::write of the 2-D spot table, shoeboxes on, with
+                          an identifier
+
+Only the reflection-table fixtures: python tests/golden/make_golden.py refl
 """
 import os
 import sys
@@ -31,6 +37,8 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 sys.path.insert(0, os.path.join(REPO, "dials-metal_gb300"))
 
 import oracle as O  # noqa: E402
+
+REFL_IDENTIFIER = "5b0f3c2e-9d41-4a7b-8e16-2c7d9a01f4b3"
 
 FUSED_SIZES = [(1, 1), (5, 7), (32, 32), (33, 65), (100, 37), (67, 300), (257, 511), (64, 96)]
 DEVICE_FRAMES = [("exact tile", 32, 32, 1, 12.0, False),
@@ -104,6 +112,11 @@ def sweep_small():
         out[f"counts_{tag}"] = np.array([r.counts[k] for k in O.COUNT_NAMES], np.uint64)
         if tag == "3d":
             lab.write_refl(os.path.join(HERE, "refl_small.refl"), shoeboxes=True)
+            lab.write_refl(os.path.join(HERE, "refl_small_opts.refl"), shoeboxes=False,
+                           identifier=REFL_IDENTIFIER, id=3, panel=1)
+        if tag == "2d":
+            lab.write_refl(os.path.join(HERE, "refl_small_2d.refl"), shoeboxes=True,
+                           identifier=REFL_IDENTIFIER)
     np.savez_compressed(os.path.join(HERE, "sweep_small.npz"), **out)
     return len(out["spots_3d"])
 
@@ -113,6 +126,11 @@ if __name__ == "__main__":
         O.build(quiet=False)
     if not O.ref_available():
         sys.exit("the reference library could not be built (no reference tree?)")
+    if sys.argv[1:] == ["refl"]:
+        # The reflection-table fixtures alone (sweep_small.npz rewritten with
+        # the same content).
+        print("sweep spots (3-D):", sweep_small())
+        sys.exit(0)
     print("fused cases:", fused_cases())
     print("device frames:", device_frames())
     print("sweep spots (3-D):", sweep_small())
