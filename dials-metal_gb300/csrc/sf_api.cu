@@ -171,6 +171,19 @@ static bool stream_path(size_t elem, const LaunchParams &P) {
   return elem == 4 && P.algorithm == SF_DISPERSION_EXTENDED && P.int_ok;
 }
 
+// 16-bit frames take the lattice path for kernel 3,3 (any gain and sigmas:
+// their tests are the reference's float ones) when whole 8-byte pieces of 4
+// pixels tile every row: 4 | width and 8-byte aligned frames.
+template <typename T>
+static bool stream16_path(const T *const *d_images, size_t n, size_t w, const LaunchParams &P) {
+  if (sizeof(T) != 2 || P.algorithm != SF_DISPERSION_EXTENDED || P.half != 3 || w % 4 != 0)
+    return false;
+  for (size_t j = 0; j < n; j++)
+    if (reinterpret_cast<uintptr_t>(d_images[j]) % 8 != 0)
+      return false;
+  return true;
+}
+
 // Frames d_images[0 .. n) (device pointers): lists at d_out + j * capacity,
 // masks at d_bits + j * words, counts at d_counts[j].
 template <typename T>
@@ -189,7 +202,8 @@ static int threshold_frames(const T *const *d_images, size_t n, size_t h, size_t
   int rc = make_launch_params(params, &P);
   if (rc != SF_OK)
     return rc;
-  const bool streamed = stream_path(sizeof(T), P);
+  const bool streamed16 = stream16_path(d_images, n, w, P);
+  const bool streamed = stream_path(sizeof(T), P) || streamed16;
   const WorkspaceLayout L = layout(h, w, capacity, streamed ? n : 1);
   if (ws_bytes < L.total)
     return SF_EBADARG;
@@ -216,7 +230,9 @@ static int threshold_frames(const T *const *d_images, size_t n, size_t h, size_t
     b.count_out = d_counts;
     const StreamMarks *marks = g_profiling && !t_capturing ? t_marks.arm() : nullptr;
     t_marks.staged = true;
-    cudaError_t e = launch_stream(F, (int)n, (int)h, (int)w, P, b, run_rows, stream, marks);
+    cudaError_t e =
+        streamed16 ? launch_stream16(F, (int)n, (int)h, (int)w, P, b, run_rows, stream, marks)
+                   : launch_stream(F, (int)n, (int)h, (int)w, P, b, run_rows, stream, marks);
     if (e != cudaSuccess)
       return fail(e, "launching the threshold");
     return SF_OK;

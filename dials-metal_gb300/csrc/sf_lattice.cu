@@ -130,12 +130,20 @@ __device__ __forceinline__ void lat_load(const uint32_t *__restrict__ image, int
 // as a lone count bit whose square wraps to 0, valid saturated at kLatCap),
 // the row sums of 7 columns at the lattice columns -1, 2, 5, 8, and the
 // masked bits of the lane's own 12 columns.
+// 16-bit frames (Pix = uint16_t) are summed as the reference sums them: in
+// 32 bits, the sum of squares modulo 2^32 (src/spots/dext.hh:31-33); their
+// pixels need no saturation (49 of them sum below 2^22).
+template <typename Pix>
 __device__ __forceinline__ void lat_row(const uint32_t v[16], uint32_t hn[4], uint32_t hq[4],
                                         uint32_t *m12, uint32_t *mh) {
+  constexpr bool k16 = sizeof(Pix) == 2;
   uint32_t ns[16], q[16];
 #pragma unroll
   for (int i = 0; i < 16; i++) {
-    ns[i] = v[i] >= 0xFFFFFFFEu ? (1u << kLatPS) : min(v[i], kLatCap);
+    if (k16)
+      ns[i] = v[i] >= 0xFFFEu ? (1u << kLatPS) : v[i];
+    else
+      ns[i] = v[i] >= 0xFFFFFFFEu ? (1u << kLatPS) : min(v[i], kLatCap);
     q[i] = ns[i] * ns[i];
   }
   // Triples of columns [3a - 4, 3a - 2], then the 7-column windows.
@@ -150,12 +158,13 @@ __device__ __forceinline__ void lat_row(const uint32_t v[16], uint32_t hn[4], ui
     hn[a] = gn[a] + gn[a + 1] + ns[3 * a + 6];
     hq[a] = gq[a] + gq[a + 1] + q[3 * a + 6];
   }
-  // A valid packed pixel is below 2^15, so shifting it right by 26 - c
-  // (c <= 11) leaves nothing: the shifted words add up to the masked bits.
+  // A valid packed 32-bit-frame pixel is below 2^15, so shifting it right by
+  // 26 - c (c <= 11) leaves nothing: the shifted words add up to the masked
+  // bits. A 16-bit pixel can reach 2^16, so its count bit is isolated first.
   uint32_t m = 0;
 #pragma unroll
   for (int c = 0; c < kLatCols; c++)
-    m += ns[4 + c] >> (kLatPS - c);
+    m += k16 ? (ns[4 + c] >> kLatPS) << c : ns[4 + c] >> (kLatPS - c);
   *m12 = m;
   *mh = ns[3] >> kLatPS;  // column -1, the first lattice column
 }
@@ -163,6 +172,23 @@ __device__ __forceinline__ void lat_row(const uint32_t v[16], uint32_t hn[4], ui
 __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+// One piece of 4 pixels: 16 bytes of a 32-bit frame, 8 of a 16-bit one.
+template <typename Pix> __device__ __forceinline__ void cp_async_piece(void *dst, const void *src) {
+  if (sizeof(Pix) == 4)
+    cp_async16(dst, src);
+  else
+    cp_async8(dst, src);
+}
+template <typename Pix> __device__ __forceinline__ void fill_piece_masked(void *dst) {
+  if (sizeof(Pix) == 4)
+    *reinterpret_cast<uint4 *>(dst) = make_uint4(~0u, ~0u, ~0u, ~0u);
+  else
+    *reinterpret_cast<uint2 *>(dst) = make_uint2(~0u, ~0u);
 }
 __device__ __forceinline__ void cp_async4(void *dst, const void *src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -180,18 +206,28 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
 // a row is the 95 16-byte pieces from column X - 4 (X the strip's first
 // output column) that the lanes read, 12 columns a lane apart. The other
 // variant loads each lane's 16 columns straight from the frame, a row ahead.
+//
+// A piece is 4 pixels: 16 bytes of a 32-bit frame, 8 of a 16-bit one (whose
+// rows, with 4 | width, start 8-byte aligned). Both fetch 95 pieces from
+// column X - 4, and a lane reads its 16 pixels from column 12 l of the slot.
 constexpr int kRingSlots = 4;
-constexpr int kRingPieces = 95;            // 16-byte pieces fetched a row
-constexpr int kRingStride = 388;           // words a slot: what lane 31 reads
-constexpr size_t kRingBytes = (size_t)kLatWarps * kRingSlots * kRingStride * sizeof(uint32_t);
+constexpr int kRingPieces = 95;   // pieces fetched a row
+constexpr int kRingStride = 388;  // pixels a slot: what lane 31 reads
+template <typename Pix>
+constexpr size_t ring_bytes() {
+  return (size_t)kLatWarps * kRingSlots * kRingStride * sizeof(Pix);
+}
 
-template <int kOcc, bool kRing>
+template <int kOcc, bool kRing, typename Pix>
 __global__ void __launch_bounds__(kLatWarps * 32, kOcc)
 lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int width, int vec,
             int nstrips, int nruns, int run_rows, const __grid_constant__ StreamTables T,
-            uint8_t *__restrict__ scr1_bytes, uint8_t *__restrict__ final_bytes,
-            size_t mask_bytes) {
-  extern __shared__ __align__(16) uint32_t lat_ring[];
+            const __grid_constant__ LaunchParams P, uint8_t *__restrict__ scr1_bytes,
+            uint8_t *__restrict__ final_bytes, size_t mask_bytes) {
+  constexpr bool k16 = sizeof(Pix) == 2;
+  static_assert(!k16 || kRing, "16-bit frames take the ring variant only");
+  extern __shared__ __align__(16) unsigned char lat_ring_raw[];
+  Pix *lat_ring = reinterpret_cast<Pix *>(lat_ring_raw);
   // Lower-bound constants by masked count m (window count 49 - m).
   __shared__ uint2 tab[kLatN0 + 1];
   __shared__ uint16_t lut[32];
@@ -206,7 +242,7 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
   const int ry = t0 % nruns, f = t0 / nruns;
   if (f >= nframes)
     return;  // whole warp
-  const uint32_t *image = F.image[f];
+  const Pix *image = reinterpret_cast<const Pix *>(F.image[f]);
   const int bytes_per_row = ((width + 31) >> 5) * 4;
   uint8_t *scr1 = scr1_bytes + (size_t)f * mask_bytes;
   uint8_t *fin = final_bytes + (size_t)f * mask_bytes;
@@ -233,9 +269,9 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
 
   // Pixel rows [pbeg, pend) of the run.
   const int pbeg = 3 * (ja - 2), pend = 3 * (ja + ntrip + 1);
-  uint32_t *ring = lat_ring + (size_t)warp * kRingSlots * kRingStride;
+  Pix *ring = lat_ring + (size_t)warp * kRingSlots * kRingStride;
   // The ring's pieces of this lane: l, l + 32, l + 64 (a warp's copy
-  // instruction covers 512 contiguous bytes), and whether each lies in the
+  // instruction covers 128 contiguous pixels), and whether each lies in the
   // frame.
   const int X = kLatOut * sx;
   const int x0 = X - 4 + 4 * lane;
@@ -246,22 +282,22 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
     pin[i] = pok[i] && x0 + 128 * i >= 0 && x0 + 128 * i + 4 <= width;
   }
   auto fetch = [&](int p) {
-    uint32_t *dst = ring + ((p - pbeg) % kRingSlots) * kRingStride + 4 * lane;
+    Pix *dst = ring + ((p - pbeg) % kRingSlots) * kRingStride + 4 * lane;
     const bool rowin = p >= 0 && p < height && p < pend;
-    const uint32_t *src = image + (size_t)(rowin ? p : 0) * width + x0;
+    const Pix *src = image + (size_t)(rowin ? p : 0) * width + x0;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       if (rowin && pin[i])
-        cp_async16(dst + 128 * i, src + 128 * i);
+        cp_async_piece<Pix>(dst + 128 * i, src + 128 * i);
       else if (pok[i])
-        *reinterpret_cast<uint4 *>(dst + 128 * i) = make_uint4(~0u, ~0u, ~0u, ~0u);
+        fill_piece_masked<Pix>(dst + 128 * i);
     }
   };
   if (kRing) {
-    // The words past the fetched pieces (read by lane 31 only) stay masked.
+    // The pixels past the fetched pieces (read by lane 31 only) stay masked.
     for (int i = 4 * kRingPieces + lane; i < kRingSlots * kRingStride; i += 32)
       if (i % kRingStride >= 4 * kRingPieces)
-        ring[i] = ~0u;
+        ring[i] = (Pix)~0u;
 #pragma unroll
     for (int i = 0; i < kRingSlots - 1; i++) {
       fetch(pbeg + i);
@@ -270,8 +306,8 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
   }
 
   uint32_t v[16];
-  if (!kRing)
-    lat_load(image, height, width, interior, cx, pbeg, v);
+  if constexpr (!kRing)
+    lat_load(reinterpret_cast<const uint32_t *>(image), height, width, interior, cx, pbeg, v);
   for (int t = 0; t < ntrip + 3; t++) {
     const int p0 = 3 * (ja - 2 + t);
     uint32_t Tn[4], Tq[4], mcur[3], cm = 0;
@@ -286,20 +322,30 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
         cp_async_commit();
         cp_async_wait<kRingSlots - 1>();
         __syncwarp();
-        const uint4 *src =
-            reinterpret_cast<const uint4 *>(ring + ((p - pbeg) % kRingSlots) * kRingStride) +
-            3 * lane;
+        const Pix *slot = ring + ((p - pbeg) % kRingSlots) * kRingStride;
+        if constexpr (k16) {
+          const uint2 *src = reinterpret_cast<const uint2 *>(slot + kLatCols * lane);
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-          const uint4 x = src[i];
-          v[4 * i] = x.x, v[4 * i + 1] = x.y, v[4 * i + 2] = x.z, v[4 * i + 3] = x.w;
+          for (int i = 0; i < 4; i++) {
+            const uint2 x = src[i];
+            v[4 * i] = x.x & 0xFFFFu, v[4 * i + 1] = x.x >> 16;
+            v[4 * i + 2] = x.y & 0xFFFFu, v[4 * i + 3] = x.y >> 16;
+          }
+        } else {
+          const uint4 *src = reinterpret_cast<const uint4 *>(slot) + 3 * lane;
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            const uint4 x = src[i];
+            v[4 * i] = x.x, v[4 * i + 1] = x.y, v[4 * i + 2] = x.z, v[4 * i + 3] = x.w;
+          }
         }
       } else if (k < 2 || t + 1 < ntrip + 3) {
         // The next row's loads go out before this row's arithmetic.
-        lat_load(image, height, width, interior, cx, p + 1, nxt);
+        lat_load(reinterpret_cast<const uint32_t *>(image), height, width, interior, cx,
+                 p + 1, nxt);
       }
       uint32_t hn[4], hq[4], mh;
-      lat_row(v, hn, hq, &mcur[k], &mh);
+      lat_row<Pix>(v, hn, hq, &mcur[k], &mh);
       if (!kRing) {
 #pragma unroll
         for (int i = 0; i < 16; i++)
@@ -342,12 +388,19 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
 #pragma unroll
     for (int a = 0; a < 4; a++) {
       const uint32_t W = Tn[a];
-      const uint2 c = tab[min(W >> kLatPS, (uint32_t)kLatN0)];  // 49 pixels: m <= 49
+      const uint32_t m = min(W >> kLatPS, (uint32_t)kLatN0);  // 49 pixels: m <= 49
       const uint32_t S = W & kLatMask;
-      const unsigned long long L = (unsigned long long)Tq[a] * c.x;
-      const unsigned long long R = (unsigned long long)S * ((S << kDec) + c.y);
-      const bool unc = S >= kLatCap - 1u;
-      b4 |= (L > R || unc) ? 1u << a : 0u;
+      bool sig;
+      if constexpr (k16) {
+        // The reference's float test, exactly (sf_common.cuh stage0_u16).
+        sig = stage0_u16((uint32_t)kLatN0 - m, S, Tq[a], P);
+      } else {
+        const uint2 c = tab[m];
+        const unsigned long long L = (unsigned long long)Tq[a] * c.x;
+        const unsigned long long Rr = (unsigned long long)S * ((S << kDec) + c.y);
+        sig = L > Rr || S >= kLatCap - 1u;
+      }
+      b4 |= sig ? 1u << a : 0u;
     }
     const uint32_t b5 = b4 | (__shfl_down_sync(0xffffffffu, b4, 1) & 1u) << 4;
     if (t >= 3) {
@@ -425,12 +478,26 @@ constexpr int kVerOcc = 5;                   // blocks an SM the kernel is built
 __host__ __device__ inline int ver_ntx(int w) { return (w + kVerTW - 1) / kVerTW; }
 __host__ __device__ inline int ver_nty(int h) { return (h + kVerRows - 1) / kVerRows; }
 
-struct VerWarp {
-  uint32_t pix[2][kVerPR][kVerPW];  // staged pixels, two tiles
-  uint32_t cw[2][kVerRows][2];      // the tile's candidate words, two tiles
-  uint2 vs[kVerDR][kVerPC + 2];     // column sums of 7 rows
-  uint32_t msk[kVerPC + 2];         // masked pixels by row, a word a column
+// Staged columns a pixel row (whole 16-byte pieces covering the 38 needed
+// from a piece boundary) and that boundary's alignment, in pixels.
+template <typename Pix> struct VerPix;
+template <> struct VerPix<uint32_t> {
+  static constexpr int kPW = kVerPW, kAlign = 4;
 };
+template <> struct VerPix<uint16_t> {
+  static constexpr int kPW = kVerPW, kAlign = 4;
+};
+
+template <typename Pix> struct VerWarp {
+  Pix pix[2][kVerPR][VerPix<Pix>::kPW];  // staged pixels, two tiles
+  uint32_t cw[2][kVerRows][2];           // the tile's candidate words, two tiles
+  uint2 vs[kVerDR][kVerPC + 2];          // column sums of 7 rows
+  uint32_t msk[kVerPC + 2];              // masked pixels by row, a word a column
+};
+
+template <typename Pix> __device__ __forceinline__ bool is_masked_px(uint32_t v) {
+  return sizeof(Pix) == 2 ? v >= 0xFFFEu : v >= 0xFFFFFFFEu;
+}
 
 // The reference's decision for one window from exact sums, out of line: the
 // callers reach it only between the two bounds.
@@ -538,7 +605,40 @@ lat_tiles(int nframes, int height, int width, const uint32_t *__restrict__ final
 
 // Copies listed tile e's pixels and candidate words into buffer s (pieces
 // off the frame are written as masked pixels / zero words).
-__device__ __forceinline__ void ver_stage(VerWarp &sm, int s, uint32_t e, const FramePtrs &F,
+// Copies a tile's pixel rows (r0 - 5 .. r0 + 12, the staged columns from xs)
+// into pix (pieces off the frame are written as masked pixels). 16-bit frames
+// come here only when 4 | width and they are 8-byte aligned.
+template <typename Pix>
+__device__ __forceinline__ void stage_pixels(Pix (*pix)[VerPix<Pix>::kPW], const Pix *image,
+                                             int height, int width, int vec, int r0, int xs,
+                                             int lane) {
+  constexpr int kPW = VerPix<Pix>::kPW, kPieces = kPW / 4;
+  if (sizeof(Pix) == 2 || vec) {
+    // Pieces of 4 pixels, each wholly inside the frame or wholly outside it.
+    for (int k = lane; k < kVerPR * kPieces; k += 32) {
+      const int r = k / kPieces, ch = k - r * kPieces;
+      const int y = r0 - 5 + r, x = xs + 4 * ch;
+      Pix *dst = &pix[r][4 * ch];
+      if (y >= 0 && y < height && x >= 0 && x + 4 <= width)
+        cp_async_piece<Pix>(dst, image + (size_t)y * width + x);
+      else
+        fill_piece_masked<Pix>(dst);
+    }
+  } else {
+    for (int k = lane; k < kVerPR * kPW; k += 32) {
+      const int r = k / kPW, c = k - r * kPW;
+      const int y = r0 - 5 + r, x = xs + c;
+      Pix *dst = &pix[r][c];
+      if (y >= 0 && y < height && x >= 0 && x < width)
+        cp_async4(dst, image + (size_t)y * width + x);
+      else
+        *dst = (Pix)~0u;
+    }
+  }
+}
+
+template <typename Pix>
+__device__ __forceinline__ void ver_stage(VerWarp<Pix> &sm, int s, uint32_t e, const FramePtrs &F,
                                           int height, int width, int vec, uint32_t ntiles,
                                           int ntx, const FastDiv &by_ntiles,
                                           const FastDiv &by_ntx,
@@ -547,31 +647,9 @@ __device__ __forceinline__ void ver_stage(VerWarp &sm, int s, uint32_t e, const 
   const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
   const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
   const int r0 = ty * kVerRows, c0 = tx * kVerTW;
-  const int xs = (c0 - 5) & ~3;
-  const uint32_t *image = F.image[f];
-  if (vec) {
-    // With 4 | width and a 16-byte aligned frame, every piece lies wholly
-    // inside the frame or wholly outside it.
-    for (int k = lane; k < kVerPR * (kVerPW / 4); k += 32) {
-      const int r = k / (kVerPW / 4), ch = k - r * (kVerPW / 4);
-      const int y = r0 - 5 + r, x = xs + 4 * ch;
-      uint32_t *dst = &sm.pix[s][r][4 * ch];
-      if (y >= 0 && y < height && x >= 0 && x + 4 <= width)
-        cp_async16(dst, image + (size_t)y * width + x);
-      else
-        *reinterpret_cast<uint4 *>(dst) = make_uint4(~0u, ~0u, ~0u, ~0u);
-    }
-  } else {
-    for (int k = lane; k < kVerPR * kVerPW; k += 32) {
-      const int r = k / kVerPW, c = k - r * kVerPW;
-      const int y = r0 - 5 + r, x = xs + c;
-      uint32_t *dst = &sm.pix[s][r][c];
-      if (y >= 0 && y < height && x >= 0 && x < width)
-        cp_async4(dst, image + (size_t)y * width + x);
-      else
-        *dst = ~0u;
-    }
-  }
+  const int xs = (c0 - 5) & ~(VerPix<Pix>::kAlign - 1);
+  stage_pixels<Pix>(sm.pix[s], reinterpret_cast<const Pix *>(F.image[f]), height, width, vec,
+                    r0, xs, lane);
   if (lane < 2 * kVerRows) {
     const int o = lane >> 1, wdx = (c0 >> 5) + (lane & 1);
     const int wpr = (width + 31) >> 5;
@@ -587,7 +665,8 @@ __device__ __forceinline__ void ver_stage(VerWarp &sm, int s, uint32_t e, const 
 // (seven column sums of seven rows; a window holds 49 pixels, so its masked
 // count m <= 49 -- callers clamp it anyway, which keeps the per-count tables
 // in bounds whatever the sums).
-__device__ __forceinline__ void ver_window(const VerWarp &sm, int d, int col, uint32_t *Wn,
+template <typename Pix>
+__device__ __forceinline__ void ver_window(const VerWarp<Pix> &sm, int d, int col, uint32_t *Wn,
                                            uint32_t *Wq) {
   uint32_t n = 0, q = 0;
 #pragma unroll
@@ -600,7 +679,7 @@ __device__ __forceinline__ void ver_window(const VerWarp &sm, int d, int col, ui
   *Wq = q;
 }
 
-template <int kOcc>
+template <int kOcc, typename Pix>
 __global__ void __launch_bounds__(kVerWarps * 32, kOcc)
 lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
            const __grid_constant__ LaunchParams P, const __grid_constant__ StreamTables T,
@@ -609,12 +688,13 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
            FastDiv by_ntx, uint32_t *__restrict__ list2) {
   extern __shared__ __align__(16) unsigned char ver_smem[];
   uint4 *tab = reinterpret_cast<uint4 *>(ver_smem);
-  VerWarp *warps = reinterpret_cast<VerWarp *>(ver_smem + sizeof(uint4) * 64);
+  constexpr bool k16 = sizeof(Pix) == 2;
+  VerWarp<Pix> *warps = reinterpret_cast<VerWarp<Pix> *>(ver_smem + sizeof(uint4) * 64);
   for (int m = threadIdx.x; m <= kLatN0; m += blockDim.x)
     tab[m] = make_uint4(T.nk[kLatN0 - m], T.clo[kLatN0 - m], T.chi[kLatN0 - m], 0u);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  VerWarp &sm = warps[warp];
+  VerWarp<Pix> &sm = warps[warp];
   const int wpr = (width + 31) >> 5;
   const int ntx = ver_ntx(width);
   const uint32_t ntiles = (uint32_t)ntx * (uint32_t)ver_nty(height);
@@ -627,22 +707,22 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   uint32_t e = k < count ? list[k] : 0u;
   uint32_t e1 = k + nw < count ? list[k + nw] : 0u;
   if (k < count)
-    ver_stage(sm, 0, e, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, final_all,
-              words, lane);
+    ver_stage<Pix>(sm, 0, e, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, final_all,
+                   words, lane);
   cp_async_commit();
   uint32_t e2 = 0u;
   for (int s = 0; k < count; k += nw, s ^= 1, e = e1, e1 = e2) {
     e2 = k + 2 * nw < count ? list[k + 2 * nw] : 0u;
     if (k + nw < count)
-      ver_stage(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx,
-                final_all, words, lane);
+      ver_stage<Pix>(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx,
+                     final_all, words, lane);
     cp_async_commit();
     cp_async_wait<1>();  // this tile's pieces have landed
     __syncwarp();
     const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
     const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
     const int r0 = ty * kVerRows, c0 = tx * kVerTW;
-    const int off = (c0 - 5) - ((c0 - 5) & ~3);
+    const int off = (c0 - 5) - ((c0 - 5) & ~(VerPix<Pix>::kAlign - 1));
     const int w0 = c0 >> 5, sh = c0 & 31;
     uint32_t cj[kVerRows];
 #pragma unroll
@@ -674,8 +754,9 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
 #pragma unroll
       for (int r = 0; r < kVerPR; r++) {
         const uint32_t v = sm.pix[s][r][col];
-        const bool masked = v >= 0xFFFFFFFEu;
-        mx = max(mx, v + 2u);
+        const bool masked = is_masked_px<Pix>(v);
+        if (!k16)
+          mx = max(mx, v + 2u);
         mk |= (masked ? 1u : 0u) << r;
         ns[r] = masked ? (1u << kLatPS) : v;
         q[r] = ns[r] * ns[r];
@@ -697,7 +778,8 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
       }
     }
     __syncwarp();
-    const bool wide = __any_sync(0xffffffffu, mx >= narrow2);
+    // 16-bit frames sum in 32 bits as the reference does: never wide.
+    const bool wide = !k16 && __any_sync(0xffffffffu, mx >= narrow2);
     if (wide && lane == 0)
       counters[kCtrBatch + (size_t)f * kCtrCount + kCtrWideFrame] = 1u;
     // The stage-0 positions within 2 of a candidate: lane d first forms row
@@ -722,7 +804,18 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
     // not signal.
     const uint32_t *image = F.image[f];
     uint32_t keep = 0xFFFFFFFFu;  // bit d: row d's window here is signal (or not needed)
-    if (wide) {
+    if constexpr (k16) {
+      // The reference's float test of every needed window, exactly.
+      while (rows) {
+        const int d = __ffs(rows) - 1;
+        rows &= rows - 1u;
+        uint32_t Wn, Wq;
+        ver_window(sm, d, lane, &Wn, &Wq);
+        const uint32_t m = min(Wn >> kLatPS, (uint32_t)kLatN0);
+        if (!stage0_u16((uint32_t)kLatN0 - m, Wn & kLatMask, Wq, P))
+          keep &= ~(1u << d);
+      }
+    } else if (wide) {
       // 64-bit sums from the frame (rare).
       while (rows) {
         const int d = __ffs(rows) - 1;
@@ -807,15 +900,16 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
 // positions of the candidate mask (mask_prefix); the mask itself is left as
 // it is until every position is taken (pass_sums clears the failures).
 // ---------------------------------------------------------------------------
-struct S2Warp {
-  uint32_t pix[2][kVerPR][kVerPW];  // staged pixels, two tiles
+template <typename Pix> struct S2Warp {
+  Pix pix[2][kVerPR][VerPix<Pix>::kPW];  // staged pixels, two tiles
   uint32_t ew[2][kVerPR][3];        // eroded-mask words over the staged columns
   uint32_t cw[2][kVerRows][2];      // candidate-mask words of the tile's rows
   uint32_t pw[2][kVerRows][2];      // their list positions
   uint2 cs[kVerRows][kVerPC + 2];   // {count, sum} of 11 rows of background
 };
 
-__device__ __forceinline__ void s2_stage(S2Warp &sm, int s, uint32_t e, const FramePtrs &F,
+template <typename Pix>
+__device__ __forceinline__ void s2_stage(S2Warp<Pix> &sm, int s, uint32_t e, const FramePtrs &F,
                                          int height, int width, int vec, uint32_t ntiles, int ntx,
                                          const FastDiv &by_ntiles, const FastDiv &by_ntx,
                                          const uint32_t *__restrict__ scr1_all,
@@ -825,29 +919,9 @@ __device__ __forceinline__ void s2_stage(S2Warp &sm, int s, uint32_t e, const Fr
   const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
   const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
   const int r0 = ty * kVerRows, c0 = tx * kVerTW;
-  const int xs = (c0 - 5) & ~3;
-  const uint32_t *image = F.image[f];
-  if (vec) {
-    for (int k = lane; k < kVerPR * (kVerPW / 4); k += 32) {
-      const int r = k / (kVerPW / 4), ch = k - r * (kVerPW / 4);
-      const int y = r0 - 5 + r, x = xs + 4 * ch;
-      uint32_t *dst = &sm.pix[s][r][4 * ch];
-      if (y >= 0 && y < height && x >= 0 && x + 4 <= width)
-        cp_async16(dst, image + (size_t)y * width + x);
-      else
-        *reinterpret_cast<uint4 *>(dst) = make_uint4(~0u, ~0u, ~0u, ~0u);
-    }
-  } else {
-    for (int k = lane; k < kVerPR * kVerPW; k += 32) {
-      const int r = k / kVerPW, c = k - r * kVerPW;
-      const int y = r0 - 5 + r, x = xs + c;
-      uint32_t *dst = &sm.pix[s][r][c];
-      if (y >= 0 && y < height && x >= 0 && x < width)
-        cp_async4(dst, image + (size_t)y * width + x);
-      else
-        *dst = ~0u;
-    }
-  }
+  const int xs = (c0 - 5) & ~(VerPix<Pix>::kAlign - 1);
+  stage_pixels<Pix>(sm.pix[s], reinterpret_cast<const Pix *>(F.image[f]), height, width, vec,
+                    r0, xs, lane);
   const int wpr = (width + 31) >> 5;
   const uint32_t *scr1 = scr1_all + (size_t)f * words;
   for (int k = lane; k < kVerPR * 3; k += 32) {
@@ -873,7 +947,7 @@ __device__ __forceinline__ void s2_stage(S2Warp &sm, int s, uint32_t e, const Fr
   }
 }
 
-template <int kOcc>
+template <int kOcc, typename Pix>
 __global__ void __launch_bounds__(kVerWarps * 32, kOcc)
 lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
            const __grid_constant__ LaunchParams P, const uint32_t *__restrict__ scr1_all,
@@ -882,7 +956,8 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
            uint32_t *__restrict__ cand_all, uint2 *__restrict__ res_all, uint32_t cand_cap,
            FastDiv by_ntiles, FastDiv by_ntx) {
   extern __shared__ __align__(16) unsigned char s2_smem[];
-  S2Warp &sm = reinterpret_cast<S2Warp *>(s2_smem)[threadIdx.x >> 5];
+  constexpr bool k16 = sizeof(Pix) == 2;
+  S2Warp<Pix> &sm = reinterpret_cast<S2Warp<Pix> *>(s2_smem)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   const int ntx = ver_ntx(width);
   const uint32_t ntiles = (uint32_t)ntx * (uint32_t)ver_nty(height);
@@ -905,20 +980,20 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   uint32_t e = next_live(blockIdx.x * kVerWarps + (threadIdx.x >> 5), &k);
   uint32_t e1 = next_live(k + nw, &k1);
   if (k < count)
-    s2_stage(sm, 0, e, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
-             final_all, prefix_all, words, lane);
+    s2_stage<Pix>(sm, 0, e, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
+                  final_all, prefix_all, words, lane);
   cp_async_commit();
   for (int s = 0; k < count; s ^= 1) {
     if (k1 < count)
-      s2_stage(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
-               final_all, prefix_all, words, lane);
+      s2_stage<Pix>(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx,
+                    scr1_all, final_all, prefix_all, words, lane);
     cp_async_commit();
     cp_async_wait<1>();
     __syncwarp();
     const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
     const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
     const int r0 = ty * kVerRows, c0 = tx * kVerTW;
-    const int xs = (c0 - 5) & ~3, off = (c0 - 5) - xs;
+    const int xs = (c0 - 5) & ~(VerPix<Pix>::kAlign - 1), off = (c0 - 5) - xs;
     const int w0 = c0 >> 5, sh = c0 & 31;
     uint32_t cj[kVerRows], late = 0;
     int incl = 0;
@@ -957,8 +1032,9 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
       for (int r = 0; r < kVerPR; r++) {
         const uint32_t v = sm.pix[s][r][j];
         const bool eroded = (sm.ew[s][r][wi] >> b) & 1u;
-        const bool bg = v < 0xFFFFFFFEu && !eroded;
-        mx = max(mx, v + 2u);
+        const bool bg = !is_masked_px<Pix>(v) && !eroded;
+        if (!k16)
+          mx = max(mx, v + 2u);
         bn[r] = bg ? 1u : 0u;
         bs[r] = bg ? v : 0u;
       }
@@ -977,7 +1053,8 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
         cs -= bs[o];
       }
     }
-    const bool wide = __any_sync(0xffffffffu, mx >= (1u << 24) + 2u);
+    // 121 16-bit pixels sum below 2^23: 16-bit frames are never wide.
+    const bool wide = !k16 && __any_sync(0xffffffffu, mx >= (1u << 24) + 2u);
     __syncwarp();
     // The tile's candidates, spread over the lanes in order.
     int pre[kVerRows];
@@ -1018,7 +1095,7 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
             const int j = off + tcol + u, x = xs + j;
             const uint32_t v = sm.pix[s][r][j];
             const bool eroded = (sm.ew[s][r][(x >> 5) - (xs >> 5)] >> (x & 31)) & 1u;
-            if (v < 0xFFFFFFFEu && !eroded) {
+            if (!is_masked_px<Pix>(v) && !eroded) {
               n++;
               S += v;
             }
@@ -1027,7 +1104,13 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
       const uint32_t p = sm.pix[s][o + 5][off + tcol + 5];
       float bg = 0.0f;
       // dext.cc:205: only pixels above the global threshold are tested.
-      const bool sig = (uint64_t)p >= P.p_min && stage2_u32(p, n, S, P, &bg);
+      bool sig = (uint64_t)p >= P.p_min;
+      if (sig) {
+        if constexpr (k16)
+          sig = stage2_u16(p, n, (uint32_t)S, P, &bg);  // the reference's float test
+        else
+          sig = stage2_u32(p, n, S, P, &bg);
+      }
       const int x = c0 + tcol, jw = (x >> 5) - w0, bit = x & 31;
       const uint32_t i = sm.pw[s][o][jw] + (uint32_t)__popc(sm.cw[s][o][jw] & ((1u << bit) - 1u));
       if (i < cand_cap) {
@@ -1043,19 +1126,101 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   cp_async_wait<0>();
 }
 
-constexpr size_t s2_smem_bytes() { return sizeof(S2Warp) * kVerWarps; }
+template <typename Pix> constexpr size_t s2_smem_bytes() {
+  return sizeof(S2Warp<Pix>) * kVerWarps;
+}
 
-constexpr size_t ver_smem_bytes() { return sizeof(uint4) * 64 + sizeof(VerWarp) * kVerWarps; }
+template <typename Pix> constexpr size_t ver_smem_bytes() {
+  return sizeof(uint4) * 64 + sizeof(VerWarp<Pix>) * kVerWarps;
+}
 
 int lat_slots() {
   static int slots = 0;
   if (!slots) {
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lat_stage01<kLatOcc, true>,
-                                                  kLatWarps * 32, kRingBytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lat_stage01<kLatOcc, true, uint32_t>,
+                                                  kLatWarps * 32, ring_bytes<uint32_t>());
     slots = std::max(1, per) * kLatWarps * device_sms();
   }
   return slots;
+}
+
+// Blocks an SM of a persistent kernel with `bytes` of dynamic shared memory,
+// once per instantiation (the attribute set first).
+template <class Kernel> cudaError_t persistent_blocks(Kernel k, size_t bytes, int *blocks) {
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  int per = 0;
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, kVerWarps * 32, bytes);
+  *blocks = std::max(1, per);
+  return e;
+}
+
+template <typename Pix>
+cudaError_t lattice_stage2(const FramePtrs &F, int nframes, int h, int w, int vec,
+                           const LaunchParams &P, const StreamBuffers &b, cudaStream_t stream) {
+  static std::once_flag configured;
+  static cudaError_t config_error = cudaSuccess;
+  static int blocks = 0;
+  std::call_once(configured, [] {
+    config_error = persistent_blocks(lat_stage2<kVerOcc, Pix>, s2_smem_bytes<Pix>(), &blocks);
+  });
+  if (config_error != cudaSuccess)
+    return config_error;
+  // The tiles the exact check left a candidate in (its second list).
+  const uint32_t *prefix = b.amb;
+  const size_t tiles = (size_t)ver_ntx(w) * (size_t)ver_nty(h);
+  const uint32_t *list = b.amb + (size_t)nframes * (b.words + tiles);
+  lat_stage2<kVerOcc, Pix><<<blocks * device_sms(), kVerWarps * 32, s2_smem_bytes<Pix>(),
+                             stream>>>(F, h, w, vec, P, b.scr1, b.bits, prefix, b.words, list,
+                                       b.counters, b.cand, b.res, b.cand_cap,
+                                       make_fastdiv((uint32_t)tiles),
+                                       make_fastdiv((uint32_t)ver_ntx(w)));
+  return cudaGetLastError();
+}
+
+template <typename Pix>
+cudaError_t lattice(const FramePtrs &F, int nframes, int h, int w, int vec, const LaunchParams &P,
+                    const StreamTables &T, const StreamBuffers &b, const LatticeGeometry &g,
+                    cudaStream_t stream) {
+  const long long warps = (long long)nframes * g.nstrips * g.nruns;
+  const size_t mask_bytes = b.words * sizeof(uint32_t);
+  const unsigned lb = (unsigned)((warps + kLatWarps - 1) / kLatWarps);
+  uint8_t *scr1 = reinterpret_cast<uint8_t *>(b.scr1), *fin = reinterpret_cast<uint8_t *>(b.bits);
+  if (sizeof(Pix) == 2 || vec)
+    lat_stage01<kLatOcc, true, Pix><<<lb, kLatWarps * 32, ring_bytes<Pix>(), stream>>>(
+        F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, T, P, scr1, fin, mask_bytes);
+  else
+    lat_stage01<kLatOcc, false, uint32_t><<<lb, kLatWarps * 32, 0, stream>>>(
+        F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, T, P, scr1, fin, mask_bytes);
+  static std::once_flag configured;
+  static cudaError_t config_error = cudaSuccess;
+  static int ver_blocks = 0;
+  std::call_once(configured, [] {
+    config_error = persistent_blocks(lat_verify<kVerOcc, Pix>, ver_smem_bytes<Pix>(),
+                                     &ver_blocks);
+  });
+  if (config_error != cudaSuccess)
+    return config_error;
+  // The ambiguous-mask buffer of the other streaming path holds, here, the
+  // candidate mask's per-word list positions (stage 2), the tile list and the
+  // list of tiles the exact check leaves a candidate in.
+  const long long tgroups = (long long)ver_nty(h) * ((ver_ntx(w) + 31) / 32);
+  const long long twarps = (tgroups * nframes + kTileRun - 1) / kTileRun;
+  const unsigned tb = (unsigned)((twarps + 7) / 8);
+  const size_t tiles = (size_t)ver_ntx(w) * (size_t)ver_nty(h);
+  uint32_t *list = b.amb + (size_t)nframes * b.words;
+  const FastDiv by_ngx = make_fastdiv((uint32_t)((ver_ntx(w) + 31) / 32));
+  const FastDiv by_fgroups = make_fastdiv((uint32_t)tgroups);
+  const FastDiv by_ntiles = make_fastdiv((uint32_t)tiles);
+  const FastDiv by_ntx = make_fastdiv((uint32_t)ver_ntx(w));
+  lat_tiles<<<tb, 256, 0, stream>>>(nframes, h, w, b.bits, b.words, list, b.counters, by_ngx,
+                                    by_fgroups);
+  lat_verify<kVerOcc, Pix><<<ver_blocks * device_sms(), kVerWarps * 32, ver_smem_bytes<Pix>(),
+                             stream>>>(F, h, w, vec, P, T, b.scr1, b.bits, b.words, list,
+                                       b.counters, by_ntiles, by_ntx,
+                                       list + (size_t)nframes * tiles);
+  return cudaGetLastError();
 }
 
 } // namespace
@@ -1063,30 +1228,10 @@ int lat_slots() {
 size_t lattice_tiles(int h, int w) { return (size_t)ver_ntx(w) * (size_t)ver_nty(h); }
 
 cudaError_t launch_lattice_stage2(const FramePtrs &F, int nframes, int h, int w, int vec,
-                                  const LaunchParams &P, const StreamBuffers &b,
+                                  int pixel_bytes, const LaunchParams &P, const StreamBuffers &b,
                                   cudaStream_t stream) {
-  static std::once_flag configured;
-  static cudaError_t config_error = cudaSuccess;
-  static int blocks = 0;
-  std::call_once(configured, [] {
-    config_error = cudaFuncSetAttribute(lat_stage2<kVerOcc>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)s2_smem_bytes());
-    int per = 0;
-    if (config_error == cudaSuccess)
-      config_error = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &per, lat_stage2<kVerOcc>, kVerWarps * 32, s2_smem_bytes());
-    blocks = std::max(1, per);
-  });
-  if (config_error != cudaSuccess)
-    return config_error;
-  // The tiles the exact check left a candidate in (its second list).
-  const uint32_t *prefix = b.amb;
-  const uint32_t *list = b.amb + (size_t)nframes * (b.words + lattice_tiles(h, w));
-  lat_stage2<kVerOcc><<<blocks * device_sms(), kVerWarps * 32, s2_smem_bytes(), stream>>>(
-      F, h, w, vec, P, b.scr1, b.bits, prefix, b.words, list, b.counters, b.cand, b.res,
-      b.cand_cap, make_fastdiv((uint32_t)lattice_tiles(h, w)), make_fastdiv((uint32_t)ver_ntx(w)));
-  return cudaGetLastError();
+  return pixel_bytes == 2 ? lattice_stage2<uint16_t>(F, nframes, h, w, vec, P, b, stream)
+                          : lattice_stage2<uint32_t>(F, nframes, h, w, vec, P, b, stream);
 }
 
 LatticeGeometry lattice_geometry(int h, int w, int nframes, int run_rows) {
@@ -1106,54 +1251,13 @@ LatticeGeometry lattice_geometry(int h, int w, int nframes, int run_rows) {
 }
 
 cudaError_t launch_lattice(const FramePtrs &F, int nframes, int h, int w, int vec,
-                           const LaunchParams &P, const StreamTables &T, const StreamBuffers &b,
-                           int run_rows, cudaStream_t stream) {
+                           int pixel_bytes, const LaunchParams &P, const StreamTables &T,
+                           const StreamBuffers &b, int run_rows, cudaStream_t stream) {
   if (P.half != kLatK)
     return cudaErrorInvalidValue;
   const LatticeGeometry g = lattice_geometry(h, w, nframes, run_rows);
-  const long long warps = (long long)nframes * g.nstrips * g.nruns;
-  const size_t mask_bytes = b.words * sizeof(uint32_t);
-  const unsigned lb = (unsigned)((warps + kLatWarps - 1) / kLatWarps);
-  if (vec)
-    lat_stage01<kLatOcc, true><<<lb, kLatWarps * 32, kRingBytes, stream>>>(
-        F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, T,
-        reinterpret_cast<uint8_t *>(b.scr1), reinterpret_cast<uint8_t *>(b.bits), mask_bytes);
-  else
-    lat_stage01<kLatOcc, false><<<lb, kLatWarps * 32, 0, stream>>>(
-        F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, T,
-        reinterpret_cast<uint8_t *>(b.scr1), reinterpret_cast<uint8_t *>(b.bits), mask_bytes);
-  static std::once_flag configured;
-  static cudaError_t config_error = cudaSuccess;
-  static int ver_blocks = 0;
-  std::call_once(configured, [] {
-    config_error = cudaFuncSetAttribute(lat_verify<kVerOcc>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)ver_smem_bytes());
-    int per = 0;
-    if (config_error == cudaSuccess)
-      config_error = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &per, lat_verify<kVerOcc>, kVerWarps * 32, ver_smem_bytes());
-    ver_blocks = std::max(1, per);
-  });
-  if (config_error != cudaSuccess)
-    return config_error;
-  // The ambiguous-mask buffer of the other streaming path holds, here, the
-  // candidate mask's per-word list positions (stage 2), the tile list and the
-  // list of tiles the exact check leaves a candidate in.
-  const long long tgroups = (long long)ver_nty(h) * ((ver_ntx(w) + 31) / 32);
-  const long long twarps = (tgroups * nframes + kTileRun - 1) / kTileRun;
-  const unsigned tb = (unsigned)((twarps + 7) / 8);
-  uint32_t *list = b.amb + (size_t)nframes * b.words;
-  const FastDiv by_ngx = make_fastdiv((uint32_t)((ver_ntx(w) + 31) / 32));
-  const FastDiv by_fgroups = make_fastdiv((uint32_t)tgroups);
-  const FastDiv by_ntiles = make_fastdiv((uint32_t)lattice_tiles(h, w));
-  const FastDiv by_ntx = make_fastdiv((uint32_t)ver_ntx(w));
-  lat_tiles<<<tb, 256, 0, stream>>>(nframes, h, w, b.bits, b.words, list, b.counters, by_ngx,
-                                    by_fgroups);
-  lat_verify<kVerOcc><<<ver_blocks * device_sms(), kVerWarps * 32, ver_smem_bytes(), stream>>>(
-      F, h, w, vec, P, T, b.scr1, b.bits, b.words, list, b.counters, by_ntiles, by_ntx,
-      list + (size_t)nframes * lattice_tiles(h, w));
-  return cudaGetLastError();
+  return pixel_bytes == 2 ? lattice<uint16_t>(F, nframes, h, w, vec, P, T, b, g, stream)
+                          : lattice<uint32_t>(F, nframes, h, w, vec, P, T, b, g, stream);
 }
 
 } // namespace sf

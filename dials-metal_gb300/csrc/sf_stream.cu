@@ -867,6 +867,7 @@ pass_sums(const uint2 *__restrict__ res_all, uint32_t cand_cap,
   }, block_sums);
 }
 
+template <typename Pix>
 __global__ void __launch_bounds__(kScanT)
 pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ cand_all,
              uint32_t cand_cap, const uint2 *__restrict__ res_all,
@@ -874,7 +875,7 @@ pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ c
              sf_signal_pixel *__restrict__ out_all, size_t out_stride, uint32_t capacity,
              uint32_t *__restrict__ count_out) {
   const int f = blockIdx.y;
-  const uint32_t *image = F.image[f];
+  const Pix *image = reinterpret_cast<const Pix *>(F.image[f]);
   const uint32_t *cand = cand_all + (size_t)f * cand_cap;
   const uint2 *res = res_all + (size_t)f * cand_cap;
   sf_signal_pixel *out = out_all + (size_t)f * out_stride;
@@ -897,7 +898,7 @@ pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ c
         const uint32_t idx = cand[i];
         sf_signal_pixel rec;
         rec.index = idx;
-        rec.value = __ldg(image + idx);
+        rec.value = (uint32_t)__ldg(image + idx);
         rec.background = __uint_as_float(r.x);
         rec.population = (uint16_t)(r.y & 0xFFFFu);
         rec.reserved = 0;
@@ -1049,7 +1050,7 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
   const int sms = device_sms();
   if (K == 3) {
     // The reference's window: the lattice bound and its exact check.
-    const cudaError_t e = launch_lattice(F, nframes, h, w, vec, P, T, b, run_rows, stream);
+    const cudaError_t e = launch_lattice(F, nframes, h, w, vec, 4, P, T, b, run_rows, stream);
     if (e != cudaSuccess)
       return e;
   } else {
@@ -1074,7 +1075,7 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
   if (K == 3) {
     // Stage 2 on the exact check's tiles, into the list positions.
     mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.amb, b.counters);
-    const cudaError_t e = launch_lattice_stage2(F, nframes, h, w, vec, P, b, stream);
+    const cudaError_t e = launch_lattice_stage2(F, nframes, h, w, vec, 4, P, b, stream);
     if (e != cudaSuccess)
       return e;
   } else {
@@ -1089,8 +1090,48 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
     cudaEventRecord(marks->stage2, stream);
   pass_sums<<<og, kScanT, 0, stream>>>(b.res, b.cand_cap, b.counters, b.block_sums, b.cand,
                                        K == 3 ? b.bits : nullptr, b.words, w);
-  pass_scatter<<<og, kScanT, 0, stream>>>(F, b.cand, b.cand_cap, b.res, b.counters, b.block_sums,
-                                          b.out, b.out_stride, b.capacity, b.count_out);
+  pass_scatter<uint32_t><<<og, kScanT, 0, stream>>>(F, b.cand, b.cand_cap, b.res, b.counters,
+                                                    b.block_sums, b.out, b.out_stride, b.capacity,
+                                                    b.count_out);
+  if (b.prefix) {
+    mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
+    mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.prefix, nullptr);
+  }
+  if (marks)
+    cudaEventRecord(marks->order, stream);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stream16(const FramePtrs &F, int nframes, int h, int w, const LaunchParams &P,
+                            const StreamBuffers &b, int run_rows, cudaStream_t stream,
+                            const StreamMarks *marks) {
+  if (nframes < 1 || nframes > kMaxBatch || P.half != 3 ||
+      P.algorithm != SF_DISPERSION_EXTENDED || w % 4 != 0)
+    return cudaErrorInvalidValue;
+  if (marks)
+    cudaEventRecord(marks->start, stream);
+  cudaError_t e =
+      cudaMemsetAsync(b.counters, 0, counter_words(nframes) * sizeof(uint32_t), stream);
+  if (e != cudaSuccess)
+    return e;
+  StreamTables T;
+  make_stream_tables(P, &T);
+  if ((e = launch_lattice(F, nframes, h, w, 1, 2, P, T, b, run_rows, stream)) != cudaSuccess)
+    return e;
+  if (marks)
+    cudaEventRecord(marks->stage01, stream);
+  const dim3 og((unsigned)order_bpf(nframes, b.words), (unsigned)nframes);
+  mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
+  mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.amb, b.counters);
+  if ((e = launch_lattice_stage2(F, nframes, h, w, 1, 2, P, b, stream)) != cudaSuccess)
+    return e;
+  if (marks)
+    cudaEventRecord(marks->stage2, stream);
+  pass_sums<<<og, kScanT, 0, stream>>>(b.res, b.cand_cap, b.counters, b.block_sums, b.cand,
+                                       b.bits, b.words, w);
+  pass_scatter<uint16_t><<<og, kScanT, 0, stream>>>(F, b.cand, b.cand_cap, b.res, b.counters,
+                                                    b.block_sums, b.out, b.out_stride, b.capacity,
+                                                    b.count_out);
   if (b.prefix) {
     mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
     mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.prefix, nullptr);

@@ -108,14 +108,22 @@ size_t lattice_tiles(int h, int w);
 // Stage 2 for kernel 3,3 on the listed tiles, after launch_lattice and
 // mask_prefix into b.amb: the candidate list and the results (b.cand, b.res).
 cudaError_t launch_lattice_stage2(const FramePtrs &frames, int nframes, int h, int w, int vec,
-                                  const LaunchParams &P, const StreamBuffers &b,
+                                  int pixel_bytes, const LaunchParams &P, const StreamBuffers &b,
                                   cudaStream_t stream);
 // Stage 0 and the erosion for kernel 3,3: the lattice bound, then the exact
 // check of its candidates; writes b.scr1 and b.bits as the first pass of
 // launch_stream does (vec: the frames allow 16-byte loads).
+// pixel_bytes 4 (32-bit frames) or 2 (16-bit frames: 4 | w, 8-byte aligned).
 cudaError_t launch_lattice(const FramePtrs &frames, int nframes, int h, int w, int vec,
-                           const LaunchParams &P, const StreamTables &T, const StreamBuffers &b,
-                           int run_rows, cudaStream_t stream);
+                           int pixel_bytes, const LaunchParams &P, const StreamTables &T,
+                           const StreamBuffers &b, int run_rows, cudaStream_t stream);
+
+// 16-bit frames, kernel 3,3, dispersion_extended (any gain and sigmas; the
+// tests are the reference's float ones): the lattice path of launch_stream.
+// The frames' width must be a multiple of 4 and each frame 8-byte aligned.
+cudaError_t launch_stream16(const FramePtrs &frames, int nframes, int h, int w,
+                            const LaunchParams &P, const StreamBuffers &b, int run_rows,
+                            cudaStream_t stream, const StreamMarks *marks = nullptr);
 
 // run_rows 0: the default geometry. marks may be null.
 cudaError_t launch_stream(const FramePtrs &frames, int nframes, int h, int w,

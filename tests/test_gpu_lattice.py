@@ -3,7 +3,9 @@ of every third row and column, the erosion bound that follows, the exact check
 on listed 8 x 28 tiles and stage 2 on the same tiles. Each frame is built to
 stress one part (masked pixels on lattice points, bands at every phase, strip
 and tile boundaries, spots in a tile's last columns, saturated and 64-bit
-pixels) and must give the oracle's list and mask bit for bit."""
+pixels) and must give the oracle's list and mask bit for bit. Frames whose
+width is a multiple of 8 also run as 16-bit frames, whose tests are the
+reference's float ones (src/spots/dext.hh:31-33)."""
 import numpy as np
 import pytest
 
@@ -44,16 +46,31 @@ def _blob(f, y, x, peak, sigma=1.2):
     f[ys, xs] = np.minimum(sub, 0xFFFFFFFD).astype(np.uint32)
 
 
-def _check_batch(api, frames, what):
+def _as_u16(f):
+    """The frame as 16-bit pixels: valid values clamped below the masked
+    sentinels, the sentinels kept."""
+    g = np.minimum(f, 0xFFFD).astype(np.uint16)
+    g[f == 0xFFFFFFFE] = 0xFFFE
+    g[f == 0xFFFFFFFF] = 0xFFFF
+    return g
+
+
+def _check_batch(api, frames, what, params=None, also16=True):
     import torch
     h, w = frames[0].shape
-    b = api.DeviceBatch(h, w, len(frames), capacity=h * w, word_prefix=True)
-    b([torch.from_numpy(f.view(np.int32)).cuda() for f in frames])
-    torch.cuda.synchronize()
-    for j, f in enumerate(frames):
-        want, mask = O.dext(f, with_mask=True)
-        _same(b.result(j), want, f"{what} frame {j}")
-        assert np.array_equal(b.mask(j), mask.astype(bool)), f"{what} frame {j} mask"
+    sets = [("u32", frames)]
+    if also16 and w % 8 == 0:
+        sets.append(("u16", [_as_u16(f) for f in frames]))
+    for kind, fs in sets:
+        b = api.DeviceBatch(h, w, len(fs), capacity=h * w, word_prefix=True,
+                            params=api.Params(**params) if params else None)
+        view = np.int32 if fs[0].dtype == np.uint32 else np.int16
+        b([torch.from_numpy(f.view(view)).cuda() for f in fs])
+        torch.cuda.synchronize()
+        for j, f in enumerate(fs):
+            want, mask = O.dext(f, O.Params(**params) if params else None, with_mask=True)
+            _same(b.result(j), want, f"{what} {kind} frame {j}")
+            assert np.array_equal(b.mask(j), mask.astype(bool)), f"{what} {kind} frame {j} mask"
 
 
 @pytest.mark.parametrize("phase", [(0, 0), (2, 2), (1, 2), (2, 0)])
@@ -74,7 +91,7 @@ def test_masked_bands_at_every_phase(api):
     # across spots: valid pixels beside a band see few lattice pixels.
     frames = []
     for k, width in enumerate((1, 2, 3, 4)):
-        f = _spots(240, 420, 150, seed=30 + k)
+        f = _spots(240, 424, 150, seed=30 + k)
         for r in range(3):
             y0, x0 = 20 + 70 * r + k, 30 + 130 * r + k
             f[y0:y0 + width, :] = 0xFFFFFFFE
@@ -137,7 +154,44 @@ def test_frame_of_signal_everywhere(api):
     # High-variance texture: nearly every window is stage-0 signal, so the
     # bound passes most of the frame and nearly every tile is listed.
     rng = np.random.default_rng(9)
-    f = (rng.integers(0, 2, size=(150, 290)) * rng.integers(50, 400, size=(150, 290)))
+    f = (rng.integers(0, 2, size=(150, 296)) * rng.integers(50, 400, size=(150, 296)))
     f = f.astype(np.uint32)
     f[::37, :] = 0xFFFFFFFE
     _check_batch(api, [f, np.ascontiguousarray(f[:, ::-1])], "signal everywhere")
+
+
+@pytest.mark.parametrize("h,w", [(1, 8), (7, 16), (9, 24), (17, 360), (31, 368), (33, 720),
+                                 (40, 728), (12, 1000), (25, 1024)])
+def test_strip_and_tile_boundaries_16bit(api, h, w):
+    # 16-bit frames with widths that are multiples of 8 take the lattice path.
+    rng = np.random.default_rng(h * 977 + w)
+    f = rng.poisson(1.0, size=(h, w)).astype(np.uint32)
+    for _ in range(max(1, h * w // 300)):
+        _blob(f, int(rng.integers(0, h)), int(rng.integers(0, w)), float(rng.uniform(40, 900)))
+    f[rng.random(f.shape) < 0.01] = 0xFFFFFFFF
+    g = _as_u16(f)
+    _same(api.find(g, capacity=h * w), O.dext(g), f"{h}x{w} u16")
+
+
+@pytest.mark.parametrize("params", [
+    dict(), dict(gain=1.5), dict(gain=0.8, sigma_b=4.5, sigma_s=2.5), dict(min_local=5),
+    dict(min_local=0), dict(global_threshold=3.0), dict(global_threshold=40.5),
+    dict(sigma_b=3.0, sigma_s=2.0)])
+def test_16bit_parameters(api, params):
+    # The 16-bit lattice path takes any gain and sigmas (its tests are float).
+    frames = [_spots(230, 400, 120, seed=60 + k) for k in range(2)]
+    frames[1][::41, :] = 0xFFFFFFFE
+    g = [_as_u16(f) for f in frames]
+    _check_batch(api, g, f"u16 {params}", params=params, also16=False)
+
+
+def test_16bit_bright_values(api):
+    # Values up to the largest valid 16-bit pixel: sums of squares wrap
+    # modulo 2^32 in the reference's 32-bit accumulators, as here.
+    rng = np.random.default_rng(12)
+    f = rng.integers(0, 50, size=(200, 320)).astype(np.uint32)
+    big = rng.random(f.shape) < 0.05
+    f[big] = rng.integers(30000, 0xFFFD, size=int(big.sum()))
+    for y, x in ((40, 40), (100, 200), (150, 300)):
+        _blob(f, y, x, 60000.0)
+    _check_batch(api, [_as_u16(f)], "u16 bright", also16=False)
