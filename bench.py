@@ -45,11 +45,11 @@ H, W = 4362, 4148
 
 
 # DRAM bytes (read + write) that one 16M frame of the eiger_16m workload costs
-# across the threshold's kernels in a timed 16-frame launch, from an ncu
-# capture of this bench without cache flushes between kernels (2,763.9 MB for
-# the launch: lat_stage01 1,387 MB, lat_verify 532 MB, lat_stage2 656 MB, the
-# scans and the list 189 MB); the algorithmic bytes are 76.5 MB a frame.
-DRAM_BYTES_PER_FRAME = 172.7e6
+# across the threshold's kernels in a timed 64-frame launch, from an ncu
+# capture of this bench without cache flushes between kernels (11,076 MB for
+# the launch: lat_stage01 5,097 MB, lat_verify 2,099 MB, lat_stage2 2,643 MB,
+# the scans and the list 1,237 MB); the algorithmic bytes are 76.5 MB a frame.
+DRAM_BYTES_PER_FRAME = 173.1e6
 
 
 def dist_env():
@@ -428,7 +428,7 @@ def run_ours(args):
             "achieved_gbs": bytes16 / (ms16 / 1e3) / 1e9,
             "frac_of_hbm": bytes16 / (ms16 / 1e3) / 1e9 / measured_peak_gbs()[0],
             "signal_pixels_frame0": n16,
-            "path": "sf_threshold_u16_batch_device, 16 frames a launch, the same frames as "
+            "path": f"sf_threshold_u16_batch_device, {B} frames a launch, the same frames as "
                     "16-bit pixels (valid values clamped below the masked sentinels)",
             "reference_published": "16M u16 frame kernel time 8.9 ms (CUDA, RTX 4060) and "
                                    "3.9 ms (Metal, M4 Max; unavailable on this box), "
@@ -441,7 +441,8 @@ def run_ours(args):
     label = None
     if not args.no_label:
         from sfgb import labeller
-        lab = labeller.DeviceLabeller(H, W)
+        # Room for a call's B lists plus the components they leave open.
+        lab = labeller.DeviceLabeller(H, W, live_capacity=(B + 16) * 200_000)
         lists_ptr = api.lib().sf_plan_lists(plan._p)
         counts_ptr = api.lib().sf_plan_counts(plan._p)
         nb = 0
@@ -467,7 +468,7 @@ def run_ours(args):
         label = {"ms_per_frame": label_ms, "frames_per_s": 1e3 / label_ms,
                  "threshold_and_label_frames_per_s": 1.0 / (1.0 / value + label_ms / 1e3),
                  "spots": int(len(res.spots)),
-                 "path": "sf_label_add_device on the plan's lists, 16 frames per call, "
+                 "path": f"sf_label_add_device on the plan's lists, {B} frames per call, "
                          "consecutive frame numbers with a gap between repeats of the pool"}
 
     # The host link's own speed: pinned frames copied to the device.
@@ -576,7 +577,7 @@ def run_ours(args):
             traffic = DRAM_BYTES_PER_FRAME * B
             traffic_source = (
                 "ncu dram__bytes_read.sum + dram__bytes_write.sum over the 8 kernels of a timed "
-                "16-frame launch of this workload, no cache flush between kernels "
+                "64-frame launch of this workload, no cache flush between kernels "
                 f"({DRAM_BYTES_PER_FRAME / 1e6:.1f} MB a frame), times the {B} frames of a launch")
         line = {
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
@@ -621,8 +622,8 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--frames-per-step", type=int, default=16)
-    ap.add_argument("--pool", type=int, default=16)
+    ap.add_argument("--frames-per-step", type=int, default=64)
+    ap.add_argument("--pool", type=int, default=64)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
