@@ -550,6 +550,46 @@ def run_ours(args):
         e2e["achieved_h2d_gbs"] = e2e["value"] * H * W * 4 / 1e9
         if h2d_gbs:
             e2e["frac_of_h2d_peak"] = e2e["achieved_h2d_gbs"] / h2d_gbs
+        if not args.no_u16:
+            # The same frames as 16-bit pixels through sf_find_u16 (the
+            # gpu::find<uint16_t> drop-in): half the bytes over the host link.
+            host16 = []
+            for f in frames[: min(pool_n, 8)]:
+                g = np.minimum(f, 0xFFFD).astype(np.uint16)
+                g[f == 0xFFFFFFFE] = 0xFFFE
+                g[f == 0xFFFFFFFF] = 0xFFFF
+                ptr = L.sf_host_alloc(g.nbytes)
+                if not ptr:
+                    raise SystemExit("sf_host_alloc failed")
+                np.ctypeslib.as_array((ctypes.c_uint16 * g.size).from_address(ptr))[:] = g.ravel()
+                host16.append(ptr)
+            slots.extend(range(T))
+            tls16 = threading.local()
+
+            def e2e_frame16(k):
+                if not hasattr(tls16, "slot"):
+                    with slot_lock:
+                        tls16.slot = slots.pop()
+                found = ctypes.c_size_t(0)
+                rc = L.sf_find_u16(host16[k % len(host16)], H, W, outs[tls16.slot],
+                                   H * W // 4, ctypes.byref(found))
+                if rc != 0:
+                    raise SystemExit(f"sf_find_u16 failed: {rc} {api.last_error()}")
+                return found.value
+
+            with ThreadPoolExecutor(max_workers=T) as ex:
+                list(ex.map(e2e_frame16, range(max(args.warmup, 1) * max(B, T))))
+                t0 = time.perf_counter()
+                list(ex.map(e2e_frame16, range(args.steps * B)))
+                t1 = time.perf_counter()
+            v16 = args.steps * B / (t1 - t0)
+            e2e["u16"] = {"value": v16, "unit": "frames/s",
+                          "h2d_bytes_per_step": B * H * W * 2,
+                          "achieved_h2d_gbs": v16 * H * W * 2 / 1e9,
+                          "path": f"sf_find_u16 from {T} host threads, the same frames as "
+                                  "16-bit pixels in pinned host memory"}
+            for ptr in host16:
+                L.sf_host_free(ptr)
         for ptr in host + outs:
             L.sf_host_free(ptr)
 
