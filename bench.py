@@ -12,6 +12,10 @@ the frames already in HBM (a pool of distinct frames larger than L2, cycled);
 `e2e` is the same metric through the C ABI's host-frame call (sf_find_u32,
 the gpu::find drop-in) with pinned host frames, so the host-to-device copy of
 each frame and the read-back of its signal list are inside the timed region.
+Its `bslz4_u32` / `bslz4_u16` entries time the same frames stored as
+bitshuffle+LZ4 chunks (as an EIGER's HDF5 files hold them) through
+sf_find_compressed: the chunk crosses the host link and is decoded and
+thresholded on the device.
 
 --impl reference times the reference's CPU path on this host's cores: the
 CPU restatement of dext() plus the streaming labeller (the reference's own
@@ -590,6 +594,57 @@ def run_ours(args):
                                   "16-bit pixels in pinned host memory"}
             for ptr in host16:
                 L.sf_host_free(ptr)
+        if not args.no_bslz4:
+            # The same frames as bitshuffle+LZ4 chunks (how an EIGER's HDF5
+            # stores them) through sf_find_compressed: only the chunk crosses
+            # the host link, decoded and thresholded on the device
+            # (find_spots.cc:772-800 with decompress::image on the device).
+            from sfgb import synth
+            for depth in (32, 16):
+                chunks = []
+                for f in frames[: min(pool_n, 8)]:
+                    if depth == 16:
+                        g = np.minimum(f, 0xFFFD).astype(np.uint16)
+                        g[f == 0xFFFFFFFE] = 0xFFFE
+                        g[f == 0xFFFFFFFF] = 0xFFFF
+                        f = g
+                    c = synth.chunk(f, "bslz4")
+                    ptr = L.sf_host_alloc(c.size)
+                    if not ptr:
+                        raise SystemExit("sf_host_alloc failed")
+                    np.ctypeslib.as_array((ctypes.c_uint8 * c.size).from_address(ptr))[:] = c
+                    chunks.append((ptr, c.size))
+                slots.extend(range(T))
+                tlsc = threading.local()
+
+                def e2e_chunk(k, depth=depth, chunks=chunks, tlsc=tlsc):
+                    if not hasattr(tlsc, "slot"):
+                        with slot_lock:
+                            tlsc.slot = slots.pop()
+                    found = ctypes.c_size_t(0)
+                    ptr, n = chunks[k % len(chunks)]
+                    rc = L.sf_find_compressed(ptr, n, b"bslz4", depth, H, W, None,
+                                              outs[tlsc.slot], H * W // 4, ctypes.byref(found))
+                    if rc != 0:
+                        raise SystemExit(f"sf_find_compressed failed: {rc} {api.last_error()}")
+                    return n
+
+                with ThreadPoolExecutor(max_workers=T) as ex:
+                    list(ex.map(e2e_chunk, range(max(args.warmup, 1) * max(B, T))))
+                    t0 = time.perf_counter()
+                    nbytes = sum(ex.map(e2e_chunk, range(args.steps * B)))
+                    t1 = time.perf_counter()
+                vc = args.steps * B / (t1 - t0)
+                e2e[f"bslz4_u{depth}"] = {
+                    "value": vc, "unit": "frames/s",
+                    "h2d_bytes_per_step": int(nbytes / args.steps),
+                    "compression": args.steps * B * H * W * depth / 8 / nbytes,
+                    "achieved_h2d_gbs": nbytes / (t1 - t0) / 1e9,
+                    "path": f"sf_find_compressed from {T} host threads: the same frames as "
+                            f"{depth}-bit bitshuffle+LZ4 chunks (8192-byte blocks) in pinned "
+                            "host memory, decoded and thresholded on the device"}
+                for ptr, _ in chunks:
+                    L.sf_host_free(ptr)
         for ptr in host + outs:
             L.sf_host_free(ptr)
 
@@ -671,6 +726,7 @@ def main(argv=None):
     ap.add_argument("--no-label", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-u16", action="store_true")
+    ap.add_argument("--no-bslz4", action="store_true")
     ap.add_argument("--served-seconds", type=float, default=4.0)
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per threshold launch from an ncu capture")

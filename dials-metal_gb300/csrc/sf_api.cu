@@ -15,6 +15,7 @@
 
 #include "sf_api.h"
 #include "sf_common.cuh"
+#include "sf_decompress.cuh"
 #include "sf_scan.cuh"
 #include "sf_stream.cuh"
 #include "sf_threshold.cuh"
@@ -296,18 +297,97 @@ public:
     cudaFree(count_);
     if (host_count_)
       cudaFreeHost(host_count_);
+    cudaFree(chunk_);
+    cudaFree(table_);
+    cudaFree(scratch_);
+    if (table_host_)
+      cudaFreeHost(table_host_);
+  }
+
+  int open() {
+    cudaError_t e;
+    if (stream_)
+      return SF_OK;
+    if ((e = cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking)) != cudaSuccess)
+      return fail(e, "cudaStreamCreate");
+    // The count and the decoder's error record: 4 words on both sides.
+    if ((e = cudaMalloc(&count_, 4 * sizeof(uint32_t))) != cudaSuccess)
+      return fail(e, "cudaMalloc for the count");
+    if ((e = cudaMallocHost(&host_count_, 4 * sizeof(uint32_t))) != cudaSuccess)
+      return fail(e, "cudaMallocHost for the count");
+    return SF_OK;
+  }
+
+  int reserve_image(size_t bytes) {
+    int rc = open();
+    return rc != SF_OK ? rc : grow(&image_, &image_cap_, bytes, "cudaMalloc for the frame");
+  }
+
+  // The decoder's buffers: the chunk's payload, its block table (and the
+  // pinned copy it is uploaded from) and, for bitshuffle blocks larger than
+  // a warp's buffer, a frame-sized scratch buffer.
+  int reserve_decode(const ChunkPlan &plan) {
+    int rc = open();
+    if (rc != SF_OK)
+      return rc;
+    const size_t table_bytes = plan.blocks.size() * sizeof(DecodeBlock);
+    if ((rc = grow(&chunk_, &chunk_cap_, plan.payload, "cudaMalloc for the chunk")) != SF_OK ||
+        (rc = grow(&table_, &table_cap_, table_bytes, "cudaMalloc for the block table")) !=
+            SF_OK ||
+        (plan.scratch &&
+         (rc = grow(&scratch_, &scratch_cap_, plan.frame_bytes, "cudaMalloc for the scratch")) !=
+             SF_OK))
+      return rc;
+    if (table_bytes > table_host_cap_) {
+      cudaStreamSynchronize(stream_);
+      if (table_host_)
+        cudaFreeHost(table_host_);
+      table_host_ = nullptr;
+      table_host_cap_ = 0;
+      cudaError_t e = cudaMallocHost(&table_host_, table_bytes);
+      if (e != cudaSuccess)
+        return fail(e, "cudaMallocHost for the block table");
+      table_host_cap_ = table_bytes;
+    }
+    return SF_OK;
+  }
+
+  // The chunk `data` (host) decoded into d_frame on the stream; the error
+  // record lands in host_count_[1 .. 3] once the stream is idle.
+  int decode(const uint8_t *data, const ChunkPlan &plan, uint8_t *d_frame) {
+    cudaError_t e;
+    const size_t table_bytes = plan.blocks.size() * sizeof(DecodeBlock);
+    std::memcpy(table_host_, plan.blocks.data(), table_bytes);
+    if ((e = cudaMemcpyAsync(chunk_, data + 12, plan.payload, cudaMemcpyHostToDevice,
+                             stream_)) != cudaSuccess)
+      return fail(e, "copying a chunk to the device");
+    if ((e = cudaMemcpyAsync(table_, table_host_, table_bytes, cudaMemcpyHostToDevice,
+                             stream_)) != cudaSuccess)
+      return fail(e, "copying the block table to the device");
+    if ((e = cudaMemsetAsync(count_ + 1, 0, 3 * sizeof(uint32_t), stream_)) != cudaSuccess)
+      return fail(e, "cudaMemsetAsync");
+    if ((e = launch_decode(chunk_, table_, plan.blocks.size(), plan.element, d_frame,
+                           scratch_, count_ + 1, stream_)) != cudaSuccess)
+      return fail(e, "launching the decoder");
+    if ((e = cudaMemcpyAsync(host_count_ + 1, count_ + 1, 3 * sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, stream_)) != cudaSuccess)
+      return fail(e, "reading the decoder's status back");
+    return SF_OK;
+  }
+
+  // After the stream is idle: SF_OK, or SF_EDATA with the reference's text.
+  int decoded(const ChunkPlan &plan) const {
+    if (host_count_[1] == kDecOk)
+      return SF_OK;
+    t_last_error = decode_error_text(plan, host_count_ + 1);
+    return SF_EDATA;
   }
 
   int reserve(size_t image_bytes, size_t h, size_t w, size_t capacity) {
     cudaError_t e;
-    if (!stream_) {
-      if ((e = cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking)) != cudaSuccess)
-        return fail(e, "cudaStreamCreate");
-      if ((e = cudaMalloc(&count_, sizeof(uint32_t))) != cudaSuccess)
-        return fail(e, "cudaMalloc for the count");
-      if ((e = cudaMallocHost(&host_count_, sizeof(uint32_t))) != cudaSuccess)
-        return fail(e, "cudaMallocHost for the count");
-    }
+    int rc = open();
+    if (rc != SF_OK)
+      return rc;
     const size_t bits_bytes = words_per_row((int)w) * h * sizeof(uint32_t);
     const size_t ws_bytes = sf_workspace_bytes(h, w, capacity);
     const size_t out_bytes = capacity * sizeof(sf_signal_pixel);
@@ -358,6 +438,21 @@ public:
     return marks_;
   }
 
+  template <typename P> int grow(P **p, size_t *cap, size_t bytes, const char *what) {
+    if (bytes <= *cap)
+      return SF_OK;
+    // Nothing may be in flight when a buffer goes.
+    cudaStreamSynchronize(stream_);
+    cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), bytes);
+    if (e != cudaSuccess)
+      return fail(e, what);
+    *cap = bytes;
+    return SF_OK;
+  }
+
   cudaStream_t stream_ = nullptr;
   void *image_ = nullptr;
   uint32_t *bits_ = nullptr;
@@ -365,7 +460,11 @@ public:
   void *ws_ = nullptr;
   uint32_t *count_ = nullptr;
   uint32_t *host_count_ = nullptr;
+  uint8_t *chunk_ = nullptr, *scratch_ = nullptr;
+  DecodeBlock *table_ = nullptr;
+  void *table_host_ = nullptr;
   size_t image_cap_ = 0, bits_cap_ = 0, ws_cap_ = 0, out_cap_ = 0;
+  size_t chunk_cap_ = 0, table_cap_ = 0, table_host_cap_ = 0, scratch_cap_ = 0;
   cudaEvent_t marks_[3] = {nullptr, nullptr, nullptr};
 };
 
@@ -383,10 +482,12 @@ struct StreamGuard {
   }
 };
 
+// One host frame thresholded; with a chunk plan, `image` is the chunk and
+// only it crosses the host link, decoded on the device.
 template <typename T>
-static int find_host(const T *image, size_t h, size_t w,
+static int find_host(const void *image, size_t h, size_t w,
                      const sf_threshold_params *params, sf_signal_pixel *out,
-                     size_t capacity, size_t *found) {
+                     size_t capacity, size_t *found, const ChunkPlan *plan = nullptr) {
   if (found)
     *found = 0;
   if (!image || !found || (!out && capacity) || !shape_ok(h, w))
@@ -403,6 +504,9 @@ static int find_host(const T *image, size_t h, size_t w,
   Workspace &ws = workspace();
   if ((rc = ws.reserve(bytes, h, w, dcap)) != SF_OK)
     return rc;
+  const bool decode = plan && plan->algorithm != kChunkNone;
+  if (decode && (rc = ws.reserve_decode(*plan)) != SF_OK)
+    return rc;
   const cudaStream_t stream = ws.stream_;
   StreamGuard idle{stream};
   const bool timing = g_profiling;
@@ -410,9 +514,14 @@ static int find_host(const T *image, size_t h, size_t w,
   cudaError_t e;
   if (timing)
     cudaEventRecord(marks[0], stream);
-  if ((e = cudaMemcpyAsync(ws.image_, image, bytes, cudaMemcpyHostToDevice, stream)) !=
-      cudaSuccess)
+  if (decode) {
+    if ((rc = ws.decode(static_cast<const uint8_t *>(image), *plan,
+                        static_cast<uint8_t *>(ws.image_))) != SF_OK)
+      return rc;
+  } else if ((e = cudaMemcpyAsync(ws.image_, image, bytes, cudaMemcpyHostToDevice, stream)) !=
+             cudaSuccess) {
     return fail(e, "copying a frame to the device");
+  }
   if (timing)
     cudaEventRecord(marks[1], stream);
   rc = threshold_device<T>(static_cast<const T *>(ws.image_), h, w, params, ws.out_,
@@ -427,6 +536,8 @@ static int find_host(const T *image, size_t h, size_t w,
     return fail(e, "reading the signal count back");
   if ((e = cudaStreamSynchronize(stream)) != cudaSuccess)
     return fail(e, "cudaStreamSynchronize");
+  if (decode && (rc = ws.decoded(*plan)) != SF_OK)
+    return rc;
   const size_t n = *ws.host_count_;
   *found = n;
   sf_stage_times times = {0, 0, 0, 0, 0, 0, 0};
@@ -556,6 +667,87 @@ int sf_find_u16_params(const uint16_t *image, size_t height, size_t width,
                        const sf_threshold_params *params, sf_signal_pixel *out,
                        size_t capacity, size_t *found) {
   return find_host<uint16_t>(image, height, width, params, out, capacity, found);
+}
+
+size_t sf_frame_bytes(size_t height, size_t width, unsigned bit_depth) {
+  return height * width * bit_depth / 8;
+}
+
+// decompress::image into host (to_device false) or device memory.
+static int decompress_to(const uint8_t *data, size_t nbytes, const char *algorithm,
+                         unsigned bit_depth, size_t height, size_t width, void *out,
+                         size_t out_bytes, bool to_device) {
+  if ((!data && nbytes) || !out || !shape_ok(height, width) || bit_depth > 64)
+    return SF_EBADARG;
+  if (to_device && reinterpret_cast<uintptr_t>(out) % 16 != 0) {
+    t_last_error = "the device frame must be 16-byte aligned";
+    return SF_EBADARG;
+  }
+  ChunkPlan plan;
+  int rc = plan_chunk(data, nbytes, algorithm, bit_depth, height, width, out_bytes, &plan);
+  if (rc != SF_OK)
+    return rc;
+  if (plan.algorithm == kChunkNone && !to_device) {
+    std::memcpy(out, data, nbytes);  // decompress.cc:93
+    return SF_OK;
+  }
+  Workspace &ws = workspace();
+  if ((rc = to_device ? ws.open() : ws.reserve_image(plan.frame_bytes)) != SF_OK)
+    return rc;
+  uint8_t *frame = static_cast<uint8_t *>(to_device ? out : ws.image_);
+  const cudaStream_t stream = ws.stream_;
+  StreamGuard idle{stream};
+  cudaError_t e;
+  if (plan.algorithm == kChunkNone) {
+    if ((e = cudaMemcpyAsync(frame, data, nbytes, cudaMemcpyHostToDevice, stream)) !=
+        cudaSuccess)
+      return fail(e, "copying a frame to the device");
+  } else {
+    if ((rc = ws.reserve_decode(plan)) != SF_OK || (rc = ws.decode(data, plan, frame)) != SF_OK)
+      return rc;
+    if (!to_device && (e = cudaMemcpyAsync(out, frame, plan.frame_bytes, cudaMemcpyDeviceToHost,
+                                           stream)) != cudaSuccess)
+      return fail(e, "copying the frame back");
+  }
+  if ((e = cudaStreamSynchronize(stream)) != cudaSuccess)
+    return fail(e, "cudaStreamSynchronize");
+  return plan.algorithm == kChunkNone ? SF_OK : ws.decoded(plan);
+}
+
+int sf_decompress_image(const uint8_t *data, size_t nbytes, const char *algorithm,
+                        unsigned bit_depth, size_t height, size_t width, uint8_t *out,
+                        size_t out_bytes) {
+  return decompress_to(data, nbytes, algorithm, bit_depth, height, width, out, out_bytes,
+                       false);
+}
+
+int sf_decompress_device(const uint8_t *data, size_t nbytes, const char *algorithm,
+                         unsigned bit_depth, size_t height, size_t width, void *d_out,
+                         size_t out_bytes) {
+  return decompress_to(data, nbytes, algorithm, bit_depth, height, width, d_out, out_bytes,
+                       true);
+}
+
+int sf_find_compressed(const uint8_t *data, size_t nbytes, const char *algorithm,
+                       unsigned bit_depth, size_t height, size_t width,
+                       const sf_threshold_params *params, sf_signal_pixel *out,
+                       size_t capacity, size_t *found) {
+  if (found)
+    *found = 0;
+  if (!data || !found || (!out && capacity) || !shape_ok(height, width))
+    return SF_EBADARG;
+  if (bit_depth != 16 && bit_depth != 32) {
+    t_last_error = "frames of 16- or 32-bit pixels are thresholded";
+    return SF_EUNSUPPORTED;
+  }
+  ChunkPlan plan;
+  const size_t frame = height * width * bit_depth / 8;
+  int rc = plan_chunk(data, nbytes, algorithm, bit_depth, height, width, frame, &plan);
+  if (rc != SF_OK)
+    return rc;
+  return bit_depth == 16
+             ? find_host<uint16_t>(data, height, width, params, out, capacity, found, &plan)
+             : find_host<uint32_t>(data, height, width, params, out, capacity, found, &plan);
 }
 
 void sf_profile_stages(int on) { g_profiling = on != 0; }

@@ -38,6 +38,22 @@ size_t sf_synth_n_spots(const sf_synth *s);
 /* Frame `frame` (0-based) of the sweep into out[height * width]. */
 int sf_synth_frame(const sf_synth *s, int frame, uint32_t *out);
 
+/* Compressed chunks as an HDF5 writer stores them (synth_chunk.c): the
+ * 12-byte filter header and bitshuffle+LZ4 ("bslz4") or LZ4 ("lz4") blocks.
+ * block_bytes 0 takes bitshuffle's default block (bslz4) or one block for the
+ * frame (lz4). Each returns the chunk's length, or -1 (bad arguments, or
+ * more than cap bytes). */
+size_t sf_chunk_bound(size_t frame_bytes, size_t block_bytes);
+int64_t sf_chunk_bslz4(const void *frame, size_t n_elems, unsigned esize, size_t block_bytes,
+                       uint8_t *out, size_t cap);
+int64_t sf_chunk_lz4(const void *frame, size_t nbytes, size_t block_bytes, uint8_t *out,
+                     size_t cap);
+/* One LZ4 block of n bytes into dst (sf_lz4_bound(n) bytes); its length. */
+size_t sf_lz4_bound(size_t n);
+size_t sf_lz4_block(const uint8_t *src, size_t n, uint8_t *dst);
+/* The bit planes of n elements (n a multiple of 8) of esize bytes. */
+void sf_bitshuffle(const uint8_t *in, uint8_t *out, size_t n, size_t esize);
+
 #ifdef __cplusplus
 }
 #endif

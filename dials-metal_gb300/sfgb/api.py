@@ -21,6 +21,7 @@ import numpy as np
 from . import _paths
 
 SF_OK, SF_EBADARG, SF_EOVERFLOW, SF_ECUDA, SF_EUNSUPPORTED = 0, -1, -2, -3, -4
+SF_EDATA = -6
 DISPERSION_EXTENDED, DISPERSION = 0, 1
 
 # src/spots/signal_pixel.hh:20-28
@@ -123,6 +124,15 @@ def lib() -> ctypes.CDLL:
             getattr(L, name).restype = vp
         L.sf_plan_result.argtypes = [vp, sz, vp, sz, ctypes.POINTER(sz)]
         L.sf_plan_result.restype = ctypes.c_int
+        L.sf_frame_bytes.argtypes = [sz, sz, ctypes.c_uint]
+        L.sf_frame_bytes.restype = sz
+        for name in ("sf_decompress_image", "sf_decompress_device"):
+            getattr(L, name).argtypes = [vp, sz, ctypes.c_char_p, ctypes.c_uint, sz, sz, vp, sz]
+            getattr(L, name).restype = ctypes.c_int
+        L.sf_find_compressed.argtypes = [vp, sz, ctypes.c_char_p, ctypes.c_uint, sz, sz,
+                                         ctypes.POINTER(ThresholdParams), vp, sz,
+                                         ctypes.POINTER(sz)]
+        L.sf_find_compressed.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -182,6 +192,84 @@ def find(frame: np.ndarray, params: Params | None = None,
         rc = fnp(frame.ctypes.data, h, w, ctypes.byref(p), out.ctypes.data, capacity,
                  ctypes.byref(found))
     _check(rc, "threshold")
+    return out[:found.value].copy()
+
+
+class DataError(SpotFinderError):
+    """A compressed chunk that does not describe its frame: where the
+    reference's decompress::image throws std::runtime_error."""
+
+
+def _chunk_bytes(data) -> np.ndarray:
+    if isinstance(data, np.ndarray):
+        return np.ascontiguousarray(data).view(np.uint8).ravel()
+    return np.frombuffer(bytes(data), np.uint8)
+
+
+def _check_chunk(rc: int, what: str) -> None:
+    if rc == SF_EDATA:
+        raise DataError(last_error())
+    if rc == SF_EUNSUPPORTED:
+        raise SpotFinderError(f"{what}: {last_error()}")
+    _check(rc, what)
+
+
+def frame_bytes(height: int, width: int, bit_depth: int) -> int:
+    """decompress::frame_bytes (src/spots/decompress.hh:18-19)."""
+    return lib().sf_frame_bytes(height, width, bit_depth)
+
+
+def decompress_image(data, algorithm: str, bit_depth: int, height: int,
+                     width: int) -> np.ndarray:
+    """decompress::image (src/spots/decompress.hh:28-30), decoded on the
+    device: a chunk as HDF5 stored it ("bslz4", "lz4", or "" for none) to a
+    (height, width) host frame. Raises DataError where the reference throws,
+    with its text."""
+    buf = _chunk_bytes(data)
+    n = frame_bytes(height, width, bit_depth)
+    dtype = {16: np.uint16, 32: np.uint32}.get(bit_depth, np.uint8)
+    out = np.empty(max(n, 1), np.uint8)
+    rc = lib().sf_decompress_image(buf.ctypes.data if buf.size else None, buf.size,
+                                   algorithm.encode(), bit_depth, height, width,
+                                   out.ctypes.data, n)
+    _check_chunk(rc, "decompress")
+    out = out[:n]
+    return out.view(dtype).reshape(height, width) if dtype is not np.uint8 else out
+
+
+def decompress_device(data, algorithm: str, bit_depth: int, height: int, width: int,
+                      out=None):
+    """As decompress_image, into a device tensor (torch, cuda; allocated
+    when `out` is None); returns it once the frame is there."""
+    import torch
+    buf = _chunk_bytes(data)
+    n = frame_bytes(height, width, bit_depth)
+    if out is None:
+        dt = {16: torch.int16, 32: torch.int32}.get(bit_depth, torch.uint8)
+        out = torch.empty((height, width) if dt is not torch.uint8 else (max(n, 1),), dtype=dt,
+                          device="cuda")
+    rc = lib().sf_decompress_device(buf.ctypes.data if buf.size else None, buf.size,
+                                    algorithm.encode(), bit_depth, height, width,
+                                    out.data_ptr(), out.numel() * out.element_size())
+    _check_chunk(rc, "decompress")
+    return out
+
+
+def find_compressed(data, algorithm: str, bit_depth: int, height: int, width: int,
+                    params: Params | None = None, capacity: int | None = None) -> np.ndarray:
+    """The chunk decoded on the device and thresholded there
+    (sf_find_compressed): the signal pixels ascending by index."""
+    buf = _chunk_bytes(data)
+    if capacity is None:
+        capacity = max(1, frame_bytes(height, width, bit_depth) // 16)
+    out = np.empty(capacity, SIGNAL_DTYPE)
+    found = ctypes.c_size_t(0)
+    p = params.c() if params is not None else None
+    rc = lib().sf_find_compressed(buf.ctypes.data if buf.size else None, buf.size,
+                                  algorithm.encode(), bit_depth, height, width,
+                                  ctypes.byref(p) if p is not None else None, out.ctypes.data,
+                                  capacity, ctypes.byref(found))
+    _check_chunk(rc, "threshold")
     return out[:found.value].copy()
 
 

@@ -1,7 +1,7 @@
 """Build the in-tree shared libraries:
 
   libsfgb.so     the CUDA kernels and the C ABI (include/sf_api.h), sm_103a
-  libsfsynth.so  the synthetic sweep generator (host C, OpenMP)
+  libsfsynth.so  the synthetic sweep generator and chunk writer (host C, OpenMP)
 
 Translation units compile in parallel; nothing is installed outside the tree.
 """
@@ -15,7 +15,7 @@ from concurrent.futures import ThreadPoolExecutor
 from . import _paths
 
 CUDA_SOURCES = ["sf_threshold.cu", "sf_stream.cu", "sf_lattice.cu", "sf_api.cu", "sf_label.cu",
-                "sf_serve.cu", "sf_refl.cu"]
+                "sf_serve.cu", "sf_refl.cu", "sf_decompress.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               # No FMA contraction anywhere: the FP64/FP32 decisions must round
@@ -57,7 +57,8 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict:
     def synth():
         tmp = _paths.synth_lib() + ".tmp"
         _run(["gcc", "-std=c11", "-O2", "-fopenmp", "-fPIC", "-shared",
-              os.path.join(_paths.CSRC, "synth.c"), "-o", tmp, "-lm"], verbose)
+              os.path.join(_paths.CSRC, "synth.c"), os.path.join(_paths.CSRC, "synth_chunk.c"),
+              "-o", tmp, "-lm"], verbose)
         os.replace(tmp, _paths.synth_lib())
 
     with ThreadPoolExecutor(max_workers=len(CUDA_SOURCES) + 1) as ex:

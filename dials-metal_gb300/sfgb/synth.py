@@ -48,6 +48,18 @@ def lib() -> ctypes.CDLL:
         L.sf_synth_n_spots.restype = ctypes.c_size_t
         L.sf_synth_frame.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.sf_synth_frame.restype = ctypes.c_int
+        sz, vp = ctypes.c_size_t, ctypes.c_void_p
+        L.sf_chunk_bound.argtypes = [sz, sz]
+        L.sf_chunk_bound.restype = sz
+        L.sf_chunk_bslz4.argtypes = [vp, sz, ctypes.c_uint, sz, vp, sz]
+        L.sf_chunk_bslz4.restype = ctypes.c_int64
+        L.sf_chunk_lz4.argtypes = [vp, sz, sz, vp, sz]
+        L.sf_chunk_lz4.restype = ctypes.c_int64
+        L.sf_lz4_bound.argtypes = [sz]
+        L.sf_lz4_bound.restype = sz
+        L.sf_lz4_block.argtypes = [vp, sz, vp]
+        L.sf_lz4_block.restype = sz
+        L.sf_bitshuffle.argtypes = [vp, vp, sz, sz]
         _lib = L
     return _lib
 
@@ -142,3 +154,48 @@ class Sweep:
         if getattr(self, "_h", None):
             lib().sf_synth_close(self._h)
             self._h = None
+
+
+def chunk(frame: np.ndarray, algorithm: str = "bslz4", block_bytes: int = 0,
+          out: np.ndarray | None = None) -> np.ndarray:
+    """The frame as an HDF5 writer stores a compressed chunk ("bslz4" or
+    "lz4", with the 12-byte filter header), as uint8. block_bytes 0 takes
+    bitshuffle's default block (bslz4) or one block for the frame (lz4). With
+    `out` the chunk is written there (a view of its first bytes returned)."""
+    frame = np.ascontiguousarray(frame)
+    nbytes = frame.nbytes
+    cap = lib().sf_chunk_bound(nbytes, block_bytes if algorithm == "bslz4" or block_bytes
+                               else max(nbytes, 1))
+    if out is None:
+        out = np.empty(cap, np.uint8)
+    elif out.nbytes < cap:
+        raise ValueError(f"chunk buffer of {out.nbytes} bytes, need {cap}")
+    ptr = frame.ctypes.data if frame.size else None
+    if algorithm == "bslz4":
+        n = lib().sf_chunk_bslz4(ptr or out.ctypes.data, frame.size, frame.itemsize,
+                                 block_bytes, out.ctypes.data, out.nbytes)
+    elif algorithm == "lz4":
+        n = lib().sf_chunk_lz4(ptr or out.ctypes.data, nbytes, block_bytes, out.ctypes.data,
+                               out.nbytes)
+    else:
+        raise ValueError(f"unknown compression algorithm {algorithm}")
+    if n < 0:
+        raise ValueError("chunk writer refused the frame")
+    return out[:n]
+
+
+def lz4_block(data: bytes) -> bytes:
+    """One LZ4 block of `data` (this module's matcher)."""
+    src = np.frombuffer(bytes(data), np.uint8)
+    dst = np.empty(lib().sf_lz4_bound(src.size), np.uint8)
+    n = lib().sf_lz4_block(src.ctypes.data if src.size else dst.ctypes.data, src.size,
+                           dst.ctypes.data)
+    return dst[:n].tobytes()
+
+
+def bitshuffle(elements: np.ndarray) -> np.ndarray:
+    """The bit planes of a block of elements (a multiple of 8 of them)."""
+    e = np.ascontiguousarray(elements)
+    out = np.empty(e.nbytes, np.uint8)
+    lib().sf_bitshuffle(e.ctypes.data, out.ctypes.data, e.size, e.itemsize)
+    return out

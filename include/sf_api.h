@@ -33,6 +33,7 @@ extern "C" {
 #define SF_ECUDA (-3)
 #define SF_EUNSUPPORTED (-4)
 #define SF_EBUSY (-5) /* the served form's device-memory budget is taken */
+#define SF_EDATA (-6) /* a compressed chunk that does not describe its frame */
 
 /* src/spots/signal_pixel.hh:20-28: one surviving pixel, 16 bytes. */
 typedef struct {
@@ -97,6 +98,40 @@ int sf_find_u32_params(const uint32_t *image, size_t height, size_t width,
                        const sf_threshold_params *params, sf_signal_pixel *out,
                        size_t capacity, size_t *found);
 int sf_find_u16_params(const uint16_t *image, size_t height, size_t width,
+                       const sf_threshold_params *params, sf_signal_pixel *out,
+                       size_t capacity, size_t *found);
+
+/*
+ * Frame decompression on the device. Replaces decompress::frame_bytes and
+ * decompress::image (src/spots/decompress.hh:18-30, decompress.cc:72-134):
+ * `data` is a chunk exactly as HDF5 stored it, filter header and all, in host
+ * memory (pinned by sf_host_alloc for full speed); `algorithm` is "bslz4"
+ * (bitshuffle+LZ4, 16- or 32-bit pixels), "lz4" or "" (uncompressed).
+ * Returns 0; -6 (SF_EDATA) where the reference throws, with its text in
+ * sf_last_error(); -1 for null pointers; -4 for bitshuffle chunks of other
+ * pixel sizes; -3.
+ *
+ * sf_decompress_image writes the frame to host memory `out`;
+ * sf_decompress_device to device memory d_out (16-byte aligned), returning
+ * once it is there. out_bytes is the room at out / d_out.
+ */
+size_t sf_frame_bytes(size_t height, size_t width, unsigned bit_depth);
+int sf_decompress_image(const uint8_t *data, size_t nbytes, const char *algorithm,
+                        unsigned bit_depth, size_t height, size_t width, uint8_t *out,
+                        size_t out_bytes);
+int sf_decompress_device(const uint8_t *data, size_t nbytes, const char *algorithm,
+                         unsigned bit_depth, size_t height, size_t width, void *d_out,
+                         size_t out_bytes);
+
+/*
+ * The worker's step of find_spots.cc:772-800 in one call: a compressed chunk
+ * (as sf_decompress_image takes it) decoded on the device and thresholded
+ * there as sf_find_u16_params / sf_find_u32_params (bit_depth 16 or 32)
+ * would threshold the decoded frame. Only the chunk crosses the host link.
+ * Returns as sf_find_u32 does, or -6 / -4 as sf_decompress_image.
+ */
+int sf_find_compressed(const uint8_t *data, size_t nbytes, const char *algorithm,
+                       unsigned bit_depth, size_t height, size_t width,
                        const sf_threshold_params *params, sf_signal_pixel *out,
                        size_t capacity, size_t *found);
 

@@ -62,10 +62,10 @@ class Params:
 def build(quiet: bool = True) -> None:
     """Compile the oracle restatement (always) and the reference library (only
     where the reference tree exists)."""
-    src = os.path.join(HERE, "sf_oracle.c")
+    srcs = [os.path.join(HERE, f) for f in ("sf_oracle.c", "sf_oracle_decompress.c")]
     tmp = LIB_PATH + ".tmp"
     subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
-                    src, "-o", tmp, "-lm"], check=True)
+                    *srcs, "-o", tmp, "-lm"], check=True)
     os.replace(tmp, LIB_PATH)
     subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True,
                    stdout=subprocess.DEVNULL if quiet else None,
@@ -101,6 +101,14 @@ def lib() -> ctypes.CDLL:
             getattr(L, name).restype = vp
         L.or_label_counts.argtypes = [vp, vp]
         L.or_label_close.argtypes = [vp]
+        L.or_lz4_decode.argtypes = [vp, sz, vp, sz]
+        L.or_lz4_decode.restype = ctypes.c_long
+        L.or_bitunshuffle.argtypes = [vp, vp, sz, sz]
+        L.or_bshuf_default_block.argtypes = [sz]
+        L.or_bshuf_default_block.restype = sz
+        L.or_decompress_image.argtypes = [vp, sz, ctypes.c_char_p, ctypes.c_uint, sz, sz, vp,
+                                          sz, ctypes.c_char_p, sz]
+        L.or_decompress_image.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -174,6 +182,47 @@ def dext(frame: np.ndarray, params: Params | None = None,
         raise ValueError(f"oracle threshold rejected the frame ({rc})")
     out = out[:found.value].copy()
     return (out, mask) if with_mask else out
+
+
+def decompress_image(data, algorithm: str, bit_depth: int, height: int,
+                     width: int) -> np.ndarray:
+    """decompress::image (src/spots/decompress.cc:77-134): the chunk as HDF5
+    stored it ("bslz4", "lz4" or "" for none) to a (height, width) frame of
+    bit_depth bits. Raises RuntimeError with the reference's text."""
+    buf = np.frombuffer(bytes(data), np.uint8) if not isinstance(data, np.ndarray) else \
+        np.ascontiguousarray(data).view(np.uint8).ravel()
+    dtype = {8: np.uint8, 16: np.uint16, 32: np.uint32}.get(bit_depth, np.uint8)
+    nbytes = height * width * bit_depth // 8
+    out = np.zeros(max(nbytes, 1), np.uint8)
+    err = ctypes.create_string_buffer(256)
+    rc = lib().or_decompress_image(_ptr(buf) if buf.size else None, buf.size,
+                                   algorithm.encode(), bit_depth, height, width, _ptr(out),
+                                   nbytes, err, 256)
+    if rc != 0:
+        raise RuntimeError(err.value.decode())
+    if bit_depth not in (8, 16, 32):
+        return out[:nbytes]
+    return out[:nbytes].view(dtype).reshape(height, width)
+
+
+def lz4_decode(block: bytes, capacity: int) -> bytes:
+    """One LZ4 block, as LZ4_decompress_safe reads it; raises ValueError with
+    the negative code on a bad stream."""
+    src = np.frombuffer(bytes(block), np.uint8)
+    out = np.zeros(max(capacity, 1), np.uint8)
+    r = lib().or_lz4_decode(_ptr(src) if src.size else None, src.size, _ptr(out), capacity)
+    if r < 0:
+        raise ValueError(r)
+    return out[:r].tobytes()
+
+
+def bitunshuffle(planes: np.ndarray, n: int, esize: int) -> np.ndarray:
+    """The elements of one bitshuffle block from its bit planes (n a
+    multiple of 8), as bytes."""
+    planes = np.ascontiguousarray(planes, np.uint8)
+    out = np.zeros(n * esize, np.uint8)
+    lib().or_bitunshuffle(_ptr(planes), _ptr(out), n, esize)
+    return out
 
 
 def ref_dext(frame: np.ndarray) -> np.ndarray:

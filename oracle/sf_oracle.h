@@ -104,6 +104,18 @@ const or_pixel *or_label_pixels(const or_labeller *l);
 void or_label_counts(const or_labeller *l, or_counts *out);
 void or_label_close(or_labeller *l);
 
+/* Frame decompression (sf_oracle_decompress.c): decompress::image
+ * (src/spots/decompress.cc:77-134) with LZ4 blocks and bitshuffle. */
+long or_lz4_decode(const uint8_t *in, size_t n, uint8_t *out, size_t cap);
+void or_bitunshuffle(const uint8_t *in, uint8_t *out, size_t n, size_t esize);
+size_t or_bshuf_default_block(size_t esize);
+long or_bshuf_decompress_lz4(const uint8_t *in, size_t n_in, uint8_t *out, size_t size,
+                             size_t esize, size_t block_size);
+size_t or_frame_bytes(size_t height, size_t width, unsigned bit_depth);
+int or_decompress_image(const uint8_t *data, size_t n, const char *algorithm,
+                        unsigned bit_depth, size_t height, size_t width, uint8_t *out,
+                        size_t out_bytes, char *err, size_t err_cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,8 +23,18 @@ Fixtures:
                           and an experiment identifier
   refl_small_2d.refl      refl::write of the 2-D spot table, shoeboxes on, with
                           an identifier
+  lz4_blocks.npz          LZ4 blocks written by the LZ4 library (pyarrow's
+                          "lz4_raw" codec) over assorted inputs, corrupted
+                          variants with whether the library accepts them, and
+                          two chunks framed as HDF5 stores them whose blocks
+                          the library wrote: "lz4" (a uint32 frame, 4096-byte
+                          blocks) and "bslz4" (a uint16 frame's bit planes,
+                          bitshuffle's default blocks, a partial last block
+                          and 4 raw tail elements)
 
 Only the reflection-table fixtures: python tests/golden/make_golden.py refl
+Only the LZ4 fixtures (needs pyarrow, not the reference):
+    python tests/golden/make_golden.py lz4
 """
 import os
 import sys
@@ -121,7 +131,79 @@ def sweep_small():
     return len(out["spots_3d"])
 
 
+def lz4_blocks():
+    """LZ4 blocks from the LZ4 library itself (pyarrow's lz4_raw codec)."""
+    import pyarrow as pa
+    from sfgb import synth
+
+    def lz4(data: bytes) -> bytes:
+        return pa.compress(data, codec="lz4_raw", asbytes=True)
+
+    def accepted(block: bytes, n: int) -> bool:
+        try:
+            return len(pa.decompress(block, decompressed_size=n, codec="lz4_raw",
+                                     asbytes=True)) == n
+        except OSError:
+            return False
+
+    rng = np.random.default_rng(2024)
+    raws = [b"", b"a", bytes(12), bytes(13), bytes(range(256)) * 3,
+            rng.integers(0, 256, 5000, dtype=np.uint8).tobytes(),
+            rng.poisson(0.7, 8192).astype(np.uint8).tobytes(),
+            (b"spotfinder" * 1000)[:9999], bytes(70000),
+            rng.integers(0, 4, 100000, dtype=np.uint8).tobytes()]
+    out = {}
+    for k, raw in enumerate(raws):
+        out[f"raw_{k}"] = np.frombuffer(raw, np.uint8)
+        out[f"blk_{k}"] = np.frombuffer(lz4(raw), np.uint8)
+    # Damaged blocks, each with the size it should decode to and whether the
+    # library accepts it: case 7 truncated, with a literal run past the end,
+    # with a byte added; a match reaching before the output's start; a match
+    # into the last 5 bytes; a match whose literals reach the last 12 bytes
+    # of output; a well-formed block of 36 bytes.
+    good = lz4(raws[7])
+    n7 = len(raws[7])
+    bad = [(good[:-1], n7), (b"\xf0\xff\xff" + good[3:], n7), (good + b"\x00", n7),
+           (b"\x40abcd\x09\x00\x50hello", 13), (b"\x40abcd\x04\x00\x00", 8),
+           (b"\x40abcd\x04\x00\x50hello", 13),
+           (b"\xf4\x01" + b"0123456789abcdef" + b"\x04\x00\xc0" + b"tail of bloc", 36)]
+    for k, (blk, n) in enumerate(bad):
+        out[f"bad_{k}"] = np.frombuffer(blk, np.uint8)
+        out[f"bad_n_{k}"] = np.array(n)
+        out[f"bad_ok_{k}"] = np.array(accepted(blk, n))
+    # An "lz4" chunk: 12-byte header, blocks of 4096 bytes.
+    f32 = rng.poisson(1.2, (96, 130)).astype(np.uint32)
+    f32[::17, :] = 0xFFFFFFFF
+    raw = f32.tobytes()
+    parts = [len(raw).to_bytes(8, "big"), (4096).to_bytes(4, "big")]
+    for at in range(0, len(raw), 4096):
+        blk = lz4(raw[at:at + 4096])
+        parts += [len(blk).to_bytes(4, "big"), blk]
+    out["frame_lz4"] = f32
+    out["chunk_lz4"] = np.frombuffer(b"".join(parts), np.uint8)
+    # A "bslz4" chunk: bitshuffle's default 4096-element blocks of a uint16
+    # frame, the last partial block, then 4 elements raw.
+    f16 = rng.poisson(2.0, (101, 84)).astype(np.uint16)
+    f16[:, 40:44] = 0xFFFF
+    e = f16.ravel()
+    bs = 4096
+    nfull, last = e.size // bs, e.size % bs - e.size % bs % 8
+    parts = [(e.size * 2).to_bytes(8, "big"), (bs * 2).to_bytes(4, "big")]
+    for b in range(nfull + (1 if last else 0)):
+        n = bs if b < nfull else last
+        blk = lz4(synth.bitshuffle(e[b * bs:b * bs + n]).tobytes())
+        parts += [len(blk).to_bytes(4, "big"), blk]
+    parts.append(e[nfull * bs + last:].tobytes())
+    out["frame_bslz4"] = f16
+    out["chunk_bslz4"] = np.frombuffer(b"".join(parts), np.uint8)
+    np.savez_compressed(os.path.join(HERE, "lz4_blocks.npz"), **out)
+    return len(raws)
+
+
 if __name__ == "__main__":
+    if sys.argv[1:] == ["lz4"]:
+        print("lz4 cases:", lz4_blocks())
+        sys.exit(0)
     if not O.ref_available():
         O.build(quiet=False)
     if not O.ref_available():

@@ -1,0 +1,308 @@
+"""Frame decompression: decompress::image (src/spots/decompress.cc:77-134)
+for chunks stored bitshuffle+LZ4 ("bslz4"), LZ4 ("lz4") or uncompressed.
+
+The oracle (oracle/sf_oracle_decompress.c) is pinned to the LZ4 library
+itself through tests/golden/lz4_blocks.npz (blocks the library wrote, and
+damaged blocks with whether the library accepts them); bitshuffle's bit
+planes are checked against their definition. The device decoder
+(sf_decompress_image, sf_decompress_device, sf_find_compressed) must give
+the oracle's frame byte for byte, and refuse what the reference refuses with
+the reference's text. Chunks of synthetic frames come from the package's
+chunk writer (synth.chunk), whose blocks the LZ4 library must read."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import GOLDEN
+
+
+def _golden():
+    return np.load(os.path.join(GOLDEN, "lz4_blocks.npz"))
+
+
+def _frame(h, w, dtype, seed, mean=1.0):
+    rng = np.random.default_rng(seed)
+    f = rng.poisson(mean, (h, w)).astype(dtype)
+    top = np.iinfo(dtype).max
+    f[rng.random((h, w)) < 0.01] = top
+    f[rng.random((h, w)) < 0.002] = rng.integers(1000, top - 2, dtype=dtype)
+    return f
+
+
+CHUNKS = [  # shape, dtype, algorithm, block bytes
+    ((1, 1), np.uint32, "bslz4", 0), ((3, 5), np.uint16, "bslz4", 0),
+    ((37, 101), np.uint32, "bslz4", 0), ((64, 64), np.uint16, "bslz4", 0),
+    ((300, 517), np.uint32, "bslz4", 0), ((300, 517), np.uint16, "bslz4", 0),
+    ((257, 300), np.uint32, "bslz4", 4096), ((200, 333), np.uint16, "bslz4", 48),
+    ((211, 190), np.uint32, "bslz4", 32768), ((150, 160), np.uint16, "bslz4", 20000),
+    ((37, 101), np.uint32, "lz4", 0), ((300, 517), np.uint32, "lz4", 8192),
+    ((120, 77), np.uint16, "lz4", 1000), ((5, 5), np.uint32, "", 0),
+]
+
+
+# ---------------------------------------------------------------------------
+# The oracle and the chunk writer, on the CPU.
+# ---------------------------------------------------------------------------
+
+def test_oracle_reads_the_lz4_librarys_blocks():
+    g = _golden()
+    k = 0
+    while f"raw_{k}" in g.files:
+        raw = g[f"raw_{k}"].tobytes()
+        assert O.lz4_decode(g[f"blk_{k}"].tobytes(), len(raw)) == raw, k
+        k += 1
+    assert k == 10
+
+
+def test_oracle_accepts_what_the_lz4_library_accepts():
+    g = _golden()
+    k = 0
+    while f"bad_{k}" in g.files:
+        n = int(g[f"bad_n_{k}"])
+        try:
+            ok = len(O.lz4_decode(g[f"bad_{k}"].tobytes(), n)) == n
+        except ValueError:
+            ok = False
+        assert ok == bool(g[f"bad_ok_{k}"]), k
+        k += 1
+    assert k == 7
+
+
+def test_oracle_reads_chunks_of_the_librarys_blocks():
+    g = _golden()
+    assert np.array_equal(O.decompress_image(g["chunk_lz4"], "lz4", 32, 96, 130),
+                          g["frame_lz4"])
+    assert np.array_equal(O.decompress_image(g["chunk_bslz4"], "bslz4", 16, 101, 84),
+                          g["frame_bslz4"])
+
+
+def test_chunk_writer_blocks_are_read_by_the_lz4_library():
+    pa = pytest.importorskip("pyarrow")
+    from sfgb import synth
+    rng = np.random.default_rng(3)
+    for n in (1, 12, 13, 100, 4096, 8192, 30000):
+        for data in (rng.integers(0, 256, n, dtype=np.uint8).tobytes(), bytes(n),
+                     rng.poisson(0.4, n).astype(np.uint8).tobytes()):
+            blk = synth.lz4_block(data)
+            back = pa.decompress(blk, decompressed_size=n, codec="lz4_raw", asbytes=True)
+            assert back == data
+            assert O.lz4_decode(blk, n) == data
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16, np.uint32, np.uint64])
+def test_bit_planes_are_bitshuffles(dtype):
+    # Plane 8j + k holds bit k of byte j of every element, element i at bit
+    # i % 8 of the plane's byte i / 8.
+    from sfgb import synth
+    rng = np.random.default_rng(4)
+    n = 2056
+    e = rng.integers(0, np.iinfo(dtype).max, n, dtype=dtype, endpoint=True)
+    planes = synth.bitshuffle(e)
+    size = e.itemsize
+    b = e.view(np.uint8).reshape(n, size)
+    for j in range(size):
+        for k in range(8):
+            row = planes[(8 * j + k) * (n // 8):(8 * j + k + 1) * (n // 8)]
+            assert np.array_equal(np.unpackbits(row, bitorder="little"), (b[:, j] >> k) & 1)
+    assert np.array_equal(O.bitunshuffle(planes, n, size).view(dtype), e)
+
+
+def test_bitshuffle_default_block():
+    # 8192 bytes' worth, a multiple of 8, at least 128 elements.
+    assert [O.lib().or_bshuf_default_block(e) for e in (1, 2, 4, 8, 100)] == \
+        [8192, 4096, 2048, 1024, 128]
+
+
+@pytest.mark.parametrize("shape,dtype,alg,block", CHUNKS)
+def test_oracle_round_trip(shape, dtype, alg, block):
+    from sfgb import synth
+    f = _frame(*shape, dtype, seed=shape[0] * 7 + shape[1])
+    data = synth.chunk(f, alg, block) if alg else f.view(np.uint8).ravel()
+    assert np.array_equal(O.decompress_image(data, alg, f.itemsize * 8, *shape), f)
+
+
+def _corrupt_cases():
+    """Chunks the host refuses before any device work, with the reference's
+    text (decompress.cc:80-134)."""
+    from sfgb import synth
+    f = _frame(40, 60, np.uint32, 9)
+    c = synth.chunk(f, "bslz4").tobytes()
+    l4 = synth.chunk(f, "lz4", 1024).tobytes()
+    size = f.nbytes
+    hdr = size.to_bytes(8, "big")
+    return [
+        ("too short", c[:11], "bslz4", 32, "too short for a filter header"),
+        ("header size", (size + 4).to_bytes(8, "big") + c[8:], "bslz4", 32,
+         f"filter header says {size + 4} bytes uncompressed, expected {size}"),
+        ("bit depth", c, "bslz4", 16,
+         f"filter header says {size} bytes uncompressed, expected {size // 2}"),
+        ("unknown", c, "zstd", 32, "unknown compression algorithm zstd"),
+        ("raw size", f.tobytes()[:-4], "", 32,
+         f"uncompressed frame is {size - 4} bytes, expected {size}"),
+        ("lz4 truncated", l4[:12 + 2], "lz4", 32, "lz4 data truncated"),
+        ("lz4 zero block", hdr + (1024).to_bytes(4, "big") + bytes(4), "lz4", 32,
+         "lz4 block size out of range"),
+        ("lz4 block past end", l4[:-1], "lz4", 32, "lz4 block size out of range"),
+        ("bslz4 block size", hdr + (12).to_bytes(4, "big") + c[12:], "bslz4", 32,
+         "bitshuffle decompression failed with code -81"),
+    ]
+
+
+def test_oracle_refusals_are_the_references():
+    for what, data, alg, depth, text in _corrupt_cases():
+        with pytest.raises(RuntimeError) as e:
+            O.decompress_image(np.frombuffer(data, np.uint8), alg, depth, 40, 60)
+        assert str(e.value) == text, what
+
+
+def test_host_refusals_need_no_device():
+    # The chunk's header and framing are checked on the host before any
+    # device work: the C ABI refuses these without a GPU, with the same text.
+    from sfgb import api
+    for what, data, alg, depth, text in _corrupt_cases():
+        with pytest.raises(api.DataError) as e:
+            api.decompress_image(data, alg, depth, 40, 60)
+        assert str(e.value) == text, what
+    assert api.frame_bytes(4362, 4148, 32) == 4362 * 4148 * 4
+    # Bitshuffle chunks of 8-bit pixels are decoded by the reference, not here.
+    from sfgb import synth
+    f8 = np.zeros((8, 8), np.uint8)
+    with pytest.raises(api.SpotFinderError):
+        api.decompress_image(synth.chunk(f8, "bslz4"), "bslz4", 8, 8, 8)
+
+
+def test_uncompressed_host_copy_needs_no_device():
+    from sfgb import api
+    f = _frame(30, 40, np.uint16, 2)
+    assert np.array_equal(api.decompress_image(f.tobytes(), "", 16, 30, 40), f)
+
+
+# ---------------------------------------------------------------------------
+# The device decoder.
+# ---------------------------------------------------------------------------
+
+@pytest.fixture(scope="module")
+def api():
+    from sfgb import api as a
+    if not a.available():
+        pytest.fail("no usable GB300: " + a.unavailable_reason())
+    return a
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,dtype,alg,block", CHUNKS)
+def test_device_decode_matches_the_oracle(api, shape, dtype, alg, block):
+    import torch
+    from sfgb import synth
+    f = _frame(*shape, dtype, seed=shape[0] * 13 + shape[1])
+    data = synth.chunk(f, alg, block) if alg else f.view(np.uint8).ravel()
+    want = O.decompress_image(data, alg, f.itemsize * 8, *shape)
+    assert np.array_equal(want, f)
+    assert np.array_equal(api.decompress_image(data, alg, f.itemsize * 8, *shape), want)
+    d = api.decompress_device(data, alg, f.itemsize * 8, *shape)
+    torch.cuda.synchronize()
+    assert np.array_equal(d.cpu().numpy().view(dtype), want)
+
+
+@pytest.mark.gpu
+def test_device_decodes_the_librarys_chunks(api):
+    g = _golden()
+    assert np.array_equal(api.decompress_image(g["chunk_lz4"], "lz4", 32, 96, 130),
+                          g["frame_lz4"])
+    assert np.array_equal(api.decompress_image(g["chunk_bslz4"], "bslz4", 16, 101, 84),
+                          g["frame_bslz4"])
+    # Each of the library's blocks as a one-block "lz4" chunk of its bytes.
+    k = 0
+    while f"raw_{k}" in g.files:
+        raw = g[f"raw_{k}"]
+        blk = g[f"blk_{k}"].tobytes()
+        if raw.size:
+            chunk = raw.size.to_bytes(8, "big") + bytes(4) + len(blk).to_bytes(4, "big") + blk
+            got = api.decompress_image(chunk, "lz4", 8, 1, raw.size)
+            assert np.array_equal(got, raw), k
+        k += 1
+
+
+@pytest.mark.gpu
+def test_device_accepts_what_the_lz4_library_accepts(api):
+    # The damaged blocks as one-block "lz4" chunks: refused (with the
+    # reference's text) exactly where the library refuses them, and the
+    # context still usable after each refusal.
+    g = _golden()
+    k = 0
+    while f"bad_{k}" in g.files:
+        n = int(g[f"bad_n_{k}"])
+        blk = g[f"bad_{k}"].tobytes()
+        chunk = n.to_bytes(8, "big") + bytes(4) + len(blk).to_bytes(4, "big") + blk
+        if bool(g[f"bad_ok_{k}"]):
+            assert api.decompress_image(chunk, "lz4", 8, 1, n).size == n
+        else:
+            with pytest.raises(api.DataError) as e:
+                api.decompress_image(chunk, "lz4", 8, 1, n)
+            assert str(e.value).startswith("lz4 "), k
+        k += 1
+    f = _frame(20, 30, np.uint32, 5)
+    from sfgb import synth
+    assert np.array_equal(api.decompress_image(synth.chunk(f), "bslz4", 32, 20, 30), f)
+
+
+@pytest.mark.gpu
+def test_device_refuses_a_damaged_bitshuffle_block(api):
+    from sfgb import synth
+    f = _frame(100, 120, np.uint32, 6)
+    c = bytearray(synth.chunk(f).tobytes())
+    c[16:20] = bytes([0xF0, 0xFF, 0xFF, 0xFF])  # the first block: a literal run past its end
+    with pytest.raises(api.DataError) as e:
+        api.decompress_image(bytes(c), "bslz4", 32, 100, 120)
+    assert str(e.value) == "bitshuffle decompression failed with code -91"
+    with pytest.raises(api.DataError):
+        api.find_compressed(bytes(c), "bslz4", 32, 100, 120)
+    assert np.array_equal(api.decompress_image(synth.chunk(f), "bslz4", 32, 100, 120), f)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype,alg,block", [(np.uint32, "bslz4", 0), (np.uint16, "bslz4", 0),
+                                             (np.uint32, "lz4", 65536), (np.uint16, "", 0)])
+def test_find_compressed_matches_the_oracle(api, dtype, alg, block):
+    from sfgb import synth
+    p = synth.preset("eiger_16m", height=700, width=900, n_frames=2, spots_per_frame=150.0,
+                     seed=41)
+    sw = synth.Sweep(p)
+    for i in range(2):
+        f = sw.frame(i)
+        if dtype == np.uint16:
+            g = np.minimum(f, 0xFFFD).astype(np.uint16)
+            g[f == 0xFFFFFFFF] = 0xFFFF
+            f = g
+        data = synth.chunk(f, alg, block) if alg else f.view(np.uint8).ravel()
+        got = api.find_compressed(data, alg, f.itemsize * 8, *f.shape)
+        want = O.dext(f)
+        assert got.tobytes() == want.tobytes(), (alg, i)
+
+
+@pytest.mark.gpu
+def test_find_compressed_with_parameters(api):
+    from sfgb import synth
+    f = _frame(333, 444, np.uint32, 8, mean=3.0)
+    for params in (api.Params(gain=1.5), api.Params(kernel_x=2, kernel_y=2),
+                   api.Params(algorithm=api.DISPERSION)):
+        got = api.find_compressed(synth.chunk(f), "bslz4", 32, 333, 444, params=params)
+        want = O.dext(f, O.Params(algorithm=params.algorithm, kernel_x=params.kernel_x,
+                                  kernel_y=params.kernel_y, gain=params.gain))
+        assert got.tobytes() == want.tobytes()
+
+
+@pytest.mark.gpu
+def test_full_frame_round_trip(api):
+    # A 4362 x 4148 frame: the decoded frame is the frame, and the signal
+    # list from its chunk is the list from the frame itself.
+    from sfgb import synth
+    f = synth.Sweep(synth.preset("eiger_16m", n_frames=1)).frame(0)
+    c = synth.chunk(f)
+    assert c.size * 8 < f.nbytes
+    assert np.array_equal(api.decompress_image(c, "bslz4", 32, *f.shape), f)
+    got = api.find_compressed(c, "bslz4", 32, *f.shape)
+    assert got.tobytes() == api.find(f).tobytes()
+    assert got.tobytes() == O.dext(f).tobytes()
