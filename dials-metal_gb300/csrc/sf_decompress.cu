@@ -2,19 +2,22 @@
 //
 // k_decode gives each block of a chunk to one warp:
 //
-//   LZ4     every lane follows the same parse of the block (its token, length
-//           and offset bytes are the same loads for the whole warp); the
-//           literal runs and matches are copied by the lanes together, 32
-//           bytes apart. A match whose offset is shorter than its length
-//           repeats a pattern of `offset` bytes: it is copied in passes of
-//           D bytes from D bytes back, D doubling from the offset up to 128,
-//           so that no pass reads what it writes.
+//   LZ4     every lane follows the same parse of the block: a sequence's
+//           token, offset and length bytes come from one load of the next 32
+//           input bytes (a byte a lane) by shuffles; the literal runs and
+//           matches are copied by the lanes together, 32 bytes apart. A match
+//           whose offset is shorter than its length repeats a pattern of
+//           `offset` bytes: a one-byte run is filled with 16-byte stores,
+//           other patterns are copied in passes of D bytes from D back, D
+//           doubling from the offset up to 128, so that no pass reads what it
+//           writes.
 //   planes  a bitshuffle block decodes into the warp's 8 KB of shared memory
-//           (bitshuffle's default block is 8192 bytes); a lane then takes 8
-//           elements at a time: for each byte j of an element, the byte of
-//           each of the 8 planes 8j .. 8j + 7 at the group's column forms an
-//           8 x 8 bit matrix whose transpose holds byte j of the 8 elements.
-//           Larger blocks decode into a frame-sized scratch buffer instead.
+//           (bitshuffle's default block is 8192 bytes); for each group of 8
+//           elements and each byte j of an element, the group's byte of each
+//           of the 8 planes 8j .. 8j + 7 forms an 8 x 8 bit matrix whose
+//           transpose holds byte j of the 8 elements. A lane takes 4 groups
+//           at a time, reading each plane's 4 bytes as one word. Larger
+//           blocks decode into a frame-sized scratch buffer instead.
 //
 // The host has already checked the framing (every block lies inside the
 // chunk); the device checks each LZ4 stream as LZ4_decompress_safe does and
@@ -41,12 +44,68 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
 
+// dst[0, n) = v by the warp: bytes up to a 16-byte boundary, 16-byte
+// stores, the bytes after the last whole 16.
+template <typename Out>
+__device__ __forceinline__ void fill_warp(Out *dst, uint8_t v, uint32_t n, int lane) {
+  const uint32_t head = min(n, (uint32_t)(-(uintptr_t)dst & 15u));
+  const uint32_t body = (n - head) & ~15u;
+  if ((uint32_t)lane < head)
+    dst[lane] = v;
+  const uint32_t word = v * 0x01010101u;
+  const uint4 w4 = make_uint4(word, word, word, word);
+  uint4 *body4 = reinterpret_cast<uint4 *>(dst + head);
+  for (uint32_t i = lane; i < body / 16; i += 32)
+    body4[i] = w4;
+  const uint32_t tail = n - head - body;
+  if ((uint32_t)lane < tail)
+    dst[head + body + lane] = v;
+  __syncwarp();
+}
+
+// dst[op, op + ml) = the match at `off` back, by the warp. A match that
+// overlaps what it writes (off < ml) repeats a pattern of `off` bytes: runs
+// of one byte are filled; otherwise it goes in passes of D bytes from D back,
+// D doubling from off up to 128, so that no pass reads what it writes.
+template <typename Out>
+__device__ __forceinline__ void copy_match(Out *dst, uint32_t op, uint32_t off, uint32_t ml,
+                                           int lane) {
+  if (off >= ml) {
+    for (uint32_t i = lane; i < ml; i += 32)
+      dst[op + i] = dst[op - off + i];
+    __syncwarp();
+    return;
+  }
+  if (off == 1) {
+    fill_warp(dst + op, dst[op - 1], ml, lane);
+    return;
+  }
+  uint32_t D = off, done = 0;
+  while (done < ml) {
+    const uint32_t m = min(ml - done, min(D, 128u));
+    Out *to = dst + op + done;
+    for (uint32_t i = lane; i < m; i += 32)
+      to[i] = to[(int)i - (int)D];
+    __syncwarp();
+    done += m;
+    if (m == D && D < 128)
+      D *= 2;
+  }
+}
+
 // One LZ4 block in[0, n) into dst[0, cap) by the whole warp. Returns the
 // bytes produced, or minus (the input position where the stream was found
 // bad) minus 1. The checks are LZ4_decompress_safe's: a literal run that
 // reaches the last 12 bytes of output or the last 8 of input must end the
 // block at the input's end; a match must start inside the output and end
 // before its last 5 bytes.
+//
+// Each sequence starts with one load of the next 32 input bytes, a byte a
+// lane. A sequence whose literal run is under 15 bytes and whose match
+// length needs at most one extra byte (most of them) lies within it: the
+// token, offset and length come by shuffles and the literals are written
+// from the lanes that hold them. Any other sequence, and any that would fail
+// a check, takes the byte-by-byte parse, which reports the error.
 template <typename Out>
 __device__ __forceinline__ long long lz4_warp(const uint8_t *__restrict__ in, uint32_t n,
                                               Out *dst, uint32_t cap, int lane) {
@@ -54,8 +113,36 @@ __device__ __forceinline__ long long lz4_warp(const uint8_t *__restrict__ in, ui
   for (;;) {
     if (ip >= n)
       return -(long long)ip - 1;
-    const uint32_t token = __ldg(in + ip++);
-    uint32_t lit = token >> 4;
+    const uint32_t w = ip + lane < n ? (uint32_t)__ldg(in + ip + lane) : 0u;
+    const uint32_t token = __shfl_sync(~0u, w, 0);
+    const uint32_t lit0 = token >> 4;
+    if (lit0 < 15 && (unsigned long long)op + lit0 + 12 <= cap &&
+        (unsigned long long)ip + lit0 + 9 <= n) {
+      // Not the last sequence: its offset (and a length byte) are in range.
+      const uint32_t off =
+          __shfl_sync(~0u, w, lit0 + 1) | __shfl_sync(~0u, w, lit0 + 2) << 8;
+      const uint32_t e = __shfl_sync(~0u, w, lit0 + 3);
+      uint32_t ml = (token & 15u) + 4u, used = lit0 + 3;
+      bool take = off != 0 && off <= op + lit0;
+      if ((token & 15u) == 15u) {
+        take = take && e != 255u && (unsigned long long)ip + used + 6 <= n;
+        ml += e;
+        used += 1;
+      }
+      take = take && (unsigned long long)op + lit0 + ml + 5 <= cap;
+      if (take) {
+        if ((uint32_t)lane >= 1 && (uint32_t)lane <= lit0)
+          dst[op + lane - 1] = (Out)w;
+        op += lit0;
+        ip += used;
+        __syncwarp();
+        copy_match(dst, op, off, ml, lane);
+        op += ml;
+        continue;
+      }
+    }
+    ip++;
+    uint32_t lit = lit0;
     if (lit == 15) {
       uint32_t s;
       do {
@@ -95,18 +182,7 @@ __device__ __forceinline__ long long lz4_warp(const uint8_t *__restrict__ in, ui
     ml += 4;
     if ((unsigned long long)op + ml + 5 > cap)
       return -(long long)ip - 1;
-    // Passes of m <= D bytes from D back; D = off * 2^k while below 128.
-    uint32_t D = off, done = 0;
-    while (done < ml) {
-      const uint32_t m = min(ml - done, min(D, 128u));
-      Out *to = dst + op + done;
-      for (uint32_t i = lane; i < m; i += 32)
-        to[i] = to[(int)i - (int)D];
-      __syncwarp();
-      done += m;
-      if (m == D && D < 128)
-        D *= 2;
-    }
+    copy_match(dst, op, off, ml, lane);
     op += ml;
   }
 }
@@ -157,6 +233,77 @@ __device__ __forceinline__ void unshuffle(const In *planes, uint32_t n, uint8_t 
   }
 }
 
+// 4 x 4 byte transpose: byte t of out[i] = byte i of in[t].
+__device__ __forceinline__ void bytes4x4(uint32_t a, uint32_t b, uint32_t c, uint32_t d,
+                                         uint32_t out[4]) {
+  const uint32_t ab0 = __byte_perm(a, b, 0x5140), ab1 = __byte_perm(a, b, 0x7362);
+  const uint32_t cd0 = __byte_perm(c, d, 0x5140), cd1 = __byte_perm(c, d, 0x7362);
+  out[0] = __byte_perm(ab0, cd0, 0x5410);
+  out[1] = __byte_perm(ab0, cd0, 0x7632);
+  out[2] = __byte_perm(ab1, cd1, 0x5410);
+  out[3] = __byte_perm(ab1, cd1, 0x7632);
+}
+
+// The 8 x 8 bit transpose of transpose8 on the two halves of x (lo: rows
+// 0-3, hi: rows 4-7): the first two exchanges stay within a half.
+__device__ __forceinline__ void transpose8_halves(uint32_t &lo, uint32_t &hi) {
+  uint32_t t;
+  t = (lo ^ (lo >> 7)) & 0x00AA00AAu;
+  lo ^= t ^ (t << 7);
+  t = (hi ^ (hi >> 7)) & 0x00AA00AAu;
+  hi ^= t ^ (t << 7);
+  t = (lo ^ (lo >> 14)) & 0x0000CCCCu;
+  lo ^= t ^ (t << 14);
+  t = (hi ^ (hi >> 14)) & 0x0000CCCCu;
+  hi ^= t ^ (t << 14);
+  t = (lo ^ (hi << 4)) & 0xF0F0F0F0u;
+  lo ^= t;
+  hi ^= t >> 4;
+}
+
+// unshuffle for planes in shared memory whose rows are whole 32-bit words
+// (n a multiple of 32): a lane takes 4 groups (32 elements) at a time, the
+// 8 planes of each element byte read as one word each.
+template <int E>
+__device__ __forceinline__ void unshuffle_words(const uint8_t *planes, uint32_t n, uint8_t *dst,
+                                                int lane) {
+  const uint32_t row = n >> 3;
+  for (uint32_t q = lane; q < row / 4; q += 32) {
+    uint32_t lo[E][4], hi[E][4];
+#pragma unroll
+    for (int j = 0; j < E; j++) {
+      uint32_t w[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++)
+        w[k] = *reinterpret_cast<const uint32_t *>(planes + (8 * j + k) * row + 4 * q);
+      bytes4x4(w[0], w[1], w[2], w[3], lo[j]);
+      bytes4x4(w[4], w[5], w[6], w[7], hi[j]);
+#pragma unroll
+      for (int t = 0; t < 4; t++)
+        transpose8_halves(lo[j][t], hi[j][t]);
+    }
+    // Group 4q + t: byte t' of lo[j][t] (hi for t' >= 4) is byte j of its
+    // element t'.
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      if (E == 4) {
+        uint32_t a[4], b[4];
+        bytes4x4(lo[0][t], lo[1 % E][t], lo[2 % E][t], lo[3 % E][t], a);
+        bytes4x4(hi[0][t], hi[1 % E][t], hi[2 % E][t], hi[3 % E][t], b);
+        uint4 *o = reinterpret_cast<uint4 *>(dst + 32 * (size_t)(4 * q + t));
+        o[0] = make_uint4(a[0], a[1], a[2], a[3]);
+        o[1] = make_uint4(b[0], b[1], b[2], b[3]);
+      } else {
+        *reinterpret_cast<uint4 *>(dst + 16 * (size_t)(4 * q + t)) =
+            make_uint4(__byte_perm(lo[0][t], lo[1 % E][t], 0x5140),
+                       __byte_perm(lo[0][t], lo[1 % E][t], 0x7362),
+                       __byte_perm(hi[0][t], hi[1 % E][t], 0x5140),
+                       __byte_perm(hi[0][t], hi[1 % E][t], 0x7362));
+      }
+    }
+  }
+}
+
 __device__ __forceinline__ void report(uint32_t *status, uint32_t kind, uint32_t block,
                                        long long code, int lane) {
   if (lane == 0 && atomicCAS(status, 0u, kind) == 0u) {
@@ -196,8 +343,12 @@ k_decode(const uint8_t *__restrict__ in, const DecodeBlock *__restrict__ blocks,
     long long r;
     if (d.out_bytes <= kDecBuf) {
       r = lz4_warp(src, d.in_bytes, buf[warp], d.out_bytes, lane);
-      if (r == (long long)d.out_bytes)
-        unshuffle<E>(buf[warp], d.elems, dst, lane);
+      if (r == (long long)d.out_bytes) {
+        if (d.elems % 32 == 0)
+          unshuffle_words<E>(buf[warp], d.elems, dst, lane);
+        else
+          unshuffle<E>(buf[warp], d.elems, dst, lane);
+      }
     } else {
       uint8_t *tmp = scratch + d.out_off;
       r = lz4_warp(src, d.in_bytes, tmp, d.out_bytes, lane);
@@ -338,8 +489,9 @@ cudaError_t launch_decode(const uint8_t *d_payload, const DecodeBlock *d_blocks,
                           uint32_t *d_status, cudaStream_t stream) {
   if (nblocks == 0)
     return cudaSuccess;
+  // One wave: the shared buffers allow 6 blocks of 4 warps an SM.
   const size_t want = (nblocks + kDecWarps - 1) / kDecWarps;
-  const int grid = (int)std::min<size_t>(want, (size_t)device_sms() * 16);
+  const int grid = (int)std::min<size_t>(want, (size_t)device_sms() * 6);
   if (element == 2)
     k_decode<2><<<grid, kDecWarps * 32, 0, stream>>>(d_payload, d_blocks, (uint32_t)nblocks,
                                                      d_frame, d_scratch, d_status);
