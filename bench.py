@@ -722,7 +722,7 @@ def main(argv=None):
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--e2e-threads", type=int, default=4)
+    ap.add_argument("--e2e-threads", type=int, default=8)
     ap.add_argument("--no-label", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-u16", action="store_true")
