@@ -16,6 +16,7 @@
 #include "sf_api.h"
 #include "sf_common.cuh"
 #include "sf_decompress.cuh"
+#include "sf_frames.cuh"
 #include "sf_scan.cuh"
 #include "sf_stream.cuh"
 #include "sf_threshold.cuh"
@@ -298,6 +299,7 @@ public:
     if (host_count_)
       cudaFreeHost(host_count_);
     cudaFree(chunk_);
+    cudaFree(narrow_);
     cudaFree(table_);
     cudaFree(scratch_);
     if (table_host_)
@@ -310,12 +312,26 @@ public:
       return SF_OK;
     if ((e = cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking)) != cudaSuccess)
       return fail(e, "cudaStreamCreate");
-    // The count and the decoder's error record: 4 words on both sides.
-    if ((e = cudaMalloc(&count_, 4 * sizeof(uint32_t))) != cudaSuccess)
+    // The small results read back: the count (word 0), the decoder's error
+    // record (1-3), the narrowing's largest value (4), a frame scan (words
+    // 6-13, four 64-bit counts); the same layout on both sides.
+    if ((e = cudaMalloc(&count_, kWords * sizeof(uint32_t))) != cudaSuccess)
       return fail(e, "cudaMalloc for the count");
-    if ((e = cudaMallocHost(&host_count_, 4 * sizeof(uint32_t))) != cudaSuccess)
+    if ((e = cudaMallocHost(&host_count_, kWords * sizeof(uint32_t))) != cudaSuccess)
       return fail(e, "cudaMallocHost for the count");
     return SF_OK;
+  }
+
+  static constexpr int kWords = 16, kWorst = 4, kScan = 6;
+  unsigned long long *scan_words() {
+    return reinterpret_cast<unsigned long long *>(count_ + kScan);
+  }
+  const unsigned long long *host_scan_words() const {
+    return reinterpret_cast<const unsigned long long *>(host_count_ + kScan);
+  }
+
+  int reserve_narrow(size_t bytes) {
+    return grow(&narrow_, &narrow_cap_, bytes, "cudaMalloc for the narrowed frame");
   }
 
   int reserve_image(size_t bytes) {
@@ -461,6 +477,8 @@ public:
   uint32_t *count_ = nullptr;
   uint32_t *host_count_ = nullptr;
   uint8_t *chunk_ = nullptr, *scratch_ = nullptr;
+  uint16_t *narrow_ = nullptr;
+  size_t narrow_cap_ = 0;
   DecodeBlock *table_ = nullptr;
   void *table_host_ = nullptr;
   size_t image_cap_ = 0, bits_cap_ = 0, ws_cap_ = 0, out_cap_ = 0;
@@ -483,11 +501,15 @@ struct StreamGuard {
 };
 
 // One host frame thresholded; with a chunk plan, `image` is the chunk and
-// only it crosses the host link, decoded on the device.
+// only it crosses the host link, decoded on the device. With `narrow` (T is
+// uint16_t) the frame is 32-bit and is narrowed to 16 bits on the device
+// before the threshold (--gpu-force, find_spots.cc:781-795); a frame with a
+// valid count at or above 0xFFFD is refused with *offending set.
 template <typename T>
 static int find_host(const void *image, size_t h, size_t w,
                      const sf_threshold_params *params, sf_signal_pixel *out,
-                     size_t capacity, size_t *found, const ChunkPlan *plan = nullptr) {
+                     size_t capacity, size_t *found, const ChunkPlan *plan = nullptr,
+                     bool narrow = false, uint32_t *offending = nullptr) {
   if (found)
     *found = 0;
   if (!image || !found || (!out && capacity) || !shape_ok(h, w))
@@ -498,7 +520,7 @@ static int find_host(const void *image, size_t h, size_t w,
   int rc = make_launch_params(params, &P);
   if (rc != SF_OK)
     return rc;
-  const size_t bytes = h * w * sizeof(T);
+  const size_t bytes = h * w * (narrow ? sizeof(uint32_t) : sizeof(T));
   // The device list needs at least one record for the kernels' pointers.
   const size_t dcap = capacity ? capacity : 1;
   Workspace &ws = workspace();
@@ -506,6 +528,8 @@ static int find_host(const void *image, size_t h, size_t w,
     return rc;
   const bool decode = plan && plan->algorithm != kChunkNone;
   if (decode && (rc = ws.reserve_decode(*plan)) != SF_OK)
+    return rc;
+  if (narrow && (rc = ws.reserve_narrow(h * w * sizeof(uint16_t))) != SF_OK)
     return rc;
   const cudaStream_t stream = ws.stream_;
   StreamGuard idle{stream};
@@ -522,11 +546,19 @@ static int find_host(const void *image, size_t h, size_t w,
              cudaSuccess) {
     return fail(e, "copying a frame to the device");
   }
+  const T *frame = static_cast<const T *>(ws.image_);
+  if (narrow) {
+    if ((e = launch_narrow(static_cast<const uint32_t *>(ws.image_), h * w, ws.narrow_,
+                           ws.count_ + Workspace::kWorst, stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(ws.host_count_ + Workspace::kWorst, ws.count_ + Workspace::kWorst,
+                             sizeof(uint32_t), cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
+      return fail(e, "narrowing the frame to 16 bits");
+    frame = reinterpret_cast<const T *>(ws.narrow_);
+  }
   if (timing)
     cudaEventRecord(marks[1], stream);
-  rc = threshold_device<T>(static_cast<const T *>(ws.image_), h, w, params, ws.out_,
-                           dcap, ws.bits_, ws.count_, nullptr, ws.ws_, ws.ws_cap_,
-                           stream);
+  rc = threshold_device<T>(frame, h, w, params, ws.out_, dcap, ws.bits_, ws.count_, nullptr,
+                           ws.ws_, ws.ws_cap_, stream);
   if (rc != SF_OK)
     return rc;
   if (timing)
@@ -538,6 +570,15 @@ static int find_host(const void *image, size_t h, size_t w,
     return fail(e, "cudaStreamSynchronize");
   if (decode && (rc = ws.decoded(*plan)) != SF_OK)
     return rc;
+  if (narrow) {
+    const uint32_t worst = ws.host_count_[Workspace::kWorst];
+    if (offending)
+      *offending = worst;
+    if (worst >= 0xFFFDu) {  // narrow_to_16's test (find_spots.cc:181)
+      t_last_error = "a count of " + std::to_string(worst) + ", too large for 16 bits";
+      return SF_EDATA;
+    }
+  }
   const size_t n = *ws.host_count_;
   *found = n;
   sf_stage_times times = {0, 0, 0, 0, 0, 0, 0};
@@ -748,6 +789,92 @@ int sf_find_compressed(const uint8_t *data, size_t nbytes, const char *algorithm
   return bit_depth == 16
              ? find_host<uint16_t>(data, height, width, params, out, capacity, found, &plan)
              : find_host<uint32_t>(data, height, width, params, out, capacity, found, &plan);
+}
+
+int sf_find_narrowed(const uint8_t *data, size_t nbytes, const char *algorithm, size_t height,
+                     size_t width, const sf_threshold_params *params, sf_signal_pixel *out,
+                     size_t capacity, size_t *found, uint32_t *offending) {
+  if (found)
+    *found = 0;
+  if (offending)
+    *offending = 0;
+  if (!data || !found || (!out && capacity) || !shape_ok(height, width))
+    return SF_EBADARG;
+  ChunkPlan plan;
+  int rc = plan_chunk(data, nbytes, algorithm, 32, height, width, height * width * 4, &plan);
+  if (rc != SF_OK)
+    return rc;
+  return find_host<uint16_t>(data, height, width, params, out, capacity, found, &plan, true,
+                             offending);
+}
+
+int sf_scan_device(const void *d_image, size_t n_pixels, unsigned bit_depth,
+                   sf_frame_scan *out) {
+  if ((!d_image && n_pixels) || !out || (bit_depth != 16 && bit_depth != 32) ||
+      n_pixels > 0x7fffffffu)
+    return SF_EBADARG;
+  if (n_pixels == 0) {
+    *out = {0, 0, 0, 0};
+    return SF_OK;
+  }
+  Workspace &ws = workspace();
+  int rc = ws.open();
+  if (rc != SF_OK)
+    return rc;
+  const cudaStream_t stream = ws.stream_;
+  StreamGuard idle{stream};
+  cudaError_t e;
+  if ((e = launch_scan(d_image, n_pixels, bit_depth, ws.scan_words(), stream)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(ws.host_count_ + Workspace::kScan, ws.scan_words(),
+                           4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(stream)) != cudaSuccess)
+    return fail(e, "scanning the frame");
+  const unsigned long long *r = ws.host_scan_words();
+  *out = {r[0], r[1], r[2], r[3]};
+  return SF_OK;
+}
+
+int sf_scan_compressed(const uint8_t *data, size_t nbytes, const char *algorithm,
+                       unsigned bit_depth, size_t height, size_t width, sf_frame_scan *out) {
+  if (!data || !out || !shape_ok(height, width))
+    return SF_EBADARG;
+  if (bit_depth != 16 && bit_depth != 32) {
+    t_last_error = std::to_string(bit_depth) + "-bit pixels";  // mxi_max.cc:165-166
+    return SF_EUNSUPPORTED;
+  }
+  ChunkPlan plan;
+  const size_t bytes = height * width * bit_depth / 8;
+  int rc = plan_chunk(data, nbytes, algorithm, bit_depth, height, width, bytes, &plan);
+  if (rc != SF_OK)
+    return rc;
+  Workspace &ws = workspace();
+  if ((rc = ws.reserve_image(bytes)) != SF_OK)
+    return rc;
+  const cudaStream_t stream = ws.stream_;
+  StreamGuard idle{stream};
+  cudaError_t e;
+  const bool decode = plan.algorithm != kChunkNone;
+  if (decode) {
+    if ((rc = ws.reserve_decode(plan)) != SF_OK ||
+        (rc = ws.decode(data, plan, static_cast<uint8_t *>(ws.image_))) != SF_OK)
+      return rc;
+  } else if ((e = cudaMemcpyAsync(ws.image_, data, bytes, cudaMemcpyHostToDevice, stream)) !=
+             cudaSuccess) {
+    return fail(e, "copying a frame to the device");
+  }
+  if ((e = launch_scan(ws.image_, height * width, bit_depth, ws.scan_words(), stream)) !=
+          cudaSuccess ||
+      (e = cudaMemcpyAsync(ws.host_count_ + Workspace::kScan, ws.scan_words(),
+                           4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(stream)) != cudaSuccess)
+    return fail(e, "scanning the frame");
+  if (decode && (rc = ws.decoded(plan)) != SF_OK)
+    return rc;
+  const unsigned long long *r = ws.host_scan_words();
+  *out = {r[0], r[1], r[2], r[3]};
+  return SF_OK;
 }
 
 void sf_profile_stages(int on) { g_profiling = on != 0; }

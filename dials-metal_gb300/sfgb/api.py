@@ -36,6 +36,11 @@ class ThresholdParams(ctypes.Structure):
                 ("min_local", ctypes.c_int), ("global_threshold", ctypes.c_double)]
 
 
+class FrameScan(ctypes.Structure):
+    _fields_ = [("largest", ctypes.c_uint64), ("bad", ctypes.c_uint64),
+                ("joins", ctypes.c_uint64), ("over", ctypes.c_uint64)]
+
+
 class StageTimes(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in
                 ("upload", "stage0", "stage1", "stage2", "fused", "copy", "sort")]
@@ -133,6 +138,15 @@ def lib() -> ctypes.CDLL:
                                          ctypes.POINTER(ThresholdParams), vp, sz,
                                          ctypes.POINTER(sz)]
         L.sf_find_compressed.restype = ctypes.c_int
+        L.sf_find_narrowed.argtypes = [vp, sz, ctypes.c_char_p, sz, sz,
+                                       ctypes.POINTER(ThresholdParams), vp, sz,
+                                       ctypes.POINTER(sz), ctypes.POINTER(ctypes.c_uint32)]
+        L.sf_find_narrowed.restype = ctypes.c_int
+        L.sf_scan_device.argtypes = [vp, sz, ctypes.c_uint, ctypes.POINTER(FrameScan)]
+        L.sf_scan_device.restype = ctypes.c_int
+        L.sf_scan_compressed.argtypes = [vp, sz, ctypes.c_char_p, ctypes.c_uint, sz, sz,
+                                         ctypes.POINTER(FrameScan)]
+        L.sf_scan_compressed.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -271,6 +285,63 @@ def find_compressed(data, algorithm: str, bit_depth: int, height: int, width: in
                                   capacity, ctypes.byref(found))
     _check_chunk(rc, "threshold")
     return out[:found.value].copy()
+
+
+class NarrowError(DataError):
+    """A 32-bit frame with a valid count too large for 16 bits (the
+    reference's --gpu-force refusal, src/spots/find_spots.cc:786-792)."""
+
+    def __init__(self, message: str, offending: int):
+        super().__init__(message)
+        self.offending = offending
+
+
+def find_narrowed(data, algorithm: str, height: int, width: int,
+                  params: Params | None = None, capacity: int | None = None) -> np.ndarray:
+    """--gpu-force on the device (sf_find_narrowed): a 32-bit frame or chunk
+    narrowed to 16 bits (narrow_to_16) and thresholded as a 16-bit frame.
+    Raises NarrowError (with .offending) for counts of 0xFFFD or more."""
+    buf = _chunk_bytes(data)
+    if capacity is None:
+        capacity = max(1, height * width * 4 // 16)
+    out = np.empty(capacity, SIGNAL_DTYPE)
+    found = ctypes.c_size_t(0)
+    worst = ctypes.c_uint32(0)
+    p = params.c() if params is not None else None
+    rc = lib().sf_find_narrowed(buf.ctypes.data if buf.size else None, buf.size,
+                                algorithm.encode(), height, width,
+                                ctypes.byref(p) if p is not None else None, out.ctypes.data,
+                                capacity, ctypes.byref(found), ctypes.byref(worst))
+    if rc == SF_EDATA and worst.value >= 0xFFFD:
+        raise NarrowError(last_error(), worst.value)
+    _check_chunk(rc, "threshold")
+    return out[:found.value].copy()
+
+
+def _scan_tuple(s: "FrameScan") -> tuple:
+    return (int(s.largest), int(s.bad), int(s.joins), int(s.over))
+
+
+def scan_device(frame) -> tuple:
+    """mxi_max's scan<T> (apps/mxi_max.cc:47-67) of a device frame (a torch
+    int16/int32 tensor holding 16- or 32-bit pixels): (largest non-marker
+    count, bad pixels, tile joins, valid pixels at 0xFFFD or above)."""
+    depth = frame.element_size() * 8
+    s = FrameScan()
+    _check(lib().sf_scan_device(frame.data_ptr(), frame.numel(), depth, ctypes.byref(s)),
+           "scan")
+    return _scan_tuple(s)
+
+
+def scan_compressed(data, algorithm: str, bit_depth: int, height: int, width: int) -> tuple:
+    """mxi_max's worker step (decompress::image, then scan<T>) with the chunk
+    decoded and scanned on the device."""
+    buf = _chunk_bytes(data)
+    s = FrameScan()
+    rc = lib().sf_scan_compressed(buf.ctypes.data if buf.size else None, buf.size,
+                                  algorithm.encode(), bit_depth, height, width, ctypes.byref(s))
+    _check_chunk(rc, "scan")
+    return _scan_tuple(s)
 
 
 def profile_stages(on: bool) -> None:

@@ -15,7 +15,7 @@ from concurrent.futures import ThreadPoolExecutor
 from . import _paths
 
 CUDA_SOURCES = ["sf_threshold.cu", "sf_stream.cu", "sf_lattice.cu", "sf_api.cu", "sf_label.cu",
-                "sf_serve.cu", "sf_refl.cu", "sf_decompress.cu"]
+                "sf_serve.cu", "sf_refl.cu", "sf_decompress.cu", "sf_frames.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               # No FMA contraction anywhere: the FP64/FP32 decisions must round

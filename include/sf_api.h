@@ -135,6 +135,35 @@ int sf_find_compressed(const uint8_t *data, size_t nbytes, const char *algorithm
                        const sf_threshold_params *params, sf_signal_pixel *out,
                        size_t capacity, size_t *found);
 
+/*
+ * --gpu-force on the device (find_spots.cc:781-795): a 32-bit frame (a chunk
+ * as above, or "" with the raw frame) decoded, narrowed to 16 bits as
+ * narrow_to_16 does (find_spots.cc:169-182: each value's low 16 bits) and
+ * thresholded as a 16-bit frame. *offending receives the largest valid
+ * count; at or above 0xFFFD the frame is refused with -6 (SF_EDATA), the
+ * reference's "too large for 16 bits" refusal.
+ */
+int sf_find_narrowed(const uint8_t *data, size_t nbytes, const char *algorithm, size_t height,
+                     size_t width, const sf_threshold_params *params, sf_signal_pixel *out,
+                     size_t capacity, size_t *found, uint32_t *offending);
+
+/*
+ * mxi_max's scan<T> (apps/mxi_max.cc:47-67) on the device: the largest
+ * count on a valid pixel (not max() - 1, a bad pixel, nor max(), a tile
+ * join), how many pixels are each marker, and how many valid pixels are at
+ * 0xFFFD or above. sf_scan_device scans a 16- or 32-bit frame in device
+ * memory; sf_scan_compressed is mxi_max's worker step (decompress::image,
+ * then scan<T>) with the chunk decoded on the device. Both return when *out
+ * is written.
+ */
+typedef struct {
+  uint64_t largest, bad, joins, over;
+} sf_frame_scan;
+int sf_scan_device(const void *d_image, size_t n_pixels, unsigned bit_depth,
+                   sf_frame_scan *out);
+int sf_scan_compressed(const uint8_t *data, size_t nbytes, const char *algorithm,
+                       unsigned bit_depth, size_t height, size_t width, sf_frame_scan *out);
+
 /* Replaces gpu::profile_stages / gpu::last_stage_times
  * (src/spots/dext_gpu.hh:89-127). Times in milliseconds for the calling
  * thread's last profiled call (host frame, device frame or batch, all its

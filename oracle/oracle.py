@@ -62,7 +62,8 @@ class Params:
 def build(quiet: bool = True) -> None:
     """Compile the oracle restatement (always) and the reference library (only
     where the reference tree exists)."""
-    srcs = [os.path.join(HERE, f) for f in ("sf_oracle.c", "sf_oracle_decompress.c")]
+    srcs = [os.path.join(HERE, f) for f in ("sf_oracle.c", "sf_oracle_decompress.c",
+                                            "sf_oracle_frames.c")]
     tmp = LIB_PATH + ".tmp"
     subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
                     *srcs, "-o", tmp, "-lm"], check=True)
@@ -109,6 +110,10 @@ def lib() -> ctypes.CDLL:
         L.or_decompress_image.argtypes = [vp, sz, ctypes.c_char_p, ctypes.c_uint, sz, sz, vp,
                                           sz, ctypes.c_char_p, sz]
         L.or_decompress_image.restype = ctypes.c_int
+        for name in ("or_scan_u16", "or_scan_u32"):
+            getattr(L, name).argtypes = [vp, sz, vp]
+        L.or_narrow_to_16.argtypes = [vp, sz, vp, vp]
+        L.or_narrow_to_16.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -223,6 +228,29 @@ def bitunshuffle(planes: np.ndarray, n: int, esize: int) -> np.ndarray:
     out = np.zeros(n * esize, np.uint8)
     lib().or_bitunshuffle(_ptr(planes), _ptr(out), n, esize)
     return out
+
+
+def scan_frame(frame: np.ndarray) -> tuple:
+    """mxi_max's scan<T> (apps/mxi_max.cc:47-67) of a uint16 or uint32
+    frame: (largest non-marker value, bad pixels, tile joins, valid pixels
+    at 0xFFFD or above)."""
+    frame = np.ascontiguousarray(frame)
+    out = np.zeros(4, np.uint64)
+    fn = lib().or_scan_u32 if frame.dtype == np.uint32 else lib().or_scan_u16
+    if frame.dtype not in (np.uint16, np.uint32):
+        raise TypeError("frames are uint16 or uint32")
+    fn(_ptr(frame), frame.size, _ptr(out))
+    return tuple(int(x) for x in out)
+
+
+def narrow_to_16(frame: np.ndarray):
+    """find_spots.cc:169-182: (the frame truncated to 16 bits, the largest
+    non-marker value, whether it is below 0xFFFD)."""
+    frame = np.ascontiguousarray(frame, np.uint32)
+    out = np.empty(frame.shape, np.uint16)
+    worst = ctypes.c_uint32(0)
+    ok = lib().or_narrow_to_16(_ptr(frame), frame.size, _ptr(out), ctypes.byref(worst))
+    return out, worst.value, bool(ok)
 
 
 def ref_dext(frame: np.ndarray) -> np.ndarray:

@@ -116,6 +116,13 @@ int or_decompress_image(const uint8_t *data, size_t n, const char *algorithm,
                         unsigned bit_depth, size_t height, size_t width, uint8_t *out,
                         size_t out_bytes, char *err, size_t err_cap);
 
+/* Frame scans (sf_oracle_frames.c): mxi_max's scan<T> (apps/mxi_max.cc:47-67)
+ * into out = {largest, bad, joins, over}, and find_spots.cc:169-182's
+ * narrow_to_16. */
+void or_scan_u16(const uint16_t *pixels, size_t n, uint64_t out[4]);
+void or_scan_u32(const uint32_t *pixels, size_t n, uint64_t out[4]);
+int or_narrow_to_16(const uint32_t *in, size_t n, uint16_t *out, uint32_t *offending);
+
 #ifdef __cplusplus
 }
 #endif

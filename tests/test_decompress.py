@@ -306,3 +306,77 @@ def test_full_frame_round_trip(api):
     got = api.find_compressed(c, "bslz4", 32, *f.shape)
     assert got.tobytes() == api.find(f).tobytes()
     assert got.tobytes() == O.dext(f).tobytes()
+    # mxi_max's scan of the chunk, and --gpu-force on it (its counts fit).
+    assert api.scan_compressed(c, "bslz4", 32, *f.shape) == O.scan_frame(f)
+    narrowed, worst, ok = O.narrow_to_16(f)
+    assert ok
+    got = api.find_narrowed(c, "bslz4", *f.shape)
+    assert got.tobytes() == O.dext(narrowed).tobytes()
+
+
+# ---------------------------------------------------------------------------
+# mxi_max's scan and the --gpu-force narrowing, on the device.
+# ---------------------------------------------------------------------------
+
+def test_scan_oracle_known_answers():
+    # Markers are max() - 1 (bad) and max() (tile join); 0xFFFD and above
+    # valid counts are "over" (apps/mxi_max.cc:47-67).
+    f = np.array([[1, 2, 0xFFFFFFFE, 0xFFFFFFFF], [70000, 0xFFFD, 5, 0]], np.uint32)
+    assert O.scan_frame(f) == (70000, 1, 1, 2)
+    g = np.array([[1, 0xFFFE, 0xFFFF, 0xFFFF], [0xFFFD, 7, 0, 0xFFFC]], np.uint16)
+    assert O.scan_frame(g) == (0xFFFD, 1, 2, 1)
+    n, worst, ok = O.narrow_to_16(f)
+    assert (worst, ok) == (70000, False)
+    assert n.ravel().tolist() == [1, 2, 0xFFFE, 0xFFFF, 70000 & 0xFFFF, 0xFFFD, 5, 0]
+    assert O.narrow_to_16(np.array([0xFFFC, 0xFFFFFFFF], np.uint32))[1:] == (0xFFFC, True)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", [np.uint16, np.uint32])
+def test_scan_matches_the_oracle(api, dtype):
+    import torch
+    from sfgb import synth
+    for h, w, seed in ((1, 1, 1), (3, 7, 2), (257, 301, 3), (1000, 1030, 4)):
+        f = _frame(h, w, dtype, seed, mean=4.0)
+        if f.size > 10:
+            f.ravel()[5] = np.iinfo(dtype).max - 1
+            f.ravel()[-3] = 0xFFFD if dtype == np.uint16 else 123456
+        want = O.scan_frame(f)
+        view = np.int16 if dtype == np.uint16 else np.int32
+        d = torch.from_numpy(f.view(view)).cuda()
+        assert api.scan_device(d) == want
+        assert api.scan_device(d.view(-1)[1:]) == O.scan_frame(f.ravel()[1:])  # unaligned
+        c = synth.chunk(f) if f.size >= 8 else f.view(np.uint8).ravel()
+        alg = "bslz4" if f.size >= 8 else ""
+        assert api.scan_compressed(c, alg, f.itemsize * 8, h, w) == want
+
+
+@pytest.mark.gpu
+def test_narrowed_threshold_matches_the_oracle(api):
+    # --gpu-force: the 32-bit frame narrowed as narrow_to_16 narrows it, then
+    # the 16-bit threshold (the reference's float tests).
+    from sfgb import synth
+    p = synth.preset("eiger_16m", height=600, width=800, n_frames=1, spots_per_frame=80.0,
+                     seed=77)
+    f = synth.Sweep(p).frame(0)
+    f = np.where(f >= 0xFFFFFFFE, f, np.minimum(f, 0xFFFC)).astype(np.uint32)
+    narrowed, worst, ok = O.narrow_to_16(f)
+    assert ok
+    want = O.dext(narrowed)
+    for alg in ("", "bslz4", "lz4"):
+        data = synth.chunk(f, alg, 65536) if alg else f.view(np.uint8).ravel()
+        got = api.find_narrowed(data, alg, *f.shape)
+        assert got.tobytes() == want.tobytes(), alg
+
+
+@pytest.mark.gpu
+def test_narrowed_threshold_refuses_large_counts(api):
+    from sfgb import synth
+    f = np.minimum(_frame(100, 128, np.uint32, 12), 0xFFFC)
+    f[50, 60] = 0xFFFD
+    with pytest.raises(api.NarrowError) as e:
+        api.find_narrowed(synth.chunk(f), "bslz4", 100, 128)
+    assert e.value.offending == 0xFFFD
+    f[50, 60] = 0xFFFC
+    got = api.find_narrowed(synth.chunk(f), "bslz4", 100, 128)
+    assert got.tobytes() == O.dext(O.narrow_to_16(f)[0]).tobytes()
