@@ -10,8 +10,8 @@
 //              non-marker value, which must be below 0xFFFD.
 //
 // Both read the frame once with 16-byte loads, four in flight a thread (a
-// grid-stride loop over 8 blocks an SM), reduce within each warp and combine
-// with one atomic per warp: HBM-bound passes.
+// grid-stride loop over one wave of blocks), reduce within each warp and
+// combine with one atomic per warp: HBM-bound passes.
 
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -141,7 +141,8 @@ k_narrow(const uint32_t *__restrict__ in, size_t n, bool vec, uint16_t *__restri
     atomicMax(worst, best);
 }
 
-int scan_grid() { return device_sms() * 8; }
+// One wave: 56 registers a thread leave room for 4 blocks of 256 an SM.
+int scan_grid() { return device_sms() * 4; }
 
 }  // namespace
 
