@@ -225,12 +225,13 @@ SERVED_DETECTORS = {
 }
 
 
-def served(seconds: float = 4.0, seed: int = 4000, rates=None) -> dict:
+def served(seconds: float = 4.0, seed: int = 4000, rates=None, chunks: bool = False) -> dict:
     """The served form on the mixed-detector workload: six sweeps (16M, 16M,
     9M, 4M, 4M, 1M) arriving at once, each with Poisson frame arrivals at a
     rate drawn from 100-750 Hz, submitted as they arrive from pinned host
-    frames; every frame thresholded and labelled. p50/p99 are submit-to-
-    labelled latencies over all frames."""
+    frames (with `chunks`, as bitshuffle+LZ4 chunks decoded on the device);
+    every frame thresholded and labelled. p50/p99 are submit-to-labelled
+    latencies over all frames."""
     import ctypes
     from sfgb import api, serve, synth
     L = api.lib()
@@ -244,10 +245,10 @@ def served(seconds: float = 4.0, seed: int = 4000, rates=None) -> dict:
         pool = []
         for i in range(4):
             f = sw.frame(i)
-            ptr = L.sf_host_alloc(f.nbytes)
-            arr = np.ctypeslib.as_array((ctypes.c_uint32 * f.size).from_address(ptr))
-            arr[:] = f.ravel()
-            pool.append(ptr)
+            data = synth.chunk(f) if chunks else f.view(np.uint8).ravel()
+            ptr = L.sf_host_alloc(data.size)
+            np.ctypeslib.as_array((ctypes.c_uint8 * data.size).from_address(ptr))[:] = data
+            pool.append((ptr, data.size))
             ptrs.append(ptr)
         pools[k] = pool
     srv = serve.Server(max_batch=16, ring=32)
@@ -269,7 +270,11 @@ def served(seconds: float = 4.0, seed: int = 4000, rates=None) -> dict:
             # The pool repeats every 4 frames: a gap in the frame numbers at
             # each repeat closes every spot there (dials_spots.cc:65-69), as
             # spots end in a real sweep, instead of stitching the repeats.
-            srv.submit(ids[i], n + n // 4, pools[kinds[i]][n % 4])
+            ptr, nbytes = pools[kinds[i]][n % 4]
+            if chunks:
+                srv.submit_chunk(ids[i], n + n // 4, ptr, "bslz4", nbytes)
+            else:
+                srv.submit(ids[i], n + n // 4, ptr)
 
     last = [0.0]
 
@@ -312,14 +317,19 @@ def served(seconds: float = 4.0, seed: int = 4000, rates=None) -> dict:
         by[k] = {"frames": int(len(sel)), "p50_ms": float(np.percentile(sel, 50)),
                  "p99_ms": float(np.percentile(sel, 99))}
     offered = float(sum(rates))
+    link = sum(len(arrivals[i]) * (pools[kinds[i]][0][1] if chunks else
+                                   SERVED_DETECTORS[kinds[i]][1] * SERVED_DETECTORS[kinds[i]][2] * 4)
+               for i in range(len(kinds))) / seconds / 1e9
     return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "frames": int(len(lat)), "frames_per_s": len(lat) / wall,
             "offered_frames_per_s": offered, "errors": bad, "spots": spots,
+            "host_link_gbs_offered": link,
             "server": stats,
             "by_detector": by,
             "workload": "6 concurrent sweeps (16M, 16M, 9M, 4M, 4M, 1M), Poisson arrivals at "
                         + ", ".join(f"{r:.0f}" for r in rates) + f" Hz for {seconds:.0f} s, "
-                        "threshold and 3-D labelling of every frame (sf_server_*)"}
+                        + ("as bitshuffle+LZ4 chunks (sf_server_submit_chunk), " if chunks else "")
+                        + "threshold and 3-D labelling of every frame (sf_server_*)"}
 
 
 def run_ours(args):
@@ -654,10 +664,16 @@ def run_ours(args):
         torch.cuda.empty_cache()
         served_line = served(args.served_seconds)
         # The same six sweeps all at the top of the 100-750 Hz range.
+        keep = ("p50_ms", "p99_ms", "frames", "frames_per_s", "offered_frames_per_s", "errors",
+                "host_link_gbs_offered")
         served_line["at_max_rate"] = {
-            k: v for k, v in served(args.served_seconds, rates=[750.0] * 6).items()
-            if k in ("p50_ms", "p99_ms", "frames", "frames_per_s", "offered_frames_per_s",
-                     "errors")}
+            k: v for k, v in served(args.served_seconds, rates=[750.0] * 6).items() if k in keep}
+        if not args.no_bslz4:
+            # The same, and at twice the rate, with the frames as chunks.
+            for tag, hz in (("bslz4_at_max_rate", 750.0), ("bslz4_at_2x_max_rate", 1500.0)):
+                served_line[tag] = {
+                    k: v for k, v in served(args.served_seconds, rates=[hz] * 6,
+                                            chunks=True).items() if k in keep}
 
     base = None
     if rank == 0 and not args.no_cpu_baseline:

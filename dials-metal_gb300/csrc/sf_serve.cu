@@ -6,7 +6,8 @@
 // and their pixels, dials_spots.cc). Sweeps are admitted against a
 // device-memory budget. Two kinds of thread run the loop:
 //   the worker   copies submitted host frames into the next free slots of
-//                their sweep on a copy stream, and as soon as frames are on
+//                their sweep on a copy stream (a compressed chunk is copied
+//                and decoded into its slot there), and as soon as frames are on
 //                the device forms a batch (continuous batching: whatever is
 //                ready across the sweeps of one frame shape and parameter
 //                set, up to max_batch), thresholds it in one launch sequence
@@ -36,6 +37,7 @@
 #include <vector>
 
 #include "sf_api.h"
+#include "sf_decompress.cuh"
 
 namespace {
 
@@ -90,9 +92,11 @@ struct Event {
 struct SrvFrame {
   int64_t sweep = 0, number = 0;
   const uint32_t *host = nullptr;
+  const uint8_t *chunk = nullptr;        // or a compressed chunk (host)
+  std::shared_ptr<sf::ChunkPlan> plan;   // and its blocks
   double t_submit = 0.0;
   int slot = -1;
-  std::shared_ptr<Event> up;  // upload done
+  std::shared_ptr<Event> up;  // upload (and decode) done
 };
 
 // A run of one sweep's frames in consecutive slots, ready once `ready` fires.
@@ -142,6 +146,13 @@ struct SrvSweep {
   std::condition_variable cv;
   std::thread thread;
   cudaStream_t stream = nullptr;
+  // Compressed chunks: per slot the decoder's error record (4 words, device
+  // and pinned host) and the chunk's block table (device, and the pinned copy
+  // it is uploaded from), sized by the first chunk that needs them.
+  uint32_t *dec_status = nullptr, *host_dec_status = nullptr;
+  std::vector<sf::DecodeBlock *> tables;
+  std::vector<void *> host_tables;
+  std::vector<size_t> table_bytes;
 
   void set_error(int rc, const char *why = nullptr) {
     if (status == 0) {
@@ -157,6 +168,14 @@ struct SrvSweep {
       sf_label_close(lab);
     for (uint32_t *p : slots)
       cudaFree(p);
+    for (sf::DecodeBlock *p : tables)
+      cudaFree(p);
+    for (void *p : host_tables)
+      if (p)
+        cudaFreeHost(p);
+    cudaFree(dec_status);
+    if (host_dec_status)
+      cudaFreeHost(host_dec_status);
     cudaFree(lists);
     cudaFree(counts);
     if (host_counts)
@@ -210,6 +229,12 @@ struct sf_server {
   cudaStream_t copy_s[kCopyStreams] = {}, comp_s = nullptr;
   int next_copy = 0;
   sf_server_stats stats{};
+  // Per copy stream, the device copy of the chunk being decoded there (and a
+  // scratch frame for bitshuffle blocks over 8 KB); reused in stream order.
+  struct DecodeStage {
+    uint8_t *chunk = nullptr, *scratch = nullptr;
+    size_t chunk_cap = 0, scratch_cap = 0;
+  } stage[kCopyStreams];
 
   bool work_ready() {
     for (auto &kv : sweeps) {
@@ -222,7 +247,56 @@ struct sf_server {
 
   void run();
   void label_loop(SrvSweep *s);
+  cudaError_t upload_chunk(SrvSweep &s, const SrvFrame &f, int ci);
 };
+
+// Copies a frame's chunk to the device on copy stream ci and decodes it into
+// the frame's slot there. The slot is free, so its table buffers are idle.
+cudaError_t sf_server::upload_chunk(SrvSweep &s, const SrvFrame &f, int ci) {
+  const cudaStream_t cs = copy_s[ci];
+  const sf::ChunkPlan &p = *f.plan;
+  DecodeStage &st = stage[ci];
+  cudaError_t e;
+  auto grow = [&](uint8_t **buf, size_t *cap, size_t bytes) {
+    if (bytes <= *cap)
+      return cudaSuccess;
+    cudaStreamSynchronize(cs);  // the stream's last decode may still read it
+    cudaFree(*buf);
+    *buf = nullptr;
+    *cap = 0;
+    const cudaError_t r = cudaMalloc(buf, bytes);
+    if (r == cudaSuccess)
+      *cap = bytes;
+    return r;
+  };
+  if ((e = grow(&st.chunk, &st.chunk_cap, p.payload)) != cudaSuccess ||
+      (p.scratch && (e = grow(&st.scratch, &st.scratch_cap, p.frame_bytes)) != cudaSuccess))
+    return e;
+  const size_t tb = p.blocks.size() * sizeof(sf::DecodeBlock);
+  const int k = f.slot;
+  if (tb > s.table_bytes[k]) {
+    cudaFree(s.tables[k]);
+    if (s.host_tables[k])
+      cudaFreeHost(s.host_tables[k]);
+    s.tables[k] = nullptr;
+    s.host_tables[k] = nullptr;
+    s.table_bytes[k] = 0;
+    if ((e = cudaMalloc(&s.tables[k], tb)) != cudaSuccess ||
+        (e = cudaMallocHost(&s.host_tables[k], tb)) != cudaSuccess)
+      return e;
+    s.table_bytes[k] = tb;
+  }
+  std::memcpy(s.host_tables[k], p.blocks.data(), tb);
+  if ((e = cudaMemcpyAsync(st.chunk, f.chunk + 12, p.payload, cudaMemcpyHostToDevice, cs)) !=
+          cudaSuccess ||
+      (e = cudaMemcpyAsync(s.tables[k], s.host_tables[k], tb, cudaMemcpyHostToDevice, cs)) !=
+          cudaSuccess ||
+      (e = cudaMemsetAsync(s.dec_status + 4 * k, 0, 3 * sizeof(uint32_t), cs)) != cudaSuccess)
+    return e;
+  return sf::launch_decode(st.chunk, s.tables[k], p.blocks.size(), p.element,
+                           reinterpret_cast<uint8_t *>(s.slots[k]), st.scratch,
+                           s.dec_status + 4 * k, cs);
+}
 
 void sf_server::label_loop(SrvSweep *s) {
   cudaSetDevice(device);
@@ -280,6 +354,12 @@ void sf_server::label_loop(SrvSweep *s) {
     const size_t k = t.frames.size();
     cudaMemcpyAsync(s->host_counts + t.first_slot, s->counts + t.first_slot,
                     k * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream);
+    bool chunks = false;
+    for (const SrvFrame &f : t.frames)
+      chunks |= f.plan != nullptr;
+    if (chunks)
+      cudaMemcpyAsync(s->host_dec_status + 4 * t.first_slot, s->dec_status + 4 * t.first_slot,
+                      k * 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream);
     int rc = s->status;
     const double t_call = now_s();
     if (rc == SF_OK) {
@@ -295,6 +375,16 @@ void sf_server::label_loop(SrvSweep *s) {
     stats.label_calls++;
     stats.label_frames += k;
     stats.label_seconds += now - t_call;
+    // A chunk the decoder refused fails its frame and the sweep, with the
+    // decoder's text (recorded before whatever labelling its frame made of).
+    std::vector<int> frc(k, rc);
+    for (size_t i = 0; i < k; i++) {
+      const uint32_t *dec = s->host_dec_status + 4 * (t.first_slot + i);
+      if (t.frames[i].plan && dec[0] != sf::kDecOk) {
+        frc[i] = SF_EDATA;
+        s->set_error(SF_EDATA, sf::decode_error_text(*t.frames[i].plan, dec).c_str());
+      }
+    }
     if (rc != SF_OK)
       s->set_error(rc);
     for (size_t i = 0; i < k; i++) {
@@ -302,7 +392,7 @@ void sf_server::label_loop(SrvSweep *s) {
       d.sweep = s->id;
       d.frame = t.frames[i].number;
       d.n_signal = s->host_counts[t.first_slot + i];
-      d.status = rc;
+      d.status = frc[i];
       d.latency_ms = (now - t.frames[i].t_submit) * 1e3;
       done.push_back(d);
     }
@@ -344,10 +434,12 @@ void sf_server::run() {
           s.nfree--;
           f.up = std::make_shared<Event>();
           const size_t bytes = s.group->h * s.group->w * sizeof(uint32_t);
-          const cudaStream_t cs = copy_s[next_copy];
+          const int ci = next_copy;
+          const cudaStream_t cs = copy_s[ci];
           next_copy = (next_copy + 1) % kCopyStreams;
-          cudaError_t e = cudaMemcpyAsync(s.slots[f.slot], f.host, bytes,
-                                          cudaMemcpyHostToDevice, cs);
+          cudaError_t e = f.plan ? upload_chunk(s, f, ci)
+                                 : cudaMemcpyAsync(s.slots[f.slot], f.host, bytes,
+                                                   cudaMemcpyHostToDevice, cs);
           if (e == cudaSuccess)
             e = cudaEventRecord(f.up->e, cs);
           if (e != cudaSuccess)
@@ -485,6 +577,10 @@ void sf_server_close(sf_server *sv) {
   cudaDeviceSynchronize();
   sv->sweeps.clear();
   sv->groups.clear();
+  for (auto &st : sv->stage) {
+    cudaFree(st.chunk);
+    cudaFree(st.scratch);
+  }
   for (cudaStream_t cs : sv->copy_s)
     cudaStreamDestroy(cs);
   cudaStreamDestroy(sv->comp_s);
@@ -561,9 +657,14 @@ int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,
       return SF_ECUDA;
     s->slots.push_back(slot);
   }
+  s->tables.assign(s->ring, nullptr);
+  s->host_tables.assign(s->ring, nullptr);
+  s->table_bytes.assign(s->ring, 0);
   if ((e = cudaMalloc(&s->lists, s->ring * capacity * sizeof(sf_signal_pixel))) != cudaSuccess ||
       (e = cudaMalloc(&s->counts, s->ring * sizeof(uint32_t))) != cudaSuccess ||
       (e = cudaMallocHost(&s->host_counts, s->ring * sizeof(uint32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&s->dec_status, s->ring * 4 * sizeof(uint32_t))) != cudaSuccess ||
+      (e = cudaMallocHost(&s->host_dec_status, s->ring * 4 * sizeof(uint32_t))) != cudaSuccess ||
       (e = cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, label_priority())) !=
           cudaSuccess)
     return SF_ECUDA;
@@ -602,6 +703,50 @@ int sf_server_submit(sf_server *sv, int64_t sweep, int64_t frame, const uint32_t
   f.sweep = sweep;
   f.number = frame;
   f.host = host_frame;
+  f.t_submit = now_s();
+  s.pending.push_back(f);
+  s.in_flight++;
+  sv->cv_work.notify_all();
+  return SF_OK;
+}
+
+int sf_server_submit_chunk(sf_server *sv, int64_t sweep, int64_t frame, const uint8_t *data,
+                           size_t nbytes, const char *algorithm) {
+  if (!sv || !data)
+    return SF_EBADARG;
+  size_t h = 0, w = 0;
+  {
+    std::lock_guard<std::mutex> lock(sv->m);
+    auto it = sv->sweeps.find(sweep);
+    if (it == sv->sweeps.end())
+      return SF_EBADARG;
+    h = it->second->group->h;
+    w = it->second->group->w;
+  }
+  // The chunk's header and framing, checked before the frame is taken
+  // (decompress.cc:77-134), off the lock.
+  auto plan = std::make_shared<sf::ChunkPlan>();
+  const int rc = sf::plan_chunk(data, nbytes, algorithm, 32, h, w, h * w * sizeof(uint32_t),
+                                plan.get());
+  if (rc != SF_OK)
+    return rc;
+  if (plan->algorithm == sf::kChunkNone)
+    return sf_server_submit(sv, sweep, frame, reinterpret_cast<const uint32_t *>(data));
+  std::lock_guard<std::mutex> lock(sv->m);
+  auto it = sv->sweeps.find(sweep);
+  if (it == sv->sweeps.end())
+    return SF_EBADARG;
+  SrvSweep &s = *it->second;
+  if (s.finishing || frame <= s.last_number)
+    return SF_EBADARG;
+  if (s.status)
+    return s.status;
+  s.last_number = frame;
+  SrvFrame f;
+  f.sweep = sweep;
+  f.number = frame;
+  f.chunk = data;
+  f.plan = std::move(plan);
   f.t_submit = now_s();
   s.pending.push_back(f);
   s.in_flight++;

@@ -59,6 +59,9 @@ def _lib():
         L.sf_server_open_sweep.restype = ctypes.c_int
         L.sf_server_submit.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, vp]
         L.sf_server_submit.restype = ctypes.c_int
+        L.sf_server_submit_chunk.argtypes = [vp, ctypes.c_int64, ctypes.c_int64, vp, sz,
+                                             ctypes.c_char_p]
+        L.sf_server_submit_chunk.restype = ctypes.c_int
         L.sf_server_poll.argtypes = [vp, ctypes.POINTER(FrameDone), sz, ctypes.c_int]
         L.sf_server_poll.restype = sz
         for name in ("sf_server_finish_sweep", "sf_server_close_sweep"):
@@ -116,6 +119,29 @@ class Server:
         else:
             ptr = int(image)
         rc = _lib().sf_server_submit(self._s, sweep, frame, ptr)
+        if rc == api.SF_EBADARG:
+            raise ValueError("submit: frames go in ascending order to an open sweep")
+        if rc != 0:
+            raise api.SpotFinderError(f"submit ({rc}): {self.sweep_error(sweep)}")
+
+    def submit_chunk(self, sweep: int, frame: int, chunk, algorithm: str = "bslz4",
+                     nbytes: int | None = None) -> None:
+        """A 32-bit frame as a compressed chunk (filter header and all):
+        a uint8 array (kept alive here until the frame is done) or an integer
+        host address with nbytes. Raises api.DataError, the frame not taken,
+        when the chunk's header or framing is wrong."""
+        if isinstance(chunk, np.ndarray):
+            chunk = np.ascontiguousarray(chunk).view(np.uint8).ravel()
+            ptr, n = chunk.ctypes.data, chunk.size
+            with self._lock:
+                self._keep[(sweep, frame)] = chunk
+        else:
+            ptr, n = int(chunk), int(nbytes)
+        rc = _lib().sf_server_submit_chunk(self._s, sweep, frame, ptr, n, algorithm.encode())
+        if rc == api.SF_EDATA:
+            with self._lock:
+                self._keep.pop((sweep, frame), None)
+            raise api.DataError(api.last_error())
         if rc == api.SF_EBADARG:
             raise ValueError("submit: frames go in ascending order to an open sweep")
         if rc != 0:

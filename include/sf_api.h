@@ -457,6 +457,15 @@ int sf_server_open_sweep(sf_server *server, size_t height, size_t width,
                          int64_t *sweep);
 int sf_server_submit(sf_server *server, int64_t sweep, int64_t frame,
                      const uint32_t *host_frame);
+/* As sf_server_submit for a frame stored as a compressed chunk (the input of
+ * decompress::image, src/spots/decompress.hh:28-30: "bslz4", "lz4", or ""
+ * for raw 32-bit pixels). The chunk's header and framing are checked here:
+ * -6 (SF_EDATA) with the reference's text, and the frame is not taken. The
+ * chunk (pinned host memory, kept until the frame is done) is copied to the
+ * device and decoded into the sweep's slot; a block the decoder refuses fails
+ * its frame and the sweep with SF_EDATA. */
+int sf_server_submit_chunk(sf_server *server, int64_t sweep, int64_t frame,
+                           const uint8_t *data, size_t nbytes, const char *algorithm);
 /* Up to max finished frames; waits up to wait_ms for the first one. */
 size_t sf_server_poll(sf_server *server, sf_frame_done *out, size_t max, int wait_ms);
 int sf_server_finish_sweep(sf_server *server, int64_t sweep);

@@ -118,3 +118,62 @@ def test_out_of_order_refused(serve):
         srv.submit(sid, 4, f)
     srv.finish_sweep(sid)
     srv.close()
+
+
+def test_compressed_chunks_served(serve):
+    # The same sweeps submitted as bitshuffle+LZ4 and LZ4 chunks (mixed with a
+    # sweep of raw frames) give the spots of the raw frames; a chunk with a
+    # bad header is refused at submit and the frame is not taken.
+    from sfgb import api, synth
+    a = (_synth(300, 350, 9, 7), list(range(9)))
+    b = (_synth(200, 260, 8, 8), list(range(8)))
+    want_a, want_b = _oracle_sweep(*a), _oracle_sweep(*b)
+    chunks_a = [synth.chunk(f, "bslz4") for f in a[0]]
+    chunks_b = [synth.chunk(f, "lz4", 4096) for f in b[0]]
+    srv = serve.Server(max_batch=4, ring=6)
+    ia, ib, ic = srv.open_sweep(300, 350), srv.open_sweep(200, 260), srv.open_sweep(300, 350)
+    bad = chunks_a[0].copy()
+    bad[7] ^= 1  # the header's frame size
+    with pytest.raises(api.DataError):
+        srv.submit_chunk(ia, 0, bad)
+    for i in range(9):
+        srv.submit_chunk(ia, a[1][i], chunks_a[i])
+        srv.submit(ic, a[1][i], a[0][i])
+        if i < 8:
+            srv.submit_chunk(ib, b[1][i], chunks_b[i], "lz4")
+    got_a, got_b, got_c = srv.finish_sweep(ia), srv.finish_sweep(ib), srv.finish_sweep(ic)
+    for got, want in ((got_a, want_a), (got_b, want_b), (got_c, want_a)):
+        assert O.spot_fields_equal(got.spots, want.spots)
+        assert got.pixels.tobytes() == want.pixels.tobytes()
+    for sid in (ia, ib, ic):
+        srv.close_sweep(sid)
+    srv.close()
+
+
+def test_undecodable_chunk_fails_its_sweep(serve):
+    # A chunk whose framing is sound but whose first block is not LZ4: the
+    # frame and its sweep fail with the decoder's text; other sweeps go on.
+    from sfgb import api, synth
+    frames = _synth(120, 160, 3, 9)
+    good = [synth.chunk(f) for f in frames]
+    broken = good[1].copy()
+    broken[16:20] = [0xF0, 0xFF, 0xFF, 0xFF]
+    srv = serve.Server(max_batch=4, ring=6)
+    s1, s2 = srv.open_sweep(120, 160), srv.open_sweep(120, 160)
+    srv.submit_chunk(s1, 0, good[0])
+    srv.submit_chunk(s1, 1, broken)
+    for i in range(3):
+        srv.submit_chunk(s2, i, good[i])
+    done = []
+    while len(done) < 5:
+        done += srv.poll(wait_ms=100)
+    status = {(d["sweep"], d["frame"]): d["status"] for d in done}
+    assert status[(s1, 1)] == api.SF_EDATA
+    assert "bitshuffle decompression failed" in srv.sweep_error(s1)
+    assert all(status[(s2, i)] == 0 for i in range(3))
+    want = _oracle_sweep(frames, [0, 1, 2])
+    got = srv.finish_sweep(s2)
+    assert O.spot_fields_equal(got.spots, want.spots)
+    srv.close_sweep(s1)
+    srv.close_sweep(s2)
+    srv.close()
