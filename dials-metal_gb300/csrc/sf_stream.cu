@@ -654,13 +654,42 @@ __device__ __forceinline__ void scan_emit(size_t lo, size_t hi, uint32_t carry, 
   }
 }
 
+// A thread's kScanPer consecutive mask words from i0 (16-byte loads where
+// the frame's words are 16-byte aligned and all 8 lie before hi).
+__device__ __forceinline__ void load_words(const uint32_t *__restrict__ bits, size_t i0,
+                                           size_t hi, bool vec, uint32_t w[kScanPer]) {
+  static_assert(kScanPer == 8, "two 16-byte loads a thread");
+  if (vec && i0 + kScanPer <= hi) {
+    const uint4 a = __ldg(reinterpret_cast<const uint4 *>(bits + i0));
+    const uint4 b = __ldg(reinterpret_cast<const uint4 *>(bits + i0 + 4));
+    w[0] = a.x, w[1] = a.y, w[2] = a.z, w[3] = a.w;
+    w[4] = b.x, w[5] = b.y, w[6] = b.z, w[7] = b.w;
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < kScanPer; k++)
+    w[k] = i0 + k < hi ? bits[i0 + k] : 0u;
+}
+
 // Popcounts of the block's share of a frame's mask words.
 __global__ void __launch_bounds__(kScanT)
 mask_sums(const uint32_t *__restrict__ bits_all, size_t words, uint32_t *__restrict__ block_sums) {
   const uint32_t *bits = bits_all + (size_t)blockIdx.y * words;
+  const bool vec = reinterpret_cast<uintptr_t>(bits) % 16 == 0;
   size_t lo, hi;
   chunk_of(words, &lo, &hi);
-  scan_count(lo, hi, [&](size_t w) { return (uint32_t)__popc(bits[w]); }, block_sums);
+  uint32_t acc = 0;
+  for (size_t base = lo; base < hi; base += kScanChunk) {
+    uint32_t w[kScanPer];
+    load_words(bits, base + (size_t)threadIdx.x * kScanPer, hi, vec, w);
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++)
+      acc += (uint32_t)__popc(w[k]);
+  }
+  uint32_t total;
+  (void)block_exclusive_scan(acc, &total);
+  if (threadIdx.x == 0)
+    block_sums[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = total;
 }
 
 // The pixel index of every set bit of the block's share, in order.
@@ -918,23 +947,35 @@ mask_prefix(const uint32_t *__restrict__ bits_all, size_t words,
   uint32_t carry = block_base(block_sums, &total);
   if (counters && blockIdx.x == 0 && threadIdx.x == 0)
     counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand] = total;  // the candidates
+  const bool vec = reinterpret_cast<uintptr_t>(bits) % 16 == 0 &&
+                   reinterpret_cast<uintptr_t>(prefix) % 16 == 0;
   size_t lo, hi;
   chunk_of(words, &lo, &hi);
   for (size_t base = lo; base < hi; base += kScanChunk) {
     const size_t i0 = base + (size_t)threadIdx.x * kScanPer;
     uint32_t c[kScanPer], tot = 0;
+    load_words(bits, i0, hi, vec, c);
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
-      c[k] = i0 + k < hi ? (uint32_t)__popc(bits[i0 + k]) : 0u;
+      c[k] = (uint32_t)__popc(c[k]);
       tot += c[k];
     }
     uint32_t t;
     uint32_t pos = carry + block_exclusive_scan(tot, &t);
+    uint32_t p[kScanPer];
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
-      if (i0 + k < hi)
-        prefix[i0 + k] = pos;
+      p[k] = pos;
       pos += c[k];
+    }
+    if (vec && i0 + kScanPer <= hi) {
+      reinterpret_cast<uint4 *>(prefix + i0)[0] = make_uint4(p[0], p[1], p[2], p[3]);
+      reinterpret_cast<uint4 *>(prefix + i0)[1] = make_uint4(p[4], p[5], p[6], p[7]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < kScanPer; k++)
+        if (i0 + k < hi)
+          prefix[i0 + k] = p[k];
     }
     carry += t;
   }
