@@ -609,23 +609,6 @@ __device__ __forceinline__ uint32_t block_base(const uint32_t *__restrict__ bloc
   return s_base;
 }
 
-// The block's count over [lo, hi): kScanPer consecutive items per thread.
-template <class Count>
-__device__ __forceinline__ void scan_count(size_t lo, size_t hi, Count count,
-                                           uint32_t *__restrict__ block_sums) {
-  uint32_t acc = 0;
-  for (size_t base = lo; base < hi; base += kScanChunk) {
-    const size_t i0 = base + (size_t)threadIdx.x * kScanPer;
-#pragma unroll
-    for (int k = 0; k < kScanPer; k++)
-      acc += i0 + k < hi ? count(i0 + k) : 0u;
-  }
-  uint32_t total;
-  (void)block_exclusive_scan(acc, &total);
-  if (threadIdx.x == 0)
-    block_sums[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = total;
-}
-
 // Every item of [lo, hi) with its count's exclusive prefix (offset by
 // carry): emit(i, item, position) for items that count.
 template <typename V, class Load, class Count, class Emit>
@@ -669,6 +652,26 @@ __device__ __forceinline__ void load_words(const uint32_t *__restrict__ bits, si
 #pragma unroll
   for (int k = 0; k < kScanPer; k++)
     w[k] = i0 + k < hi ? bits[i0 + k] : 0u;
+}
+
+// A thread's kScanPer consecutive stage-2 results from i0 (16-byte loads,
+// two results each, where the frame's results are 16-byte aligned and all 8
+// lie before hi); zeros past hi.
+__device__ __forceinline__ void load_res(const uint2 *__restrict__ res, size_t i0, size_t hi,
+                                         bool vec, uint2 r[kScanPer]) {
+  if (vec && i0 + kScanPer <= hi) {
+    const uint4 *r4 = reinterpret_cast<const uint4 *>(res + i0);
+#pragma unroll
+    for (int k = 0; k < kScanPer / 2; k++) {
+      const uint4 x = __ldg(r4 + k);
+      r[2 * k] = make_uint2(x.x, x.y);
+      r[2 * k + 1] = make_uint2(x.z, x.w);
+    }
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < kScanPer; k++)
+    r[k] = i0 + k < hi ? res[i0 + k] : make_uint2(0u, 0u);
 }
 
 // Popcounts of the block's share of a frame's mask words.
@@ -884,16 +887,31 @@ pass_sums(const uint2 *__restrict__ res_all, uint32_t cand_cap,
   const uint32_t *cand = cand_all + (size_t)f * cand_cap;
   uint32_t *fin = final_all ? final_all + (size_t)f * words : nullptr;
   const uint32_t wpr = ((uint32_t)width + 31u) >> 5;
+  const bool vec = reinterpret_cast<uintptr_t>(res) % 16 == 0;
   size_t lo, hi;
   chunk_of(nc, &lo, &hi);
-  scan_count(lo, hi, [&](size_t i) {
-    const uint32_t pass = (res[i].y >> 16) & 1u;
-    if (fin && !pass) {
-      const uint32_t idx = cand[i], y = idx / (uint32_t)width, x = idx - y * (uint32_t)width;
-      atomicAnd(fin + (size_t)y * wpr + (x >> 5), ~(1u << (x & 31)));
+  uint32_t acc = 0;
+  for (size_t base = lo; base < hi; base += kScanChunk) {
+    const size_t i0 = base + (size_t)threadIdx.x * kScanPer;
+    uint2 r[kScanPer];
+    load_res(res, i0, hi, vec, r);
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+      if (i0 + k >= hi)
+        break;
+      const uint32_t pass = (r[k].y >> 16) & 1u;
+      if (fin && !pass) {
+        const uint32_t idx = cand[i0 + k], y = idx / (uint32_t)width,
+                       x = idx - y * (uint32_t)width;
+        atomicAnd(fin + (size_t)y * wpr + (x >> 5), ~(1u << (x & 31)));
+      }
+      acc += pass;
     }
-    return pass;
-  }, block_sums);
+  }
+  uint32_t total;
+  (void)block_exclusive_scan(acc, &total);
+  if (threadIdx.x == 0)
+    block_sums[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = total;
 }
 
 template <typename Pix>
@@ -916,23 +934,38 @@ pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ c
     // The signal found; all ones if the candidate list overflowed, as for a
     // count above capacity (the list is then incomplete).
     count_out[f] = ncand > cand_cap ? 0xFFFFFFFFu : total;
+  const bool vec = reinterpret_cast<uintptr_t>(res) % 16 == 0;
   size_t lo, hi;
   chunk_of(nc, &lo, &hi);
-  scan_emit<uint2>(
-      lo, hi, carry, [&](size_t i) { return res[i]; },
-      [](uint2 r) { return (r.y >> 16) & 1u; },
-      [&](size_t i, uint2 r, uint32_t pos) {
-        if (pos >= capacity)
-          return;
-        const uint32_t idx = cand[i];
+  uint32_t run = carry;
+  for (size_t base = lo; base < hi; base += kScanChunk) {
+    const size_t i0 = base + (size_t)threadIdx.x * kScanPer;
+    uint2 r[kScanPer];
+    load_res(res, i0, hi, vec, r);
+    uint32_t c[kScanPer], tot = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+      c[k] = i0 + k < hi ? (r[k].y >> 16) & 1u : 0u;
+      tot += c[k];
+    }
+    uint32_t t;
+    uint32_t pos = run + block_exclusive_scan(tot, &t);
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+      if (c[k] && pos < capacity) {
+        const uint32_t idx = cand[i0 + k];
         sf_signal_pixel rec;
         rec.index = idx;
         rec.value = (uint32_t)__ldg(image + idx);
-        rec.background = __uint_as_float(r.x);
-        rec.population = (uint16_t)(r.y & 0xFFFFu);
+        rec.background = __uint_as_float(r[k].x);
+        rec.population = (uint16_t)(r[k].y & 0xFFFFu);
         rec.reserved = 0;
         out[pos] = rec;
-      });
+      }
+      pos += c[k];
+    }
+    run += t;
+  }
 }
 
 // Optional: per final-mask word, the list position of its first pixel.
