@@ -50,10 +50,10 @@ H, W = 4362, 4148
 
 # DRAM bytes (read + write) that one 16M frame of the eiger_16m workload costs
 # across the threshold's kernels in a timed 64-frame launch, from an ncu
-# capture of this bench without cache flushes between kernels (11,076 MB for
-# the launch: lat_stage01 5,097 MB, lat_verify 2,099 MB, lat_stage2 2,643 MB,
-# the scans and the list 1,237 MB); the algorithmic bytes are 76.5 MB a frame.
-DRAM_BYTES_PER_FRAME = 173.1e6
+# capture of this bench without cache flushes between kernels (11,235 MB for
+# the launch: lat_stage01 5,266 MB, lat_verify 2,098 MB, lat_stage2 2,621 MB,
+# the scans and the list 1,250 MB); the algorithmic bytes are 76.5 MB a frame.
+DRAM_BYTES_PER_FRAME = 175.6e6
 
 
 def dist_env():
