@@ -935,6 +935,7 @@ pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ c
     // count above capacity (the list is then incomplete).
     count_out[f] = ncand > cand_cap ? 0xFFFFFFFFu : total;
   const bool vec = reinterpret_cast<uintptr_t>(res) % 16 == 0;
+  const bool vec_c = reinterpret_cast<uintptr_t>(cand) % 16 == 0;
   size_t lo, hi;
   chunk_of(nc, &lo, &hi);
   uint32_t run = carry;
@@ -942,10 +943,15 @@ pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ c
     const size_t i0 = base + (size_t)threadIdx.x * kScanPer;
     uint2 r[kScanPer];
     load_res(res, i0, hi, vec, r);
-    uint32_t c[kScanPer], tot = 0;
+    uint32_t idx[kScanPer];
+    load_words(cand, i0, hi, vec_c, idx);
+    // The passing pixels' values: every load in flight before the scan
+    // (none waits for another).
+    uint32_t c[kScanPer], val[kScanPer], tot = 0;
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
       c[k] = i0 + k < hi ? (r[k].y >> 16) & 1u : 0u;
+      val[k] = c[k] ? (uint32_t)__ldg(image + idx[k]) : 0u;
       tot += c[k];
     }
     uint32_t t;
@@ -953,10 +959,9 @@ pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ c
 #pragma unroll
     for (int k = 0; k < kScanPer; k++) {
       if (c[k] && pos < capacity) {
-        const uint32_t idx = cand[i0 + k];
         sf_signal_pixel rec;
-        rec.index = idx;
-        rec.value = (uint32_t)__ldg(image + idx);
+        rec.index = idx[k];
+        rec.value = val[k];
         rec.background = __uint_as_float(r[k].x);
         rec.population = (uint16_t)(r[k].y & 0xFFFFu);
         rec.reserved = 0;
