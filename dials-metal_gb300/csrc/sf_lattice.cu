@@ -537,7 +537,9 @@ __device__ __noinline__ bool lat_wide(const uint32_t *__restrict__ image, int he
 // Tiles of a tile row come in groups of 32 consecutive ones: 32 tiles of 28
 // columns span 28 mask words (29 with the last tile's straddle), so lane l
 // ORs word 28 g + l over the tile row's 8 rows and each lane tests its tile
-// from two lanes' ORs. A warp takes a run of kTileRun groups (of any frames),
+// from two lanes' ORs. A warp takes a run of up to kTileRun groups (of any
+// frames; fewer when a launch has too few groups to give every SM a few
+// warps, so that a one-frame launch is not a few warps walking long runs),
 // keeps their ballots, and takes its list space with one atomic: the
 // counter is shared by the whole launch, so fewer atomics contend less.
 constexpr int kTileRun = 16;
@@ -545,14 +547,14 @@ constexpr int kTileRun = 16;
 __global__ void __launch_bounds__(256)
 lat_tiles(int nframes, int height, int width, const uint32_t *__restrict__ final_all,
           size_t words, uint32_t *__restrict__ list, uint32_t *__restrict__ counters,
-          FastDiv by_ngx, FastDiv by_fgroups) {
+          FastDiv by_ngx, FastDiv by_fgroups, int run) {
   const int lane = threadIdx.x & 31;
   const int wpr = (width + 31) >> 5, ntx = ver_ntx(width), nty = ver_nty(height);
   const int ngx = (ntx + 31) / 32;
   const uint32_t ntiles = (uint32_t)ntx * (uint32_t)nty;
   const uint32_t fgroups = (uint32_t)nty * (uint32_t)ngx;  // groups a frame
   const uint32_t total = fgroups * (uint32_t)nframes;
-  const uint32_t g0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kTileRun;
+  const uint32_t g0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (uint32_t)run;
   if (g0 >= total)
     return;  // whole warp
   unsigned bal[kTileRun];
@@ -561,7 +563,7 @@ lat_tiles(int nframes, int height, int width, const uint32_t *__restrict__ final
   for (int i = 0; i < kTileRun; i++) {
     const uint32_t g = g0 + i;
     bool any = false;
-    if (g < total) {  // warp-uniform
+    if (i < run && g < total) {  // warp-uniform
       const uint32_t f = fast_div(g, by_fgroups), gf = g - f * fgroups;
       const uint32_t ty = fast_div(gf, by_ngx), gx = gf - ty * (uint32_t)ngx;
       const uint32_t *fin = final_all + (size_t)f * words;
@@ -1206,7 +1208,11 @@ cudaError_t lattice(const FramePtrs &F, int nframes, int h, int w, int vec, cons
   // candidate mask's per-word list positions (stage 2), the tile list and the
   // list of tiles the exact check leaves a candidate in.
   const long long tgroups = (long long)ver_nty(h) * ((ver_ntx(w) + 31) / 32);
-  const long long twarps = (tgroups * nframes + kTileRun - 1) / kTileRun;
+  // Runs of kTileRun groups a warp, shorter when that would leave fewer than
+  // 8 warps an SM (one frame: runs of 2).
+  const int trun = (int)std::max(1ll, std::min((long long)kTileRun,
+                                               tgroups * nframes / (8ll * device_sms())));
+  const long long twarps = (tgroups * nframes + trun - 1) / trun;
   const unsigned tb = (unsigned)((twarps + 7) / 8);
   const size_t tiles = (size_t)ver_ntx(w) * (size_t)ver_nty(h);
   uint32_t *list = b.amb + (size_t)nframes * b.words;
@@ -1215,7 +1221,7 @@ cudaError_t lattice(const FramePtrs &F, int nframes, int h, int w, int vec, cons
   const FastDiv by_ntiles = make_fastdiv((uint32_t)tiles);
   const FastDiv by_ntx = make_fastdiv((uint32_t)ver_ntx(w));
   lat_tiles<<<tb, 256, 0, stream>>>(nframes, h, w, b.bits, b.words, list, b.counters, by_ngx,
-                                    by_fgroups);
+                                    by_fgroups, trun);
   lat_verify<kVerOcc, Pix><<<ver_blocks * device_sms(), kVerWarps * 32, ver_smem_bytes<Pix>(),
                              stream>>>(F, h, w, vec, P, T, b.scr1, b.bits, b.words, list,
                                        b.counters, by_ntiles, by_ntx,
