@@ -539,10 +539,13 @@ __device__ __noinline__ bool lat_wide(const uint32_t *__restrict__ image, int he
 // ORs word 28 g + l over the tile row's 8 rows and each lane tests its tile
 // from two lanes' ORs. A warp takes a run of up to kTileRun groups (of any
 // frames; fewer when a launch has too few groups to give every SM a few
-// warps, so that a one-frame launch is not a few warps walking long runs),
+// warps, so that a one-frame launch is not a few warps walking long runs):
+// each group is a round trip to memory, so the run sets the kernel's length
+// (a 64-frame launch: 131 us with runs of 32, 69 with 16, 45 with 8, 49 with
+// 4, where the list's one counter starts to take the atomics in turn),
 // keeps their ballots, and takes its list space with one atomic: the
 // counter is shared by the whole launch, so fewer atomics contend less.
-constexpr int kTileRun = 16;
+constexpr int kTileRun = 8;
 
 __global__ void __launch_bounds__(256)
 lat_tiles(int nframes, int height, int width, const uint32_t *__restrict__ final_all,
