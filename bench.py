@@ -364,8 +364,7 @@ def run_ours(args):
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
-    clocks = ClockSampler(local, os.path.join(REPO, "gpurun_out", "bench_clocks.csv")
-                          if os.path.isdir(os.path.join(REPO, "gpurun_out")) else None)
+    clocks = ClockSampler(local, args.clocks_csv)
     clocks.start()
     if world > 1:
         torch.distributed.barrier()
@@ -744,6 +743,8 @@ def main(argv=None):
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-u16", action="store_true")
     ap.add_argument("--no-bslz4", action="store_true")
+    ap.add_argument("--clocks-csv", default=None,
+                    help="also write the nvidia-smi samples of the timed region here")
     ap.add_argument("--served-seconds", type=float, default=4.0)
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per threshold launch from an ncu capture")
