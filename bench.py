@@ -520,7 +520,7 @@ def run_ours(args):
             arr = np.ctypeslib.as_array((ctypes.c_uint32 * f.size).from_address(ptr))
             arr[:] = f.ravel()
             host.append(ptr)
-        T = args.e2e_threads
+        T = args.e2e_threads or os.cpu_count() or 8
         outs = []
         for _ in range(T):
             ptr = L.sf_host_alloc(H * W // 4 * 16)
@@ -738,7 +738,8 @@ def main(argv=None):
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--e2e-threads", type=int, default=8)
+    ap.add_argument("--e2e-threads", type=int, default=0,
+                    help="host threads of the end-to-end legs (0: one a core, as mxi_find -j)")
     ap.add_argument("--no-label", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-u16", action="store_true")
