@@ -173,6 +173,41 @@ def test_host_refusals_need_no_device():
         api.decompress_image(synth.chunk(f8, "bslz4"), "bslz4", 8, 8, 8)
 
 
+def test_more_host_refusals_need_no_device():
+    # Framing errors of bitshuffle chunks past their end (code -1, where
+    # bitshuffle itself would read past the chunk), pixel sizes the device
+    # path does not take, and the find / scan entry points refusing the same
+    # chunks before any device work.
+    from sfgb import api, synth
+    f = _frame(20, 24, np.uint32, 3)  # 480 elements: one partial block
+    c = synth.chunk(f, "bslz4").tobytes()
+    for cut in (14, 17, len(c) - 1):
+        with pytest.raises(api.DataError) as e:
+            api.decompress_image(c[:cut], "bslz4", 32, 20, 24)
+        assert str(e.value) == "bitshuffle decompression failed with code -1"
+        with pytest.raises(RuntimeError) as e:
+            O.decompress_image(np.frombuffer(c[:cut], np.uint8), "bslz4", 32, 20, 24)
+        assert str(e.value) == "bitshuffle decompression failed with code -1"
+    g = _frame(7, 9, np.uint32, 4)  # 63 elements: a block of 56 and 7 raw
+    cg = synth.chunk(g, "bslz4").tobytes()
+    with pytest.raises(api.DataError):
+        api.decompress_image(cg[:-2], "bslz4", 32, 7, 9)  # the raw tail cut short
+    with pytest.raises(api.DataError) as e:
+        api.find_compressed(c[:11], "bslz4", 32, 20, 24)
+    assert str(e.value) == "too short for a filter header"
+    with pytest.raises(api.SpotFinderError):
+        api.find_compressed(c, "bslz4", 8, 20, 24)  # thresholds take 16 or 32 bits
+    with pytest.raises(api.SpotFinderError) as e:
+        api.scan_compressed(c, "bslz4", 8, 20, 24)
+    assert "8-bit pixels" in str(e.value)
+    with pytest.raises(api.DataError) as e:
+        api.scan_compressed(c, "zstd", 32, 20, 24)
+    assert str(e.value) == "unknown compression algorithm zstd"
+    with pytest.raises(api.DataError) as e:
+        api.find_narrowed(c[:12 + 3], "bslz4", 20, 24)
+    assert str(e.value) == "bitshuffle decompression failed with code -1"
+
+
 def test_uncompressed_host_copy_needs_no_device():
     from sfgb import api
     f = _frame(30, 40, np.uint16, 2)
