@@ -953,17 +953,24 @@ int sf_threshold_u16_batch_device(const uint16_t *const *d_images, size_t n_fram
 // synchronisation an allocation can cause. For them the threshold's scratch
 // (the unordered signal list, the per-tile bases and the per-tile-row counts)
 // lives in a fixed array in this library's device image instead of a
-// caller-supplied workspace. The array is part of the module, so every GPU
-// that loads the library holds it until the process exits.
+// caller-supplied workspace. The array is part of the module that holds this
+// file's code: the driver reserves it on a device when that module is first
+// loaded there (under CUDA's lazy module loading, at the first use of the
+// module on that device, at the latest at this entry point's first call) and
+// keeps it until the process exits.
 // ---------------------------------------------------------------------------
 
 namespace sf {
 
-// 24 MiB: 8 MiB of staging (524,288 signal records of 16 bytes) and the
-// per-word and per-tile bookkeeping (eroded mask, word prefixes, tile sums)
-// of frames up to 2^25 pixels (the EIGER2 16M is 18.1 M).
+// 32 MiB. What one call needs is the workspace layout of (height, width,
+// capacity): the tile path's staging list (16 bytes a record), the candidate
+// list and stage-2 results (12 bytes a slot, min(h w, 2 capacity + 65536)
+// slots), the eroded mask, word prefixes and tile bookkeeping. A call is
+// refused unless that layout fits. It does at the full 524,288 records for an
+// EIGER2 16M frame (4362 x 4148: 27.2 MB) and for every frame of up to 2^25
+// pixels whose sides are both at least 256 (at most 31.7 MB).
 constexpr size_t kNoAllocCapacity = 524288;
-constexpr size_t kNoAllocScratchBytes = (size_t)24 << 20;
+constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -1009,7 +1016,7 @@ extern "C" int sf_threshold_u32_device_noalloc(
     return SF_EBADARG;
   }
   if (layout(height, width, capacity).total > kNoAllocScratchBytes) {
-    t_last_error = "frame too large for the fixed scratch's tile bookkeeping";
+    t_last_error = "frame and capacity together need more than the fixed scratch's 32 MiB";
     return SF_EBADARG;
   }
   void *scratch = nullptr;

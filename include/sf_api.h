@@ -385,15 +385,22 @@ int sf_label_write_refl(const sf_labeller *labeller, const char *path,
  * memory: a plugin inside a host application whose own allocator owns all
  * device memory, or a detector-stream loop that must not stall on an
  * allocation. It has no counterpart in the reference. Its scratch is a fixed
- * 24 MiB array inside this library (held on every GPU that loads the library
- * until exit), so it takes no workspace and calls no allocator; the caller
- * still passes the frame and every output.
- *   - capacity may be at most 524288 records, and the frame at most about
- *     2^25 pixels; beyond either it returns -1 with the reason in
- *     sf_last_error().
- *   - The first call on each device looks up the array's device address
- *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ * 32 MiB array inside this library, so it takes no workspace and calls no
+ * allocator; the caller still passes the frame and every output.
+ *   - A call needs the workspace layout of (height, width, capacity), i.e.
+ *     sf_workspace_bytes(height, width, capacity), to fit in the 32 MiB, and
+ *     capacity at most 524288 records; otherwise it returns -1 with the
+ *     reason in sf_last_error(). Both hold for an EIGER2 16M frame
+ *     (4362 x 4148) at the full 524288 records, and for any frame of up to
+ *     2^25 pixels whose sides are both at least 256.
+ *   - The driver reserves the 32 MiB on a device when this library's module
+ *     holding the array is first loaded there (with CUDA's lazy module
+ *     loading, at the first use of that module on the device, which may
+ *     synchronise), and keeps it until the process exits. The first call on
+ *     each device also looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current. So make one warm-up
+ *     call on each device before acquisition starts and before any stream
+ *     capture.
  *   - Every call shares the one array: calls whose work overlaps on the GPU
  *     (different streams, or different host threads) race and corrupt each
  *     other's results. Serialise them, e.g. on one stream.

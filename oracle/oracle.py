@@ -66,7 +66,7 @@ def build(quiet: bool = True) -> None:
                                             "sf_oracle_frames.c")]
     tmp = LIB_PATH + ".tmp"
     subprocess.run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
-                    *srcs, "-o", tmp, "-lm"], check=True)
+                    *srcs, "-o", tmp, "-lm", "-lpthread"], check=True)
     os.replace(tmp, LIB_PATH)
     subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True,
                    stdout=subprocess.DEVNULL if quiet else None,

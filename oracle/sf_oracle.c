@@ -6,6 +6,7 @@
 #include "sf_oracle.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -20,6 +21,47 @@ void or_default_params(or_params *p) {
   p->sigma_s = 3.0;
   p->min_local = 2;
   p->global_threshold = 0.0;
+}
+
+/* Per-thread scratch of the threshold, grown as needed and kept for the
+ * thread's life, as the reference's worker threads keep a thread_local
+ * Scratch (src/spots/find_spots.cc:407-408, src/spots/dext.hh:49-74) instead
+ * of allocating 26 bytes a pixel for every frame. Freed at thread exit. */
+typedef struct {
+  unsigned char *buf;
+  size_t bytes;
+} or_scratch;
+
+static pthread_key_t g_scratch_key;
+static pthread_once_t g_scratch_once = PTHREAD_ONCE_INIT;
+
+static void or_scratch_free(void *p) {
+  or_scratch *s = (or_scratch *)p;
+  if (s) {
+    free(s->buf);
+    free(s);
+  }
+}
+
+static void or_scratch_key_init(void) { pthread_key_create(&g_scratch_key, or_scratch_free); }
+
+/* At least `bytes` of this thread's scratch, or NULL. */
+static unsigned char *or_scratch_get(size_t bytes) {
+  pthread_once(&g_scratch_once, or_scratch_key_init);
+  or_scratch *s = (or_scratch *)pthread_getspecific(g_scratch_key);
+  if (!s) {
+    s = (or_scratch *)calloc(1, sizeof(or_scratch));
+    if (!s || pthread_setspecific(g_scratch_key, s) != 0) {
+      free(s);
+      return NULL;
+    }
+  }
+  if (s->bytes < bytes) {
+    free(s->buf);
+    s->buf = (unsigned char *)malloc(bytes);
+    s->bytes = s->buf ? bytes : 0;
+  }
+  return s->buf;
 }
 
 #define OR_FN or_dext_u32

@@ -70,3 +70,35 @@ def test_workspace_size_rejects_bad_shapes():
     from sfgb import api
     assert api.lib().sf_workspace_bytes(0, 5, 10) == 0
     assert api.lib().sf_workspace_bytes(4362, 4148, 1000) > 1000 * 16
+
+
+def test_noalloc_limits_are_the_documented_ones():
+    """The entry point that allocates nothing accepts a call when the
+    workspace layout fits its fixed 32 MiB and capacity is at most 524,288
+    records: an EIGER2 16M frame at the full capacity fits, one record more
+    is refused, and so is a frame whose layout is too large. Refusals happen
+    on the host, before any device is touched."""
+    from sfgb import api
+    L = api.lib()
+    f = L.sf_threshold_u32_device_noalloc
+    vp, sz = ctypes.c_void_p, ctypes.c_size_t
+    f.argtypes = [vp, sz, sz, ctypes.POINTER(api.ThresholdParams), vp, sz, vp, vp, vp, vp]
+    f.restype = ctypes.c_int
+    limit = 32 << 20
+    assert L.sf_workspace_bytes(4362, 4148, 524_288) <= limit
+    params = api.Params().c()
+    # Host-side refusals only: the pointers are never dereferenced.
+    fake = 1 << 20
+    assert f(fake, 4362, 4148, ctypes.byref(params), fake, 524_289, fake, fake, None,
+             None) == -1
+    assert "capacity" in api.last_error()
+    # A 2^25-pixel frame 16 pixels wide has too many tiles for the array.
+    h, w = (1 << 25) // 16, 16
+    assert L.sf_workspace_bytes(h, w, 524_288) > limit
+    assert f(fake, h, w, ctypes.byref(params), fake, 524_288, fake, fake, None, None) == -1
+    assert "32 MiB" in api.last_error()
+    # Every frame of up to 2^25 pixels with both sides at least 256 fits.
+    for h in (256, 1024, 4096, 5793, 32768, 131072):
+        w = (1 << 25) // h
+        if w >= 256:
+            assert L.sf_workspace_bytes(h, w, 524_288) <= limit, (h, w)

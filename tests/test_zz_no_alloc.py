@@ -46,7 +46,11 @@ def _host(o, capacity):
             o["bits"].cpu().numpy().tobytes(), o["prefix"].cpu().numpy().tobytes())
 
 
-def test_noalloc_matches_workspace_entry_point_twice():
+# The default parameters take the streamed lattice path; a non-integral
+# sigma_b takes the tile path, which uses the array's staging list, tile bases
+# and row totals as well.
+@pytest.mark.parametrize("param_set", [{}, {"sigma_b": 6.5}], ids=["lattice", "tile"])
+def test_noalloc_matches_workspace_entry_point_twice(param_set):
     torch = pytest.importorskip("torch")
     from sfgb import api, synth
     if not api.available():
@@ -56,7 +60,7 @@ def test_noalloc_matches_workspace_entry_point_twice():
     h, w, capacity = 1536, 1300, 200_000
     sweep = synth.Sweep(synth.preset("eiger_16m", height=h, width=w, n_frames=2,
                                      spots_per_frame=500.0, seed=4242))
-    params = api.Params().c()
+    params = api.Params(**param_set).c()
     stream = torch.cuda.current_stream()
     ws = torch.empty(L.sf_workspace_bytes(h, w, capacity), dtype=torch.uint8,
                      device="cuda")
