@@ -562,3 +562,43 @@ class Plan:
                                   ctypes.byref(found))
         _check(rc, "plan result")
         return out[: found.value].copy()
+
+    @property
+    def lists_ptr(self) -> int:
+        """Device address of frame 0's list (frame j's at + j * capacity records)."""
+        return lib().sf_plan_lists(self._p)
+
+    @property
+    def counts_ptr(self) -> int:
+        """Device address of the per-frame counts (uint32)."""
+        return lib().sf_plan_counts(self._p)
+
+    def mask(self, j: int) -> np.ndarray:
+        """Frame j's strong-pixel mask as booleans (h, w), after the plan's
+        work (host copy)."""
+        words_per_row = (self.w + 31) // 32
+        words = np.empty(self.words, np.uint32)
+        cudart = _cudart()
+        if cudart.cudaDeviceSynchronize() != 0:
+            raise SpotFinderError("cudaDeviceSynchronize failed")
+        src = lib().sf_plan_masks(self._p) + j * self.words * 4
+        if cudart.cudaMemcpy(ctypes.c_void_p(words.ctypes.data), ctypes.c_void_p(src),
+                             ctypes.c_size_t(words.nbytes), 2) != 0:
+            raise SpotFinderError("reading a plan's mask failed")
+        bits = np.unpackbits(words.view(np.uint8).reshape(self.h, words_per_row * 4), axis=1,
+                             bitorder="little")
+        return bits[:, : self.w].astype(bool)
+
+
+_cudart_lib = None
+
+
+def _cudart() -> ctypes.CDLL:
+    """The CUDA runtime libsfgb.so was linked against (already loaded)."""
+    global _cudart_lib
+    if _cudart_lib is None:
+        lib()
+        _cudart_lib = ctypes.CDLL("libcudart.so.13")
+        _cudart_lib.cudaMemcpy.restype = ctypes.c_int
+        _cudart_lib.cudaDeviceSynchronize.restype = ctypes.c_int
+    return _cudart_lib
