@@ -7,15 +7,18 @@ masked, Poisson background 0.3 at the edge rising to 1.5 at the centre, 3000
 spots per frame spanning 2-5 frames, dispersion_extended at the reference's
 defaults. Seeded synthetic frames stand in for detector data.
 
-A step is one batch of frames through the hot path. `value` is frames/s with
-the frames already in HBM (a pool of distinct frames larger than L2, cycled);
-`e2e` is the same metric through the C ABI's host-frame call (sf_find_u32,
-the gpu::find drop-in) with pinned host frames, so the host-to-device copy of
-each frame and the read-back of its signal list are inside the timed region.
-Its `bslz4_u32` / `bslz4_u16` entries time the same frames stored as
-bitshuffle+LZ4 chunks (as an EIGER's HDF5 files hold them) through
-sf_find_compressed: the chunk crosses the host link and is decoded and
-thresholded on the device.
+A step is one batch of 64 frames through the whole hot path: the threshold
+(a tuned plan's launch sequence replayed as a CUDA graph) and the 3-D
+labelling of the batch's signal lists into spots (sf_label_add_device), both
+on the device. `value` is frames/s with the frames already in HBM (a pool of
+distinct frames larger than L2, cycled); the roofline is the threshold's
+launch sequence, timed inside each step. `e2e` is the same path through the
+served API (sf_server_*): pinned host frames submitted at full rate, each
+copied in, thresholded and labelled in order, and every sweep's spot table
+read back, inside the timed region. Its `threshold_only` entry is the
+threshold alone through the C ABI's host-frame call (sf_find_u32, the
+gpu::find drop-in) from one host thread a core, with `u16` / `bslz4_u*`
+variants (16-bit frames; bitshuffle+LZ4 chunks decoded on the device).
 
 --impl reference times the reference's CPU path on this host's cores: the
 CPU restatement of dext() plus the streaming labeller (the reference's own
@@ -54,6 +57,14 @@ H, W = 4362, 4148
 # the launch: lat_stage01 5,266 MB, lat_verify 2,098 MB, lat_stage2 2,621 MB,
 # the scans and the list 1,250 MB); the algorithmic bytes are 76.5 MB a frame.
 DRAM_BYTES_PER_FRAME = 175.6e6
+
+
+# Kernels a timed step launches: the threshold plan's graph (lat_stage01,
+# lat_tiles, lat_verify, mask_sums, mask_prefix, lat_stage2, pass_sums,
+# pass_scatter) and the labeller's (27 kernels and six three-kernel
+# exclusive scans; sf_label.cu, Labeller::enqueue).
+THRESHOLD_KERNELS = 8
+LABEL_KERNELS = 45
 
 
 def dist_env():
@@ -332,6 +343,85 @@ def served(seconds: float = 4.0, seed: int = 4000, rates=None, chunks: bool = Fa
                         + "threshold and 3-D labelling of every frame (sf_server_*)"}
 
 
+def served_e2e(n_frames: int, frames_per_step: int, h2d_gbs=None, n_sweeps: int = 4,
+               pool: int = 8, chunks: bool = False) -> dict:
+    """The whole path end to end through the served API (sf_server_*): four
+    16M sweeps of pinned host frames (or, with `chunks`, their bitshuffle+LZ4
+    chunks) submitted as fast as the calls return, each frame copied in,
+    thresholded and labelled in order on the device; then every sweep
+    finished and its spot table read back to the host. Timed from the first
+    submit to the last spot table on the host."""
+    import ctypes
+    from sfgb import labeller, serve, synth
+    L = lab = serve._lib()
+    p = synth.preset("eiger_16m", n_frames=pool)
+    p.seed = p.seed + 77
+    sw = synth.Sweep(p)
+    host = []
+    for i in range(pool):
+        f = sw.frame(i)
+        data = synth.chunk(f) if chunks else f.view(np.uint8).ravel()
+        ptr = L.sf_host_alloc(data.size)
+        if not ptr:
+            raise SystemExit("sf_host_alloc failed")
+        np.ctypeslib.as_array((ctypes.c_uint8 * data.size).from_address(ptr))[:] = data
+        host.append((ptr, data.size))
+    srv = serve.Server(max_batch=16, ring=32)
+
+    def run(n_per_sweep):
+        ids = [srv.open_sweep(H, W) for _ in range(n_sweeps)]
+        for k in range(n_per_sweep):
+            # Consecutive frame numbers, a gap where the pool repeats.
+            for i, sid in enumerate(ids):
+                ptr, nbytes = host[(k + i) % pool]
+                if chunks:
+                    srv.submit_chunk(sid, k + k // pool, ptr, "bslz4", nbytes)
+                else:
+                    srv.submit(sid, k + k // pool, ptr)
+        want, got = n_per_sweep * n_sweeps, 0
+        deadline = time.perf_counter() + 120.0
+        while got < want and time.perf_counter() < deadline:
+            got += len(srv.poll(4096, 20))
+        if got < want:
+            raise SystemExit(f"served e2e: {got} of {want} frames done")
+        d2h = 0
+        for sid in ids:
+            srv.finish_sweep(sid, read=False)
+            h = L.sf_server_labeller(srv._s, sid)
+            ns = lab.sf_label_n_spots(h)
+            spots = np.empty(ns, labeller.SPOT_DTYPE)
+            if lab.sf_label_spots(h, spots.ctypes.data, ns) != 0:
+                raise SystemExit("served e2e: reading spots failed")
+            d2h += spots.nbytes
+            srv.close_sweep(sid)
+        return d2h
+
+    run(2 * pool)  # warm-up: every launch shape captured once
+    per = max(1, n_frames // n_sweeps)
+    t0 = time.perf_counter()
+    d2h = run(per)
+    dt = time.perf_counter() - t0
+    srv.close()
+    frames = per * n_sweeps
+    steps = frames / frames_per_step
+    h2d = sum(n for _, n in host) / pool * frames
+    for ptr, _ in host:
+        L.sf_host_free(ptr)
+    out = {"value": frames / dt, "unit": "frames/s",
+           "h2d_bytes_per_step": int(h2d / steps), "d2h_bytes_per_step": int(d2h / steps),
+           "frames": frames, "seconds": dt, "achieved_h2d_gbs": h2d / dt / 1e9,
+           "path": f"sf_server_* (the served API): {n_sweeps} 16M sweeps of "
+                   + ("bitshuffle+LZ4 chunks decoded on the device" if chunks else
+                      "raw uint32 frames") + " in pinned host memory, submitted at full rate, "
+                   "copied in, thresholded and labelled in frame order on the device; every "
+                   "sweep finished and its spot table read back to the host inside the timed "
+                   "region"}
+    if h2d_gbs and not chunks:
+        out["h2d_peak_gbs"] = h2d_gbs
+        out["frac_of_h2d_peak"] = out["achieved_h2d_gbs"] / h2d_gbs
+    return out
+
+
 def run_ours(args):
     import torch
     from sfgb import api
@@ -362,8 +452,35 @@ def run_ours(args):
     counts = np.array([len(plan.result(j)) for j in range(B)])
     n_signal = int(counts.mean())
 
+    # The timed step: the batch's threshold (the plan's graph) and the 3-D
+    # labelling of its lists on the device (sf_label_add_device: its launch
+    # sequence replayed as a graph, the call's status read back), so a step
+    # covers the path the reference's CPU arm times. Frame numbers are
+    # consecutive within a step, with a gap between steps (the same frames
+    # come round again) that closes the spots there.
+    from sfgb import labeller
+    lab = labeller.DeviceLabeller(H, W, live_capacity=(B + 16) * 200_000)
+    lists_ptr, counts_ptr = plan.lists_ptr, plan.counts_ptr
+    nb = [0]
+
+    def step():
+        plan(views, stream=stream)
+        ev_mid = torch.cuda.Event(enable_timing=True)
+        ev_mid.record(stream)
+        nb[0] += 1
+        lab.add_device(list(range(nb[0], nb[0] + B)), lists_ptr, plan.capacity, counts_ptr,
+                       stream.cuda_stream)
+        nb[0] += B
+        return ev_mid
+
+    with torch.cuda.stream(stream):
+        for w in range(args.warmup):
+            step()
+    stream.synchronize()
+
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
+    mids = []
     clocks = ClockSampler(local, args.clocks_csv)
     clocks.start()
     if world > 1:
@@ -374,7 +491,7 @@ def run_ours(args):
         start.record(stream)
         for s in range(args.steps):
             ev[s][0].record(stream)
-            plan(views, stream=stream)
+            mids.append(step())
             ev[s][1].record(stream)
         end.record(stream)
     torch.cuda.synchronize(dev)
@@ -385,7 +502,12 @@ def run_ours(args):
     elapsed_ms = max_over_ranks(elapsed_ms, world, dev)
     frames_done = sum_over_ranks(args.steps * B, world, dev)
     value = frames_done / (elapsed_ms / 1e3)
-    launch_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    # The threshold's share of each step (the plan's graph, CUDA events on
+    # its stream) sets the roofline; the labelling's the rest.
+    launch_ms = statistics.mean(a.elapsed_time(m) for (a, _), m in zip(ev, mids))
+    label_ms = statistics.mean(m.elapsed_time(b) for (_, b), m in zip(ev, mids))
+    label_res = lab.finish()
+    del lab
     graphs = plan.graphs
 
     # Roofline of the threshold launch sequence: algorithmic bytes per frame
@@ -393,6 +515,17 @@ def run_ours(args):
     algo_bytes = B * (H * W * 4 + (H * W + 7) // 8 + 16 * n_signal)
     peak, peak_kind = measured_peak_gbs()
     achieved = algo_bytes / (launch_ms / 1e3) / 1e9
+
+    # The threshold alone, the same plan and frames (the figure before the
+    # labelling joined the step).
+    with torch.cuda.stream(stream):
+        ta, tb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ta.record(stream)
+        for _ in range(args.steps):
+            plan(views, stream=stream)
+        tb.record(stream)
+    torch.cuda.synchronize(dev)
+    threshold_only = args.steps * B / (ta.elapsed_time(tb) / 1e3)
 
     # The plain per-frame device path (one launch sequence per frame).
     single = api.DeviceThreshold(H, W)
@@ -449,40 +582,11 @@ def run_ours(args):
         }
         del batch16, pool16, views16
 
-    # 3-D labelling of the batch's lists on the device (reported beside the
-    # threshold; its bytes are O(signal), outside the threshold roofline).
-    label = None
-    if not args.no_label:
-        from sfgb import labeller
-        # Room for a call's B lists plus the components they leave open.
-        lab = labeller.DeviceLabeller(H, W, live_capacity=(B + 16) * 200_000)
-        lists_ptr = api.lib().sf_plan_lists(plan._p)
-        counts_ptr = api.lib().sf_plan_counts(plan._p)
-        nb = 0
-        with torch.cuda.stream(stream):
-            plan(views, stream=stream)
-            # Warm-up calls also grow the labeller's host result buffers.
-            for w in range(max(args.warmup, 3)):
-                nb += 1
-                lab.add_device(list(range(nb, nb + B)), lists_ptr, plan.capacity, counts_ptr,
-                               stream.cuda_stream)
-                nb += B
-            torch.cuda.synchronize(dev)
-            t0 = time.perf_counter()
-            for s in range(args.steps):
-                # A gap between repeats of the pool closes its spots.
-                nb += 1
-                lab.add_device(list(range(nb, nb + B)), lists_ptr, plan.capacity, counts_ptr,
-                               stream.cuda_stream)
-                nb += B
-            t1 = time.perf_counter()
-            res = lab.finish()
-        label_ms = (t1 - t0) * 1e3 / (args.steps * B)
-        label = {"ms_per_frame": label_ms, "frames_per_s": 1e3 / label_ms,
-                 "threshold_and_label_frames_per_s": 1.0 / (1.0 / value + label_ms / 1e3),
-                 "spots": int(len(res.spots)),
-                 "path": f"sf_label_add_device on the plan's lists, {B} frames per call, "
-                         "consecutive frame numbers with a gap between repeats of the pool"}
+    label = {"ms_per_frame": label_ms / B, "frames_per_s": B / (label_ms / 1e3),
+             "spots": int(len(label_res.spots)),
+             "path": f"sf_label_add_device on the plan's lists, {B} frames per call (its "
+                     "launch sequence replayed as a CUDA graph, the call's status read "
+                     "back), inside each timed step after the threshold; CUDA events"}
 
     # The host link's own speed: pinned frames copied to the device.
     h2d_gbs = None
@@ -507,7 +611,7 @@ def run_ours(args):
 
     # End to end through the C ABI host-frame call (gpu::find drop-in), from
     # several host threads as mxi_find's -j workers call it.
-    e2e = None
+    e2e_thr = None
     if not args.no_e2e:
         import ctypes
         from concurrent.futures import ThreadPoolExecutor
@@ -551,7 +655,7 @@ def run_ours(args):
             d2h = sum(4 + 16 * n for n in ex.map(e2e_frame, range(n_e2e)))
             t1 = time.perf_counter()
         e_ms = max_over_ranks((t1 - t0) * 1e3, world, dev)
-        e2e = {"value": sum_over_ranks(n_e2e, world, dev) / (e_ms / 1e3),
+        e2e_thr = {"value": sum_over_ranks(n_e2e, world, dev) / (e_ms / 1e3),
                "unit": "frames/s", "h2d_bytes_per_step": B * H * W * 4,
                "d2h_bytes_per_step": int(d2h / args.steps),
                "path": f"sf_find_u32 (C ABI, gpu::find<uint32_t> drop-in) from {T} host "
@@ -560,9 +664,9 @@ def run_ours(args):
                "h2d_peak_gbs": h2d_gbs,
                "achieved_h2d_gbs": None,
                "frac_of_h2d_peak": None}
-        e2e["achieved_h2d_gbs"] = e2e["value"] * H * W * 4 / 1e9
+        e2e_thr["achieved_h2d_gbs"] = e2e_thr["value"] * H * W * 4 / 1e9
         if h2d_gbs:
-            e2e["frac_of_h2d_peak"] = e2e["achieved_h2d_gbs"] / h2d_gbs
+            e2e_thr["frac_of_h2d_peak"] = e2e_thr["achieved_h2d_gbs"] / h2d_gbs
         if not args.no_u16:
             # The same frames as 16-bit pixels through sf_find_u16 (the
             # gpu::find<uint16_t> drop-in): half the bytes over the host link.
@@ -596,7 +700,7 @@ def run_ours(args):
                 list(ex.map(e2e_frame16, range(args.steps * B)))
                 t1 = time.perf_counter()
             v16 = args.steps * B / (t1 - t0)
-            e2e["u16"] = {"value": v16, "unit": "frames/s",
+            e2e_thr["u16"] = {"value": v16, "unit": "frames/s",
                           "h2d_bytes_per_step": B * H * W * 2,
                           "achieved_h2d_gbs": v16 * H * W * 2 / 1e9,
                           "path": f"sf_find_u16 from {T} host threads, the same frames as "
@@ -644,7 +748,7 @@ def run_ours(args):
                     nbytes = sum(ex.map(e2e_chunk, range(args.steps * B)))
                     t1 = time.perf_counter()
                 vc = args.steps * B / (t1 - t0)
-                e2e[f"bslz4_u{depth}"] = {
+                e2e_thr[f"bslz4_u{depth}"] = {
                     "value": vc, "unit": "frames/s",
                     "h2d_bytes_per_step": int(nbytes / args.steps),
                     "compression": args.steps * B * H * W * depth / 8 / nbytes,
@@ -656,6 +760,15 @@ def run_ours(args):
                     L.sf_host_free(ptr)
         for ptr in host + outs:
             L.sf_host_free(ptr)
+
+    # End to end through the served API (the whole path: host frames in,
+    # threshold, 3-D labelling, the spot tables read back), fed at full rate.
+    e2e = None
+    if not args.no_e2e:
+        e2e = served_e2e(args.steps * B, B, h2d_gbs)
+        e2e["threshold_only"] = e2e_thr
+        if not args.no_bslz4:
+            e2e["bslz4_u32"] = served_e2e(args.steps * B, B, h2d_gbs, chunks=True)
 
     served_line = None
     if rank == 0 and not args.no_served:
@@ -700,11 +813,14 @@ def run_ours(args):
                                      f"({pool_n * H * W * 4 / 1e9:.2f} GB), cycled",
                        "l2": "inputs larger than L2: each frame is 72.4 MB and "
                              "consecutive frames differ",
-                       "stage": "threshold (all three dext stages + ordered emit), "
-                                f"{B} frames per launch sequence",
+                       "stage": "threshold (all three dext stages + ordered emit) and 3-D "
+                                f"labelling (grouping, filters, spot table), {B} frames a step",
                        "signal_pixels_per_frame": n_signal,
+                       "threshold_only_frames_per_s": threshold_only,
                        "plain_per_frame_frames_per_s": per_frame,
-                       "batched_over_plain": value / per_frame,
+                       "batched_over_plain": threshold_only / per_frame,
+                       "threshold_ms_per_step": launch_ms,
+                       "labelling_ms_per_step": label_ms,
                        "tuned_run_rows": run_rows, "cuda_graphs": graphs},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
@@ -719,7 +835,7 @@ def run_ours(args):
             "cpu_baseline": base, "e2e": e2e, "labelling": label, "u16": u16_line,
             "served": served_line,
             "clocks": clock,
-            "gpu_launches": 8 * args.steps,
+            "gpu_launches": (THRESHOLD_KERNELS + LABEL_KERNELS) * args.steps,
         }
         print(json.dumps(line))
     if world > 1:
@@ -740,7 +856,6 @@ def main(argv=None):
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-threads", type=int, default=0,
                     help="host threads of the end-to-end legs (0: one a core, as mxi_find -j)")
-    ap.add_argument("--no-label", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-u16", action="store_true")
     ap.add_argument("--no-bslz4", action="store_true")

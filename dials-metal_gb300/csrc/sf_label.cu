@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <climits>
 #include <cstring>
 #include <mutex>
@@ -41,15 +42,20 @@ int fail(cudaError_t e, const char *what);
 
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr int kThreads = 256;
-constexpr int kGrid = 2 * 152;          // persistent grid-stride launches
+constexpr int kGrid = 2 * 152;          // the bucket partition's chunks
+constexpr int kPassGrid = 8 * 152;      // grid-stride passes over pixels / candidates
+constexpr int kSortGrid = 6 * 152;      // warp sorts: 6 blocks an SM (registers)
 constexpr int kWarpSortMax = 1024;      // members sorted by one warp
 constexpr int kBlockSortMax = 8192;     // members sorted by one block
 constexpr int kUnionRetries = 1 << 20;  // cap on a union's CAS retries
+// Frames up to this many rows get per-row start tables, so that a pixel's
+// neighbours above and on the previous frame are searched for within one row
+// of the ascending list instead of the whole frame.
+constexpr uint32_t kRowTableMaxRows = 1u << 16;
 
 enum : uint32_t {
   kErrLiveFull = 1u,   // more open pixels than the live pool holds
   kErrUnion = 2u,      // a union did not settle within kUnionRetries
-  kErrSpotSize = 4u,   // an accepted spot larger than kBlockSortMax
   kErrOutFull = 8u,    // more spots / kept pixels than the batch outputs hold
   kErrListOverflow = 16u, // an input list's count exceeds its stride
 };
@@ -62,6 +68,8 @@ struct LabelStatus {
   uint32_t prev_start;  // first live position of the last added frame
   uint32_t n_total;     // n_live + the batch's pixels
   uint32_t n_closing, n_cand, n_cand_pixels, n_accept, n_accept_pixels, n_open;
+  uint32_t n_big;       // candidates beyond a warp's sort, listed for the block sorts
+  uint32_t n_edges;     // edges k_link listed for k_unite
   uint32_t frame_off[kLabelMaxBatch + 1];
   unsigned long long counts[6];
 };
@@ -77,6 +85,7 @@ struct BatchArgs {
   int finishing;        // close everything (finish(), dials_spots.cc:147-151)
   int two_d;
   uint32_t width, npix;
+  uint32_t wdiv_m, wdiv_s1, wdiv_s2;  // division by width (multiply-high)
   uint32_t min_size, max_size;
   double max_separation;
   int32_t frames[kLabelMaxBatch];
@@ -121,14 +130,17 @@ __device__ __forceinline__ void uf_unite(uint32_t *parent, uint32_t a, uint32_t 
   atomicOr(&st->error, kErrUnion);
 }
 
-__device__ __forceinline__ uint32_t lower_bound(const uint32_t *v, uint32_t lo, uint32_t hi,
-                                                uint32_t key) {
-  while (lo < hi) {
-    const uint32_t mid = lo + ((hi - lo) >> 1);
-    if (v[mid] < key)
-      lo = mid + 1;
-    else
-      hi = mid;
+// lower_bound with the same number of steps in every lane of the warp (the
+// longest range's), so that the lanes stay together; all lanes call it.
+__device__ __forceinline__ uint32_t lower_bound_warp(const uint32_t *__restrict__ v,
+                                                     uint32_t lo, uint32_t hi, uint32_t key) {
+  uint32_t len = hi - lo;
+  const uint32_t longest = __reduce_max_sync(0xffffffffu, len);
+  for (int steps = 32 - __clz(longest); steps > 0; steps--) {
+    const uint32_t half = len >> 1;
+    const bool right = len > 0 && v[lo + half] < key;
+    lo = right ? lo + half + 1 : lo;
+    len = right ? len - half - 1 : half;
   }
   return lo;
 }
@@ -156,6 +168,8 @@ __global__ void k_offsets(LabelStatus *st, const BatchArgs *__restrict__ ap,
     off += counts[j];
   }
   st->frame_off[a.nb] = off;
+  st->n_big = 0;
+  st->n_edges = 0;
   const unsigned long long total = (unsigned long long)st->n_live + off;
   if (total > capacity) {
     st->error |= kErrLiveFull;
@@ -165,6 +179,12 @@ __global__ void k_offsets(LabelStatus *st, const BatchArgs *__restrict__ ap,
   st->counts[kCntSignal] += off;
 }
 
+// The batch's lists into the pool. Each warp appends 32 consecutive pixels
+// and points each one straight at the first pixel of its run (consecutive
+// indices of one row) within those 32: the union-find then starts from trees
+// one level deep instead of chains along the rows, whose finds would walk
+// the row at memory latency. Runs crossing a warp's boundary are joined by
+// k_link's left-neighbour union.
 __global__ void k_append(LabelStatus *st, const BatchArgs *__restrict__ ap, int32_t *frame,
                          uint32_t *index, uint32_t *value, uint32_t *parent) {
   if (st->error)
@@ -175,22 +195,112 @@ __global__ void k_append(LabelStatus *st, const BatchArgs *__restrict__ ap, int3
   const int j = blockIdx.y;
   const uint32_t n = st->frame_off[j + 1] - st->frame_off[j];
   const uint32_t base = st->n_live + st->frame_off[j];
+  const uint32_t width = a.width;
   const sf_signal_pixel *list = lists + (size_t)j * stride;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += gridDim.x * blockDim.x) {
-    const sf_signal_pixel s = list[i];
-    const uint32_t p = base + i;
-    frame[p] = a.frames[j];
-    index[p] = s.index;
-    value[p] = s.value;
-    parent[p] = p;
+  const int lane = threadIdx.x & 31;
+  for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < n;
+       i0 += gridDim.x * blockDim.x) {  // warp-uniform
+    const uint32_t i = i0 + lane;
+    const bool in = i < n;
+    sf_signal_pixel s;
+    s.index = 0;
+    s.value = 0;
+    if (in)
+      s = list[i];
+    const uint32_t before = __shfl_up_sync(0xffffffffu, s.index, 1);
+    const bool starts = !in || lane == 0 || s.index % width == 0 || before != s.index - 1;
+    const unsigned mask = __ballot_sync(0xffffffffu, starts) & (0xffffffffu >> (31 - lane));
+    if (in) {
+      const uint32_t p = base + i;
+      frame[p] = a.frames[j];
+      index[p] = s.index;
+      value[p] = s.value;
+      parent[p] = base + i0 + (31 - __clz(mask));
+    }
+  }
+}
+
+// Per-row start tables of the frames a batch links: segment 0 is the frame
+// before the batch (the live pool's tail, [prev_start, n_live)), segment
+// j + 1 the batch's frame j. rows[s * (height + 1) + y] is the first position
+// of segment s whose index is at or beyond row y; entry `height` is the
+// segment's end. Every entry is written once: by the pixel that starts the
+// row (or the first pixel after a run of empty rows), or by the segment's
+// last pixel for the rows after it.
+__global__ void k_rows(LabelStatus *st, const BatchArgs *__restrict__ ap,
+                       const uint32_t *__restrict__ index, uint32_t *__restrict__ rows,
+                       uint32_t height) {
+  if (st->error)
+    return;
+  const BatchArgs &a = *ap;
+  const int s = blockIdx.y;
+  uint32_t lo, hi;
+  if (s == 0) {
+    if (!a.link_prev[0])
+      return;  // the batch's first frame does not link back: no table needed
+    lo = st->prev_start;
+    hi = st->n_live;
+  } else {
+    lo = st->n_live + st->frame_off[s - 1];
+    hi = st->n_live + st->frame_off[s];
+  }
+  uint32_t *row = rows + (size_t)s * (height + 1);
+  const uint32_t width = a.width;
+  const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+  if (lo == hi) {
+    for (uint32_t y = t0; y <= height; y += nt)
+      row[y] = lo;
+    return;
+  }
+  for (uint32_t p = lo + t0; p < hi; p += nt) {
+    const uint32_t y = index[p] / width;
+    const uint32_t first = p == lo ? 0u : index[p - 1] / width + 1u;
+    for (uint32_t r = first; r <= y; r++)
+      row[r] = p;
+    if (p == hi - 1)
+      for (uint32_t r = y + 1; r <= height; r++)
+        row[r] = hi;
+  }
+}
+
+// Appends this lane's edge (p, q), if `want`, to the batch's edge list (one
+// atomic a warp); a lane whose edge finds the list full joins it at once.
+__device__ __forceinline__ void push_edge(bool want, uint32_t p, uint32_t q, LabelStatus *st,
+                                          uint2 *edges, uint32_t edge_cap, uint32_t *parent) {
+  const unsigned m = __ballot_sync(0xffffffffu, want);
+  if (!m)
+    return;
+  const int lane = threadIdx.x & 31;
+  uint32_t base = 0;
+  if (lane == __ffs(m) - 1)
+    base = atomicAdd(&st->n_edges, (uint32_t)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+  if (want) {
+    const uint32_t at = base + __popc(m & ((1u << lane) - 1u));
+    if (at < edge_cap)
+      edges[at] = make_uint2(p, q);
+    else
+      uf_unite(parent, p, q, st);
   }
 }
 
 // dials_spots.cc:106-137: left (same row), above (same frame), and the same
-// index on the previous frame when it is the one before.
+// index on the previous frame when it is the one before. With row tables
+// (rows non-null) the searches stay within one row of the list. The edges
+// found go to a list that k_unite joins with every lane busy (here most lanes
+// have none, and the joins' loops would run with a lane or two).
+//
+// Only the unions the others do not already imply are listed: k_append
+// joined each run within its 32-pixel chunk, so the left link is needed only
+// at a chunk's first pixel; and a pixel whose left neighbour (same run) has
+// its own neighbour above (or on the previous frame) just left of this
+// pixel's is joined through them -- those two are consecutive in their row,
+// so in one run. Each overlap of two runs is listed once, at its first pixel.
+// The components, and so the roots (lowest positions), are the same.
 __global__ void k_link(LabelStatus *st, const BatchArgs *__restrict__ ap,
-                       const uint32_t *__restrict__ index, uint32_t *parent) {
+                       const uint32_t *__restrict__ index, uint32_t *parent,
+                       const uint32_t *__restrict__ rows, uint32_t height, uint2 *edges,
+                       uint32_t edge_cap) {
   const BatchArgs &a = *ap;
   if (st->error)
     return;
@@ -203,22 +313,51 @@ __global__ void k_link(LabelStatus *st, const BatchArgs *__restrict__ ap,
     plo = j == 0 ? st->prev_start : st->n_live + st->frame_off[j - 1];
     phi = j == 0 ? st->n_live : start;
   }
-  for (uint32_t p = start + blockIdx.x * blockDim.x + threadIdx.x; p < end;
-       p += gridDim.x * blockDim.x) {
-    const uint32_t idx = index[p];
-    if (p > start && idx % width != 0 && index[p - 1] == idx - 1)
-      uf_unite(parent, p, p - 1, st);
-    if (idx >= width) {
+  const uint32_t *own = rows ? rows + (size_t)(j + 1) * (height + 1) : nullptr;
+  const uint32_t *before = rows ? rows + (size_t)j * (height + 1) : nullptr;
+  const int lane = threadIdx.x & 31;
+  for (uint32_t p0 = start + blockIdx.x * blockDim.x + (threadIdx.x & ~31u); p0 < end;
+       p0 += gridDim.x * blockDim.x) {  // warp-uniform
+    const uint32_t p = p0 + lane;
+    const bool in = p < end;
+    const uint32_t idx = in ? index[p] : 0u;
+    const uint32_t y = idx / width, x = idx - y * width;
+    const bool left = in && p > start && x != 0 && index[p - 1] == idx - 1;
+    push_edge(left && ((p - start) & 31u) == 0, p, p - 1, st, edges, edge_cap, parent);
+    {
       const uint32_t t = idx - width;
-      const uint32_t q = lower_bound(index, start, p, t);
-      if (q < p && index[q] == t)
-        uf_unite(parent, p, q, st);
+      uint32_t lo = 0, hi = 0;
+      if (in && y > 0) {
+        lo = own ? own[y - 1] : start;
+        hi = own ? own[y] : p;
+      }
+      const uint32_t q = lower_bound_warp(index, lo, hi, t);
+      push_edge(q < hi && index[q] == t && !(left && q > lo && index[q - 1] == t - 1), p, q,
+                st, edges, edge_cap, parent);
     }
-    if (phi > plo) {
-      const uint32_t q = lower_bound(index, plo, phi, idx);
-      if (q < phi && index[q] == idx)
-        uf_unite(parent, p, q, st);
+    if (phi > plo) {  // uniform: the frame links back or not
+      uint32_t lo = 0, hi = 0;
+      if (in) {
+        lo = before ? before[y] : plo;
+        hi = before ? before[y + 1] : phi;
+      }
+      const uint32_t q = lower_bound_warp(index, lo, hi, idx);
+      push_edge(q < hi && index[q] == idx && !(left && q > lo && index[q - 1] == idx - 1), p,
+                q, st, edges, edge_cap, parent);
     }
+  }
+}
+
+// The listed edges joined, a thread each.
+__global__ void k_unite(LabelStatus *st, const uint2 *__restrict__ edges, uint32_t edge_cap,
+                        uint32_t *parent) {
+  if (st->error)
+    return;
+  const uint32_t n = min(st->n_edges, edge_cap);
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += gridDim.x * blockDim.x) {
+    const uint2 pq = edges[e];
+    uf_unite(parent, pq.x, pq.y, st);
   }
 }
 
@@ -472,26 +611,32 @@ __global__ void k_gather(LabelStatus *st, const uint32_t *__restrict__ root,
   }
 }
 
-// Bitonic sort of m values (padded to a power of two with kNone) in shared
-// memory by `nt` cooperating threads numbered t.
-__device__ void bitonic_sort(uint32_t *s, int m, int t, int nt, bool warp_only) {
+// Bitonic sort of s[0 .. n) in shared memory by `nt` cooperating threads
+// numbered t, ascending. Every comparator puts the smaller value first (each
+// merge starts by comparing element i with its mirror in its block), so the
+// length needs no padding: a comparator whose second element lies at or
+// beyond n would leave the first in place, as if against +infinity, and is
+// skipped. Threads walk the comparators, not the elements.
+__device__ void bitonic_sort(uint32_t *s, int n, int t, int nt, bool warp_only) {
   int size = 1;
-  while (size < m)
+  while (size < n)
     size <<= 1;
-  for (int i = m + t; i < size; i += nt)
-    s[i] = kNone;
-  if (warp_only)
-    __syncwarp();
-  else
-    __syncthreads();
   for (int k = 2; k <= size; k <<= 1) {
     for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = t; i < size; i += nt) {
-        const int l = i ^ j;
-        if (l > i) {
+      const int lj = __ffs(j) - 1;
+      for (int q = t; q < (size >> 1); q += nt) {
+        const int blk = q >> lj, r = q & (j - 1);
+        int i, l;
+        if (j == (k >> 1)) {
+          i = blk * k + r;
+          l = blk * k + k - 1 - r;
+        } else {
+          i = (blk << (lj + 1)) + r;
+          l = i + j;
+        }
+        if (l < n) {
           const uint32_t x = s[i], y = s[l];
-          const bool up = (i & k) == 0;
-          if ((x > y) == up) {
+          if (x > y) {
             s[i] = y;
             s[l] = x;
           }
@@ -503,6 +648,27 @@ __device__ void bitonic_sort(uint32_t *s, int m, int t, int nt, bool warp_only) 
         __syncthreads();
     }
   }
+}
+
+// The same network for at most 32 values, one a lane, in registers: lane
+// `lane` returns the lane-th smallest (values of lanes at or beyond n are
+// +infinity).
+__device__ __forceinline__ uint32_t warp_sort32(uint32_t v, int n, int lane) {
+  if (lane >= n)
+    v = kNone;
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      // Partner: the mirror within the block of k at the merge's first step,
+      // else the lane j away; the lower lane keeps the smaller value.
+      const int partner = j == (k >> 1) ? (lane ^ (k - 1)) : (lane ^ j);
+      const uint32_t o = __shfl_sync(0xffffffffu, v, partner);
+      const bool low = lane < partner;
+      v = low ? min(v, o) : max(v, o);
+    }
+  }
+  return v;
 }
 
 // The first-pass sums of the reference's emit() (dials_spots.cc:240-276) in
@@ -551,93 +717,118 @@ __device__ __forceinline__ void fp_add(FirstPass &f, uint32_t k, uint32_t v, int
   }
 }
 
-__device__ __forceinline__ void fp_merge(FirstPass &f, const FirstPass &g) {
-  f.S += g.S;
-  f.Q2 += g.Q2;
-  for (int a = 0; a < 3; a++)
-    f.W[a] += g.W[a];
-  for (int a = 0; a < 6; a += 2) {
-    f.bb[a] = min(f.bb[a], g.bb[a]);
-    f.bb[a + 1] = max(f.bb[a + 1], g.bb[a + 1]);
-  }
-  if (g.peak_k != 0xFFFFFFFFu &&
-      (g.peak_v > f.peak_v || (g.peak_v == f.peak_v && g.peak_k < f.peak_k))) {
-    f.peak_v = g.peak_v;
-    f.peak_k = g.peak_k;
-  }
-  f.exact = f.exact && g.exact;
-}
-
 __device__ __forceinline__ bool fp_finish(FirstPass &f) {
   const unsigned long long lim = 1ull << 53;
   f.exact = f.exact && f.S < lim && f.Q2 < lim && f.W[0] < lim && f.W[1] < lim && f.W[2] < lim;
   return f.exact;
 }
 
-// The member's pixel: (x, y, z) and value.
-__device__ __forceinline__ void member(const uint32_t q, const int32_t *frame,
-                                       const uint32_t *index, const uint32_t *value,
-                                       uint32_t width, int32_t *x, int32_t *y, int32_t *z,
-                                       uint32_t *v) {
-  const uint32_t idx = index[q];
-  *x = (int32_t)(idx % width);
-  *y = (int32_t)(idx / width);
-  *z = frame[q];
-  *v = value[q];
+// ---------------------------------------------------------------------------
+// Emission (dials_spots.cc:221-360), arranged for GB300's FP64 rate (a small
+// fraction of its integer rate: an FP64 instruction takes its issue slots on
+// the FP64 pipe however few of its lanes are used). Every FP64 operation is
+// the reference's, in its order; the work is laid out so that the lanes of
+// each FP64 instruction are busy:
+//
+//   k_sort         a warp per candidate (a block beyond kWarpSortMax members,
+//                  a block sorting in global memory beyond kBlockSortMax):
+//                  members sorted into (frame, index) order and copied out as
+//                  pixel records, each tagged with its candidate.
+//   k_first        a warp per candidate: the first pass as exact integer
+//                  sums across the lanes (redux.sync); its FP64 part (the
+//                  centroid divisions, the peak-separation test) then runs
+//                  for 32 candidates at once, one a lane.
+//   k_pix          a thread per member: the accepted spots' pixels out.
+//   k_terms        a thread per member: its three variance-pass terms
+//                  RN(RN(v d) d), d = (c + 0.5) - centre.
+//   k_perm_*       the candidates ordered by size (largest first), so that
+//                  the candidates sharing a warp in k_var have similar sizes.
+//   k_var          four lanes per candidate, in size order: one axis a lane,
+//                  the terms summed with rounding in member order (the one
+//                  part whose order matters), the variances, the spot record.
+//
+// Where the integer sums could be inexact (a value of 2^26 or more, a
+// coordinate beyond 2^20, sums beyond 2^53) the thread runs the reference's
+// double sequence instead.
+// ---------------------------------------------------------------------------
+
+// What k_var needs of a candidate, from the first pass.
+struct CandSpot {
+  double pos[3];      // xyzobs (after the single-frame z and zero-sum rules)
+  double cz;          // the z centroid before the single-frame rule: the variance pass's centre
+  double sum, sum_sq; // intensity and the sum of squares
+  int32_t bb[6];
+  uint32_t n, mode;   // mode: kModeExact | kModeSpread
+};
+enum : uint32_t { kModeExact = 1u, kModeSpread = 2u };
+
+// Members whose loads a thread keeps in flight in its sequential passes.
+constexpr int kPipe = 8;
+
+// x = index mod width, y = index / width by the batch's multiply-high
+// divisor (Granlund & Montgomery's round-up method, exact for every 32-bit
+// index and width).
+__device__ __forceinline__ void pixel_xyz(const sf_pixel &px, const BatchArgs &a, int32_t *x,
+                                          int32_t *y, int32_t *z) {
+  const uint32_t t = __umulhi(px.index, a.wdiv_m);
+  const uint32_t y0 = (t + ((px.index - t) >> a.wdiv_s1)) >> a.wdiv_s2;
+  *x = (int32_t)(px.index - y0 * a.width);
+  *y = (int32_t)y0;
+  *z = px.frame;
 }
 
-// The reference's emit() (dials_spots.cc:240-353) over members sorted into
-// (frame, index) order: the first pass from exact integers when they are
-// exact (else the double sequence), then the variance pass sequentially in
-// double, the same operations in the same order as the reference. The
-// variance pass is skipped when only acceptance is wanted. Returns false if
-// the peak-centroid filter rejects the spot.
-__device__ bool emit_spot(const uint32_t *mem, uint32_t n, const int32_t *frame,
-                          const uint32_t *index, const uint32_t *value, uint32_t width,
-                          double max_separation, sf_spot *spot, bool variance = true,
-                          const FirstPass *given = nullptr) {
-  FirstPass f;
-  if (given) {
-    f = *given;
-  } else {
-    fp_init(f);
-    for (uint32_t k = 0; k < n; k++) {
-      int32_t x, y, z;
-      uint32_t v;
-      member(mem[k], frame, index, value, width, &x, &y, &z, &v);
-      fp_add(f, k, v, x, y, z);
-    }
-    fp_finish(f);
-  }
-  double sum, sum_sq, weighted[3], peak[3];
+// c + 0.5 as a double for an integer 0 <= c < 2^30, built from the bits of
+// 2c + 1 (exactly the value (double)c + 0.5 rounds to, with no FP64 work).
+__device__ __forceinline__ double half_up(uint32_t c) {
+  const uint32_t u = 2u * c + 1u;
+  const int e = 31 - __clz(u);
+  const unsigned long long m = ((unsigned long long)u << (52 - e)) & ((1ull << 52) - 1ull);
+  return __longlong_as_double(((unsigned long long)(1022 + e) << 52) | m);
+}
+
+// (double)v for an unsigned 32-bit v, from its bits.
+__device__ __forceinline__ double exact_double(uint32_t v) {
+  if (v == 0)
+    return 0.0;
+  const int e = 31 - __clz(v);
+  const unsigned long long m = ((unsigned long long)v << (52 - e)) & ((1ull << 52) - 1ull);
+  return __longlong_as_double(((unsigned long long)(1023 + e) << 52) | m);
+}
+
+// The FP64 part of the first pass of emit() and the peak-separation test
+// (dials_spots.cc:240-330) for one candidate whose members mp[0 .. n) are in
+// member order: from the exact integer sums f when f.exact, else the
+// reference's double sequence over the members. Fills *out and returns
+// acceptance.
+__device__ bool accept_candidate(const sf_pixel *mp, uint32_t n, const BatchArgs &a,
+                                 const FirstPass &f, CandSpot *out) {
+  CandSpot c;
+  double weighted[3], peak[3] = {0.0, 0.0, 0.0};
   if (f.exact) {
-    sum = (double)f.S;
-    sum_sq = (double)f.Q2;
+    c.sum = (double)f.S;
+    c.sum_sq = (double)f.Q2;
     for (int ax = 0; ax < 3; ax++)
       weighted[ax] = __dmul_rn((double)f.W[ax], 0.5);  // exact: W < 2^53
-    peak[0] = peak[1] = peak[2] = 0.0;
     if (f.peak_k != 0xFFFFFFFFu) {
       int32_t px, py, pz;
-      uint32_t pv;
-      member(mem[f.peak_k], frame, index, value, width, &px, &py, &pz, &pv);
+      pixel_xyz(mp[f.peak_k], a, &px, &py, &pz);
       peak[0] = __dadd_rn((double)px, 0.5);
       peak[1] = __dadd_rn((double)py, 0.5);
       peak[2] = __dadd_rn((double)pz, 0.5);
     }
   } else {
-    sum = sum_sq = 0.0;
+    c.sum = c.sum_sq = 0.0;
     weighted[0] = weighted[1] = weighted[2] = 0.0;
-    peak[0] = peak[1] = peak[2] = 0.0;
     uint32_t peak_value = 0;
     for (uint32_t k = 0; k < n; k++) {
       int32_t x, y, z;
-      uint32_t v;
-      member(mem[k], frame, index, value, width, &x, &y, &z, &v);
+      pixel_xyz(mp[k], a, &x, &y, &z);
+      const uint32_t v = mp[k].value;
       const double val = (double)v;
       const double pos[3] = {__dadd_rn((double)x, 0.5), __dadd_rn((double)y, 0.5),
                              __dadd_rn((double)z, 0.5)};
-      sum = __dadd_rn(sum, val);
-      sum_sq = __dadd_rn(sum_sq, __dmul_rn(val, val));
+      c.sum = __dadd_rn(c.sum, val);
+      c.sum_sq = __dadd_rn(c.sum_sq, __dmul_rn(val, val));
       for (int ax = 0; ax < 3; ax++)
         weighted[ax] = __dadd_rn(weighted[ax], __dmul_rn(val, pos[ax]));
       if (v > peak_value) {
@@ -646,291 +837,459 @@ __device__ bool emit_spot(const uint32_t *mem, uint32_t n, const int32_t *frame,
       }
     }
   }
-  sf_spot s;
-  for (int a = 0; a < 6; a++)
-    s.bbox[a] = f.bb[a];
-  s.intensity = sum;
-  s.intensity_variance = sum;
-  s.n_signal = n;
-  s.first = 0;
-  s.variance[0] = s.variance[1] = s.variance[2] = 0.0;
-  const double pixel_variance = 1.0 / 12.0;
-  if (sum > 0.0) {
+  for (int b = 0; b < 6; b++)
+    c.bb[b] = f.bb[b];
+  c.n = n;
+  c.mode = (f.exact ? kModeExact : 0u) | (c.sum > 0.0 ? kModeSpread : 0u);
+  if (c.sum > 0.0) {
     for (int ax = 0; ax < 3; ax++)
-      s.position[ax] = __ddiv_rn(weighted[ax], sum);
-    if (variance) {
-      double delta_sq[3] = {0.0, 0.0, 0.0};
-      for (uint32_t k = 0; k < n; k++) {
-        int32_t x, y, z;
-        uint32_t v;
-        member(mem[k], frame, index, value, width, &x, &y, &z, &v);
-        const double val = (double)v;
-        const double pos[3] = {__dadd_rn((double)x, 0.5), __dadd_rn((double)y, 0.5),
-                               __dadd_rn((double)z, 0.5)};
-        for (int ax = 0; ax < 3; ax++) {
-          const double d = __dsub_rn(pos[ax], s.position[ax]);
-          delta_sq[ax] = __dadd_rn(delta_sq[ax], __dmul_rn(__dmul_rn(val, d), d));
-        }
-      }
-      const double ss = __dmul_rn(sum, sum);
-      if (ss > sum_sq) {
-        for (int ax = 0; ax < 3; ax++) {
-          const double var = __ddiv_rn(__dmul_rn(delta_sq[ax], sum), __dsub_rn(ss, sum_sq));
-          s.variance[ax] = __dadd_rn(__ddiv_rn(var, sum), pixel_variance);
-        }
-      } else {
-        for (int ax = 0; ax < 3; ax++)
-          s.variance[ax] = pixel_variance;
-      }
-    }
-    if (s.bbox[5] == s.bbox[4] + 1)
-      s.position[2] = __dadd_rn((double)s.bbox[4], 0.5);
+      c.pos[ax] = __ddiv_rn(weighted[ax], c.sum);
+    c.cz = c.pos[2];
+    if (c.bb[5] == c.bb[4] + 1)
+      c.pos[2] = __dadd_rn((double)c.bb[4], 0.5);
   } else {
-    s.position[0] = __ddiv_rn((double)(s.bbox[1] + s.bbox[0]), 2.0);
-    s.position[1] = __ddiv_rn((double)(s.bbox[3] + s.bbox[2]), 2.0);
-    s.position[2] = __ddiv_rn((double)(s.bbox[5] + s.bbox[4]), 2.0);
+    c.pos[0] = __ddiv_rn((double)(c.bb[1] + c.bb[0]), 2.0);
+    c.pos[1] = __ddiv_rn((double)(c.bb[3] + c.bb[2]), 2.0);
+    c.pos[2] = __ddiv_rn((double)(c.bb[5] + c.bb[4]), 2.0);
+    c.cz = c.pos[2];
   }
-  *spot = s;
-  if (max_separation > 0.0) {
-    const double dx = __dsub_rn(peak[0], s.position[0]);
-    const double dy = __dsub_rn(peak[1], s.position[1]);
-    const double dz = __dsub_rn(peak[2], s.position[2]);
-    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-    if (__dsqrt_rn(d2) > max_separation)
+  *out = c;
+  if (a.max_separation > 0.0) {
+    const double dx = __dsub_rn(peak[0], c.pos[0]);
+    const double dy = __dsub_rn(peak[1], c.pos[1]);
+    const double dz = __dsub_rn(peak[2], c.pos[2]);
+    const double d2 =
+        __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    if (__dsqrt_rn(d2) > a.max_separation)
       return false;
   }
   return true;
 }
 
-// One warp per candidate of up to kWarpSortMax members (or one block per
-// candidate of up to kBlockSortMax): sort the members into (frame, index)
-// order, write them back, run emit() and record acceptance.
+// Member k (in member order) of candidate c: its pixel record and tag.
+__device__ __forceinline__ void put_member(uint32_t q, uint32_t k, uint32_t c, uint32_t off,
+                                           const int32_t *__restrict__ frame,
+                                           const uint32_t *__restrict__ index,
+                                           const uint32_t *__restrict__ value, sf_pixel *mpix,
+                                           uint32_t *mcand) {
+  sf_pixel px;
+  px.frame = frame[q];
+  px.index = index[q];
+  px.value = value[q];
+  mpix[off + k] = px;
+  mcand[off + k] = c;
+}
+
+// Candidates of up to kWarpSortMax members, a warp each (BLOCK false), or of
+// up to kBlockSortMax, a block each (BLOCK true, from the list the warps
+// made): member positions sorted in shared memory by bitonic sort, then
+// copied out in member order as pixel records.
 template <bool BLOCK>
 __global__ void __launch_bounds__(kThreads)
-k_sort_accept(LabelStatus *st, const BatchArgs *__restrict__ ap,
-              const uint32_t *__restrict__ cand_n,
-              const uint32_t *__restrict__ cand_off, uint32_t *members,
-              const int32_t *__restrict__ frame, const uint32_t *__restrict__ index,
-              const uint32_t *__restrict__ value, uint32_t *acc, uint32_t *acc_n) {
-  const BatchArgs &a = *ap;
+k_sort(LabelStatus *st, const uint32_t *__restrict__ cand_n,
+       const uint32_t *__restrict__ cand_off, const uint32_t *__restrict__ members,
+       const int32_t *__restrict__ frame, const uint32_t *__restrict__ index,
+       const uint32_t *__restrict__ value, sf_pixel *mpix, uint32_t *mcand, uint32_t *big) {
   if (st->error)
     return;
   extern __shared__ __align__(16) uint32_t s_sort[];
   const uint32_t ncand = st->n_cand;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
-  uint32_t separated = 0;
   if (!BLOCK) {
     uint32_t *s = s_sort + warp * kWarpSortMax;
     for (uint32_t c = blockIdx.x * nwarps + warp; c < ncand; c += gridDim.x * nwarps) {
       const uint32_t n = cand_n[c];
-      if (n > (uint32_t)kWarpSortMax)
+      if (n > (uint32_t)kWarpSortMax) {
+        if (lane == 0)
+          big[atomicAdd(&st->n_big, 1u)] = c;  // for the block sorts, in any order
         continue;
-      uint32_t *m = members + cand_off[c];
+      }
+      const uint32_t off = cand_off[c];
+      const uint32_t *m = members + off;
+      if (n <= 32) {
+        const uint32_t q = warp_sort32(lane < (int)n ? m[lane] : kNone, (int)n, lane);
+        if (lane < (int)n)
+          put_member(q, lane, c, off, frame, index, value, mpix, mcand);
+        continue;
+      }
       for (uint32_t i = lane; i < n; i += 32)
         s[i] = m[i];
       __syncwarp();
       bitonic_sort(s, (int)n, lane, 32, true);
       for (uint32_t i = lane; i < n; i += 32)
-        m[i] = s[i];
-      // The first pass across the warp, exact in integers.
-      FirstPass f;
-      fp_init(f);
-      for (uint32_t i = lane; i < n; i += 32) {
-        int32_t x, y, z;
-        uint32_t v;
-        member(s[i], frame, index, value, a.width, &x, &y, &z, &v);
-        fp_add(f, i, v, x, y, z);
-      }
-#pragma unroll
-      for (int o = 16; o; o >>= 1) {
-        FirstPass g;
-        g.S = __shfl_xor_sync(0xffffffffu, f.S, o);
-        g.Q2 = __shfl_xor_sync(0xffffffffu, f.Q2, o);
-        for (int ax = 0; ax < 3; ax++)
-          g.W[ax] = __shfl_xor_sync(0xffffffffu, f.W[ax], o);
-        for (int b = 0; b < 6; b++)
-          g.bb[b] = __shfl_xor_sync(0xffffffffu, f.bb[b], o);
-        g.peak_v = __shfl_xor_sync(0xffffffffu, f.peak_v, o);
-        g.peak_k = __shfl_xor_sync(0xffffffffu, f.peak_k, o);
-        g.exact = __shfl_xor_sync(0xffffffffu, f.exact ? 1 : 0, o) != 0;
-        fp_merge(f, g);
-      }
-      __syncwarp();
-      if (lane == 0) {
-        fp_finish(f);
-        sf_spot spot;
-        const bool ok = emit_spot(s, n, frame, index, value, a.width, a.max_separation, &spot,
-                                  false, f.exact ? &f : nullptr);
-        acc[c] = ok ? 1u : 0u;
-        acc_n[c] = ok ? n : 0u;
-        separated += ok ? 0u : 1u;
-      }
-      __syncwarp();
+        put_member(s[i], i, c, off, frame, index, value, mpix, mcand);
+      __syncwarp();  // the next candidate reuses the shared rows
     }
   } else {
-    __shared__ sf_spot s_spot;
-    __shared__ uint32_t s_ok;
-    for (uint32_t c = blockIdx.x; c < ncand; c += gridDim.x) {
+    const uint32_t nbig = st->n_big;
+    for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+      const uint32_t c = big[b];
       const uint32_t n = cand_n[c];
-      if (n <= (uint32_t)kWarpSortMax)
+      if (n > (uint32_t)kBlockSortMax)
         continue;
-      if (n > (uint32_t)kBlockSortMax) {
-        if (threadIdx.x == 0) {
-          atomicOr(&st->error, kErrSpotSize);
-          acc[c] = 0;
-          acc_n[c] = 0;
-        }
-        continue;
-      }
-      uint32_t *m = members + cand_off[c];
+      const uint32_t off = cand_off[c];
+      const uint32_t *m = members + off;
       for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
         s_sort[i] = m[i];
       __syncthreads();
       bitonic_sort(s_sort, (int)n, threadIdx.x, blockDim.x, false);
       for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
-        m[i] = s_sort[i];
-      if (threadIdx.x == 0) {
-        s_ok = emit_spot(s_sort, n, frame, index, value, a.width, a.max_separation, &s_spot,
-                         false)
-                   ? 1u : 0u;
-        acc[c] = s_ok;
-        acc_n[c] = s_ok ? n : 0u;
-        separated += s_ok ? 0u : 1u;
-      }
+        put_member(s_sort[i], i, c, off, frame, index, value, mpix, mcand);
       __syncthreads();
     }
   }
-  if (separated)
-    atomicAdd(&st->counts[kCntSeparated], (unsigned long long)separated);
 }
 
-// Accepted spots and their pixels into the batch outputs (dials_spots.cc:
-// 355-359): spot k's pixels at acc_off[k] in member order. Four lanes to a
-// candidate: the first pass split four ways (exact integers), then each of
-// three lanes runs one axis of the variance pass -- a sequence of rounded
-// double additions in member order, as the reference -- and lane 0 writes
-// the spot. Where the integers could be inexact lane 0 runs the whole
-// reference sequence alone.
+// Candidates beyond kBlockSortMax members (possible when max_spot_size allows
+// them): a block each sorts the member positions in place in global memory
+// with a bitonic network whose every comparator puts the smaller value first
+// (each merge starts by comparing element i with its mirror in the block), so
+// the length needs no padding -- a comparator whose second element lies
+// beyond the end would leave the first in place, as if against +infinity.
 __global__ void __launch_bounds__(kThreads)
-k_write(LabelStatus *st, const BatchArgs *__restrict__ ap,
-        const uint32_t *__restrict__ cand_n,
-        const uint32_t *__restrict__ cand_off, const uint32_t *__restrict__ members,
-        const int32_t *__restrict__ frame, const uint32_t *__restrict__ index,
-        const uint32_t *__restrict__ value, const uint32_t *__restrict__ acc,
-        const uint32_t *__restrict__ acc_idx, const uint32_t *__restrict__ acc_off,
-        sf_spot *spots, size_t spots_cap, sf_pixel *pixels, size_t pixels_cap) {
+k_sort_big(LabelStatus *st, const uint32_t *__restrict__ cand_n,
+           const uint32_t *__restrict__ cand_off, uint32_t *members,
+           const int32_t *__restrict__ frame, const uint32_t *__restrict__ index,
+           const uint32_t *__restrict__ value, sf_pixel *mpix, uint32_t *mcand,
+           const uint32_t *__restrict__ big) {
+  if (st->error)
+    return;
+  const uint32_t nbig = st->n_big;
+  for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+    const uint32_t c = big[b];
+    const uint32_t n = cand_n[c];
+    if (n <= (uint32_t)kBlockSortMax)
+      continue;
+    const uint32_t off = cand_off[c];
+    uint32_t *m = members + off;
+    uint32_t size = 1;
+    while (size < n)
+      size <<= 1;
+    for (uint32_t k = 2; k <= size; k <<= 1) {
+      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+        for (uint32_t t = threadIdx.x; t < size / 2; t += blockDim.x) {
+          const uint32_t blk = t / j, r = t - blk * j;
+          uint32_t i, l;
+          if (j == (k >> 1)) {  // the mirror comparator of the merge's first step
+            i = blk * k + r;
+            l = blk * k + k - 1 - r;
+          } else {
+            i = blk * 2 * j + r;
+            l = i + j;
+          }
+          if (l < n) {
+            const uint32_t x = m[i], y = m[l];
+            if (x > y) {
+              m[i] = y;
+              m[l] = x;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+      put_member(m[i], i, c, off, frame, index, value, mpix, mcand);
+    __syncthreads();
+  }
+}
+
+// The candidates ordered by size, largest first (a counting sort over
+// kSizeBins bins; sizes of kSizeBins - 1 and more share the first bin, and
+// the order within a bin is arbitrary): perm[i] is the i-th candidate to
+// process. hist holds 2 * kSizeBins words.
+constexpr int kSizeBins = 1024;
+
+__device__ __forceinline__ uint32_t size_bin(uint32_t n) {
+  return (uint32_t)(kSizeBins - 1) - min(n, (uint32_t)(kSizeBins - 1));
+}
+
+__global__ void k_perm_hist(LabelStatus *st, const uint32_t *__restrict__ cand_n,
+                            uint32_t *hist) {
+  if (st->error)
+    return;
+  __shared__ uint32_t h[kSizeBins];
+  for (int b = threadIdx.x; b < kSizeBins; b += blockDim.x)
+    h[b] = 0;
+  __syncthreads();
+  const uint32_t ncand = st->n_cand;
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncand;
+       c += gridDim.x * blockDim.x)
+    atomicAdd(&h[size_bin(cand_n[c])], 1u);
+  __syncthreads();
+  for (int b = threadIdx.x; b < kSizeBins; b += blockDim.x)
+    if (h[b])
+      atomicAdd(&hist[b], h[b]);
+}
+
+// One block: the bins' exclusive offsets (into the cursors, hist +
+// kSizeBins), and the counts cleared for the next call.
+__global__ void __launch_bounds__(kSizeBins) k_perm_offsets(LabelStatus *st, uint32_t *hist) {
+  if (st->error)
+    return;
+  uint32_t total;
+  const uint32_t v = hist[threadIdx.x];
+  const uint32_t e = block_exclusive_scan(v, &total);
+  hist[kSizeBins + threadIdx.x] = e;
+  hist[threadIdx.x] = 0;
+}
+
+__global__ void k_perm_scatter(LabelStatus *st, const uint32_t *__restrict__ cand_n,
+                               uint32_t *hist, uint32_t *perm) {
+  if (st->error)
+    return;
+  const uint32_t ncand = st->n_cand;
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncand;
+       c += gridDim.x * blockDim.x)
+    perm[atomicAdd(&hist[kSizeBins + size_bin(cand_n[c])], 1u)] = c;
+}
+
+// Warp-wide sum modulo 2^64 of one 64-bit value a lane, by redux.sync on
+// 22-bit limbs (each limb's sum over 32 lanes fits in 32 bits).
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+  const uint32_t l0 = (uint32_t)v & 0x3FFFFFu, l1 = (uint32_t)(v >> 22) & 0x3FFFFFu,
+                 l2 = (uint32_t)(v >> 44);
+  return (unsigned long long)__reduce_add_sync(0xffffffffu, l0) +
+         ((unsigned long long)__reduce_add_sync(0xffffffffu, l1) << 22) +
+         ((unsigned long long)__reduce_add_sync(0xffffffffu, l2) << 44);
+}
+
+// A warp per candidate: the first pass (exact integer sums, dials_spots.cc:
+// 240-276) over the members, a lane every 32nd, reduced across the warp. The
+// finished first passes wait, one a lane, until 32 are ready; then their FP64
+// part (acceptance) runs for 32 candidates at once, every lane busy.
+__global__ void __launch_bounds__(kThreads)
+k_first(LabelStatus *st, const BatchArgs *__restrict__ ap, const uint32_t *__restrict__ cand_n,
+        const uint32_t *__restrict__ cand_off, const sf_pixel *__restrict__ mpix, CandSpot *cs,
+        uint32_t *acc, uint32_t *acc_n) {
   const BatchArgs &a = *ap;
   if (st->error)
     return;
   const uint32_t ncand = st->n_cand;
-  const int lane = threadIdx.x & 31, sub = lane & 3;
-  const uint32_t per_pass = (gridDim.x * blockDim.x) >> 2;
-  for (uint32_t base = (blockIdx.x * blockDim.x) >> 2; base < ncand; base += per_pass) {
-    const uint32_t c = base + (threadIdx.x >> 2);
-    bool live = c < ncand && acc[c];
-    uint32_t n = 0, si = 0, po = 0;
-    const uint32_t *m = nullptr;
-    if (live) {
-      n = cand_n[c];
-      si = acc_idx[c];
-      po = acc_off[c];
-      m = members + cand_off[c];
-      if (si >= spots_cap || (size_t)po + n > pixels_cap) {
-        if (sub == 0)
-          atomicOr(&st->error, kErrOutFull);
-        live = false;
-      }
+  const int lane = threadIdx.x & 31;
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  FirstPass held;
+  fp_init(held);
+  uint32_t held_c = 0, held_n = 0, separated = 0;
+  int nheld = 0;
+  auto flush = [&]() {
+    if (lane < nheld) {
+      CandSpot spot;
+      const bool ok = accept_candidate(mpix + cand_off[held_c], held_n, a, held, &spot);
+      cs[held_c] = spot;
+      acc[held_c] = ok ? 1u : 0u;
+      acc_n[held_c] = ok ? held_n : 0u;
+      separated += ok ? 0u : 1u;
     }
+    nheld = 0;
+  };
+  for (uint32_t c = gw; c < ncand; c += nw) {
+    const uint32_t n = cand_n[c];
+    const sf_pixel *mp = mpix + cand_off[c];
     FirstPass f;
     fp_init(f);
-    if (live)
-      for (uint32_t k = sub; k < n; k += 4) {
-        const uint32_t q = m[k];
-        int32_t x, y, z;
-        uint32_t v;
-        member(q, frame, index, value, a.width, &x, &y, &z, &v);
-        fp_add(f, k, v, x, y, z);
-        sf_pixel px;
-        px.frame = z;
-        px.index = index[q];
-        px.value = v;
-        pixels[po + k] = px;
-      }
-#pragma unroll
-    for (int o = 1; o <= 2; o <<= 1) {
-      FirstPass g;
-      g.S = __shfl_xor_sync(0xffffffffu, f.S, o);
-      g.Q2 = __shfl_xor_sync(0xffffffffu, f.Q2, o);
-      for (int ax = 0; ax < 3; ax++)
-        g.W[ax] = __shfl_xor_sync(0xffffffffu, f.W[ax], o);
-      for (int bb = 0; bb < 6; bb++)
-        g.bb[bb] = __shfl_xor_sync(0xffffffffu, f.bb[bb], o);
-      g.peak_v = __shfl_xor_sync(0xffffffffu, f.peak_v, o);
-      g.peak_k = __shfl_xor_sync(0xffffffffu, f.peak_k, o);
-      g.exact = __shfl_xor_sync(0xffffffffu, f.exact ? 1 : 0, o) != 0;
-      fp_merge(f, g);
+    for (uint32_t k = lane; k < n; k += 32) {
+      int32_t x, y, z;
+      const sf_pixel px = mp[k];
+      pixel_xyz(px, a, &x, &y, &z);
+      fp_add(f, k, px.value, x, y, z);
     }
-    fp_finish(f);
+    FirstPass g;
+    g.S = warp_sum_u64(f.S);
+    g.Q2 = warp_sum_u64(f.Q2);
+    for (int ax = 0; ax < 3; ax++)
+      g.W[ax] = warp_sum_u64(f.W[ax]);
+    for (int b = 0; b < 6; b += 2) {
+      g.bb[b] = __reduce_min_sync(0xffffffffu, f.bb[b]);
+      g.bb[b + 1] = __reduce_max_sync(0xffffffffu, f.bb[b + 1]);
+    }
+    // The brightest value, and the first member holding it.
+    const bool has = f.peak_k != 0xFFFFFFFFu;
+    g.peak_v = __reduce_max_sync(0xffffffffu, has ? f.peak_v : 0u);
+    g.peak_k = __reduce_min_sync(0xffffffffu,
+                                 has && g.peak_v > 0 && f.peak_v == g.peak_v ? f.peak_k
+                                                                             : 0xFFFFFFFFu);
+    g.exact = __all_sync(0xffffffffu, f.exact) != 0;
+    fp_finish(g);
+    if (lane == nheld) {
+      held = g;
+      held_c = c;
+      held_n = n;
+    }
+    if (++nheld == 32)
+      flush();
+  }
+  if (nheld)
+    flush();
+  separated = __reduce_add_sync(0xffffffffu, separated);
+  if (lane == 0 && separated)
+    atomicAdd(&st->counts[kCntSeparated], (unsigned long long)separated);
+}
+
+// A thread per member of the batch's candidates whose sums are exact and
+// positive: the member's three variance-pass terms RN(RN(v d) d), d =
+// (c + 0.5) - centre (dials_spots.cc:331-341), every lane busy. c + 0.5 and
+// v are built as doubles from their bits (coordinates below 2^20, values
+// below 2^26 there).
+__global__ void k_terms(LabelStatus *st, const BatchArgs *__restrict__ ap,
+                        const sf_pixel *__restrict__ mpix, const uint32_t *__restrict__ mcand,
+                        const uint32_t *__restrict__ acc, const CandSpot *__restrict__ cs,
+                        double *__restrict__ terms, size_t terms_stride) {
+  const BatchArgs &a = *ap;
+  if (st->error)
+    return;
+  const uint32_t n = st->n_cand_pixels;
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < n;
+       m += gridDim.x * blockDim.x) {
+    const uint32_t c = mcand[m];
+    if (!acc[c] || (cs[c].mode & (kModeExact | kModeSpread)) != (kModeExact | kModeSpread))
+      continue;
+    const sf_pixel px = mpix[m];
+    int32_t coord[3];
+    pixel_xyz(px, a, &coord[0], &coord[1], &coord[2]);
+    const double centre[3] = {cs[c].pos[0], cs[c].pos[1], cs[c].cz};
+    const double val = exact_double(px.value);
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+      const double d = __dsub_rn(half_up((uint32_t)coord[ax]), centre[ax]);
+      terms[ax * terms_stride + m] = __dmul_rn(__dmul_rn(val, d), d);
+    }
+  }
+}
+
+// A thread per member of the batch's candidates: the accepted spots' pixels
+// into the batch output, in member order (dials_spots.cc:355-359).
+__global__ void k_pix(LabelStatus *st, const sf_pixel *__restrict__ mpix,
+                      const uint32_t *__restrict__ mcand, const uint32_t *__restrict__ cand_off,
+                      const uint32_t *__restrict__ acc, const uint32_t *__restrict__ acc_off,
+                      sf_pixel *pixels, size_t pixels_cap) {
+  if (st->error)
+    return;
+  const uint32_t n = st->n_cand_pixels;
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < n;
+       m += gridDim.x * blockDim.x) {
+    const uint32_t c = mcand[m];
+    if (!acc[c])
+      continue;
+    const size_t at = (size_t)acc_off[c] + (m - cand_off[c]);
+    if (at >= pixels_cap) {
+      atomicOr(&st->error, kErrOutFull);
+      continue;
+    }
+    pixels[at] = mpix[m];
+  }
+}
+
+// The reference's variance pass (dials_spots.cc:331-353) over members in
+// order, in double, as it writes it.
+__device__ void variance_sequence(const sf_pixel *mp, uint32_t n, const BatchArgs &a,
+                                  const double centre[3], double delta_sq[3]) {
+  delta_sq[0] = delta_sq[1] = delta_sq[2] = 0.0;
+  for (uint32_t k = 0; k < n; k++) {
+    int32_t coord[3];
+    pixel_xyz(mp[k], a, &coord[0], &coord[1], &coord[2]);
+    const double val = (double)mp[k].value;
+    for (int ax = 0; ax < 3; ax++) {
+      const double d = __dsub_rn(__dadd_rn((double)coord[ax], 0.5), centre[ax]);
+      delta_sq[ax] = __dadd_rn(delta_sq[ax], __dmul_rn(__dmul_rn(val, d), d));
+    }
+  }
+}
+
+// Four lanes per candidate, in size order (so that the candidates sharing a
+// warp have similar sizes): lanes 0-2 each run one axis of the variance pass
+// -- the reference's rounded additions of the member terms, in member order
+// (dials_spots.cc:331-353) -- and the variance formula; lane 0 writes the
+// accepted spot's record. Where the first pass was not exact, lane 0 runs the
+// whole sequence alone.
+__global__ void k_var(LabelStatus *st, const BatchArgs *__restrict__ ap,
+                      const uint32_t *__restrict__ perm, const uint32_t *__restrict__ cand_off,
+                      const uint32_t *__restrict__ acc, const uint32_t *__restrict__ acc_idx,
+                      const uint32_t *__restrict__ acc_off, const CandSpot *__restrict__ cs,
+                      const sf_pixel *__restrict__ mpix, const double *__restrict__ terms,
+                      size_t terms_stride, sf_spot *spots, size_t spots_cap) {
+  const BatchArgs &a = *ap;
+  if (st->error)
+    return;
+  const uint32_t ncand = st->n_cand;
+  const int sub = threadIdx.x & 3;
+  const uint32_t per_pass = (gridDim.x * blockDim.x) >> 2;
+  for (uint32_t base = (blockIdx.x * blockDim.x) >> 2; base < ncand; base += per_pass) {
+    const uint32_t i = base + (threadIdx.x >> 2);
+    const uint32_t c = i < ncand ? perm[i] : 0u;
+    const bool live = i < ncand && acc[c];
     double var_ax = 0.0;
-    sf_spot spot;
-    if (live && f.exact) {
-      // This lane's axis of the variance pass (lanes 0, 1, 2).
-      const double sum = (double)f.S, sum_sq = (double)f.Q2;
-      double pos_c[3];
-      for (int ax = 0; ax < 3; ax++)
-        pos_c[ax] = __ddiv_rn(__dmul_rn((double)f.W[ax], 0.5), sum);
-      if (sub < 3 && sum > 0.0) {
-        double delta_sq = 0.0;
-        const double centre = pos_c[sub];
-        for (uint32_t k = 0; k < n; k++) {
-          const uint32_t q = m[k];
-          int32_t x, y, z;
-          uint32_t v;
-          member(q, frame, index, value, a.width, &x, &y, &z, &v);
-          const int32_t coord = sub == 0 ? x : sub == 1 ? y : z;
-          const double d = __dsub_rn(__dadd_rn((double)coord, 0.5), centre);
-          delta_sq = __dadd_rn(delta_sq, __dmul_rn(__dmul_rn((double)v, d), d));
+    CandSpot cd;
+    if (live) {
+      cd = cs[c];
+      const uint32_t off = cand_off[c];
+      if ((cd.mode & (kModeExact | kModeSpread)) == (kModeExact | kModeSpread) && sub < 3) {
+        const double *t = terms + sub * terms_stride + off;
+        double sum = 0.0;
+        uint32_t k = 0;
+        for (; k + kPipe <= cd.n; k += kPipe) {
+          double x[kPipe];
+#pragma unroll
+          for (int u = 0; u < kPipe; u++)
+            x[u] = t[k + u];
+#pragma unroll
+          for (int u = 0; u < kPipe; u++)
+            sum = __dadd_rn(sum, x[u]);
         }
-        const double ss = __dmul_rn(sum, sum);
-        var_ax = ss > sum_sq
-                     ? __dadd_rn(__ddiv_rn(__ddiv_rn(__dmul_rn(delta_sq, sum),
-                                                     __dsub_rn(ss, sum_sq)),
-                                           sum),
+        for (; k < cd.n; k++)
+          sum = __dadd_rn(sum, t[k]);
+        const double ss = __dmul_rn(cd.sum, cd.sum);
+        var_ax = ss > cd.sum_sq
+                     ? __dadd_rn(__ddiv_rn(__ddiv_rn(__dmul_rn(sum, cd.sum),
+                                                     __dsub_rn(ss, cd.sum_sq)),
+                                           cd.sum),
                                  1.0 / 12.0)
                      : 1.0 / 12.0;
       }
-      for (int b6 = 0; b6 < 6; b6++)
-        spot.bbox[b6] = f.bb[b6];
-      spot.intensity = sum;
-      spot.intensity_variance = sum;
-      spot.n_signal = n;
-      if (sum > 0.0) {
-        spot.position[0] = pos_c[0];
-        spot.position[1] = pos_c[1];
-        spot.position[2] = spot.bbox[5] == spot.bbox[4] + 1
-                               ? __dadd_rn((double)spot.bbox[4], 0.5) : pos_c[2];
-      } else {
-        spot.position[0] = __ddiv_rn((double)(spot.bbox[1] + spot.bbox[0]), 2.0);
-        spot.position[1] = __ddiv_rn((double)(spot.bbox[3] + spot.bbox[2]), 2.0);
-        spot.position[2] = __ddiv_rn((double)(spot.bbox[5] + spot.bbox[4]), 2.0);
-      }
     }
-    // Lane 0 of each group gathers the three axes' variances.
     const double v1 = __shfl_down_sync(0xffffffffu, var_ax, 1);
     const double v2 = __shfl_down_sync(0xffffffffu, var_ax, 2);
-    if (live && sub == 0) {
-      if (f.exact) {
-        const bool spread = (double)f.S > 0.0;
-        spot.variance[0] = spread ? var_ax : 0.0;
-        spot.variance[1] = spread ? v1 : 0.0;
-        spot.variance[2] = spread ? v2 : 0.0;
-      } else {
-        emit_spot(m, n, frame, index, value, a.width, a.max_separation, &spot);
-      }
-      spot.first = a.pixel_base + po;
-      spots[si] = spot;
+    if (!live || sub != 0)
+      continue;
+    const uint32_t si = acc_idx[c];
+    if (si >= spots_cap) {
+      atomicOr(&st->error, kErrOutFull);
+      continue;
     }
+    sf_spot spot;
+    for (int b = 0; b < 6; b++)
+      spot.bbox[b] = cd.bb[b];
+    spot.position[0] = cd.pos[0];
+    spot.position[1] = cd.pos[1];
+    spot.position[2] = cd.pos[2];
+    spot.intensity = cd.sum;
+    spot.intensity_variance = cd.sum;
+    spot.n_signal = cd.n;
+    spot.variance[0] = spot.variance[1] = spot.variance[2] = 0.0;
+    if (cd.mode & kModeSpread) {
+      if (cd.mode & kModeExact) {
+        spot.variance[0] = var_ax;
+        spot.variance[1] = v1;
+        spot.variance[2] = v2;
+      } else {
+        double delta_sq[3];
+        const double centre[3] = {cd.pos[0], cd.pos[1], cd.cz};
+        variance_sequence(mpix + cand_off[c], cd.n, a, centre, delta_sq);
+        const double ss = __dmul_rn(cd.sum, cd.sum);
+        for (int ax = 0; ax < 3; ax++)
+          spot.variance[ax] =
+              ss > cd.sum_sq
+                  ? __dadd_rn(__ddiv_rn(__ddiv_rn(__dmul_rn(delta_sq[ax], cd.sum),
+                                                  __dsub_rn(ss, cd.sum_sq)),
+                                        cd.sum),
+                              1.0 / 12.0)
+                  : 1.0 / 12.0;
+      }
+    }
+    spot.first = a.pixel_base + acc_off[c];
+    spots[si] = spot;
   }
 }
 
@@ -1075,6 +1434,14 @@ struct Labeller {
            *members = nullptr, *acc = nullptr, *acc_n = nullptr, *acc_idx = nullptr,
            *acc_off = nullptr, *hist = nullptr, *block_sums = nullptr;
   int32_t *zlast = nullptr;
+  // Per-row start tables (frames of at most kRowTableMaxRows rows), the
+  // candidates' members as pixel records in member order with their
+  // candidate, the candidates' first passes, and the variance terms.
+  uint32_t *rows = nullptr, *mcand = nullptr, *big = nullptr, *perm = nullptr, *phist = nullptr;
+  sf_pixel *mpix = nullptr;
+  CandSpot *cspots = nullptr;
+  double *terms = nullptr;
+  uint2 *edges = nullptr;  // the unions k_link lists, capacity of them
   LabelStatus *st = nullptr;
   LabelStatus *host_st = nullptr;
   BatchArgs *d_args = nullptr, *h_args = nullptr;
@@ -1120,6 +1487,15 @@ struct Labeller {
         if (g)
           cudaGraphExecDestroy(g);
     cudaFree(zlast);
+    cudaFree(rows);
+    cudaFree(mcand);
+    cudaFree(big);
+    cudaFree(mpix);
+    cudaFree(cspots);
+    cudaFree(perm);
+    cudaFree(phist);
+    cudaFree(terms);
+    cudaFree(edges);
     cudaFree(st);
     cudaFree(d_args);
     if (h_args)
@@ -1169,8 +1545,19 @@ struct Labeller {
     SF_ALLOC(hist, (size_t)kGrid * kBuckets);
     SF_ALLOC(block_sums, kScanBlocks);
     SF_ALLOC(zlast, n);
-    // At most one accepted spot per min_spot_size pixels closed in a batch.
+    // At most one accepted spot (and one candidate) per min_spot_size pixels
+    // closed in a batch.
     spots_cap = n / (opt.min_spot_size ? opt.min_spot_size : 1) + 1;
+    if (height <= kRowTableMaxRows)
+      SF_ALLOC(rows, (size_t)(kLabelMaxBatch + 1) * (height + 1));
+    SF_ALLOC(mcand, n);
+    SF_ALLOC(big, n / (kWarpSortMax + 1) + 1);
+    SF_ALLOC(mpix, n);
+    SF_ALLOC(cspots, spots_cap);
+    SF_ALLOC(perm, spots_cap);
+    SF_ALLOC(phist, 2 * kSizeBins);
+    SF_ALLOC(terms, 3 * n);
+    SF_ALLOC(edges, n);
     SF_ALLOC(d_spots, spots_cap);
     SF_ALLOC(d_pixels, n);
     SF_ALLOC(d_counts, kLabelMaxBatch);
@@ -1187,7 +1574,9 @@ struct Labeller {
       return fail(e, "cudaMallocHost for the labeller's arguments");
     if ((e = cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking)) != cudaSuccess)
       return fail(e, "cudaStreamCreate");
-    if ((e = cudaMemsetAsync(st, 0, sizeof(LabelStatus), own_stream)) != cudaSuccess)
+    if ((e = cudaMemsetAsync(st, 0, sizeof(LabelStatus), own_stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(phist, 0, 2 * kSizeBins * sizeof(uint32_t), own_stream)) !=
+            cudaSuccess)
       return fail(e, "clearing the labeller status");
     if ((e = cudaStreamSynchronize(own_stream)) != cudaSuccess)
       return fail(e, "cudaStreamSynchronize");
@@ -1203,45 +1592,58 @@ struct Labeller {
     cudaError_t e;
     k_offsets<<<1, 32, 0, s>>>(st, ap, (uint32_t)capacity);
     k_append<<<g2, kThreads, 0, s>>>(st, ap, frame[c], index[c], value[c], parent[c]);
-    k_link<<<g2, kThreads, 0, s>>>(st, ap, index[c], parent[c]);
-    k_flatten<<<kGrid, kThreads, 0, s>>>(st, parent[c], root, zlast, csize, candid);
-    k_comp_stats<<<kGrid, kThreads, 0, s>>>(st, root, frame[c], zlast, csize);
-    k_closing_flags<<<kGrid, kThreads, 0, s>>>(st, ap, root, zlast, flag, open);
+    if (rows)
+      k_rows<<<dim3(kGrid / 4 > 0 ? kGrid / 4 : 1, nb + 1), kThreads, 0, s>>>(
+          st, ap, index[c], rows, (uint32_t)height);
+    k_link<<<g2, kThreads, 0, s>>>(st, ap, index[c], parent[c], rows, (uint32_t)height, edges,
+                                   (uint32_t)capacity);
+    k_unite<<<kPassGrid, kThreads, 0, s>>>(st, edges, (uint32_t)capacity, parent[c]);
+    k_flatten<<<kPassGrid, kThreads, 0, s>>>(st, parent[c], root, zlast, csize, candid);
+    k_comp_stats<<<kPassGrid, kThreads, 0, s>>>(st, root, frame[c], zlast, csize);
+    k_closing_flags<<<kPassGrid, kThreads, 0, s>>>(st, ap, root, zlast, flag, open);
     const uint32_t *err = &st->error;
     if ((e = exclusive_scan(flag, posa, &st->n_total, &st->n_closing, block_sums, err, s)) !=
         cudaSuccess)
       return e;
-    k_closing_list<<<kGrid, kThreads, 0, s>>>(st, ap, flag, posa, zlast, clist, cbucket);
+    k_closing_list<<<kPassGrid, kThreads, 0, s>>>(st, ap, flag, posa, zlast, clist, cbucket);
     k_bucket_hist<<<kGrid, kThreads, 0, s>>>(st, cbucket, hist);
     k_bucket_offsets<<<1, 128, 0, s>>>(st, hist);
     k_bucket_scatter<<<kGrid, kThreads, 0, s>>>(st, clist, cbucket, hist, order);
-    k_size_filter<<<kGrid, kThreads, 0, s>>>(st, ap, order, csize, cflag);
+    k_size_filter<<<kPassGrid, kThreads, 0, s>>>(st, ap, order, csize, cflag);
     if ((e = exclusive_scan(cflag, cpos, &st->n_closing, &st->n_cand, block_sums, err, s)) !=
         cudaSuccess)
       return e;
-    k_cand_list<<<kGrid, kThreads, 0, s>>>(st, order, csize, cflag, cpos, cand_root, cand_n,
+    k_cand_list<<<kPassGrid, kThreads, 0, s>>>(st, order, csize, cflag, cpos, cand_root, cand_n,
                                            candid, cursor);
     if ((e = exclusive_scan(cand_n, cand_off, &st->n_cand, &st->n_cand_pixels, block_sums,
                             err, s)) != cudaSuccess)
       return e;
-    k_gather<<<kGrid, kThreads, 0, s>>>(st, root, candid, cand_off, cursor, members);
-    k_sort_accept<false><<<kGrid, kThreads, (kThreads / 32) * kWarpSortMax * 4, s>>>(
-        st, ap, cand_n, cand_off, members, frame[c], index[c], value[c], acc, acc_n);
-    k_sort_accept<true><<<kGrid / 2, kThreads, kBlockSortMax * 4, s>>>(
-        st, ap, cand_n, cand_off, members, frame[c], index[c], value[c], acc, acc_n);
+    k_gather<<<kPassGrid, kThreads, 0, s>>>(st, root, candid, cand_off, cursor, members);
+    k_sort<false><<<kSortGrid, kThreads, (kThreads / 32) * kWarpSortMax * 4, s>>>(
+        st, cand_n, cand_off, members, frame[c], index[c], value[c], mpix, mcand, big);
+    k_sort<true><<<kGrid / 2, kThreads, kBlockSortMax * 4, s>>>(
+        st, cand_n, cand_off, members, frame[c], index[c], value[c], mpix, mcand, big);
+    k_sort_big<<<kGrid / 8, kThreads, 0, s>>>(st, cand_n, cand_off, members, frame[c],
+                                              index[c], value[c], mpix, mcand, big);
+    k_perm_hist<<<kGrid, kThreads, 0, s>>>(st, cand_n, phist);
+    k_perm_offsets<<<1, kSizeBins, 0, s>>>(st, phist);
+    k_perm_scatter<<<kPassGrid, kThreads, 0, s>>>(st, cand_n, phist, perm);
+    k_first<<<kPassGrid, kThreads, 0, s>>>(st, ap, cand_n, cand_off, mpix, cspots, acc, acc_n);
     if ((e = exclusive_scan(acc, acc_idx, &st->n_cand, &st->n_accept, block_sums, err, s)) !=
         cudaSuccess)
       return e;
     if ((e = exclusive_scan(acc_n, acc_off, &st->n_cand, &st->n_accept_pixels, block_sums,
                             err, s)) != cudaSuccess)
       return e;
-    k_write<<<kGrid, kThreads, 0, s>>>(st, ap, cand_n, cand_off, members, frame[c], index[c],
-                                       value[c], acc, acc_idx, acc_off, d_spots, spots_cap,
-                                       d_pixels, capacity);
+    k_pix<<<kPassGrid, kThreads, 0, s>>>(st, mpix, mcand, cand_off, acc, acc_off, d_pixels,
+                                         capacity);
+    k_terms<<<kPassGrid, kThreads, 0, s>>>(st, ap, mpix, mcand, acc, cspots, terms, capacity);
+    k_var<<<kPassGrid, kThreads, 0, s>>>(st, ap, perm, cand_off, acc, acc_idx, acc_off, cspots,
+                                         mpix, terms, capacity, d_spots, spots_cap);
     if ((e = exclusive_scan(open, posb, &st->n_total, &st->n_open, block_sums, err, s)) !=
         cudaSuccess)
       return e;
-    k_compact<<<kGrid, kThreads, 0, s>>>(st, open, posb, root, frame[c], index[c], value[c],
+    k_compact<<<kPassGrid, kThreads, 0, s>>>(st, open, posb, root, frame[c], index[c], value[c],
                                          frame[o], index[o], value[o], parent[o]);
     k_end_batch<<<1, 32, 0, s>>>(st, ap);
     return cudaGetLastError();
@@ -1297,6 +1699,16 @@ struct Labeller {
     a.finishing = finishing ? 1 : 0;
     a.two_d = opt.two_d ? 1 : 0;
     a.width = (uint32_t)width;
+    {
+      // Granlund & Montgomery's round-up divisor for width (as in the
+      // threshold's tile counts): exact for every 32-bit numerator.
+      int l = 0;
+      while ((1ull << l) < width)
+        l++;
+      a.wdiv_m = (uint32_t)(((((unsigned long long)1 << l) - width) << 32) / width + 1);
+      a.wdiv_s1 = l < 1 ? (uint32_t)l : 1u;
+      a.wdiv_s2 = l > 1 ? (uint32_t)(l - 1) : 0u;
+    }
     a.npix = (uint32_t)(height * width);
     a.min_size = (uint32_t)std::min<size_t>(opt.min_spot_size, 0xffffffffu);
     a.max_size = (uint32_t)std::min<size_t>(opt.max_spot_size, 0xffffffffu);
@@ -1344,8 +1756,6 @@ struct Labeller {
       t_last_error = (err & kErrLiveFull)
                          ? "more signal pixels held open at once than the labeller's "
                            "capacity"
-                     : (err & kErrSpotSize)
-                         ? "a spot within the size limits is larger than 8192 pixels"
                      : (err & kErrOutFull) ? "labeller outputs overflowed"
                      : (err & kErrListOverflow)
                          ? "a signal list's count exceeds its capacity (the threshold "
@@ -1400,6 +1810,22 @@ static int read_store(const Labeller &L, const DeviceStore<T> &v, T *out, size_t
 namespace sf {
 
 size_t label_width(const sf_labeller *l) { return l ? l->impl.width : 0; }
+
+size_t label_device_bytes(size_t height, size_t capacity, size_t min_spot_size) {
+  // The pools (two of frame, index, value, parent), 22 scratch words, the
+  // batch's kept pixels, the member records and tags, three variance terms
+  // and an edge a slot; a spot record, a candidate record and a size-order
+  // entry per possible spot.
+  const size_t per =
+      2 * 4 * 4 + 22 * 4 + sizeof(sf_pixel) + 4 + sizeof(sf_pixel) + 3 * 8 + 8 + 1;
+  const size_t spots = capacity / std::max<size_t>(min_spot_size, 1) + 1;
+  const size_t rows =
+      height <= kRowTableMaxRows ? (size_t)(kLabelMaxBatch + 1) * (height + 1) * 4 : 0;
+  return capacity * per + spots * (sizeof(sf_spot) + sizeof(CandSpot) + 4) + rows +
+         2 * kSizeBins * 4 +
+         (size_t)kGrid * kBuckets * 4 + (size_t)kScanBlocks * 4 + kLabelMaxBatch * 4 +
+         2 * sizeof(LabelStatus) + 2 * sizeof(BatchArgs);
+}
 
 int label_gather_pixels(const sf_labeller *l, sf_pixel *d_out, cudaStream_t *stream) {
   const Labeller &L = l->impl;

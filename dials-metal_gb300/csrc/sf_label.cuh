@@ -18,4 +18,8 @@ constexpr int kLabelMaxBatch = 64;
 size_t label_width(const sf_labeller *labeller);
 int label_gather_pixels(const sf_labeller *labeller, sf_pixel *d_out, cudaStream_t *stream);
 
+// Device bytes sf_label_open(height, ., options, capacity) allocates before
+// any result is stored: pools, scratch, row tables and batch outputs.
+size_t label_device_bytes(size_t height, size_t capacity, size_t min_spot_size);
+
 } // namespace sf

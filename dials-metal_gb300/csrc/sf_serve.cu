@@ -38,6 +38,7 @@
 
 #include "sf_api.h"
 #include "sf_decompress.cuh"
+#include "sf_label.cuh"
 
 namespace {
 
@@ -191,10 +192,8 @@ size_t labeller_capacity(size_t h, size_t w) {
 
 // Device bytes of a labeller of the given capacity (its pools, scratch and
 // outputs, as sf_label_open allocates them), with a margin.
-size_t labeller_bytes(size_t capacity, size_t min_spot_size) {
-  const size_t per = 2 * 4 * 4 + 22 * 4 + 12;
-  const size_t spots = capacity / std::max<size_t>(min_spot_size, 1) + 1;
-  return capacity * per + spots * sizeof(sf_spot) + ((size_t)16 << 20);
+size_t labeller_bytes(size_t height, size_t capacity, size_t min_spot_size) {
+  return sf::label_device_bytes(height, capacity, min_spot_size) + ((size_t)16 << 20);
 }
 
 size_t group_bytes(size_t h, size_t w, size_t capacity, size_t max_batch) {
@@ -595,7 +594,7 @@ size_t sf_server_sweep_bytes(const sf_server *sv, size_t height, size_t width,
   const size_t capacity = std::max<size_t>(1, height * width / sv->opt.capacity_divisor);
   return sv->opt.ring * (height * width * sizeof(uint32_t) + capacity * sizeof(sf_signal_pixel) +
                          sizeof(uint32_t)) +
-         labeller_bytes(labeller_capacity(height, width), min_size);
+         labeller_bytes(height, labeller_capacity(height, width), min_size);
 }
 
 int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,

@@ -242,3 +242,61 @@ def test_live_capacity_overflow_is_reported():
     d = labeller.DeviceLabeller(100, 100, live_capacity=16)
     with pytest.raises(RuntimeError):
         d.add(0, flat(list(range(0, 40, 2))))
+
+
+def _disc_sweep(h, w, seed):
+    """Four frames of host lists: a disc of radius 45 on frames 0-2 (a 3-D
+    spot of about 19,000 pixels, beyond a block's shared-memory sort), a disc
+    of radius 22 on every frame (about 6,000, sorted by one block), and
+    scattered pixels (small spots and singles)."""
+    rng = np.random.default_rng(seed)
+    yy, xx = np.mgrid[0:h, 0:w]
+    lists = []
+    for f in range(4):
+        m = (yy - 100) ** 2 + (xx - 560) ** 2 < 22 ** 2
+        if f < 3:
+            m |= (yy - 300) ** 2 + (xx - 200) ** 2 < 45 ** 2
+        m |= rng.random((h, w)) < 0.04
+        # Peaked at each disc's centre (so the peak-separation filter keeps
+        # the discs), with noise.
+        prof = (4000 * np.exp(-((yy - 300) ** 2 + (xx - 200) ** 2) / 800.0) +
+                2000 * np.exp(-((yy - 100) ** 2 + (xx - 560) ** 2) / 200.0))
+        idx = np.flatnonzero(m)
+        s = np.zeros(len(idx), O.SIGNAL_DTYPE)
+        s["index"] = idx
+        s["value"] = prof.ravel()[idx].astype(np.uint32) + rng.integers(1, 20, len(idx))
+        lists.append(s)
+    return lists
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("max_spot_size", [20000, 1000])
+def test_spots_beyond_shared_memory_sorts_against_oracle(max_spot_size):
+    import torch
+    from sfgb import labeller
+    h, w = 600, 700
+    lists = _disc_sweep(h, w, 77)
+    opts = dict(max_spot_size=max_spot_size, max_separation=2.0)
+    lab = O.Labeller(h, w, **opts)
+    for f, s in enumerate(lists):
+        lab.add(f, s)
+    want = lab.finish()
+    if max_spot_size == 20000:
+        assert want.spots["n_signal"].max() > 16000  # the big disc is accepted
+    else:
+        assert want.counts["too_large"] >= 2
+    # One frame a call from host lists.
+    d = labeller.DeviceLabeller(h, w, **opts)
+    for f, s in enumerate(lists):
+        d.add(f, s)
+    _same(d.finish(), want, f"host lists, max_spot_size {max_spot_size}")
+    # All four frames in one call from device lists.
+    cap = max(len(s) for s in lists)
+    dev = torch.zeros((4, cap * 16), dtype=torch.uint8, device="cuda")
+    for j, s in enumerate(lists):
+        dev[j, : len(s) * 16] = torch.from_numpy(s.view(np.uint8).copy()).cuda()
+    counts = torch.tensor([len(s) for s in lists], dtype=torch.int32, device="cuda")
+    d = labeller.DeviceLabeller(h, w, **opts)
+    d.add_device([0, 1, 2, 3], dev.data_ptr(), cap, counts.data_ptr(),
+                 torch.cuda.current_stream().cuda_stream)
+    _same(d.finish(), want, f"one call, max_spot_size {max_spot_size}")
