@@ -644,7 +644,14 @@ def run_ours(args):
                                ctypes.byref(found))
             if rc != 0:
                 raise SystemExit(f"sf_find_u32 failed: {rc} {api.last_error()}")
-            return found.value
+            # The drop-in's last step (shim/dext_sfgb.cc): the records found
+            # copied out of the thread's pinned staging into the caller's
+            # own vector, sized to the count.
+            n = found.value
+            signal = np.empty(n * 16, np.uint8)
+            if n:
+                ctypes.memmove(signal.ctypes.data, outs[tls.slot], n * 16)
+            return n
 
         with ThreadPoolExecutor(max_workers=T) as ex:
             list(ex.map(e2e_frame, range(max(args.warmup, 1) * max(B, T))))
@@ -658,9 +665,11 @@ def run_ours(args):
         e2e_thr = {"value": sum_over_ranks(n_e2e, world, dev) / (e_ms / 1e3),
                "unit": "frames/s", "h2d_bytes_per_step": B * H * W * 4,
                "d2h_bytes_per_step": int(d2h / args.steps),
-               "path": f"sf_find_u32 (C ABI, gpu::find<uint32_t> drop-in) from {T} host "
-                       "threads, pinned host frames; per frame the copy in, the threshold "
-                       "and the signal list's read-back",
+               "path": f"sf_find_u32 (C ABI) from {T} host threads in the call sequence of "
+                       "the gpu::find<uint32_t> drop-in (shim/dext_sfgb.cc): pinned host "
+                       "frames; per frame the copy in, the threshold, the list's read-back "
+                       "into the thread's pinned staging and its copy into a list sized to "
+                       "the count",
                "h2d_peak_gbs": h2d_gbs,
                "achieved_h2d_gbs": None,
                "frac_of_h2d_peak": None}
