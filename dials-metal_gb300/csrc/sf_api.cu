@@ -580,6 +580,10 @@ static int find_host(const void *image, size_t h, size_t w,
     }
   }
   const size_t n = *ws.host_count_;
+  if (n == kCountFault) {
+    t_last_error = "a bounded device wait ran out of time (a frame tile's load)";
+    return SF_ECUDA;
+  }
   *found = n;
   sf_stage_times times = {0, 0, 0, 0, 0, 0, 0};
   if (timing) {
@@ -1255,6 +1259,10 @@ int sf_plan_result(sf_plan *plan, size_t j, sf_signal_pixel *out, size_t capacit
   uint32_t n = 0;
   if ((e = cudaMemcpy(&n, p.counts + j, sizeof(n), cudaMemcpyDeviceToHost)) != cudaSuccess)
     return fail(e, "reading a plan's count");
+  if (n == kCountFault) {
+    t_last_error = "a bounded device wait ran out of time (a frame tile's load)";
+    return SF_ECUDA;
+  }
   *found = n;
   if (n > p.capacity || n > capacity)
     return SF_EOVERFLOW;

@@ -37,10 +37,14 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
+
+#include <cudaTypedefs.h>
 
 #include "sf_common.cuh"
 #include "sf_stream.cuh"
+#include "sf_tma.cuh"
 
 namespace sf {
 namespace {
@@ -479,20 +483,35 @@ __host__ __device__ inline int ver_ntx(int w) { return (w + kVerTW - 1) / kVerTW
 __host__ __device__ inline int ver_nty(int h) { return (h + kVerRows - 1) / kVerRows; }
 
 // Staged columns a pixel row (whole 16-byte pieces covering the 38 needed
-// from a piece boundary) and that boundary's alignment, in pixels.
+// from a 16-byte boundary) and that boundary's alignment, in pixels: a TMA
+// box row must be a multiple of 16 bytes and start on one.
 template <typename Pix> struct VerPix;
 template <> struct VerPix<uint32_t> {
   static constexpr int kPW = kVerPW, kAlign = 4;
 };
 template <> struct VerPix<uint16_t> {
-  static constexpr int kPW = kVerPW, kAlign = 4;
+  static constexpr int kPW = 48, kAlign = 8;
 };
 
-template <typename Pix> struct VerWarp {
-  Pix pix[2][kVerPR][VerPix<Pix>::kPW];  // staged pixels, two tiles
+// One staged tile: 18 pixel rows (r0 - 5 .. r0 + 12) of kPW pixels from the
+// aligned column xs, dense, as a TMA box lands in shared memory (128-byte
+// aligned, the box load's destination rule).
+template <typename Pix> struct alignas(128) TileBuf {
+  Pix px[kVerPR][VerPix<Pix>::kPW];
+};
+
+template <typename Pix> struct alignas(128) VerWarp {
+  TileBuf<Pix> pix[2];                   // staged pixels, two tiles
+  uint64_t bar[2];                       // their TMA mbarriers
   uint32_t cw[2][kVerRows][2];           // the tile's candidate words, two tiles
   uint2 vs[kVerDR][kVerPC + 2];          // column sums of 7 rows
   uint32_t msk[kVerPC + 2];              // masked pixels by row, a word a column
+};
+
+// The frames' 2-D tensor maps, boxes of one tile (kPW x 18 pixels), for the
+// TMA staging of the exact check and stage 2.
+struct TileMaps {
+  CUtensorMap map[kMaxBatch];
 };
 
 template <typename Pix> __device__ __forceinline__ bool is_masked_px(uint32_t v) {
@@ -642,19 +661,75 @@ __device__ __forceinline__ void stage_pixels(Pix (*pix)[VerPix<Pix>::kPW], const
   }
 }
 
+// The tile's pixels by one TMA box load of frame f's map at (xs, r0 - 5),
+// issued by lane 0 once the warp is done with the buffer; it lands on bar.
+template <typename Pix>
+__device__ __forceinline__ void tma_stage(TileBuf<Pix> &buf, uint64_t *bar, const TileMaps &M,
+                                          int f, int r0, int xs, int lane) {
+  __syncwarp();
+  if (lane == 0) {
+    fence_proxy_async_smem();
+    mbar_expect_tx(bar, (uint32_t)sizeof(buf.px));
+    tma_load_2d(buf.px, &M.map[f], xs, r0 - 5, bar);
+  }
+}
+
+// Waits for a TMA-staged tile (every lane, bounded; false in every lane if
+// any lane's wait ran out) and, for a tile that reaches past the frame, turns
+// the box's zero-filled pixels off the frame into masked ones, as the
+// per-lane staging writes them.
+template <typename Pix>
+__device__ __forceinline__ bool tma_landed(TileBuf<Pix> &buf, uint64_t *bar, uint32_t parity,
+                                           int height, int width, int r0, int xs, int lane) {
+  constexpr int kPW = VerPix<Pix>::kPW;
+  if (!__all_sync(0xffffffffu, mbar_wait(bar, parity)))
+    return false;
+  const int y0 = r0 - 5;
+  if (y0 < 0 || y0 + kVerPR > height || xs < 0 || xs + kPW > width) {  // warp-uniform
+    for (int k = lane; k < kVerPR * kPW; k += 32) {
+      const int r = k / kPW, c = k - r * kPW;
+      const int y = y0 + r, x = xs + c;
+      if (y < 0 || y >= height || x < 0 || x >= width)
+        buf.px[r][c] = (Pix)~0u;
+    }
+  }
+  __syncwarp();
+  return true;
+}
+
+// The tile origin of list entry e: frame, first output row and column.
+struct TileAt {
+  int f, r0, c0;
+};
+__device__ __forceinline__ TileAt tile_at(uint32_t e, uint32_t ntiles, int ntx,
+                                          const FastDiv &by_ntiles, const FastDiv &by_ntx) {
+  const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
+  TileAt a;
+  a.f = (int)fu;
+  a.r0 = (int)tyu * kVerRows;
+  a.c0 = (int)(t - tyu * (uint32_t)ntx) * kVerTW;
+  return a;
+}
+// The staged columns' first column (aligned) for a tile starting at c0.
+template <typename Pix> __device__ __forceinline__ int tile_xs(int c0) {
+  return (c0 - 5) & ~(VerPix<Pix>::kAlign - 1);
+}
+
 template <typename Pix>
 __device__ __forceinline__ void ver_stage(VerWarp<Pix> &sm, int s, uint32_t e, const FramePtrs &F,
-                                          int height, int width, int vec, uint32_t ntiles,
-                                          int ntx, const FastDiv &by_ntiles,
-                                          const FastDiv &by_ntx,
+                                          const TileMaps &M, int tma, int height, int width,
+                                          int vec, uint32_t ntiles, int ntx,
+                                          const FastDiv &by_ntiles, const FastDiv &by_ntx,
                                           const uint32_t *__restrict__ final_all,
                                           size_t words, int lane) {
-  const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
-  const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
-  const int r0 = ty * kVerRows, c0 = tx * kVerTW;
-  const int xs = (c0 - 5) & ~(VerPix<Pix>::kAlign - 1);
-  stage_pixels<Pix>(sm.pix[s], reinterpret_cast<const Pix *>(F.image[f]), height, width, vec,
-                    r0, xs, lane);
+  const TileAt a = tile_at(e, ntiles, ntx, by_ntiles, by_ntx);
+  const int f = a.f, r0 = a.r0, c0 = a.c0;
+  const int xs = tile_xs<Pix>(c0);
+  if (tma)
+    tma_stage<Pix>(sm.pix[s], &sm.bar[s], M, f, r0, xs, lane);
+  else
+    stage_pixels<Pix>(sm.pix[s].px, reinterpret_cast<const Pix *>(F.image[f]), height, width,
+                      vec, r0, xs, lane);
   if (lane < 2 * kVerRows) {
     const int o = lane >> 1, wdx = (c0 >> 5) + (lane & 1);
     const int wpr = (width + 31) >> 5;
@@ -686,20 +761,30 @@ __device__ __forceinline__ void ver_window(const VerWarp<Pix> &sm, int d, int co
 
 template <int kOcc, typename Pix>
 __global__ void __launch_bounds__(kVerWarps * 32, kOcc)
-lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
-           const __grid_constant__ LaunchParams P, const __grid_constant__ StreamTables T,
-           uint32_t *__restrict__ scr1_all, uint32_t *__restrict__ final_all, size_t words,
-           const uint32_t *__restrict__ list, uint32_t *__restrict__ counters, FastDiv by_ntiles,
-           FastDiv by_ntx, uint32_t *__restrict__ list2) {
-  extern __shared__ __align__(16) unsigned char ver_smem[];
+lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps M, int tma,
+           int height, int width, int vec, const __grid_constant__ LaunchParams P,
+           const __grid_constant__ StreamTables T, uint32_t *__restrict__ scr1_all,
+           uint32_t *__restrict__ final_all, size_t words, const uint32_t *__restrict__ list,
+           uint32_t *__restrict__ counters, FastDiv by_ntiles, FastDiv by_ntx,
+           uint32_t *__restrict__ list2) {
+  extern __shared__ __align__(128) unsigned char ver_smem_raw[];
+  // The launch gives 128 bytes more than the layout needs: the tile buffers
+  // start on a 128-byte boundary whatever the base's alignment.
+  unsigned char *ver_smem = ver_smem_raw + ((128u - (smem_addr(ver_smem_raw) & 127u)) & 127u);
   uint4 *tab = reinterpret_cast<uint4 *>(ver_smem);
   constexpr bool k16 = sizeof(Pix) == 2;
   VerWarp<Pix> *warps = reinterpret_cast<VerWarp<Pix> *>(ver_smem + sizeof(uint4) * 64);
   for (int m = threadIdx.x; m <= kLatN0; m += blockDim.x)
     tab[m] = make_uint4(T.nk[kLatN0 - m], T.clo[kLatN0 - m], T.chi[kLatN0 - m], 0u);
-  __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   VerWarp<Pix> &sm = warps[warp];
+  if (tma && lane == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  uint32_t parity = 0;  // bit b: the phase the next wait on bar[b] waits for
   const int wpr = (width + 31) >> 5;
   const int ntx = ver_ntx(width);
   const uint32_t ntiles = (uint32_t)ntx * (uint32_t)ver_nty(height);
@@ -712,22 +797,34 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   uint32_t e = k < count ? list[k] : 0u;
   uint32_t e1 = k + nw < count ? list[k + nw] : 0u;
   if (k < count)
-    ver_stage<Pix>(sm, 0, e, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, final_all,
-                   words, lane);
+    ver_stage<Pix>(sm, 0, e, F, M, tma, height, width, vec, ntiles, ntx, by_ntiles, by_ntx,
+                   final_all, words, lane);
   cp_async_commit();
   uint32_t e2 = 0u;
+  uint32_t inflight = k < count ? 1u : 0u;  // bit b: a TMA load into buffer b not waited for
   for (int s = 0; k < count; k += nw, s ^= 1, e = e1, e1 = e2) {
     e2 = k + 2 * nw < count ? list[k + 2 * nw] : 0u;
-    if (k + nw < count)
-      ver_stage<Pix>(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx,
-                     final_all, words, lane);
+    if (k + nw < count) {
+      ver_stage<Pix>(sm, s ^ 1, e1, F, M, tma, height, width, vec, ntiles, ntx, by_ntiles,
+                     by_ntx, final_all, words, lane);
+      inflight |= 2u >> s;
+    }
     cp_async_commit();
     cp_async_wait<1>();  // this tile's pieces have landed
     __syncwarp();
-    const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
-    const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
-    const int r0 = ty * kVerRows, c0 = tx * kVerTW;
-    const int off = (c0 - 5) - ((c0 - 5) & ~(VerPix<Pix>::kAlign - 1));
+    const TileAt a = tile_at(e, ntiles, ntx, by_ntiles, by_ntx);
+    const int f = a.f, r0 = a.r0, c0 = a.c0;
+    if (tma) {
+      inflight &= ~(1u << s);
+      if (!tma_landed<Pix>(sm.pix[s], &sm.bar[s], (parity >> s) & 1u, height, width, r0,
+                           tile_xs<Pix>(c0), lane)) {
+        if (lane == 0)
+          atomicOr(counters + kCtrFault, 1u);
+        break;  // whole warp
+      }
+      parity ^= 1u << s;
+    }
+    const int off = (c0 - 5) - tile_xs<Pix>(c0);
     const int w0 = c0 >> 5, sh = c0 & 31;
     uint32_t cj[kVerRows];
 #pragma unroll
@@ -758,7 +855,7 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
       uint32_t ns[kVerPR], q[kVerPR], mk = 0;
 #pragma unroll
       for (int r = 0; r < kVerPR; r++) {
-        const uint32_t v = sm.pix[s][r][col];
+        const uint32_t v = sm.pix[s].px[r][col];
         const bool masked = is_masked_px<Pix>(v);
         if (!k16)
           mx = max(mx, v + 2u);
@@ -890,6 +987,10 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
     if (lane == 0)
       list2[k] = left ? e : kNoTile;  // same place as in the tile list: no atomics
   }
+  // After a fault: the load still in flight (bounded) before the buffers go.
+  for (int b = 0; b < 2; b++)
+    if (tma && ((inflight >> b) & 1u))
+      (void)mbar_wait(&sm.bar[b], (parity >> b) & 1u);
   cp_async_wait<0>();
 }
 
@@ -905,8 +1006,9 @@ lat_verify(const __grid_constant__ FramePtrs F, int height, int width, int vec,
 // positions of the candidate mask (mask_prefix); the mask itself is left as
 // it is until every position is taken (pass_sums clears the failures).
 // ---------------------------------------------------------------------------
-template <typename Pix> struct S2Warp {
-  Pix pix[2][kVerPR][VerPix<Pix>::kPW];  // staged pixels, two tiles
+template <typename Pix> struct alignas(128) S2Warp {
+  TileBuf<Pix> pix[2];              // staged pixels, two tiles
+  uint64_t bar[2];                  // their TMA mbarriers
   uint32_t ew[2][kVerPR][3];        // eroded-mask words over the staged columns
   uint32_t cw[2][kVerRows][2];      // candidate-mask words of the tile's rows
   uint32_t pw[2][kVerRows][2];      // their list positions
@@ -915,18 +1017,21 @@ template <typename Pix> struct S2Warp {
 
 template <typename Pix>
 __device__ __forceinline__ void s2_stage(S2Warp<Pix> &sm, int s, uint32_t e, const FramePtrs &F,
-                                         int height, int width, int vec, uint32_t ntiles, int ntx,
+                                         const TileMaps &M, int tma, int height, int width,
+                                         int vec, uint32_t ntiles, int ntx,
                                          const FastDiv &by_ntiles, const FastDiv &by_ntx,
                                          const uint32_t *__restrict__ scr1_all,
                                          const uint32_t *__restrict__ final_all,
                                          const uint32_t *__restrict__ prefix_all, size_t words,
                                          int lane) {
-  const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
-  const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
-  const int r0 = ty * kVerRows, c0 = tx * kVerTW;
-  const int xs = (c0 - 5) & ~(VerPix<Pix>::kAlign - 1);
-  stage_pixels<Pix>(sm.pix[s], reinterpret_cast<const Pix *>(F.image[f]), height, width, vec,
-                    r0, xs, lane);
+  const TileAt a = tile_at(e, ntiles, ntx, by_ntiles, by_ntx);
+  const int f = a.f, r0 = a.r0, c0 = a.c0;
+  const int xs = tile_xs<Pix>(c0);
+  if (tma)
+    tma_stage<Pix>(sm.pix[s], &sm.bar[s], M, f, r0, xs, lane);
+  else
+    stage_pixels<Pix>(sm.pix[s].px, reinterpret_cast<const Pix *>(F.image[f]), height, width,
+                      vec, r0, xs, lane);
   const int wpr = (width + 31) >> 5;
   const uint32_t *scr1 = scr1_all + (size_t)f * words;
   for (int k = lane; k < kVerPR * 3; k += 32) {
@@ -954,16 +1059,31 @@ __device__ __forceinline__ void s2_stage(S2Warp<Pix> &sm, int s, uint32_t e, con
 
 template <int kOcc, typename Pix>
 __global__ void __launch_bounds__(kVerWarps * 32, kOcc)
-lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
-           const __grid_constant__ LaunchParams P, const uint32_t *__restrict__ scr1_all,
-           const uint32_t *__restrict__ final_all, const uint32_t *__restrict__ prefix_all,
-           size_t words, const uint32_t *__restrict__ list, const uint32_t *__restrict__ counters,
+lat_stage2(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps M, int tma,
+           int height, int width, int vec, const __grid_constant__ LaunchParams P,
+           const uint32_t *__restrict__ scr1_all, const uint32_t *__restrict__ final_all,
+           const uint32_t *__restrict__ prefix_all, size_t words,
+           const uint32_t *__restrict__ list, uint32_t *__restrict__ counters,
            uint32_t *__restrict__ cand_all, uint2 *__restrict__ res_all, uint32_t cand_cap,
            FastDiv by_ntiles, FastDiv by_ntx) {
-  extern __shared__ __align__(16) unsigned char s2_smem[];
+  extern __shared__ __align__(128) unsigned char s2_smem_raw[];
+  // 128 bytes more than the layout: the tile buffers start on a 128-byte
+  // boundary whatever the base's alignment.
+  unsigned char *s2_smem = s2_smem_raw + ((128u - (smem_addr(s2_smem_raw) & 127u)) & 127u);
   constexpr bool k16 = sizeof(Pix) == 2;
+  // A fault in the exact check leaves its tile list partly unwritten: nothing
+  // to do (the launch's counts report the fault).
+  if (counters[kCtrFault])
+    return;
   S2Warp<Pix> &sm = reinterpret_cast<S2Warp<Pix> *>(s2_smem)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
+  if (tma && lane == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+  uint32_t parity = 0;  // bit b: the phase the next wait on bar[b] waits for
   const int ntx = ver_ntx(width);
   const uint32_t ntiles = (uint32_t)ntx * (uint32_t)ver_nty(height);
   // The exact check's tile list with the tiles left without a candidate
@@ -985,20 +1105,32 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
   uint32_t e = next_live(blockIdx.x * kVerWarps + (threadIdx.x >> 5), &k);
   uint32_t e1 = next_live(k + nw, &k1);
   if (k < count)
-    s2_stage<Pix>(sm, 0, e, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
-                  final_all, prefix_all, words, lane);
+    s2_stage<Pix>(sm, 0, e, F, M, tma, height, width, vec, ntiles, ntx, by_ntiles, by_ntx,
+                  scr1_all, final_all, prefix_all, words, lane);
   cp_async_commit();
+  uint32_t inflight = k < count ? 1u : 0u;  // bit b: a TMA load into buffer b not waited for
   for (int s = 0; k < count; s ^= 1) {
-    if (k1 < count)
-      s2_stage<Pix>(sm, s ^ 1, e1, F, height, width, vec, ntiles, ntx, by_ntiles, by_ntx,
-                    scr1_all, final_all, prefix_all, words, lane);
+    if (k1 < count) {
+      s2_stage<Pix>(sm, s ^ 1, e1, F, M, tma, height, width, vec, ntiles, ntx, by_ntiles,
+                    by_ntx, scr1_all, final_all, prefix_all, words, lane);
+      inflight |= 2u >> s;
+    }
     cp_async_commit();
     cp_async_wait<1>();
     __syncwarp();
-    const uint32_t fu = fast_div(e, by_ntiles), t = e - fu * ntiles, tyu = fast_div(t, by_ntx);
-    const int f = (int)fu, ty = (int)tyu, tx = (int)(t - tyu * (uint32_t)ntx);
-    const int r0 = ty * kVerRows, c0 = tx * kVerTW;
-    const int xs = (c0 - 5) & ~(VerPix<Pix>::kAlign - 1), off = (c0 - 5) - xs;
+    const TileAt a = tile_at(e, ntiles, ntx, by_ntiles, by_ntx);
+    const int f = a.f, r0 = a.r0, c0 = a.c0;
+    const int xs = tile_xs<Pix>(c0), off = (c0 - 5) - xs;
+    if (tma) {
+      inflight &= ~(1u << s);
+      if (!tma_landed<Pix>(sm.pix[s], &sm.bar[s], (parity >> s) & 1u, height, width, r0, xs,
+                           lane)) {
+        if (lane == 0)
+          atomicOr(counters + kCtrFault, 1u);
+        break;  // whole warp
+      }
+      parity ^= 1u << s;
+    }
     const int w0 = c0 >> 5, sh = c0 & 31;
     uint32_t cj[kVerRows], late = 0;
     int incl = 0;
@@ -1035,7 +1167,7 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
       uint32_t bn[kVerPR], bs[kVerPR];
 #pragma unroll
       for (int r = 0; r < kVerPR; r++) {
-        const uint32_t v = sm.pix[s][r][j];
+        const uint32_t v = sm.pix[s].px[r][j];
         const bool eroded = (sm.ew[s][r][wi] >> b) & 1u;
         const bool bg = !is_masked_px<Pix>(v) && !eroded;
         if (!k16)
@@ -1098,7 +1230,7 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
         for (int r = o; r < o + 11; r++)
           for (int u = 0; u < 11; u++) {
             const int j = off + tcol + u, x = xs + j;
-            const uint32_t v = sm.pix[s][r][j];
+            const uint32_t v = sm.pix[s].px[r][j];
             const bool eroded = (sm.ew[s][r][(x >> 5) - (xs >> 5)] >> (x & 31)) & 1u;
             if (!is_masked_px<Pix>(v) && !eroded) {
               n++;
@@ -1106,7 +1238,7 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
             }
           }
       }
-      const uint32_t p = sm.pix[s][o + 5][off + tcol + 5];
+      const uint32_t p = sm.pix[s].px[o + 5][off + tcol + 5];
       float bg = 0.0f;
       // dext.cc:205: only pixels above the global threshold are tested.
       bool sig = (uint64_t)p >= P.p_min;
@@ -1128,16 +1260,24 @@ lat_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
     e = e1;
     e1 = next_live(k1 + nw, &k1);
   }
+  // After a fault: the load still in flight (bounded) before the buffers go.
+  for (int b = 0; b < 2; b++)
+    if (tma && ((inflight >> b) & 1u))
+      (void)mbar_wait(&sm.bar[b], (parity >> b) & 1u);
   cp_async_wait<0>();
 }
 
+// Both add 128 bytes for aligning the tile buffers (see the kernels).
 template <typename Pix> constexpr size_t s2_smem_bytes() {
-  return sizeof(S2Warp<Pix>) * kVerWarps;
+  return sizeof(S2Warp<Pix>) * kVerWarps + 128;
 }
 
 template <typename Pix> constexpr size_t ver_smem_bytes() {
-  return sizeof(uint4) * 64 + sizeof(VerWarp<Pix>) * kVerWarps;
+  return sizeof(uint4) * 64 + sizeof(VerWarp<Pix>) * kVerWarps + 128;
 }
+static_assert(sizeof(uint4) * 64 % 128 == 0, "the verify warps start 128-byte aligned");
+static_assert((ver_smem_bytes<uint32_t>() + 1024) * kVerOcc <= 228 * 1024,
+              "five exact-check blocks an SM");
 
 int lat_slots() {
   static int slots = 0;
@@ -1161,6 +1301,19 @@ template <class Kernel> cudaError_t persistent_blocks(Kernel k, size_t bytes, in
   return e;
 }
 
+// The launch's frames mapped for the TMA staging of tiles (1), or not
+// mappable (0: a frame not 16-byte aligned, a row pitch that is not a
+// multiple of 16 bytes, no driver entry point), the per-lane staging then.
+template <typename Pix> int make_tile_maps(const FramePtrs &F, int nframes, int h, int w,
+                                           TileMaps *M) {
+  std::memset(M, 0, sizeof(*M));
+  for (int f = 0; f < nframes; f++)
+    if (!encode_frame_map(&M->map[f], F.image[f], h, w, (int)sizeof(Pix), VerPix<Pix>::kPW,
+                          kVerPR))
+      return 0;
+  return 1;
+}
+
 template <typename Pix>
 cudaError_t lattice_stage2(const FramePtrs &F, int nframes, int h, int w, int vec,
                            const LaunchParams &P, const StreamBuffers &b, cudaStream_t stream) {
@@ -1176,9 +1329,11 @@ cudaError_t lattice_stage2(const FramePtrs &F, int nframes, int h, int w, int ve
   const uint32_t *prefix = b.amb;
   const size_t tiles = (size_t)ver_ntx(w) * (size_t)ver_nty(h);
   const uint32_t *list = b.amb + (size_t)nframes * (b.words + tiles);
+  TileMaps M;
+  const int tma = make_tile_maps<Pix>(F, nframes, h, w, &M);
   lat_stage2<kVerOcc, Pix><<<blocks * device_sms(), kVerWarps * 32, s2_smem_bytes<Pix>(),
-                             stream>>>(F, h, w, vec, P, b.scr1, b.bits, prefix, b.words, list,
-                                       b.counters, b.cand, b.res, b.cand_cap,
+                             stream>>>(F, M, tma, h, w, vec, P, b.scr1, b.bits, prefix, b.words,
+                                       list, b.counters, b.cand, b.res, b.cand_cap,
                                        make_fastdiv((uint32_t)tiles),
                                        make_fastdiv((uint32_t)ver_ntx(w)));
   return cudaGetLastError();
@@ -1225,14 +1380,47 @@ cudaError_t lattice(const FramePtrs &F, int nframes, int h, int w, int vec, cons
   const FastDiv by_ntx = make_fastdiv((uint32_t)ver_ntx(w));
   lat_tiles<<<tb, 256, 0, stream>>>(nframes, h, w, b.bits, b.words, list, b.counters, by_ngx,
                                     by_fgroups, trun);
+  TileMaps M;
+  const int tma = make_tile_maps<Pix>(F, nframes, h, w, &M);
   lat_verify<kVerOcc, Pix><<<ver_blocks * device_sms(), kVerWarps * 32, ver_smem_bytes<Pix>(),
-                             stream>>>(F, h, w, vec, P, T, b.scr1, b.bits, b.words, list,
+                             stream>>>(F, M, tma, h, w, vec, P, T, b.scr1, b.bits, b.words, list,
                                        b.counters, by_ntiles, by_ntx,
                                        list + (size_t)nframes * tiles);
   return cudaGetLastError();
 }
 
 } // namespace
+
+bool encode_frame_map(CUtensorMap *map, const void *base, int h, int w, int bytes_per_pixel,
+                      int box_w, int box_h) {
+  // The driver's encoder, looked up once (no link against libcuda).
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      fn = nullptr;
+    }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  const size_t pitch = (size_t)w * (size_t)bytes_per_pixel;
+  if (!encode || !base || reinterpret_cast<uintptr_t>(base) % 16 != 0 || pitch % 16 != 0 ||
+      h < 1 || w < 1 || (bytes_per_pixel != 2 && bytes_per_pixel != 4))
+    return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)w, (cuuint64_t)h};
+  const cuuint64_t strides[1] = {(cuuint64_t)pitch};
+  const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+  const cuuint32_t step[2] = {1, 1};
+  return encode(map,
+                bytes_per_pixel == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32
+                                     : CU_TENSOR_MAP_DATA_TYPE_UINT16,
+                2, const_cast<void *>(base), dims, strides, box, step,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 size_t lattice_tiles(int h, int w) { return (size_t)ver_ntx(w) * (size_t)ver_nty(h); }
 

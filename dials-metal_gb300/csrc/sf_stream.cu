@@ -880,6 +880,11 @@ pass_sums(const uint2 *__restrict__ res_all, uint32_t cand_cap,
           const uint32_t *__restrict__ cand_all, uint32_t *__restrict__ final_all, size_t words,
           int width) {
   const int f = blockIdx.y;
+  if (counters[kCtrFault]) {  // the stage-2 results are void: touch nothing
+    if (threadIdx.x == 0)
+      block_sums[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = 0;
+    return;
+  }
   const uint2 *res = res_all + (size_t)f * cand_cap;
   const uint32_t nc = min(counters[kCtrBatch + (size_t)f * kCtrCount + kCtrCand], cand_cap);
   // final_all given: the candidates that failed stage 2 leave the final mask
@@ -922,6 +927,11 @@ pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ c
              sf_signal_pixel *__restrict__ out_all, size_t out_stride, uint32_t capacity,
              uint32_t *__restrict__ count_out) {
   const int f = blockIdx.y;
+  if (counters[kCtrFault]) {  // a bounded device wait ran out: no list
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+      count_out[f] = kCountFault;
+    return;
+  }
   const Pix *image = reinterpret_cast<const Pix *>(F.image[f]);
   const uint32_t *cand = cand_all + (size_t)f * cand_cap;
   const uint2 *res = res_all + (size_t)f * cand_cap;

@@ -41,12 +41,17 @@ enum {
   kCtrWide = 0,   // batch: runs handed to the 64-bit path
   kCtrTiles = 1,  // batch: tiles listed for the exact check (kernel 3,3)
   kCtrTiles2 = 2, // batch: tiles with a candidate left after it (stage 2's list)
+  kCtrFault = 3,  // batch: a bounded device wait ran out (the launch's lists are void)
   kCtrBatch = 4,  // first frame's counters
   kCtrCand = 0,   // frame: candidates (set bits of the candidate mask)
   kCtrWideFrame = 1,  // frame: a valid pixel may be too large for 32-bit stage-2 sums
   kCtrCount = 4
 };
 inline size_t counter_words(int nframes) { return kCtrBatch + (size_t)nframes * kCtrCount; }
+
+// A frame's signal count when its launch met a device fault (kCtrFault):
+// no list, whatever the capacity.
+constexpr uint32_t kCountFault = 0xFFFFFFFEu;
 
 // Strips of 240 output columns (one warp each) by runs of run_rows rows.
 struct SegGeometry {

@@ -188,7 +188,9 @@ void sf_last_stage_times(sf_stage_times *out);
  *   d_out        room for `capacity` records; filled ascending by index
  *   d_bits       ceil(width/32) * height words: the strong-pixel bitmask
  *   d_count      one uint32: the number of signal pixels found (may exceed
- *                capacity, in which case the list is incomplete)
+ *                capacity, in which case the list is incomplete); 0xFFFFFFFE
+ *                if a bounded device wait of the launch ran out (no list;
+ *                the host-frame calls return -3 for it)
  *   d_word_prefix optional (NULL): per bitmask word, the list position of
  *                its first pixel
  *   d_workspace  sf_workspace_bytes(height, width, capacity) bytes
