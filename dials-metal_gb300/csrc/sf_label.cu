@@ -1350,6 +1350,11 @@ template <typename T> struct DeviceStore {
   };
   std::vector<Chunk> chunks;
   size_t n = 0, cap = 0;
+  // A caller's say over growth (the served form's memory budget): asked for
+  // the bytes of each new chunk before it is allocated; a refusal leaves the
+  // store as it is and sets `refused`.
+  LabelGrowth growth{};
+  bool refused = false;
   DeviceStore() = default;
   DeviceStore(const DeviceStore &) = delete;
   DeviceStore &operator=(const DeviceStore &) = delete;
@@ -1365,6 +1370,10 @@ template <typename T> struct DeviceStore {
     while (cap < n + m) {
       size_t c = chunks.empty() ? kFirst : std::min(chunks.back().cap * 2, kMax);
       c = std::max(c, std::min(n + m - cap, kMax));
+      if (growth.ok && !growth.ok(growth.ctx, c * sizeof(T))) {
+        refused = true;
+        return cudaErrorMemoryAllocation;
+      }
       T *q = nullptr;
       const cudaError_t e = cudaMalloc(&q, c * sizeof(T));
       if (e != cudaSuccess)
@@ -1414,6 +1423,30 @@ template <typename T> struct DeviceStore {
   }
 };
 
+// Every kernel of a label call loaded on the current device (a no-op once
+// they are), by asking for each one's attributes.
+static cudaError_t load_label_kernels() {
+  const void *kernels[] = {
+      (const void *)k_offsets,        (const void *)k_append,        (const void *)k_rows,
+      (const void *)k_link,           (const void *)k_unite,         (const void *)k_flatten,
+      (const void *)k_comp_stats,     (const void *)k_closing_flags, (const void *)k_closing_list,
+      (const void *)k_bucket_hist,    (const void *)k_bucket_offsets,
+      (const void *)k_bucket_scatter, (const void *)k_size_filter,   (const void *)k_cand_list,
+      (const void *)k_gather,         (const void *)k_sort<false>,   (const void *)k_sort<true>,
+      (const void *)k_sort_big,       (const void *)k_perm_hist,     (const void *)k_perm_offsets,
+      (const void *)k_perm_scatter,   (const void *)k_first,         (const void *)k_pix,
+      (const void *)k_terms,          (const void *)k_var,           (const void *)k_compact,
+      (const void *)k_end_batch,      (const void *)scan_sums,       (const void *)scan_block_sums,
+      (const void *)scan_apply};
+  for (const void *k : kernels) {
+    cudaFuncAttributes a;
+    const cudaError_t e = cudaFuncGetAttributes(&a, k);
+    if (e != cudaSuccess)
+      return e;
+  }
+  return cudaSuccess;
+}
+
 struct Labeller {
   size_t height = 0, width = 0, capacity = 0, spots_cap = 0;
   sf_label_options opt;
@@ -1462,6 +1495,10 @@ struct Labeller {
   // and the readers wait for it before touching the batch outputs or the
   // stores.
   cudaEvent_t appended = nullptr;
+  // With blocking waits (label_set_blocking_wait), a call's end is waited
+  // for on this event, created with cudaEventBlockingSync: the calling thread
+  // sleeps instead of spinning (the served form runs a thread per sweep).
+  cudaEvent_t call_done = nullptr;
   sf_counts counts{};
   uint32_t live = 0;
   std::string error;
@@ -1507,6 +1544,8 @@ struct Labeller {
       cudaFreeHost(host_st);
     if (appended)
       cudaEventDestroy(appended);
+    if (call_done)
+      cudaEventDestroy(call_done);
   }
 
   int init() {
@@ -1654,11 +1693,11 @@ struct Labeller {
   // every kernel is loaded before a capture), then replayed on any stream.
   // Null if capture is not possible (the caller's stream is itself being
   // captured, or the capture failed): the sequence then runs directly.
-  cudaGraphExec_t graph_for(int nb, int c, cudaStream_t s) {
+  cudaGraphExec_t graph_for(int nb, int c, cudaStream_t s, bool now = false) {
     cudaGraphExec_t &g = graphs[c][nb];
     if (g || !use_graphs)
       return g;
-    if (!seen[c][nb]) {
+    if (!seen[c][nb] && !now) {
       seen[c][nb] = true;
       return nullptr;
     }
@@ -1683,6 +1722,20 @@ struct Labeller {
       cudaGetLastError();
     }
     return g;
+  }
+
+  // Every batch size up to max_nb captured now, on both live pools, so that
+  // no later call pays a capture (the served form prepares a sweep's
+  // labeller when the sweep opens). The kernels are loaded first: a capture
+  // must not be what loads them.
+  int prepare(int max_nb) {
+    if (load_label_kernels() != cudaSuccess)
+      return fail(cudaGetLastError(), "loading the labeller's kernels");
+    for (int c = 0; c < 2 && use_graphs; c++)
+      for (int nb = 1; nb <= max_nb && nb <= kLabelMaxBatch && use_graphs; nb++)
+        graph_for(nb, c, own_stream, true);
+    cudaStreamSynchronize(own_stream);
+    return SF_OK;
   }
 
   // One batch: frames[j]'s list at lists + j * stride, count counts[j].
@@ -1749,8 +1802,13 @@ struct Labeller {
     if ((e = cudaMemcpyAsync(host_st, st, sizeof(LabelStatus), cudaMemcpyDeviceToHost, s)) !=
         cudaSuccess)
       return fail(e, "reading the labeller status");
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess)
+    if (call_done) {
+      if ((e = cudaEventRecord(call_done, s)) != cudaSuccess ||
+          (e = cudaEventSynchronize(call_done)) != cudaSuccess)
+        return fail(e, "waiting for the labeller");
+    } else if ((e = cudaStreamSynchronize(s)) != cudaSuccess) {
       return fail(e, "cudaStreamSynchronize");
+    }
     if (host_st->error) {
       const uint32_t err = host_st->error;
       t_last_error = (err & kErrLiveFull)
@@ -1765,8 +1823,14 @@ struct Labeller {
     }
     const uint32_t na = host_st->n_accept, npx = host_st->n_accept_pixels;
     if ((e = spots.append(d_spots, na, s)) != cudaSuccess ||
-        (e = pixels.append(d_pixels, npx, s)) != cudaSuccess)
+        (e = pixels.append(d_pixels, npx, s)) != cudaSuccess) {
+      if (spots.refused || pixels.refused) {
+        cudaGetLastError();
+        t_last_error = "the sweep's spots and pixels would grow past the device-memory budget";
+        return SF_EBUSY;
+      }
       return fail(e, "storing the labeller's results");
+    }
     if ((e = cudaEventRecord(appended, s)) != cudaSuccess)
       return fail(e, "cudaEventRecord");
     const unsigned long long *c = host_st->counts;
@@ -1825,6 +1889,32 @@ size_t label_device_bytes(size_t height, size_t capacity, size_t min_spot_size) 
          2 * kSizeBins * 4 +
          (size_t)kGrid * kBuckets * 4 + (size_t)kScanBlocks * 4 + kLabelMaxBatch * 4 +
          2 * sizeof(LabelStatus) + 2 * sizeof(BatchArgs);
+}
+
+void label_set_growth(sf_labeller *l, LabelGrowth growth) {
+  if (!l)
+    return;
+  l->impl.spots.growth = growth;
+  l->impl.pixels.growth = growth;
+}
+
+size_t label_result_bytes(const sf_labeller *l) {
+  return l ? l->impl.spots.cap * sizeof(sf_spot) + l->impl.pixels.cap * sizeof(sf_pixel) : 0;
+}
+
+int label_set_blocking_wait(sf_labeller *l) {
+  if (!l)
+    return SF_EBADARG;
+  Labeller &L = l->impl;
+  if (L.call_done)
+    return SF_OK;
+  const cudaError_t e =
+      cudaEventCreateWithFlags(&L.call_done, cudaEventBlockingSync | cudaEventDisableTiming);
+  return e == cudaSuccess ? SF_OK : fail(e, "cudaEventCreate");
+}
+
+int label_prepare(sf_labeller *l, int max_batch) {
+  return l ? l->impl.prepare(max_batch) : SF_EBADARG;
 }
 
 int label_gather_pixels(const sf_labeller *l, sf_pixel *d_out, cudaStream_t *stream) {

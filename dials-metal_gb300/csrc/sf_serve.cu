@@ -130,6 +130,8 @@ struct SrvSweep {
   SrvGroup *group = nullptr;
   sf_labeller *lab = nullptr;
   size_t bytes = 0, ring = 0;
+  size_t result_bytes = 0;              // its labeller's spot and pixel stores, granted
+  sf_server *server = nullptr;
   std::vector<uint32_t *> slots;        // frames
   sf_signal_pixel *lists = nullptr;     // ring * capacity records
   uint32_t *counts = nullptr;           // ring
@@ -248,6 +250,20 @@ struct sf_server {
   void label_loop(SrvSweep *s);
   cudaError_t upload_chunk(SrvSweep &s, const SrvFrame &f, int ci);
 };
+
+// A sweep's results are counted against the budget as its labeller's stores
+// grow: a chunk that would take the server past its budget is refused, and
+// the sweep fails with SF_EBUSY instead of growing (other sweeps go on).
+static bool results_may_grow(void *ctx, size_t bytes) {
+  SrvSweep *s = static_cast<SrvSweep *>(ctx);
+  sf_server *sv = s->server;
+  std::lock_guard<std::mutex> lock(sv->m);
+  if (sv->used + bytes > sv->opt.hbm_budget)
+    return false;
+  sv->used += bytes;
+  s->result_bytes += bytes;
+  return true;
+}
 
 // Copies a frame's chunk to the device on copy stream ci and decodes it into
 // the frame's slot there. The slot is free, so its table buffers are idle.
@@ -374,6 +390,7 @@ void sf_server::label_loop(SrvSweep *s) {
     stats.label_calls++;
     stats.label_frames += k;
     stats.label_seconds += now - t_call;
+    stats.label_max_seconds = std::max(stats.label_max_seconds, now - t_call);
     // A chunk the decoder refused fails its frame and the sweep, with the
     // decoder's text (recorded before whatever labelling its frame made of).
     std::vector<int> frc(k, rc);
@@ -497,7 +514,9 @@ void sf_server::run() {
     std::lock_guard<std::mutex> lock(m);
     stats.batches++;
     stats.batch_frames += batch.size();
-    stats.launch_seconds += now_s() - t_launch;
+    const double launch_s = now_s() - t_launch;
+    stats.launch_seconds += launch_s;
+    stats.launch_max_seconds = std::max(stats.launch_max_seconds, launch_s);
     size_t j = 0;
     while (j < batch.size()) {
       SrvSweep &s = *sweeps[batch[j].sweep];
@@ -650,6 +669,18 @@ int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,
   s->lab = sf_label_open(height, width, &lo, labeller_capacity(height, width));
   if (!s->lab)
     return SF_EBADARG;
+  s->server = sv;
+  sf::LabelGrowth growth;
+  growth.ok = results_may_grow;
+  growth.ctx = s.get();
+  sf::label_set_growth(s->lab, growth);
+  // Its label thread sleeps while a call runs, and every call shape is
+  // captured now rather than in the middle of the sweep's frames.
+  int lrc = sf::label_set_blocking_wait(s->lab);
+  if (lrc == SF_OK)
+    lrc = sf::label_prepare(s->lab, (int)sv->opt.max_batch);
+  if (lrc != SF_OK)
+    return lrc;
   for (size_t i = 0; i < s->ring; i++) {
     uint32_t *slot = nullptr;
     if ((e = cudaMalloc(&slot, height * width * sizeof(uint32_t))) != cudaSuccess)
@@ -820,7 +851,7 @@ int sf_server_close_sweep(sf_server *sv, int64_t sweep) {
   std::unique_ptr<SrvSweep> gone = std::move(it->second);
   sv->sweeps.erase(it);
   SrvGroup *g = gone->group;
-  sv->used -= gone->bytes;
+  sv->used -= gone->bytes + gone->result_bytes;
   std::unique_ptr<SrvGroup> gone_group;
   if (--g->users == 0) {
     sv->used -= g->bytes;

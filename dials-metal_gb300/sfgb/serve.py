@@ -30,7 +30,8 @@ class FrameDone(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [("batches", ctypes.c_uint64), ("batch_frames", ctypes.c_uint64),
                 ("label_calls", ctypes.c_uint64), ("label_frames", ctypes.c_uint64),
-                ("launch_seconds", ctypes.c_double), ("label_seconds", ctypes.c_double)]
+                ("launch_seconds", ctypes.c_double), ("label_seconds", ctypes.c_double),
+                ("launch_max_seconds", ctypes.c_double), ("label_max_seconds", ctypes.c_double)]
 
 
 class Busy(RuntimeError):

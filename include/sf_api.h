@@ -431,7 +431,10 @@ int sf_threshold_u32_device_noalloc(const uint32_t *d_image, size_t height,
  * A frame's results do not depend on the other sweeps in the mix.
  */
 typedef struct {
-  size_t hbm_budget;       /* device bytes for sweeps; 0: 80% of the free memory */
+  size_t hbm_budget;       /* device bytes for sweeps and the spots and pixels they
+                              hold on the device; 0: 80% of the free memory. A
+                              sweep whose results would take the server past it
+                              fails with -5 (SF_EBUSY) instead of growing */
   size_t max_batch;        /* frames per threshold launch, 1..SF_MAX_BATCH (16) */
   size_t ring;             /* device frame slots per sweep, >= max_batch (32) */
   size_t capacity_divisor; /* signal-list capacity = pixels / this (16) */
@@ -447,10 +450,12 @@ typedef struct {
 
 /* Counters since sf_server_open: threshold launches and the frames in them,
  * label calls and their frames, host seconds spent launching batches and in
- * label calls (summed over the sweeps' labellers). */
+ * label calls (summed over the sweeps' labellers), and the longest single
+ * launch and label call. */
 typedef struct {
   uint64_t batches, batch_frames, label_calls, label_frames;
   double launch_seconds, label_seconds;
+  double launch_max_seconds, label_max_seconds;
 } sf_server_stats;
 
 typedef struct sf_server sf_server;

@@ -107,6 +107,47 @@ def test_admission_by_budget(serve):
     srv.close()
 
 
+def test_results_count_against_the_budget(serve):
+    """A sweep's spots and pixels held on the device count against the
+    budget: with room for one sweep and about 3 MiB of results, a long dense
+    sweep fails with SF_EBUSY once its stores would grow past the budget,
+    instead of growing; the server never holds more than its budget."""
+    from sfgb import api
+    h, w, n = 512, 640, 80
+    frames = _synth(h, w, n, seed=91)
+    probe = serve.Server(hbm_budget=1 << 40, max_batch=4, ring=8)
+    sid = probe.open_sweep(h, w)
+    one = probe.used_bytes  # the sweep and its shape group, no results yet
+    for i in range(n):
+        probe.submit(sid, i, frames[i])
+    probe.finish_sweep(sid, read=False)
+    # The results are counted, and they outgrow the budget below.
+    assert probe.used_bytes - one > (3 << 20)
+    probe.close_sweep(sid)
+    assert probe.used_bytes == 0
+    probe.close()
+
+    budget = one + (3 << 20)
+    srv = serve.Server(hbm_budget=budget, max_batch=4, ring=8)
+    sid = srv.open_sweep(h, w)
+    done = []
+    for i in range(n):
+        try:
+            srv.submit(sid, i, frames[i])
+        except api.SpotFinderError:
+            break  # the sweep has already failed
+        assert srv.used_bytes <= budget
+    with pytest.raises(api.SpotFinderError):
+        srv.finish_sweep(sid)
+    assert "budget" in srv.sweep_error(sid)
+    done += srv.poll(4096, 100)
+    assert any(d["status"] == serve.SF_EBUSY for d in done)
+    assert srv.used_bytes <= budget
+    srv.close_sweep(sid)
+    assert srv.used_bytes == 0
+    srv.close()
+
+
 def test_out_of_order_refused(serve):
     srv = serve.Server(max_batch=2, ring=2)
     sid = srv.open_sweep(64, 64)
