@@ -422,6 +422,99 @@ def served_e2e(n_frames: int, frames_per_step: int, h2d_gbs=None, n_sweeps: int 
     return out
 
 
+def batched_legs(dev, steps: int = 5, warmup: int = 3) -> dict:
+    """The batched form's own workload: 4M (2162x2068) and 9M (3262x3108)
+    frames, Poisson 1.0, 1500 spots a frame, 64 distinct frames in HBM a
+    shape (larger than L2). Per kernel size 2,2 / 3,3 / 4,4
+    (dispersion_extended) and for the dispersion algorithm (kernel 3,3), a
+    plan tuned on the frames (frames a launch sequence, 64/32/16, and the
+    strip run length) replayed as a CUDA graph, beside the plain per-frame
+    device path on the same frames; and a mixed batch of the served
+    detectors (4 frames each of 16M, 9M, 4M and 1M) in one launch sequence
+    beside the same frames thresholded shape by shape."""
+    import torch
+    from sfgb import api, synth
+    stream = torch.cuda.Stream(device=dev)
+    peak = measured_peak_gbs()[0]
+
+    def timed(fn, reps):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                fn()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                fn()
+            b.record(stream)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b) / reps
+
+    out = {}
+    settings = {"dispersion_extended_k2": dict(kernel_x=2, kernel_y=2),
+                "dispersion_extended_k3": dict(),
+                "dispersion_extended_k4": dict(kernel_x=4, kernel_y=4),
+                "dispersion_k3": dict(algorithm=1)}
+    for name, (h, w) in {"batch_4m": (2162, 2068), "batch_9m": (3262, 3108)}.items():
+        n = 64
+        sw = synth.Sweep(synth.preset(name, n_frames=n))
+        pool = torch.stack([torch.from_numpy(sw.frame(i).view(np.int32))
+                            for i in range(n)]).to(dev)
+        views = [pool[j] for j in range(n)]
+        per = {}
+        for key, kw in settings.items():
+            params = api.Params(**kw)
+            plan = api.Plan(h, w, n, capacity=h * w // 16, params=params)
+            with torch.cuda.stream(stream):
+                rr = plan.tune(views, stream=stream)
+            ms = timed(lambda: plan(views, stream=stream), steps)
+            sig = int(np.mean([len(plan.result(j)) for j in range(0, n, 8)]))
+            single = api.DeviceThreshold(h, w, params=params, capacity=h * w // 16)
+
+            def plain():
+                for v in views:
+                    single(v, stream=stream)
+            ms1 = timed(plain, 2)
+            algo = n * (h * w * 4 + (h * w + 7) // 8 + 16 * sig)
+            per[key] = {"frames_per_s": n / (ms / 1e3), "us_per_frame": ms * 1e3 / n,
+                        "achieved_gbs": algo / (ms / 1e3) / 1e9,
+                        "frac_of_hbm": algo / (ms / 1e3) / 1e9 / peak,
+                        "tuned_run_rows": rr,
+                        "tuned_frames_per_launch": plan.frames_per_launch or n,
+                        "plain_per_frame_frames_per_s": n / (ms1 / 1e3),
+                        "batched_over_plain": ms1 / ms, "signal_pixels_per_frame": sig}
+            plan.close()
+            del single
+        out[name] = per
+        del pool, views
+
+    # Mixed detector sizes in one launch sequence.
+    shapes = [("eiger_16m", H, W), ("batch_9m", 3262, 3108), ("batch_4m", 2162, 2068),
+              ("plain_1m", 1065, 1030)]
+    frames = []
+    for name, h, w in shapes:
+        sw = synth.Sweep(synth.preset(name, height=h, width=w, n_frames=4))
+        frames += [torch.from_numpy(sw.frame(i).view(np.int32)).to(dev) for i in range(4)]
+    mixed = api.MixedBatch([tuple(f.shape) for f in frames], capacity=H * W // 16)
+    ms_mixed = timed(lambda: mixed(frames, stream=stream), steps)
+    groups = [api.DeviceBatch(h, w, 4, capacity=H * W // 16) for _, h, w in shapes]
+
+    def by_shape():
+        for k, g in enumerate(groups):
+            g(frames[4 * k:4 * k + 4], stream=stream)
+    ms_shapes = timed(by_shape, steps)
+    px = sum(int(f.numel()) for f in frames)
+    out["mixed_detectors"] = {
+        "frames": len(frames), "one_launch_us": ms_mixed * 1e3,
+        "frames_per_s": len(frames) / (ms_mixed / 1e3),
+        "megapixels_per_s": px / (ms_mixed / 1e3) / 1e6,
+        "per_shape_launches_us": ms_shapes * 1e3,
+        "one_launch_over_per_shape": ms_shapes / ms_mixed,
+        "path": "sf_threshold_u32_mixed_batch_device: 4 frames each of 4362x4148, 3262x3108, "
+                "2162x2068 and 1065x1030 in one launch sequence, against "
+                "sf_threshold_u32_batch_device once per shape"}
+    return out
+
+
 def run_ours(args):
     import torch
     from sfgb import api
@@ -779,6 +872,10 @@ def run_ours(args):
         if not args.no_bslz4:
             e2e["bslz4_u32"] = served_e2e(args.steps * B, B, h2d_gbs, chunks=True)
 
+    batched = None
+    if rank == 0 and not args.no_batched:
+        batched = batched_legs(dev)
+
     served_line = None
     if rank == 0 and not args.no_served:
         del plan
@@ -843,6 +940,7 @@ def run_ours(args):
                          "traffic_source": traffic_source},
             "cpu_baseline": base, "e2e": e2e, "labelling": label, "u16": u16_line,
             "served": served_line,
+            "batched": batched,
             "clocks": clock,
             "gpu_launches": (THRESHOLD_KERNELS + LABEL_KERNELS) * args.steps,
         }
@@ -866,6 +964,8 @@ def main(argv=None):
     ap.add_argument("--e2e-threads", type=int, default=0,
                     help="host threads of the end-to-end legs (0: one a core, as mxi_find -j)")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the 4M/9M tuned-plan and mixed-detector legs")
     ap.add_argument("--no-u16", action="store_true")
     ap.add_argument("--no-bslz4", action="store_true")
     ap.add_argument("--clocks-csv", default=None,

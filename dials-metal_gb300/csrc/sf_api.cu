@@ -177,43 +177,108 @@ static bool stream_path(size_t elem, const LaunchParams &P) {
 // their tests are the reference's float ones) when whole 8-byte pieces of 4
 // pixels tile every row: 4 | width and 8-byte aligned frames.
 template <typename T>
-static bool stream16_path(const T *const *d_images, size_t n, size_t w, const LaunchParams &P) {
-  if (sizeof(T) != 2 || P.algorithm != SF_DISPERSION_EXTENDED || P.half != 3 || w % 4 != 0)
+static bool stream16_path(const T *const *d_images, size_t n, const size_t *widths,
+                          const LaunchParams &P) {
+  if (sizeof(T) != 2 || P.algorithm != SF_DISPERSION_EXTENDED || P.half != 3)
     return false;
   for (size_t j = 0; j < n; j++)
-    if (reinterpret_cast<uintptr_t>(d_images[j]) % 8 != 0)
+    if (widths[j] % 4 != 0 || reinterpret_cast<uintptr_t>(d_images[j]) % 8 != 0)
       return false;
   return true;
 }
 
-// Frames d_images[0 .. n) (device pointers): lists at d_out + j * capacity,
-// masks at d_bits + j * words, counts at d_counts[j].
+// The batch's envelope: its tallest and widest frame (each checked).
+static bool envelope(size_t n, const size_t *heights, const size_t *widths, size_t *h,
+                     size_t *w) {
+  *h = *w = 0;
+  for (size_t j = 0; j < n; j++) {
+    if (!shape_ok(heights[j], widths[j]))
+      return false;
+    *h = std::max(*h, heights[j]);
+    *w = std::max(*w, widths[j]);
+  }
+  return n > 0 && shape_ok(*h, *w);
+}
+
+template <typename T>
+static int threshold_frames_mixed(const T *const *d_images, size_t n, const size_t *heights,
+                                  const size_t *widths, const sf_threshold_params *params,
+                                  sf_signal_pixel *d_out, size_t capacity, uint32_t *d_bits,
+                                  uint32_t *d_counts, uint32_t *d_word_prefix, void *d_ws,
+                                  size_t ws_bytes, int run_rows, cudaStream_t stream);
+
+// Frames d_images[0 .. n) (device pointers), all h x w: lists at
+// d_out + j * capacity, masks at d_bits + j * words, counts at d_counts[j].
 template <typename T>
 static int threshold_frames(const T *const *d_images, size_t n, size_t h, size_t w,
                             const sf_threshold_params *params, sf_signal_pixel *d_out,
                             size_t capacity, uint32_t *d_bits, uint32_t *d_counts,
                             uint32_t *d_word_prefix, void *d_ws, size_t ws_bytes,
                             int run_rows, cudaStream_t stream) {
-  if (!d_images || n == 0 || n > (size_t)kMaxBatch || !d_out || !d_bits || !d_counts || !d_ws ||
-      !shape_ok(h, w) || capacity > 0xffffffffu)
+  if (n == 0 || n > (size_t)kMaxBatch)
     return SF_EBADARG;
+  size_t hs[kMaxBatch], wsz[kMaxBatch];
   for (size_t j = 0; j < n; j++)
+    hs[j] = h, wsz[j] = w;
+  return threshold_frames_mixed<T>(d_images, n, hs, wsz, params, d_out, capacity, d_bits,
+                                   d_counts, d_word_prefix, d_ws, ws_bytes, run_rows, stream);
+}
+
+// Frames d_images[0 .. n) of shapes heights[j] x widths[j], laid out for the
+// envelope H x W (the tallest and the widest): lists at d_out + j * capacity,
+// frame j's mask at d_bits + j * ceil(W / 32) * H in its own rows of
+// ceil(widths[j] / 32) words, counts at d_counts[j]. The kernel-3,3 lattice
+// path takes the mixed frames in one launch sequence; other settings run
+// frames of another shape one launch sequence each.
+template <typename T>
+static int threshold_frames_mixed(const T *const *d_images, size_t n, const size_t *heights,
+                                  const size_t *widths, const sf_threshold_params *params,
+                                  sf_signal_pixel *d_out, size_t capacity, uint32_t *d_bits,
+                                  uint32_t *d_counts, uint32_t *d_word_prefix, void *d_ws,
+                                  size_t ws_bytes, int run_rows, cudaStream_t stream) {
+  size_t h = 0, w = 0;
+  if (!d_images || !heights || !widths || n == 0 || n > (size_t)kMaxBatch || !d_out ||
+      !d_bits || !d_counts || !d_ws || capacity > 0xffffffffu ||
+      !envelope(n, heights, widths, &h, &w))
+    return SF_EBADARG;
+  bool mixed = false;
+  for (size_t j = 0; j < n; j++) {
     if (!d_images[j])
       return SF_EBADARG;
+    mixed |= heights[j] != h || widths[j] != w;
+  }
   LaunchParams P;
   int rc = make_launch_params(params, &P);
   if (rc != SF_OK)
     return rc;
-  const bool streamed16 = stream16_path(d_images, n, w, P);
+  const bool streamed16 = stream16_path(d_images, n, widths, P);
   const bool streamed = stream_path(sizeof(T), P) || streamed16;
   const WorkspaceLayout L = layout(h, w, capacity, streamed ? n : 1);
   if (ws_bytes < L.total)
     return SF_EBADARG;
+  if (mixed && streamed && P.half != 3) {
+    // The strip path of kernel sizes 2 and 4 takes one shape a launch: each
+    // frame alone, into its slots (its workspace fits in the batch's).
+    for (size_t j = 0; j < n; j++) {
+      const T *one[1] = {d_images[j]};
+      rc = threshold_frames_mixed<T>(one, 1, heights + j, widths + j, params,
+                                     d_out + j * capacity, capacity, d_bits + j * L.words,
+                                     d_counts + j,
+                                     d_word_prefix ? d_word_prefix + j * L.words : nullptr, d_ws,
+                                     ws_bytes, run_rows, stream);
+      if (rc != SF_OK)
+        return rc;
+    }
+    return SF_OK;
+  }
   unsigned char *ws = static_cast<unsigned char *>(d_ws);
   if (streamed) {
     FramePtrs F;
-    for (size_t j = 0; j < n; j++)
+    for (size_t j = 0; j < n; j++) {
       F.image[j] = reinterpret_cast<const uint32_t *>(d_images[j]);
+      F.h[j] = (int)heights[j];
+      F.w[j] = (int)widths[j];
+    }
     StreamBuffers b;
     b.bits = d_bits;
     b.words = L.words;
@@ -254,7 +319,8 @@ static int threshold_frames(const T *const *d_images, size_t n, size_t h, size_t
     fb.row_total = reinterpret_cast<uint32_t *>(ws + L.row_total);
     fb.total = d_counts + j;
     fb.capacity = (uint32_t)capacity;
-    cudaError_t e = launch_threshold<T>(d_images[j], (int)h, (int)w, P, fb, stream);
+    cudaError_t e =
+        launch_threshold<T>(d_images[j], (int)heights[j], (int)widths[j], P, fb, stream);
     if (e != cudaSuccess)
       return fail(e, "launching the threshold");
   }
@@ -946,6 +1012,36 @@ int sf_threshold_u16_batch_device(const uint16_t *const *d_images, size_t n_fram
                                     workspace_bytes, 0, static_cast<cudaStream_t>(stream));
 }
 
+size_t sf_mixed_batch_workspace_bytes(size_t n_frames, const size_t *heights,
+                                      const size_t *widths, size_t capacity) {
+  size_t h = 0, w = 0;
+  if (!heights || !widths || n_frames == 0 || n_frames > (size_t)kMaxBatch ||
+      !envelope(n_frames, heights, widths, &h, &w))
+    return 0;
+  return layout(h, w, capacity, n_frames).total;
+}
+
+size_t sf_mixed_batch_mask_words(size_t n_frames, const size_t *heights, const size_t *widths) {
+  size_t h = 0, w = 0;
+  if (!heights || !widths || n_frames == 0 || n_frames > (size_t)kMaxBatch ||
+      !envelope(n_frames, heights, widths, &h, &w))
+    return 0;
+  return (w + 31) / 32 * h;
+}
+
+int sf_threshold_u32_mixed_batch_device(const uint32_t *const *d_images, const size_t *heights,
+                                        const size_t *widths, size_t n_frames,
+                                        const sf_threshold_params *params,
+                                        sf_signal_pixel *d_out, size_t capacity,
+                                        uint32_t *d_bits, uint32_t *d_counts,
+                                        uint32_t *d_word_prefix, void *d_workspace,
+                                        size_t workspace_bytes, void *stream) {
+  return threshold_frames_mixed<uint32_t>(d_images, n_frames, heights, widths, params, d_out,
+                                          capacity, d_bits, d_counts, d_word_prefix,
+                                          d_workspace, workspace_bytes, 0,
+                                          static_cast<cudaStream_t>(stream));
+}
+
 } // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -1051,6 +1147,9 @@ struct Plan {
   size_t h = 0, w = 0, max_frames = 0, capacity = 0, words = 0;
   sf_threshold_params params{};
   int run_rows = 0;  // 0: the default geometry
+  // Frames a launch sequence takes (0: all of a call's frames in one); a
+  // call of more runs as consecutive sequences on its stream.
+  size_t per_launch = 0;
   void *ws = nullptr;
   size_t ws_bytes = 0;
   sf_signal_pixel *lists = nullptr;
@@ -1078,8 +1177,16 @@ struct Plan {
     graphs.clear();
   }
   int launch(const uint32_t *const *images, size_t n, cudaStream_t s) {
-    return threshold_frames<uint32_t>(images, n, h, w, &params, lists, capacity, masks, counts,
-                                      nullptr, ws, ws_bytes, run_rows, s);
+    const size_t step = per_launch ? per_launch : n;
+    for (size_t j = 0; j < n; j += step) {
+      const size_t m = std::min(step, n - j);
+      const int rc = threshold_frames<uint32_t>(images + j, m, h, w, &params, lists + j * capacity,
+                                                capacity, masks + j * words, counts + j, nullptr,
+                                                ws, ws_bytes, run_rows, s);
+      if (rc != SF_OK)
+        return rc;
+    }
+    return SF_OK;
   }
 };
 
@@ -1202,44 +1309,77 @@ int sf_plan_tune(sf_plan *plan, const uint32_t *const *d_images, size_t n_frames
     return rc;
   if (P.algorithm != SF_DISPERSION_EXTENDED || !P.int_ok)
     return SF_OK;  // the tile path has nothing to tune
-  const int base = stream_default_run_rows(P, (int)p.h, (int)p.w, (int)n_frames);
-  std::vector<int> cands = {base, base / 2, base / 3, base / 4, 2 * base, 64, 128, 256, 512};
+  // Two knobs, timed together on the given frames (median of 3 runs each):
+  // the frames a launch sequence takes (all of them, 32 or 16: fewer frames
+  // a launch keep more of a batch's tiles in L2 between the passes, more
+  // frames fill the GPU with fewer launches) and, for each, the strip run
+  // length around its default geometry.
+  std::vector<size_t> per = {n_frames};
+  for (size_t q : {(size_t)32, (size_t)16})
+    if (q < n_frames && n_frames % q == 0)
+      per.push_back(q);
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
   float best_ms = 1e30f;
-  int best = base;
-  for (int rr : cands) {
-    if (rr < kMinRunRows || rr > (int)p.h)
-      continue;
-    p.run_rows = rr;
-    float ms[3];
-    for (int it = 0; it < 4; it++) {
-      cudaEventRecord(a, s);
-      if ((rc = p.launch(d_images, n_frames, s)) != SF_OK)
+  int best = 0;
+  size_t best_per = 0;
+  for (size_t q : per) {
+    const int base = stream_default_run_rows(P, (int)p.h, (int)p.w, (int)q);
+    std::vector<int> cands = {base, base / 2, base / 3, base / 4, 2 * base, 64, 128, 256, 512};
+    std::sort(cands.begin(), cands.end());
+    cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
+    p.per_launch = q == n_frames ? 0 : q;
+    for (int rr : cands) {
+      if (rr < kMinRunRows || rr > (int)p.h)
+        continue;
+      p.run_rows = rr;
+      float ms[3];
+      for (int it = 0; it < 4; it++) {
+        cudaEventRecord(a, s);
+        if ((rc = p.launch(d_images, n_frames, s)) != SF_OK)
+          break;
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        if (it)
+          cudaEventElapsedTime(&ms[it - 1], a, b);
+      }
+      if (rc != SF_OK)
         break;
-      cudaEventRecord(b, s);
-      cudaEventSynchronize(b);
-      if (it)
-        cudaEventElapsedTime(&ms[it - 1], a, b);
+      std::sort(ms, ms + 3);
+      if (ms[1] < best_ms) {
+        best_ms = ms[1];
+        best = rr;
+        best_per = p.per_launch;
+      }
     }
     if (rc != SF_OK)
       break;
-    std::sort(ms, ms + 3);
-    if (ms[1] < best_ms) {
-      best_ms = ms[1];
-      best = rr;
-    }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   p.run_rows = best;
+  p.per_launch = best_per;
   p.drop_graphs();
   p.warm = true;
   return rc;
 }
 
 int sf_plan_run_rows(const sf_plan *plan) { return plan ? plan->impl.run_rows : 0; }
+size_t sf_plan_frames_per_launch(const sf_plan *plan) {
+  return plan ? plan->impl.per_launch : 0;
+}
+
+int sf_plan_configure(sf_plan *plan, int run_rows, size_t frames_per_launch) {
+  using namespace sf;
+  if (!plan || run_rows < 0 || frames_per_launch > plan->impl.max_frames)
+    return SF_EBADARG;
+  Plan &p = plan->impl;
+  p.run_rows = run_rows;
+  p.per_launch = frames_per_launch;
+  p.drop_graphs();
+  return SF_OK;
+}
 size_t sf_plan_graphs(const sf_plan *plan) { return plan ? plan->impl.graphs.size() : 0; }
 sf_signal_pixel *sf_plan_lists(const sf_plan *plan) { return plan ? plan->impl.lists : nullptr; }
 uint32_t *sf_plan_counts(const sf_plan *plan) { return plan ? plan->impl.counts : nullptr; }

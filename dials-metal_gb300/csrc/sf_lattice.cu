@@ -224,7 +224,7 @@ constexpr size_t ring_bytes() {
 
 template <int kOcc, bool kRing, typename Pix>
 __global__ void __launch_bounds__(kLatWarps * 32, kOcc)
-lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int width, int vec,
+lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int env_h, int env_w, int vec,
             int nstrips, int nruns, int run_rows, const __grid_constant__ StreamTables T,
             const __grid_constant__ LaunchParams P, uint8_t *__restrict__ scr1_bytes,
             uint8_t *__restrict__ final_bytes, size_t mask_bytes) {
@@ -245,6 +245,11 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int height, int wi
   const int sx = gw % nstrips, t0 = gw / nstrips;
   const int ry = t0 % nruns, f = t0 / nruns;
   if (f >= nframes)
+    return;  // whole warp
+  // The strips and runs cover the batch's largest frame; a smaller frame of
+  // a mixed batch has nothing past its own last mask word and row.
+  const int height = F.h[f], width = F.w[f];
+  if (kLatOut * sx >= ((width + 31) >> 5) * 32 || ry * run_rows >= height)
     return;  // whole warp
   const Pix *image = reinterpret_cast<const Pix *>(F.image[f]);
   const int bytes_per_row = ((width + 31) >> 5) * 4;
@@ -567,11 +572,13 @@ __device__ __noinline__ bool lat_wide(const uint32_t *__restrict__ image, int he
 constexpr int kTileRun = 8;
 
 __global__ void __launch_bounds__(256)
-lat_tiles(int nframes, int height, int width, const uint32_t *__restrict__ final_all,
-          size_t words, uint32_t *__restrict__ list, uint32_t *__restrict__ counters,
-          FastDiv by_ngx, FastDiv by_fgroups, int run) {
+lat_tiles(const __grid_constant__ FramePtrs F, int nframes, int env_h, int env_w,
+          const uint32_t *__restrict__ final_all, size_t words, uint32_t *__restrict__ list,
+          uint32_t *__restrict__ counters, FastDiv by_ngx, FastDiv by_fgroups, int run) {
   const int lane = threadIdx.x & 31;
-  const int wpr = (width + 31) >> 5, ntx = ver_ntx(width), nty = ver_nty(height);
+  // Groups and tile numbers are laid out over the batch's largest frame; each
+  // frame's own shape bounds its tiles.
+  const int ntx = ver_ntx(env_w), nty = ver_nty(env_h);
   const int ngx = (ntx + 31) / 32;
   const uint32_t ntiles = (uint32_t)ntx * (uint32_t)nty;
   const uint32_t fgroups = (uint32_t)nty * (uint32_t)ngx;  // groups a frame
@@ -589,6 +596,8 @@ lat_tiles(int nframes, int height, int width, const uint32_t *__restrict__ final
       const uint32_t f = fast_div(g, by_fgroups), gf = g - f * fgroups;
       const uint32_t ty = fast_div(gf, by_ngx), gx = gf - ty * (uint32_t)ngx;
       const uint32_t *fin = final_all + (size_t)f * words;
+      const int height = F.h[f], width = F.w[f];
+      const int wpr = (width + 31) >> 5;
       const int wd = 28 * (int)gx + lane, r0 = (int)ty * kVerRows;
       uint32_t acc = 0;
       if (lane < 29 && wd < wpr) {
@@ -601,8 +610,8 @@ lat_tiles(int nframes, int height, int width, const uint32_t *__restrict__ final
       const uint32_t lo = __shfl_sync(0xffffffffu, acc, lw);
       const uint32_t hi = __shfl_sync(0xffffffffu, acc, lw + 1);
       const int tx = 32 * (int)gx + lane;
-      any = tx < ntx && ((uint32_t)(((unsigned long long)hi << 32 | lo) >> sh) &
-                         ((1u << kVerTW) - 1u)) != 0u;
+      any = tx < ver_ntx(width) && r0 < height &&
+            ((uint32_t)(((unsigned long long)hi << 32 | lo) >> sh) & ((1u << kVerTW) - 1u)) != 0u;
     }
     bal[i] = __ballot_sync(0xffffffffu, any);
     mine |= any ? 1u << i : 0u;
@@ -717,13 +726,14 @@ template <typename Pix> __device__ __forceinline__ int tile_xs(int c0) {
 
 template <typename Pix>
 __device__ __forceinline__ void ver_stage(VerWarp<Pix> &sm, int s, uint32_t e, const FramePtrs &F,
-                                          const TileMaps &M, int tma, int height, int width,
-                                          int vec, uint32_t ntiles, int ntx,
-                                          const FastDiv &by_ntiles, const FastDiv &by_ntx,
+                                          const TileMaps &M, int tma, int vec, uint32_t ntiles,
+                                          int ntx, const FastDiv &by_ntiles,
+                                          const FastDiv &by_ntx,
                                           const uint32_t *__restrict__ final_all,
                                           size_t words, int lane) {
   const TileAt a = tile_at(e, ntiles, ntx, by_ntiles, by_ntx);
   const int f = a.f, r0 = a.r0, c0 = a.c0;
+  const int height = F.h[f], width = F.w[f];
   const int xs = tile_xs<Pix>(c0);
   if (tma)
     tma_stage<Pix>(sm.pix[s], &sm.bar[s], M, f, r0, xs, lane);
@@ -762,7 +772,7 @@ __device__ __forceinline__ void ver_window(const VerWarp<Pix> &sm, int d, int co
 template <int kOcc, typename Pix>
 __global__ void __launch_bounds__(kVerWarps * 32, kOcc)
 lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps M, int tma,
-           int height, int width, int vec, const __grid_constant__ LaunchParams P,
+           int env_h, int env_w, int vec, const __grid_constant__ LaunchParams P,
            const __grid_constant__ StreamTables T, uint32_t *__restrict__ scr1_all,
            uint32_t *__restrict__ final_all, size_t words, const uint32_t *__restrict__ list,
            uint32_t *__restrict__ counters, FastDiv by_ntiles, FastDiv by_ntx,
@@ -785,9 +795,9 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
   }
   __syncthreads();
   uint32_t parity = 0;  // bit b: the phase the next wait on bar[b] waits for
-  const int wpr = (width + 31) >> 5;
-  const int ntx = ver_ntx(width);
-  const uint32_t ntiles = (uint32_t)ntx * (uint32_t)ver_nty(height);
+  // Tile numbers are laid out over the batch's largest frame.
+  const int ntx = ver_ntx(env_w);
+  const uint32_t ntiles = (uint32_t)ntx * (uint32_t)ver_nty(env_h);
   const uint32_t narrow2 = T.narrow_max + 2u;
   const uint32_t count = counters[kCtrTiles];
   const uint32_t nw = gridDim.x * kVerWarps;
@@ -797,16 +807,16 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
   uint32_t e = k < count ? list[k] : 0u;
   uint32_t e1 = k + nw < count ? list[k + nw] : 0u;
   if (k < count)
-    ver_stage<Pix>(sm, 0, e, F, M, tma, height, width, vec, ntiles, ntx, by_ntiles, by_ntx,
-                   final_all, words, lane);
+    ver_stage<Pix>(sm, 0, e, F, M, tma, vec, ntiles, ntx, by_ntiles, by_ntx, final_all, words,
+                   lane);
   cp_async_commit();
   uint32_t e2 = 0u;
   uint32_t inflight = k < count ? 1u : 0u;  // bit b: a TMA load into buffer b not waited for
   for (int s = 0; k < count; k += nw, s ^= 1, e = e1, e1 = e2) {
     e2 = k + 2 * nw < count ? list[k + 2 * nw] : 0u;
     if (k + nw < count) {
-      ver_stage<Pix>(sm, s ^ 1, e1, F, M, tma, height, width, vec, ntiles, ntx, by_ntiles,
-                     by_ntx, final_all, words, lane);
+      ver_stage<Pix>(sm, s ^ 1, e1, F, M, tma, vec, ntiles, ntx, by_ntiles, by_ntx, final_all,
+                     words, lane);
       inflight |= 2u >> s;
     }
     cp_async_commit();
@@ -814,6 +824,7 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
     __syncwarp();
     const TileAt a = tile_at(e, ntiles, ntx, by_ntiles, by_ntx);
     const int f = a.f, r0 = a.r0, c0 = a.c0;
+    const int height = F.h[f], width = F.w[f], wpr = (width + 31) >> 5;
     if (tma) {
       inflight &= ~(1u << s);
       if (!tma_landed<Pix>(sm.pix[s], &sm.bar[s], (parity >> s) & 1u, height, width, r0,
@@ -1017,15 +1028,16 @@ template <typename Pix> struct alignas(128) S2Warp {
 
 template <typename Pix>
 __device__ __forceinline__ void s2_stage(S2Warp<Pix> &sm, int s, uint32_t e, const FramePtrs &F,
-                                         const TileMaps &M, int tma, int height, int width,
-                                         int vec, uint32_t ntiles, int ntx,
-                                         const FastDiv &by_ntiles, const FastDiv &by_ntx,
+                                         const TileMaps &M, int tma, int vec, uint32_t ntiles,
+                                         int ntx, const FastDiv &by_ntiles,
+                                         const FastDiv &by_ntx,
                                          const uint32_t *__restrict__ scr1_all,
                                          const uint32_t *__restrict__ final_all,
                                          const uint32_t *__restrict__ prefix_all, size_t words,
                                          int lane) {
   const TileAt a = tile_at(e, ntiles, ntx, by_ntiles, by_ntx);
   const int f = a.f, r0 = a.r0, c0 = a.c0;
+  const int height = F.h[f], width = F.w[f];
   const int xs = tile_xs<Pix>(c0);
   if (tma)
     tma_stage<Pix>(sm.pix[s], &sm.bar[s], M, f, r0, xs, lane);
@@ -1060,7 +1072,7 @@ __device__ __forceinline__ void s2_stage(S2Warp<Pix> &sm, int s, uint32_t e, con
 template <int kOcc, typename Pix>
 __global__ void __launch_bounds__(kVerWarps * 32, kOcc)
 lat_stage2(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps M, int tma,
-           int height, int width, int vec, const __grid_constant__ LaunchParams P,
+           int env_h, int env_w, int vec, const __grid_constant__ LaunchParams P,
            const uint32_t *__restrict__ scr1_all, const uint32_t *__restrict__ final_all,
            const uint32_t *__restrict__ prefix_all, size_t words,
            const uint32_t *__restrict__ list, uint32_t *__restrict__ counters,
@@ -1084,8 +1096,9 @@ lat_stage2(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
   }
   __syncwarp();
   uint32_t parity = 0;  // bit b: the phase the next wait on bar[b] waits for
-  const int ntx = ver_ntx(width);
-  const uint32_t ntiles = (uint32_t)ntx * (uint32_t)ver_nty(height);
+  // Tile numbers are laid out over the batch's largest frame.
+  const int ntx = ver_ntx(env_w);
+  const uint32_t ntiles = (uint32_t)ntx * (uint32_t)ver_nty(env_h);
   // The exact check's tile list with the tiles left without a candidate
   // marked kNoTile; a warp takes every nw-th entry and stages the next one it
   // will check while it checks the current one.
@@ -1105,14 +1118,14 @@ lat_stage2(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
   uint32_t e = next_live(blockIdx.x * kVerWarps + (threadIdx.x >> 5), &k);
   uint32_t e1 = next_live(k + nw, &k1);
   if (k < count)
-    s2_stage<Pix>(sm, 0, e, F, M, tma, height, width, vec, ntiles, ntx, by_ntiles, by_ntx,
-                  scr1_all, final_all, prefix_all, words, lane);
+    s2_stage<Pix>(sm, 0, e, F, M, tma, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
+                  final_all, prefix_all, words, lane);
   cp_async_commit();
   uint32_t inflight = k < count ? 1u : 0u;  // bit b: a TMA load into buffer b not waited for
   for (int s = 0; k < count; s ^= 1) {
     if (k1 < count) {
-      s2_stage<Pix>(sm, s ^ 1, e1, F, M, tma, height, width, vec, ntiles, ntx, by_ntiles,
-                    by_ntx, scr1_all, final_all, prefix_all, words, lane);
+      s2_stage<Pix>(sm, s ^ 1, e1, F, M, tma, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
+                    final_all, prefix_all, words, lane);
       inflight |= 2u >> s;
     }
     cp_async_commit();
@@ -1120,6 +1133,7 @@ lat_stage2(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
     __syncwarp();
     const TileAt a = tile_at(e, ntiles, ntx, by_ntiles, by_ntx);
     const int f = a.f, r0 = a.r0, c0 = a.c0;
+    const int height = F.h[f], width = F.w[f];
     const int xs = tile_xs<Pix>(c0), off = (c0 - 5) - xs;
     if (tma) {
       inflight &= ~(1u << s);
@@ -1308,8 +1322,8 @@ template <typename Pix> int make_tile_maps(const FramePtrs &F, int nframes, int 
                                            TileMaps *M) {
   std::memset(M, 0, sizeof(*M));
   for (int f = 0; f < nframes; f++)
-    if (!encode_frame_map(&M->map[f], F.image[f], h, w, (int)sizeof(Pix), VerPix<Pix>::kPW,
-                          kVerPR))
+    if (!encode_frame_map(&M->map[f], F.image[f], F.h[f], F.w[f], (int)sizeof(Pix),
+                          VerPix<Pix>::kPW, kVerPR))
       return 0;
   return 1;
 }
@@ -1378,7 +1392,7 @@ cudaError_t lattice(const FramePtrs &F, int nframes, int h, int w, int vec, cons
   const FastDiv by_fgroups = make_fastdiv((uint32_t)tgroups);
   const FastDiv by_ntiles = make_fastdiv((uint32_t)tiles);
   const FastDiv by_ntx = make_fastdiv((uint32_t)ver_ntx(w));
-  lat_tiles<<<tb, 256, 0, stream>>>(nframes, h, w, b.bits, b.words, list, b.counters, by_ngx,
+  lat_tiles<<<tb, 256, 0, stream>>>(F, nframes, h, w, b.bits, b.words, list, b.counters, by_ngx,
                                     by_fgroups, trun);
   TileMaps M;
   const int tma = make_tile_maps<Pix>(F, nframes, h, w, &M);

@@ -59,10 +59,12 @@ double now_s() {
       .count();
 }
 
-// Each frame's list from a batch's outputs into its sweep's slot.
+// Each frame's list from a batch's outputs into its sweep's slot (which
+// holds dst_cap[j] records: the sweep's own capacity, at most the batch's).
 struct CopyArgs {
   sf_signal_pixel *dst[SF_MAX_BATCH];
   uint32_t *dst_count[SF_MAX_BATCH];
+  size_t dst_cap[SF_MAX_BATCH];
 };
 
 __global__ void k_copy_lists(const sf_signal_pixel *__restrict__ src,
@@ -70,7 +72,8 @@ __global__ void k_copy_lists(const sf_signal_pixel *__restrict__ src,
                              const __grid_constant__ CopyArgs a) {
   const int j = blockIdx.y;
   const uint32_t c = counts[j];
-  const size_t n = c < capacity ? c : capacity;
+  const size_t cap = capacity < a.dst_cap[j] ? capacity : a.dst_cap[j];
+  const size_t n = c < cap ? c : cap;
   const uint4 *s = reinterpret_cast<const uint4 *>(src + (size_t)j * capacity);
   uint4 *d = reinterpret_cast<uint4 *>(a.dst[j]);
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -107,7 +110,9 @@ struct LabelTask {
   std::shared_ptr<Event> ready;
 };
 
-// Frames of one shape and parameter set share launches and outputs.
+// Sweeps of one parameter set whose frames fit in the group's shape (the
+// shape of the sweep that made it) share launches and outputs: a launch may
+// mix detector sizes, laid out for the group's shape.
 struct SrvGroup {
   size_t h = 0, w = 0, capacity = 0;
   sf_threshold_params params{};
@@ -128,6 +133,7 @@ struct SrvGroup {
 struct SrvSweep {
   int64_t id = 0;
   SrvGroup *group = nullptr;
+  size_t h = 0, w = 0, capacity = 0;    // its frames' shape, its lists' capacity
   sf_labeller *lab = nullptr;
   size_t bytes = 0, ring = 0;
   size_t result_bytes = 0;              // its labeller's spot and pixel stores, granted
@@ -315,7 +321,7 @@ cudaError_t sf_server::upload_chunk(SrvSweep &s, const SrvFrame &f, int ci) {
 
 void sf_server::label_loop(SrvSweep *s) {
   cudaSetDevice(device);
-  const size_t cap = s->group->capacity;
+  const size_t cap = s->capacity;
   while (true) {
     LabelTask t;
     {
@@ -449,7 +455,7 @@ void sf_server::run() {
           s.head = (s.head + 1) % (int)s.ring;
           s.nfree--;
           f.up = std::make_shared<Event>();
-          const size_t bytes = s.group->h * s.group->w * sizeof(uint32_t);
+          const size_t bytes = s.h * s.w * sizeof(uint32_t);
           const int ci = next_copy;
           const cudaStream_t cs = copy_s[ci];
           next_copy = (next_copy + 1) % kCopyStreams;
@@ -488,22 +494,26 @@ void sf_server::run() {
     // 3. Threshold the batch, then each list into its sweep's slot.
     const double t_launch = now_s();
     std::vector<const uint32_t *> images;
+    std::vector<size_t> heights, widths;
     CopyArgs ca;
     {
       std::lock_guard<std::mutex> lock(m);
       for (size_t j = 0; j < batch.size(); j++) {
         SrvSweep &s = *sweeps[batch[j].sweep];
         images.push_back(s.slots[batch[j].slot]);
-        ca.dst[j] = s.lists + (size_t)batch[j].slot * g->capacity;
+        heights.push_back(s.h);
+        widths.push_back(s.w);
+        ca.dst[j] = s.lists + (size_t)batch[j].slot * s.capacity;
         ca.dst_count[j] = s.counts + batch[j].slot;
+        ca.dst_cap[j] = s.capacity;
       }
     }
     for (SrvFrame &f : batch)
       cudaStreamWaitEvent(comp_s, f.up->e, 0);
-    const int rc = sf_threshold_u32_batch_device(images.data(), images.size(), g->h, g->w,
-                                                 &g->params, g->out, g->capacity, g->bits,
-                                                 g->counts, nullptr, g->ws, g->ws_bytes,
-                                                 comp_s);
+    // One launch sequence for the batch, whatever detector sizes it mixes.
+    const int rc = sf_threshold_u32_mixed_batch_device(
+        images.data(), heights.data(), widths.data(), images.size(), &g->params, g->out,
+        g->capacity, g->bits, g->counts, nullptr, g->ws, g->ws_bytes, comp_s);
     if (rc == SF_OK)
       k_copy_lists<<<dim3(8, (unsigned)batch.size()), 256, 0, comp_s>>>(g->out, g->counts,
                                                                        g->capacity, ca);
@@ -630,7 +640,7 @@ int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,
   std::unique_lock<std::mutex> lock(sv->m);
   SrvGroup *g = nullptr;
   for (auto &gr : sv->groups)
-    if (gr->h == height && gr->w == width && same_params(gr->params, p))
+    if (!g && height <= gr->h && width <= gr->w && same_params(gr->params, p))
       g = gr.get();
   const size_t need = sf_server_sweep_bytes(sv, height, width, label);
   const size_t gb = g ? 0 : group_bytes(height, width, capacity, sv->opt.max_batch);
@@ -658,6 +668,9 @@ int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,
       return SF_ECUDA;
   }
   std::unique_ptr<SrvSweep> s(new SrvSweep);
+  s->h = height;
+  s->w = width;
+  s->capacity = capacity;
   s->bytes = need;
   s->ring = sv->opt.ring;
   s->nfree = s->ring;
@@ -750,8 +763,8 @@ int sf_server_submit_chunk(sf_server *sv, int64_t sweep, int64_t frame, const ui
     auto it = sv->sweeps.find(sweep);
     if (it == sv->sweeps.end())
       return SF_EBADARG;
-    h = it->second->group->h;
-    w = it->second->group->w;
+    h = it->second->h;
+    w = it->second->w;
   }
   // The chunk's header and framing, checked before the frame is taken
   // (decompress.cc:77-134), off the lock.

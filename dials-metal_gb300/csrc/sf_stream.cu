@@ -676,11 +676,12 @@ __device__ __forceinline__ void load_res(const uint2 *__restrict__ res, size_t i
 
 // Popcounts of the block's share of a frame's mask words.
 __global__ void __launch_bounds__(kScanT)
-mask_sums(const uint32_t *__restrict__ bits_all, size_t words, uint32_t *__restrict__ block_sums) {
+mask_sums(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ bits_all, size_t words,
+          uint32_t *__restrict__ block_sums) {
   const uint32_t *bits = bits_all + (size_t)blockIdx.y * words;
   const bool vec = reinterpret_cast<uintptr_t>(bits) % 16 == 0;
   size_t lo, hi;
-  chunk_of(words, &lo, &hi);
+  chunk_of(frame_words(F, blockIdx.y), &lo, &hi);
   uint32_t acc = 0;
   for (size_t base = lo; base < hi; base += kScanChunk) {
     uint32_t w[kScanPer];
@@ -875,10 +876,9 @@ seg_stage2(const __grid_constant__ FramePtrs F, int height, int width, int vec,
 // ascending pixel order (src/spots/dext.cc:212-220 emits in scan order).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kScanT)
-pass_sums(const uint2 *__restrict__ res_all, uint32_t cand_cap,
+pass_sums(const __grid_constant__ FramePtrs F, const uint2 *__restrict__ res_all, uint32_t cand_cap,
           const uint32_t *__restrict__ counters, uint32_t *__restrict__ block_sums,
-          const uint32_t *__restrict__ cand_all, uint32_t *__restrict__ final_all, size_t words,
-          int width) {
+          const uint32_t *__restrict__ cand_all, uint32_t *__restrict__ final_all, size_t words) {
   const int f = blockIdx.y;
   if (counters[kCtrFault]) {  // the stage-2 results are void: touch nothing
     if (threadIdx.x == 0)
@@ -891,6 +891,7 @@ pass_sums(const uint2 *__restrict__ res_all, uint32_t cand_cap,
   // here (their stage 2 left it alone).
   const uint32_t *cand = cand_all + (size_t)f * cand_cap;
   uint32_t *fin = final_all ? final_all + (size_t)f * words : nullptr;
+  const int width = F.w[f];
   const uint32_t wpr = ((uint32_t)width + 31u) >> 5;
   const bool vec = reinterpret_cast<uintptr_t>(res) % 16 == 0;
   size_t lo, hi;
@@ -985,9 +986,9 @@ pass_scatter(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ c
 
 // Optional: per final-mask word, the list position of its first pixel.
 __global__ void __launch_bounds__(kScanT)
-mask_prefix(const uint32_t *__restrict__ bits_all, size_t words,
-            const uint32_t *__restrict__ block_sums, uint32_t *__restrict__ prefix_all,
-            uint32_t *__restrict__ counters) {
+mask_prefix(const __grid_constant__ FramePtrs F, const uint32_t *__restrict__ bits_all,
+            size_t words, const uint32_t *__restrict__ block_sums,
+            uint32_t *__restrict__ prefix_all, uint32_t *__restrict__ counters) {
   const int f = blockIdx.y;
   const uint32_t *bits = bits_all + (size_t)f * words;
   uint32_t *prefix = prefix_all + (size_t)f * words;
@@ -998,7 +999,7 @@ mask_prefix(const uint32_t *__restrict__ bits_all, size_t words,
   const bool vec = reinterpret_cast<uintptr_t>(bits) % 16 == 0 &&
                    reinterpret_cast<uintptr_t>(prefix) % 16 == 0;
   size_t lo, hi;
-  chunk_of(words, &lo, &hi);
+  chunk_of(frame_words(F, f), &lo, &hi);
   for (size_t base = lo; base < hi; base += kScanChunk) {
     const size_t i0 = base + (size_t)threadIdx.x * kScanPer;
     uint32_t c[kScanPer], tot = 0;
@@ -1132,9 +1133,9 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
     return config_error;
   StreamTables T;
   make_stream_tables(P, &T);
-  int vec = w % 4 == 0 ? 1 : 0;
+  int vec = 1;
   for (int f = 0; f < nframes; f++)
-    if (reinterpret_cast<uintptr_t>(F.image[f]) % 16 != 0)
+    if (F.w[f] % 4 != 0 || reinterpret_cast<uintptr_t>(F.image[f]) % 16 != 0)
       vec = 0;
   const int sms = device_sms();
   if (K == 3) {
@@ -1160,10 +1161,10 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
   if (marks)
     cudaEventRecord(marks->stage01, stream);
   const dim3 og((unsigned)order_bpf(nframes, b.words), (unsigned)nframes);
-  mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
+  mask_sums<<<og, kScanT, 0, stream>>>(F, b.bits, b.words, b.block_sums);
   if (K == 3) {
     // Stage 2 on the exact check's tiles, into the list positions.
-    mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.amb, b.counters);
+    mask_prefix<<<og, kScanT, 0, stream>>>(F, b.bits, b.words, b.block_sums, b.amb, b.counters);
     const cudaError_t e = launch_lattice_stage2(F, nframes, h, w, vec, 4, P, b, stream);
     if (e != cudaSuccess)
       return e;
@@ -1177,14 +1178,14 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
   }
   if (marks)
     cudaEventRecord(marks->stage2, stream);
-  pass_sums<<<og, kScanT, 0, stream>>>(b.res, b.cand_cap, b.counters, b.block_sums, b.cand,
-                                       K == 3 ? b.bits : nullptr, b.words, w);
+  pass_sums<<<og, kScanT, 0, stream>>>(F, b.res, b.cand_cap, b.counters, b.block_sums, b.cand,
+                                       K == 3 ? b.bits : nullptr, b.words);
   pass_scatter<uint32_t><<<og, kScanT, 0, stream>>>(F, b.cand, b.cand_cap, b.res, b.counters,
                                                     b.block_sums, b.out, b.out_stride, b.capacity,
                                                     b.count_out);
   if (b.prefix) {
-    mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
-    mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.prefix, nullptr);
+    mask_sums<<<og, kScanT, 0, stream>>>(F, b.bits, b.words, b.block_sums);
+    mask_prefix<<<og, kScanT, 0, stream>>>(F, b.bits, b.words, b.block_sums, b.prefix, nullptr);
   }
   if (marks)
     cudaEventRecord(marks->order, stream);
@@ -1194,9 +1195,11 @@ static cudaError_t launch_stream_k(const FramePtrs &F, int nframes, int h, int w
 cudaError_t launch_stream16(const FramePtrs &F, int nframes, int h, int w, const LaunchParams &P,
                             const StreamBuffers &b, int run_rows, cudaStream_t stream,
                             const StreamMarks *marks) {
-  if (nframes < 1 || nframes > kMaxBatch || P.half != 3 ||
-      P.algorithm != SF_DISPERSION_EXTENDED || w % 4 != 0)
+  if (nframes < 1 || nframes > kMaxBatch || P.half != 3 || P.algorithm != SF_DISPERSION_EXTENDED)
     return cudaErrorInvalidValue;
+  for (int f = 0; f < nframes; f++)
+    if (F.w[f] % 4 != 0)
+      return cudaErrorInvalidValue;
   if (marks)
     cudaEventRecord(marks->start, stream);
   cudaError_t e =
@@ -1210,20 +1213,20 @@ cudaError_t launch_stream16(const FramePtrs &F, int nframes, int h, int w, const
   if (marks)
     cudaEventRecord(marks->stage01, stream);
   const dim3 og((unsigned)order_bpf(nframes, b.words), (unsigned)nframes);
-  mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
-  mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.amb, b.counters);
+  mask_sums<<<og, kScanT, 0, stream>>>(F, b.bits, b.words, b.block_sums);
+  mask_prefix<<<og, kScanT, 0, stream>>>(F, b.bits, b.words, b.block_sums, b.amb, b.counters);
   if ((e = launch_lattice_stage2(F, nframes, h, w, 1, 2, P, b, stream)) != cudaSuccess)
     return e;
   if (marks)
     cudaEventRecord(marks->stage2, stream);
-  pass_sums<<<og, kScanT, 0, stream>>>(b.res, b.cand_cap, b.counters, b.block_sums, b.cand,
-                                       b.bits, b.words, w);
+  pass_sums<<<og, kScanT, 0, stream>>>(F, b.res, b.cand_cap, b.counters, b.block_sums, b.cand,
+                                       b.bits, b.words);
   pass_scatter<uint16_t><<<og, kScanT, 0, stream>>>(F, b.cand, b.cand_cap, b.res, b.counters,
                                                     b.block_sums, b.out, b.out_stride, b.capacity,
                                                     b.count_out);
   if (b.prefix) {
-    mask_sums<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums);
-    mask_prefix<<<og, kScanT, 0, stream>>>(b.bits, b.words, b.block_sums, b.prefix, nullptr);
+    mask_sums<<<og, kScanT, 0, stream>>>(F, b.bits, b.words, b.block_sums);
+    mask_prefix<<<og, kScanT, 0, stream>>>(F, b.bits, b.words, b.block_sums, b.prefix, nullptr);
   }
   if (marks)
     cudaEventRecord(marks->order, stream);

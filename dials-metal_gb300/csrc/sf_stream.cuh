@@ -32,9 +32,19 @@ int device_sms();
 // Frames one launch sequence takes.
 constexpr int kMaxBatch = 64;
 
+// A launch's frames and each one's shape. Frames of one launch may differ
+// in shape on the kernel-3,3 lattice path (launch_stream, launch_stream16:
+// every buffer is laid out for the largest, h x w, and each frame uses its
+// own rows of it); the other paths take frames of one shape.
 struct FramePtrs {
   const uint32_t *image[kMaxBatch];
+  int h[kMaxBatch], w[kMaxBatch];
 };
+
+// Mask words of frame f (its own rows of ceil(w / 32) words).
+__host__ __device__ inline size_t frame_words(const FramePtrs &F, int f) {
+  return (size_t)((F.w[f] + 31) >> 5) * (size_t)F.h[f];
+}
 
 // Counter words: the batch's own first, then kCtrCount per frame.
 enum {

@@ -114,12 +114,25 @@ def lib() -> ctypes.CDLL:
             getattr(L, name).argtypes = [vp, sz, sz, sz, ctypes.POINTER(ThresholdParams), vp,
                                          sz, u32p, u32p, u32p, vp, sz, vp]
             getattr(L, name).restype = ctypes.c_int
+        szp = ctypes.POINTER(sz)
+        L.sf_mixed_batch_workspace_bytes.argtypes = [sz, szp, szp, sz]
+        L.sf_mixed_batch_workspace_bytes.restype = sz
+        L.sf_mixed_batch_mask_words.argtypes = [sz, szp, szp]
+        L.sf_mixed_batch_mask_words.restype = sz
+        L.sf_threshold_u32_mixed_batch_device.argtypes = [vp, szp, szp, sz,
+                                                          ctypes.POINTER(ThresholdParams), vp,
+                                                          sz, u32p, u32p, u32p, vp, sz, vp]
+        L.sf_threshold_u32_mixed_batch_device.restype = ctypes.c_int
         L.sf_plan_create.argtypes = [sz, sz, sz, sz, ctypes.POINTER(ThresholdParams)]
         L.sf_plan_create.restype = vp
         L.sf_plan_destroy.argtypes = [vp]
         for name in ("sf_plan_run", "sf_plan_tune"):
             getattr(L, name).argtypes = [vp, vp, sz, vp]
             getattr(L, name).restype = ctypes.c_int
+        L.sf_plan_configure.argtypes = [vp, ctypes.c_int, sz]
+        L.sf_plan_configure.restype = ctypes.c_int
+        L.sf_plan_frames_per_launch.argtypes = [vp]
+        L.sf_plan_frames_per_launch.restype = sz
         L.sf_plan_run_rows.argtypes = [vp]
         L.sf_plan_run_rows.restype = ctypes.c_int
         L.sf_plan_graphs.argtypes = [vp]
@@ -421,6 +434,87 @@ class DeviceThreshold:
 MAX_BATCH = 64
 
 
+class MixedBatch:
+    """Batched device threshold of frames of different shapes
+    (sf_threshold_u32_mixed_batch_device): up to MAX_BATCH 32-bit frames in
+    HBM per call, each with its own shape, one launch sequence on the
+    reference's window; each frame's list, mask and count as a single-frame
+    call gives. Outputs are laid out for the batch's envelope."""
+
+    def __init__(self, shapes, capacity: int | None = None, params: Params | None = None,
+                 word_prefix: bool = False):
+        import torch
+        n = len(shapes)
+        if not 1 <= n <= MAX_BATCH:
+            raise ValueError(f"1 to {MAX_BATCH} frames per batch")
+        self.shapes = [(int(h), int(w)) for h, w in shapes]
+        self.n = n
+        self._hs = (ctypes.c_size_t * n)(*[h for h, _ in self.shapes])
+        self._ws = (ctypes.c_size_t * n)(*[w for _, w in self.shapes])
+        H = max(h for h, _ in self.shapes)
+        W = max(w for _, w in self.shapes)
+        self.capacity = capacity if capacity is not None else max(1, H * W // 4)
+        self.params = (params or Params()).c()
+        L = lib()
+        self.slot = L.sf_mixed_batch_mask_words(n, self._hs, self._ws)
+        nbytes = L.sf_mixed_batch_workspace_bytes(n, self._hs, self._ws, self.capacity)
+        if nbytes == 0 or self.slot == 0:
+            raise ValueError("frame shapes or batch size rejected")
+        dev = torch.device("cuda")
+        self.out = torch.empty((n, self.capacity * 16), dtype=torch.uint8, device=dev)
+        self.bits = torch.empty((n, self.slot), dtype=torch.int32, device=dev)
+        self.counts = torch.zeros(n, dtype=torch.int32, device=dev)
+        self.word_prefix = (torch.empty((n, self.slot), dtype=torch.int32, device=dev)
+                            if word_prefix else None)
+        self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        self._ptrs = (ctypes.c_void_p * MAX_BATCH)()
+
+    def __call__(self, frames, stream=None) -> None:
+        """frames: contiguous 32-bit CUDA tensors, frame j of shapes[j]."""
+        import torch
+        frames = list(frames)
+        if len(frames) != self.n:
+            raise ValueError(f"{self.n} frames")
+        for j, f in enumerate(frames):
+            if f.device.type != "cuda" or not f.is_contiguous() or \
+                    f.dtype not in (torch.int32, torch.uint32):
+                raise ValueError("contiguous 32-bit CUDA tensors")
+            if tuple(f.shape) != self.shapes[j]:
+                raise ValueError(f"frame {j} is not {self.shapes[j]}")
+            self._ptrs[j] = f.data_ptr()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        rc = lib().sf_threshold_u32_mixed_batch_device(
+            ctypes.cast(self._ptrs, ctypes.c_void_p), self._hs, self._ws, self.n,
+            ctypes.byref(self.params), self.out.data_ptr(), self.capacity,
+            self.bits.data_ptr(), self.counts.data_ptr(),
+            self.word_prefix.data_ptr() if self.word_prefix is not None else None,
+            self.workspace.data_ptr(), self.workspace.numel(), s.cuda_stream)
+        _check(rc, "mixed-shape batched device threshold")
+
+    def count(self, j: int) -> int:
+        import torch
+        torch.cuda.current_stream().synchronize()
+        return int(self.counts[j].item()) & 0xffffffff
+
+    def result(self, j: int) -> np.ndarray:
+        n = self.count(j)
+        if n > self.capacity:
+            raise OverflowError_(f"{n} signal pixels, capacity {self.capacity}")
+        return self.out[j, : n * 16].cpu().numpy().view(SIGNAL_DTYPE).copy()
+
+    def words(self, j: int, which=None) -> np.ndarray:
+        """Frame j's mask words (or word positions), its own rows."""
+        h, w = self.shapes[j]
+        src = self.bits if which is None else which
+        return src[j, : (w + 31) // 32 * h].cpu().numpy().view(np.uint32)
+
+    def mask(self, j: int) -> np.ndarray:
+        h, w = self.shapes[j]
+        words = self.words(j).reshape(h, (w + 31) // 32)
+        bits = np.unpackbits(words.view(np.uint8).reshape(h, -1), axis=1, bitorder="little")
+        return bits[:, :w].astype(bool)
+
+
 class DeviceBatch:
     """Batched device threshold (sf_threshold_*_batch_device): up to
     MAX_BATCH same-shaped frames already in HBM per call, one launch
@@ -549,6 +643,14 @@ class Plan:
         _check(lib().sf_plan_tune(self._p, ctypes.cast(self._ptrs, ctypes.c_void_p), n,
                                   s.cuda_stream), "plan tune")
         return lib().sf_plan_run_rows(self._p)
+
+    def configure(self, run_rows: int = 0, frames_per_launch: int = 0) -> None:
+        _check(lib().sf_plan_configure(self._p, run_rows, frames_per_launch), "plan configure")
+
+    @property
+    def frames_per_launch(self) -> int:
+        """The tuned frames per launch sequence (0: all of a call's)."""
+        return int(lib().sf_plan_frames_per_launch(self._p))
 
     @property
     def graphs(self) -> int:

@@ -240,14 +240,40 @@ int sf_threshold_u16_batch_device(const uint16_t *const *d_images, size_t n_fram
                                   size_t workspace_bytes, void *stream);
 
 /*
+ * Batches of frames of different shapes (detectors of different sizes; no
+ * reference counterpart: the reference thresholds one frame a call,
+ * src/spots/dext_cuda.cu:711-869). Frame j is heights[j] x widths[j]; every
+ * output is laid out for the batch's envelope H x W (the largest height and
+ * the largest width): frame j's list at d_out + j * capacity, its count at
+ * d_counts[j], its mask at d_bits + j * sf_mixed_batch_mask_words(...) (=
+ * ceil(W/32) * H words) in its own rows of ceil(widths[j]/32) words, the
+ * optional word positions likewise. For 32-bit frames with the reference's
+ * window (kernel 3,3, dispersion_extended, gain 1, integral sigmas) the
+ * whole batch is one launch sequence; other settings run frames of another
+ * shape one launch sequence each. The workspace is
+ * sf_mixed_batch_workspace_bytes (the batch workspace of the envelope).
+ */
+size_t sf_mixed_batch_workspace_bytes(size_t n_frames, const size_t *heights,
+                                      const size_t *widths, size_t capacity);
+size_t sf_mixed_batch_mask_words(size_t n_frames, const size_t *heights, const size_t *widths);
+int sf_threshold_u32_mixed_batch_device(const uint32_t *const *d_images, const size_t *heights,
+                                        const size_t *widths, size_t n_frames,
+                                        const sf_threshold_params *params,
+                                        sf_signal_pixel *d_out, size_t capacity,
+                                        uint32_t *d_bits, uint32_t *d_counts,
+                                        uint32_t *d_word_prefix, void *d_workspace,
+                                        size_t workspace_bytes, void *stream);
+
+/*
  * Batch plans (no reference counterpart): one frame shape with its device
  * outputs and workspace. sf_plan_run enqueues the batched threshold of
  * n_frames <= max_frames device frames (as sf_threshold_u32_batch_device);
  * after the first run the launch sequence is captured as a CUDA graph and
  * replayed whenever the same frame pointers come again (up to 16 pointer
- * sets are kept). sf_plan_tune times the strip run lengths on the given
- * frames and keeps the fastest; the results are the same for any run
- * length. Outputs (device pointers, valid until sf_plan_destroy): frame j's
+ * sets are kept). sf_plan_tune times, on the given frames, the frames a
+ * launch sequence takes (all, 32 or 16; sf_plan_frames_per_launch, 0 for
+ * all) and the strip run lengths (sf_plan_run_rows), and keeps the fastest
+ * pair; the results are the same for any of them. Outputs (device pointers, valid until sf_plan_destroy): frame j's
  * list at sf_plan_lists(p) + j * capacity, its count at sf_plan_counts(p)[j],
  * its mask at sf_plan_masks(p) + j * ceil(width/32) * height. NULL on failure
  * (the reason in sf_last_error()).
@@ -259,6 +285,11 @@ void sf_plan_destroy(sf_plan *plan);
 int sf_plan_run(sf_plan *plan, const uint32_t *const *d_images, size_t n_frames, void *stream);
 int sf_plan_tune(sf_plan *plan, const uint32_t *const *d_images, size_t n_frames, void *stream);
 int sf_plan_run_rows(const sf_plan *plan);
+size_t sf_plan_frames_per_launch(const sf_plan *plan);
+/* Sets what sf_plan_tune would choose (a run length, 0 for the default
+ * geometry; frames a launch sequence, 0 for all), e.g. from an earlier
+ * tuning of the same detector; drops the plan's graphs. */
+int sf_plan_configure(sf_plan *plan, int run_rows, size_t frames_per_launch);
 size_t sf_plan_graphs(const sf_plan *plan);
 sf_signal_pixel *sf_plan_lists(const sf_plan *plan);
 uint32_t *sf_plan_counts(const sf_plan *plan);

@@ -143,3 +143,65 @@ def test_batch_near_threshold_windows(api, kernel):
         want, mask = O.dext(f, O.Params(**params), with_mask=True)
         _same(b.result(j), want, f"kernel {kernel} frame {j}")
         assert np.array_equal(b.mask(j), mask.astype(bool))
+
+
+def _run_mixed(api, frames, params=None, capacity=None):
+    import torch
+    b = api.MixedBatch([f.shape for f in frames], capacity=capacity, params=params,
+                       word_prefix=True)
+    b([torch.from_numpy(f.view(np.int32)).cuda() for f in frames])
+    torch.cuda.synchronize()
+    return b
+
+
+def _check_mixed(b, frames, params=None, what=""):
+    for j, f in enumerate(frames):
+        want, mask = O.dext(f, O.Params(**params) if params else None, with_mask=True)
+        _same(b.result(j), want, f"{what} frame {j} ({f.shape[0]}x{f.shape[1]})")
+        assert np.array_equal(b.mask(j), mask.astype(bool)), f"{what} mask of frame {j}"
+        wp = b.words(j, b.word_prefix)
+        counts = np.array([bin(int(x)).count("1") for x in b.words(j)])
+        assert np.array_equal(wp, np.concatenate([[0], np.cumsum(counts)[:-1]])), what
+
+
+# Frames of several detector shapes in one launch sequence (the lattice path
+# for the reference's window), each compared with the oracle alone: the
+# largest first, last and in the middle, frames narrower and shorter than the
+# envelope, a frame handed to the 64-bit path and a dense one among them.
+MIXED_SHAPES_ALIGNED = [(520, 712), (300, 480), (1030, 1064), (64, 96), (257, 700),
+                        (40, 300), (300, 1064)]
+MIXED_SHAPES_ODD = [(257, 701), (300, 480), (1030, 1065), (31, 33), (520, 700)]
+
+
+@pytest.mark.parametrize("shapes", [MIXED_SHAPES_ALIGNED, MIXED_SHAPES_ODD],
+                         ids=["aligned", "odd_widths"])
+def test_mixed_shapes_against_oracle(api, shapes):
+    frames = []
+    for k, (h, w) in enumerate(shapes):
+        frames += _mixed_frames(h, w, 4, seed=7 * k + h)[k % 4:k % 4 + 1]
+    b = _run_mixed(api, frames)
+    _check_mixed(b, frames, what="mixed")
+
+
+@pytest.mark.parametrize("params", [dict(kernel_x=2, kernel_y=2), dict(kernel_x=4, kernel_y=4),
+                                    dict(algorithm=1), dict(gain=1.5)])
+def test_mixed_shapes_other_settings(api, params):
+    # Settings off the lattice path: frames of another shape run one launch
+    # sequence each, into the same envelope layout.
+    frames = [_mixed_frames(h, w, 4, seed=h + w)[0]
+              for h, w in [(200, 333), (120, 512), (257, 96)]]
+    b = _run_mixed(api, frames, params=api.Params(**params))
+    _check_mixed(b, frames, params, what=str(params))
+
+
+def test_mixed_detector_sizes_full(api):
+    # The served workload's detectors in one launch: a 16M frame (EIGER2
+    # gaps), a 9M, a 4M and a 1M one, as their sweeps would batch.
+    from sfgb import synth
+    frames = []
+    for name, h, w in [("eiger_16m", 4362, 4148), ("eiger_16m", 3262, 3108),
+                       ("eiger_16m", 2162, 2068), ("plain_1m", 1030, 1064)]:
+        p = synth.preset(name, height=h, width=w, n_frames=2)
+        frames.append(synth.Sweep(p).frame(1))
+    b = _run_mixed(api, frames, capacity=frames[0].size // 4)
+    _check_mixed(b, frames, what="detectors")

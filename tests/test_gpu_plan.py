@@ -57,3 +57,27 @@ def test_plan_refuses_bad_shapes(api):
         api.Plan(0, 10, 4)
     with pytest.raises(api.SpotFinderError):
         api.Plan(10, 10, 65)
+
+
+@pytest.mark.parametrize("per_launch,run_rows", [(16, 0), (32, 48), (0, 96)])
+def test_plan_frames_per_launch(api, per_launch, run_rows):
+    # A 48-frame call split into launch sequences of per_launch frames (the
+    # tuner's other knob) gives every frame the oracle's list.
+    import torch
+    h, w = 160, 384
+    frames = _frames(h, w, 48, seed=5 + per_launch)
+    want = [O.dext(f) for f in frames]
+    dev = [torch.from_numpy(f.view(np.int32)).cuda() for f in frames]
+    plan = api.Plan(h, w, 48, capacity=h * w // 4)
+    plan.configure(run_rows, per_launch)
+    for rep in range(2):  # direct, then a captured graph
+        plan(dev)
+        for j in range(48):
+            assert plan.result(j).tobytes() == want[j].tobytes(), (rep, j)
+    assert plan.frames_per_launch == per_launch
+    plan.tune(dev)
+    assert plan.frames_per_launch in (0, 16, 32)
+    plan(dev)
+    for j in range(0, 48, 7):
+        assert plan.result(j).tobytes() == want[j].tobytes()
+    plan.close()
