@@ -263,24 +263,40 @@ __global__ void k_rows(LabelStatus *st, const BatchArgs *__restrict__ ap,
   }
 }
 
-// Appends this lane's edge (p, q), if `want`, to the batch's edge list (one
-// atomic a warp); a lane whose edge finds the list full joins it at once.
-__device__ __forceinline__ void push_edge(bool want, uint32_t p, uint32_t q, LabelStatus *st,
-                                          uint2 *edges, uint32_t edge_cap, uint32_t *parent) {
-  const unsigned m = __ballot_sync(0xffffffffu, want);
-  if (!m)
-    return;
+// Appends this lane's edges (p, q[k]) for the k with bit k of `want` set (at
+// most three: left, above, previous frame) to the batch's edge list, with
+// one atomic for the whole warp's edges; a lane whose edge finds the list
+// full joins it at once.
+__device__ __forceinline__ void push_edges(uint32_t want, uint32_t p, const uint32_t q[3],
+                                           LabelStatus *st, uint2 *edges, uint32_t edge_cap,
+                                           uint32_t *parent) {
   const int lane = threadIdx.x & 31;
+  const uint32_t mine = (uint32_t)__popc(want);
+  // The warp's inclusive prefix of edge counts.
+  uint32_t inc = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o)
+      inc += t;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+  if (total == 0)
+    return;
   uint32_t base = 0;
-  if (lane == __ffs(m) - 1)
-    base = atomicAdd(&st->n_edges, (uint32_t)__popc(m));
-  base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
-  if (want) {
-    const uint32_t at = base + __popc(m & ((1u << lane) - 1u));
-    if (at < edge_cap)
-      edges[at] = make_uint2(p, q);
-    else
-      uf_unite(parent, p, q, st);
+  if (lane == 31)
+    base = atomicAdd(&st->n_edges, total);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  uint32_t at = base + inc - mine;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    if ((want >> k) & 1u) {
+      if (at < edge_cap)
+        edges[at] = make_uint2(p, q[k]);
+      else
+        uf_unite(parent, p, q[k], st);
+      at++;
+    }
   }
 }
 
@@ -323,7 +339,8 @@ __global__ void k_link(LabelStatus *st, const BatchArgs *__restrict__ ap,
     const uint32_t idx = in ? index[p] : 0u;
     const uint32_t y = idx / width, x = idx - y * width;
     const bool left = in && p > start && x != 0 && index[p - 1] == idx - 1;
-    push_edge(left && ((p - start) & 31u) == 0, p, p - 1, st, edges, edge_cap, parent);
+    uint32_t want = left && ((p - start) & 31u) == 0 ? 1u : 0u;
+    uint32_t q[3] = {p - 1, 0u, 0u};
     {
       const uint32_t t = idx - width;
       uint32_t lo = 0, hi = 0;
@@ -331,9 +348,9 @@ __global__ void k_link(LabelStatus *st, const BatchArgs *__restrict__ ap,
         lo = own ? own[y - 1] : start;
         hi = own ? own[y] : p;
       }
-      const uint32_t q = lower_bound_warp(index, lo, hi, t);
-      push_edge(q < hi && index[q] == t && !(left && q > lo && index[q - 1] == t - 1), p, q,
-                st, edges, edge_cap, parent);
+      q[1] = lower_bound_warp(index, lo, hi, t);
+      if (q[1] < hi && index[q[1]] == t && !(left && q[1] > lo && index[q[1] - 1] == t - 1))
+        want |= 2u;
     }
     if (phi > plo) {  // uniform: the frame links back or not
       uint32_t lo = 0, hi = 0;
@@ -341,10 +358,12 @@ __global__ void k_link(LabelStatus *st, const BatchArgs *__restrict__ ap,
         lo = before ? before[y] : plo;
         hi = before ? before[y + 1] : phi;
       }
-      const uint32_t q = lower_bound_warp(index, lo, hi, idx);
-      push_edge(q < hi && index[q] == idx && !(left && q > lo && index[q - 1] == idx - 1), p,
-                q, st, edges, edge_cap, parent);
+      q[2] = lower_bound_warp(index, lo, hi, idx);
+      if (q[2] < hi && index[q[2]] == idx &&
+          !(left && q[2] > lo && index[q[2] - 1] == idx - 1))
+        want |= 4u;
     }
+    push_edges(want, p, q, st, edges, edge_cap, parent);
   }
 }
 
@@ -384,11 +403,22 @@ __global__ void k_comp_stats(LabelStatus *st, const uint32_t *__restrict__ root,
   if (st->error)
     return;
   const uint32_t n = st->n_total;
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n;
-       p += gridDim.x * blockDim.x) {
-    const uint32_t r = root[p];
-    atomicMax(&zlast[r], frame[p]);
-    atomicAdd(&csize[r], 1u);
+  const int lane = threadIdx.x & 31;
+  // Whole warps walk the pool (the loop bound is warp-uniform); the lanes of
+  // one component (consecutive pixels mostly share their root) add their
+  // count and latest frame with one atomic each.
+  for (uint32_t p0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); p0 < n;
+       p0 += gridDim.x * blockDim.x) {
+    const uint32_t p = p0 + lane;
+    const bool in = p < n;
+    const uint32_t r = in ? root[p] : kNone;
+    const int32_t z = in ? frame[p] : INT_MIN;
+    const unsigned same = __match_any_sync(0xffffffffu, r);
+    const int32_t zmax = __reduce_max_sync(same, z);
+    if (in && lane == __ffs(same) - 1) {
+      atomicMax(&zlast[r], zmax);
+      atomicAdd(&csize[r], (uint32_t)__popc(same));
+    }
   }
 }
 
@@ -601,13 +631,21 @@ __global__ void k_gather(LabelStatus *st, const uint32_t *__restrict__ root,
   if (st->error)
     return;
   const uint32_t n = st->n_total;
-  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n;
-       p += gridDim.x * blockDim.x) {
-    const uint32_t c = candid[root[p]];
-    if (c != kNone) {
-      const uint32_t slot = atomicAdd(&cursor[c], 1u);
-      members[cand_off[c] + slot] = p;
-    }
+  const int lane = threadIdx.x & 31;
+  // The lanes of one candidate take their member slots with one atomic (the
+  // members are sorted afterwards, so their order here does not matter).
+  for (uint32_t p0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); p0 < n;
+       p0 += gridDim.x * blockDim.x) {
+    const uint32_t p = p0 + lane;
+    const uint32_t c = p < n ? candid[root[p]] : kNone;
+    const unsigned same = __match_any_sync(0xffffffffu, c);
+    const int leader = __ffs(same) - 1;
+    uint32_t slot = 0;
+    if (c != kNone && lane == leader)
+      slot = atomicAdd(&cursor[c], (uint32_t)__popc(same));
+    slot = __shfl_sync(0xffffffffu, slot, leader);
+    if (c != kNone)
+      members[cand_off[c] + slot + __popc(same & ((1u << lane) - 1u))] = p;
   }
 }
 

@@ -95,6 +95,29 @@ __device__ __forceinline__ uint32_t fast_div(uint32_t n, const FastDiv &f) {
 
 static_assert(kLatN0 * kLatCap < (1u << kLatPS), "saturated sums stay below the count field");
 
+// Where each frame's share of a launch's warps (lat_stage01: strips x runs)
+// or tile groups (lat_tiles: tile rows x groups of 32 tiles) starts, and how
+// many make one of its rows: every frame of a batch, mixed shapes or not,
+// gets exactly its own.
+struct FrameSpans {
+  int start[kMaxBatch + 1];
+  FastDiv by_row[kMaxBatch];
+};
+
+// The frame whose span holds item g (start[f] <= g < start[f + 1]); g below
+// start[nframes].
+__device__ __forceinline__ int span_frame(const FrameSpans &S, int nframes, int g) {
+  int lo = 0, hi = nframes;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (S.start[mid] <= g)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
 // The 12 bound bits of a lane from the lattice bits b0-b4 at its columns
 // -1, 2, 5, 8 and 11 (b4 is the next lane's b0): column c keeps the lattice
 // columns within 2 of it.
@@ -224,8 +247,9 @@ constexpr size_t ring_bytes() {
 
 template <int kOcc, bool kRing, typename Pix>
 __global__ void __launch_bounds__(kLatWarps * 32, kOcc)
-lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int env_h, int env_w, int vec,
-            int nstrips, int nruns, int run_rows, const __grid_constant__ StreamTables T,
+lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
+            const __grid_constant__ FrameSpans S, int run_rows,
+            const __grid_constant__ StreamTables T,
             const __grid_constant__ LaunchParams P, uint8_t *__restrict__ scr1_bytes,
             uint8_t *__restrict__ final_bytes, size_t mask_bytes) {
   constexpr bool k16 = sizeof(Pix) == 2;
@@ -242,15 +266,14 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int env_h, int env
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gw = blockIdx.x * kLatWarps + warp;
-  const int sx = gw % nstrips, t0 = gw / nstrips;
-  const int ry = t0 % nruns, f = t0 / nruns;
-  if (f >= nframes)
+  if (gw >= S.start[nframes])
     return;  // whole warp
-  // The strips and runs cover the batch's largest frame; a smaller frame of
-  // a mixed batch has nothing past its own last mask word and row.
+  // This warp's frame, strip and run (each frame has its own strips x runs).
+  const int f = span_frame(S, nframes, gw);
+  const uint32_t local = (uint32_t)(gw - S.start[f]);
+  const int ry = (int)fast_div(local, S.by_row[f]);
+  const int sx = (int)(local - (uint32_t)ry * S.by_row[f].d);
   const int height = F.h[f], width = F.w[f];
-  if (kLatOut * sx >= ((width + 31) >> 5) * 32 || ry * run_rows >= height)
-    return;  // whole warp
   const Pix *image = reinterpret_cast<const Pix *>(F.image[f]);
   const int bytes_per_row = ((width + 31) >> 5) * 4;
   uint8_t *scr1 = scr1_bytes + (size_t)f * mask_bytes;
@@ -574,27 +597,29 @@ constexpr int kTileRun = 8;
 __global__ void __launch_bounds__(256)
 lat_tiles(const __grid_constant__ FramePtrs F, int nframes, int env_h, int env_w,
           const uint32_t *__restrict__ final_all, size_t words, uint32_t *__restrict__ list,
-          uint32_t *__restrict__ counters, FastDiv by_ngx, FastDiv by_fgroups, int run) {
+          uint32_t *__restrict__ counters, const __grid_constant__ FrameSpans S, int run) {
   const int lane = threadIdx.x & 31;
-  // Groups and tile numbers are laid out over the batch's largest frame; each
-  // frame's own shape bounds its tiles.
+  // Tile numbers are laid out over the batch's largest frame; each frame has
+  // its own tile groups (S) and its own shape bounds its tiles.
   const int ntx = ver_ntx(env_w), nty = ver_nty(env_h);
-  const int ngx = (ntx + 31) / 32;
   const uint32_t ntiles = (uint32_t)ntx * (uint32_t)nty;
-  const uint32_t fgroups = (uint32_t)nty * (uint32_t)ngx;  // groups a frame
-  const uint32_t total = fgroups * (uint32_t)nframes;
+  const uint32_t total = (uint32_t)S.start[nframes];
   const uint32_t g0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (uint32_t)run;
   if (g0 >= total)
     return;  // whole warp
   unsigned bal[kTileRun];
+  uint32_t first[kTileRun];  // the tile number of each group's first tile
   uint32_t mine = 0, n = 0;
 #pragma unroll
   for (int i = 0; i < kTileRun; i++) {
     const uint32_t g = g0 + i;
     bool any = false;
+    first[i] = 0;
     if (i < run && g < total) {  // warp-uniform
-      const uint32_t f = fast_div(g, by_fgroups), gf = g - f * fgroups;
-      const uint32_t ty = fast_div(gf, by_ngx), gx = gf - ty * (uint32_t)ngx;
+      const int f = span_frame(S, nframes, (int)g);
+      const uint32_t gf = g - (uint32_t)S.start[f];
+      const uint32_t ty = fast_div(gf, S.by_row[f]), gx = gf - ty * S.by_row[f].d;
+      first[i] = (uint32_t)f * ntiles + ty * (uint32_t)ntx + 32 * gx;
       const uint32_t *fin = final_all + (size_t)f * words;
       const int height = F.h[f], width = F.w[f];
       const int wpr = (width + 31) >> 5;
@@ -610,7 +635,7 @@ lat_tiles(const __grid_constant__ FramePtrs F, int nframes, int env_h, int env_w
       const uint32_t lo = __shfl_sync(0xffffffffu, acc, lw);
       const uint32_t hi = __shfl_sync(0xffffffffu, acc, lw + 1);
       const int tx = 32 * (int)gx + lane;
-      any = tx < ver_ntx(width) && r0 < height &&
+      any = tx < ver_ntx(width) &&
             ((uint32_t)(((unsigned long long)hi << 32 | lo) >> sh) & ((1u << kVerTW) - 1u)) != 0u;
     }
     bal[i] = __ballot_sync(0xffffffffu, any);
@@ -626,12 +651,8 @@ lat_tiles(const __grid_constant__ FramePtrs F, int nframes, int env_h, int env_w
   const unsigned below = (1u << lane) - 1u;
 #pragma unroll
   for (int i = 0; i < kTileRun; i++) {
-    if ((mine >> i) & 1u) {
-      const uint32_t g = g0 + i;
-      const uint32_t f = fast_div(g, by_fgroups), gf = g - f * fgroups;
-      const uint32_t ty = fast_div(gf, by_ngx), gx = gf - ty * (uint32_t)ngx;
-      list[base + __popc(bal[i] & below)] = f * ntiles + ty * (uint32_t)ntx + 32 * gx + lane;
-    }
+    if ((mine >> i) & 1u)
+      list[base + __popc(bal[i] & below)] = first[i] + lane;
     base += (uint32_t)__popc(bal[i]);
   }
 }
@@ -1353,20 +1374,31 @@ cudaError_t lattice_stage2(const FramePtrs &F, int nframes, int h, int w, int ve
   return cudaGetLastError();
 }
 
+// Strips of a frame w wide (whole mask rows: the last strip reaches the end
+// of the row's last word).
+int lat_strips(int w) { return ((w + 31) / 32 * 32 + kLatOut - 1) / kLatOut; }
+
 template <typename Pix>
 cudaError_t lattice(const FramePtrs &F, int nframes, int h, int w, int vec, const LaunchParams &P,
-                    const StreamTables &T, const StreamBuffers &b, const LatticeGeometry &g,
+                    const StreamTables &T, const StreamBuffers &b, int run_rows,
                     cudaStream_t stream) {
-  const long long warps = (long long)nframes * g.nstrips * g.nruns;
+  // Each frame's strips x runs of run_rows rows, frame after frame.
+  FrameSpans S;
+  S.start[0] = 0;
+  for (int f = 0; f < nframes; f++) {
+    const int strips = lat_strips(F.w[f]);
+    S.start[f + 1] = S.start[f] + strips * ((F.h[f] + run_rows - 1) / run_rows);
+    S.by_row[f] = make_fastdiv((uint32_t)strips);
+  }
   const size_t mask_bytes = b.words * sizeof(uint32_t);
-  const unsigned lb = (unsigned)((warps + kLatWarps - 1) / kLatWarps);
+  const unsigned lb = (unsigned)((S.start[nframes] + kLatWarps - 1) / kLatWarps);
   uint8_t *scr1 = reinterpret_cast<uint8_t *>(b.scr1), *fin = reinterpret_cast<uint8_t *>(b.bits);
   if (sizeof(Pix) == 2 || vec)
     lat_stage01<kLatOcc, true, Pix><<<lb, kLatWarps * 32, ring_bytes<Pix>(), stream>>>(
-        F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, T, P, scr1, fin, mask_bytes);
+        F, nframes, vec, S, run_rows, T, P, scr1, fin, mask_bytes);
   else
     lat_stage01<kLatOcc, false, uint32_t><<<lb, kLatWarps * 32, 0, stream>>>(
-        F, nframes, h, w, vec, g.nstrips, g.nruns, g.run_rows, T, P, scr1, fin, mask_bytes);
+        F, nframes, vec, S, run_rows, T, P, scr1, fin, mask_bytes);
   static std::once_flag configured;
   static cudaError_t config_error = cudaSuccess;
   static int ver_blocks = 0;
@@ -1379,21 +1411,27 @@ cudaError_t lattice(const FramePtrs &F, int nframes, int h, int w, int vec, cons
   // The ambiguous-mask buffer of the other streaming path holds, here, the
   // candidate mask's per-word list positions (stage 2), the tile list and the
   // list of tiles the exact check leaves a candidate in.
-  const long long tgroups = (long long)ver_nty(h) * ((ver_ntx(w) + 31) / 32);
+  // Tile groups: each frame's tile rows x groups of 32 tiles.
+  FrameSpans G;
+  G.start[0] = 0;
+  for (int f = 0; f < nframes; f++) {
+    const int ngx = (ver_ntx(F.w[f]) + 31) / 32;
+    G.start[f + 1] = G.start[f] + ver_nty(F.h[f]) * ngx;
+    G.by_row[f] = make_fastdiv((uint32_t)ngx);
+  }
+  const long long tgroups = G.start[nframes];
   // Runs of kTileRun groups a warp, shorter when that would leave fewer than
   // 8 warps an SM (one frame: runs of 2).
   const int trun = (int)std::max(1ll, std::min((long long)kTileRun,
-                                               tgroups * nframes / (8ll * device_sms())));
-  const long long twarps = (tgroups * nframes + trun - 1) / trun;
+                                               tgroups / (8ll * device_sms())));
+  const long long twarps = (tgroups + trun - 1) / trun;
   const unsigned tb = (unsigned)((twarps + 7) / 8);
   const size_t tiles = (size_t)ver_ntx(w) * (size_t)ver_nty(h);
   uint32_t *list = b.amb + (size_t)nframes * b.words;
-  const FastDiv by_ngx = make_fastdiv((uint32_t)((ver_ntx(w) + 31) / 32));
-  const FastDiv by_fgroups = make_fastdiv((uint32_t)tgroups);
   const FastDiv by_ntiles = make_fastdiv((uint32_t)tiles);
   const FastDiv by_ntx = make_fastdiv((uint32_t)ver_ntx(w));
-  lat_tiles<<<tb, 256, 0, stream>>>(F, nframes, h, w, b.bits, b.words, list, b.counters, by_ngx,
-                                    by_fgroups, trun);
+  lat_tiles<<<tb, 256, 0, stream>>>(F, nframes, h, w, b.bits, b.words, list, b.counters, G,
+                                    trun);
   TileMaps M;
   const int tma = make_tile_maps<Pix>(F, nframes, h, w, &M);
   lat_verify<kVerOcc, Pix><<<ver_blocks * device_sms(), kVerWarps * 32, ver_smem_bytes<Pix>(),
@@ -1445,18 +1483,23 @@ cudaError_t launch_lattice_stage2(const FramePtrs &F, int nframes, int h, int w,
                           : lattice_stage2<uint32_t>(F, nframes, h, w, vec, P, b, stream);
 }
 
-LatticeGeometry lattice_geometry(int h, int w, int nframes, int run_rows) {
-  LatticeGeometry g;
-  // Whole mask rows: the last strip reaches the end of the row's last word.
-  const int cols = (w + 31) / 32 * 32;
-  g.nstrips = (cols + kLatOut - 1) / kLatOut;
+// The run length for a launch whose tallest frame has h rows and whose
+// frames have `strips` strips in all: the resident warps filled once (no
+// tail wave) by the tallest frame's runs, unless run_rows is given; at least
+// kMinRunRows, in whole triples of rows.
+static int lat_run_rows(int h, long long strips, int run_rows) {
   if (run_rows <= 0) {
-    const long long per = (long long)nframes * g.nstrips;
-    const long long nruns = std::max(1ll, (long long)lat_slots() / per);
+    const long long nruns = std::max(1ll, (long long)lat_slots() / std::max(1ll, strips));
     run_rows = (int)((h + nruns - 1) / nruns);
   }
   run_rows = std::max(run_rows, kMinRunRows);
-  g.run_rows = (run_rows + 2) / 3 * 3;  // whole triples of rows
+  return (run_rows + 2) / 3 * 3;
+}
+
+LatticeGeometry lattice_geometry(int h, int w, int nframes, int run_rows) {
+  LatticeGeometry g;
+  g.nstrips = lat_strips(w);
+  g.run_rows = lat_run_rows(h, (long long)nframes * g.nstrips, run_rows);
   g.nruns = (h + g.run_rows - 1) / g.run_rows;
   return g;
 }
@@ -1466,9 +1509,12 @@ cudaError_t launch_lattice(const FramePtrs &F, int nframes, int h, int w, int ve
                            const StreamBuffers &b, int run_rows, cudaStream_t stream) {
   if (P.half != kLatK)
     return cudaErrorInvalidValue;
-  const LatticeGeometry g = lattice_geometry(h, w, nframes, run_rows);
-  return pixel_bytes == 2 ? lattice<uint16_t>(F, nframes, h, w, vec, P, T, b, g, stream)
-                          : lattice<uint32_t>(F, nframes, h, w, vec, P, T, b, g, stream);
+  long long strips = 0;
+  for (int f = 0; f < nframes; f++)
+    strips += lat_strips(F.w[f]);
+  const int rr = lat_run_rows(h, strips, run_rows);
+  return pixel_bytes == 2 ? lattice<uint16_t>(F, nframes, h, w, vec, P, T, b, rr, stream)
+                          : lattice<uint32_t>(F, nframes, h, w, vec, P, T, b, rr, stream);
 }
 
 } // namespace sf
