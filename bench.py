@@ -56,7 +56,7 @@ H, W = 4362, 4148
 # capture of this bench without cache flushes between kernels (11,235 MB for
 # the launch: lat_stage01 5,266 MB, lat_verify 2,098 MB, lat_stage2 2,621 MB,
 # the scans and the list 1,250 MB); the algorithmic bytes are 76.5 MB a frame.
-DRAM_BYTES_PER_FRAME = 175.6e6
+DRAM_BYTES_PER_FRAME = 169.1e6
 
 
 # Kernels a timed step launches: the threshold plan's graph (lat_stage01,
@@ -233,10 +233,12 @@ SERVED_DETECTORS = {
     "4M": ("batch_4m", 2162, 2068),
     "9M": ("batch_9m", 3262, 3108),
     "16M": ("eiger_16m", H, W),
+    "16M-dense": ("dense_16m", H, W),
 }
 
 
-def served(seconds: float = 4.0, seed: int = 4000, rates=None, chunks: bool = False) -> dict:
+def served(seconds: float = 4.0, seed: int = 4000, rates=None, chunks: bool = False,
+           kinds=None, label_capacity: int = 0, capacity_divisor: int = 16) -> dict:
     """The served form on the mixed-detector workload: six sweeps (16M, 16M,
     9M, 4M, 4M, 1M) arriving at once, each with Poisson frame arrivals at a
     rate drawn from 100-750 Hz, submitted as they arrive from pinned host
@@ -247,7 +249,7 @@ def served(seconds: float = 4.0, seed: int = 4000, rates=None, chunks: bool = Fa
     from sfgb import api, serve, synth
     L = api.lib()
     rng = np.random.default_rng(seed)
-    kinds = ["16M", "16M", "9M", "4M", "4M", "1M"]
+    kinds = kinds or ["16M", "16M", "9M", "4M", "4M", "1M"]
     pools, ptrs = {}, []
     for k in set(kinds):
         name, h, w = SERVED_DETECTORS[k]
@@ -262,7 +264,8 @@ def served(seconds: float = 4.0, seed: int = 4000, rates=None, chunks: bool = Fa
             pool.append((ptr, data.size))
             ptrs.append(ptr)
         pools[k] = pool
-    srv = serve.Server(max_batch=16, ring=32)
+    srv = serve.Server(max_batch=16, ring=32, label_capacity=label_capacity,
+                       capacity_divisor=capacity_divisor)
     drawn = rng.uniform(100.0, 750.0, size=len(kinds))
     rates = drawn if rates is None else np.asarray(rates, dtype=float)
     ids = [srv.open_sweep(SERVED_DETECTORS[k][1], SERVED_DETECTORS[k][2]) for k in kinds]
@@ -307,8 +310,12 @@ def served(seconds: float = 4.0, seed: int = 4000, rates=None, chunks: bool = Fa
     for t in feeders:
         t.join()
     spots = 0
+    failed = []
     for sid in ids:
-        srv.finish_sweep(sid, read=False)
+        try:
+            srv.finish_sweep(sid, read=False)
+        except api.SpotFinderError as e:  # reported in the line, not fatal to the run
+            failed.append(str(e))
         spots += srv.n_spots(sid)
     stop.set()
     col.join()
@@ -335,9 +342,10 @@ def served(seconds: float = 4.0, seed: int = 4000, rates=None, chunks: bool = Fa
             "frames": int(len(lat)), "frames_per_s": len(lat) / wall,
             "offered_frames_per_s": offered, "errors": bad, "spots": spots,
             "host_link_gbs_offered": link,
+            "failed_sweeps": failed,
             "server": stats,
             "by_detector": by,
-            "workload": "6 concurrent sweeps (16M, 16M, 9M, 4M, 4M, 1M), Poisson arrivals at "
+            "workload": f"{len(kinds)} concurrent sweeps ({', '.join(kinds)}), Poisson arrivals at "
                         + ", ".join(f"{r:.0f}" for r in rates) + f" Hz for {seconds:.0f} s, "
                         + ("as bitshuffle+LZ4 chunks (sf_server_submit_chunk), " if chunks else "")
                         + "threshold and 3-D labelling of every frame (sf_server_*)"}
@@ -487,6 +495,37 @@ def batched_legs(dev, steps: int = 5, warmup: int = 3) -> dict:
         out[name] = per
         del pool, views
 
+    # The dense-background stress frames (Poisson 20 plus rings, 20000 spots,
+    # 2% overloads at 10^6 counts, 500 hot pixels): 16 frames in HBM through
+    # a tuned plan, and their labelling on the device, 16 frames a call.
+    from sfgb import labeller
+    n = 16
+    sw = synth.Sweep(synth.preset("dense_16m", n_frames=n))
+    pool = torch.stack([torch.from_numpy(sw.frame(i).view(np.int32)) for i in range(n)]).to(dev)
+    views = [pool[j] for j in range(n)]
+    plan = api.Plan(H, W, n, capacity=H * W // 4)
+    with torch.cuda.stream(stream):
+        plan.tune(views, stream=stream)
+    ms = timed(lambda: plan(views, stream=stream), steps)
+    sig = int(np.mean([len(plan.result(j)) for j in range(0, n, 4)]))
+    lab = labeller.DeviceLabeller(H, W, live_capacity=32 << 20)
+    nb = [0]
+
+    def label():
+        nb[0] += 1
+        lab.add_device(list(range(nb[0], nb[0] + n)), plan.lists_ptr, plan.capacity,
+                       plan.counts_ptr, stream.cuda_stream)
+        nb[0] += n
+    ms_l = timed(label, steps)
+    algo = n * (H * W * 4 + (H * W + 7) // 8 + 16 * sig)
+    out["dense_16m"] = {"threshold_us_per_frame": ms * 1e3 / n,
+                        "threshold_frac_of_hbm": algo / (ms / 1e3) / 1e9 / peak,
+                        "labelling_us_per_frame": ms_l * 1e3 / n,
+                        "frames_per_s": n / ((ms + ms_l) / 1e3),
+                        "signal_pixels_per_frame": sig,
+                        "spots": int(lab.finish().spots.size)}
+    del lab, plan, pool, views
+
     # Mixed detector sizes in one launch sequence.
     shapes = [("eiger_16m", H, W), ("batch_9m", 3262, 3108), ("batch_4m", 2162, 2068),
               ("plain_1m", 1065, 1030)]
@@ -515,6 +554,11 @@ def batched_legs(dev, steps: int = 5, warmup: int = 3) -> dict:
     return out
 
 
+def plan_run_rows(plan) -> int:
+    from sfgb import api
+    return int(api.lib().sf_plan_run_rows(plan._p))
+
+
 def run_ours(args):
     import torch
     from sfgb import api
@@ -538,7 +582,9 @@ def run_ours(args):
     # replayed as a CUDA graph (the same frame buffers every step).
     plan = api.Plan(H, W, B)
     with torch.cuda.stream(stream):
-        run_rows = plan.tune(views, stream=stream)
+        # --no-tune keeps the default geometry (a short, fixed launch count
+        # before the timed steps, for profiler captures).
+        run_rows = 0 if args.no_tune else plan.tune(views, stream=stream)
         for w in range(args.warmup):
             plan(views, stream=stream)
     stream.synchronize()
@@ -553,7 +599,6 @@ def run_ours(args):
     # come round again) that closes the spots there.
     from sfgb import labeller
     lab = labeller.DeviceLabeller(H, W, live_capacity=(B + 16) * 200_000)
-    lists_ptr, counts_ptr = plan.lists_ptr, plan.counts_ptr
     nb = [0]
 
     def step():
@@ -561,8 +606,8 @@ def run_ours(args):
         ev_mid = torch.cuda.Event(enable_timing=True)
         ev_mid.record(stream)
         nb[0] += 1
-        lab.add_device(list(range(nb[0], nb[0] + B)), lists_ptr, plan.capacity, counts_ptr,
-                       stream.cuda_stream)
+        lab.add_device(list(range(nb[0], nb[0] + B)), plan.lists_ptr, plan.capacity,
+                       plan.counts_ptr, stream.cuda_stream)
         nb[0] += B
         return ev_mid
 
@@ -599,6 +644,47 @@ def run_ours(args):
     # its stream) sets the roofline; the labelling's the rest.
     launch_ms = statistics.mean(a.elapsed_time(m) for (a, _), m in zip(ev, mids))
     label_ms = statistics.mean(m.elapsed_time(b) for (_, b), m in zip(ev, mids))
+
+    # The same batches pipelined as a detector stream would run them: batch
+    # s + 1's threshold is queued before batch s is labelled on a second,
+    # higher-priority stream, so the two overlap on the device (two plans of
+    # the same tuning hold alternate batches' lists). Reported beside the
+    # step: the overlap slows each threshold launch, so the roofline stays
+    # with the timed step above.
+    plans = [plan, api.Plan(H, W, B)]
+    plans[1].configure(plan_run_rows(plan), plan.frames_per_launch)
+    lstream = torch.cuda.Stream(device=dev, priority=-1)
+
+    def pipelined(n):
+        def threshold(k):
+            plans[k % 2](views, stream=stream)
+            t = torch.cuda.Event()
+            t.record(stream)
+            return t
+
+        pending = threshold(0)
+        for k in range(n):
+            done = pending
+            if k + 1 < n:
+                pending = threshold(k + 1)
+            lstream.wait_event(done)
+            nb[0] += 1
+            pk = plans[k % 2]
+            lab.add_device(list(range(nb[0], nb[0] + B)), pk.lists_ptr, pk.capacity,
+                           pk.counts_ptr, lstream.cuda_stream)
+            nb[0] += B
+
+    with torch.cuda.stream(stream):
+        pipelined(args.warmup)
+        torch.cuda.synchronize(dev)
+        pa, pb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pa.record(stream)
+        pipelined(args.steps)
+        lstream.wait_stream(stream)
+        pb.record(lstream)
+    torch.cuda.synchronize(dev)
+    pipelined_fps = args.steps * B / (pa.elapsed_time(pb) / 1e3)
+    plans[1].close()
     label_res = lab.finish()
     del lab
     graphs = plan.graphs
@@ -883,7 +969,7 @@ def run_ours(args):
         served_line = served(args.served_seconds)
         # The same six sweeps all at the top of the 100-750 Hz range.
         keep = ("p50_ms", "p99_ms", "frames", "frames_per_s", "offered_frames_per_s", "errors",
-                "host_link_gbs_offered")
+                "host_link_gbs_offered", "failed_sweeps")
         served_line["at_max_rate"] = {
             k: v for k, v in served(args.served_seconds, rates=[750.0] * 6).items() if k in keep}
         if not args.no_bslz4:
@@ -893,6 +979,15 @@ def run_ours(args):
                 served_line[tag] = {
                     k: v for k, v in served(args.served_seconds, rates=[hz] * 6,
                                             chunks=True).items() if k in keep}
+        # The dense-background stress: eight 16M sweeps of Poisson 20 plus
+        # rings, 20000 spots and 2% overloads a frame, at 50 Hz each. A dense
+        # frame has about 800,000 signal pixels and several million candidates
+        # of the erosion bound: lists of one record per 4 pixels, and
+        # labellers that hold a whole call of such frames.
+        dense = served(args.served_seconds, rates=[50.0] * 8, kinds=["16M-dense"] * 8,
+                       label_capacity=32 << 20, capacity_divisor=4)
+        served_line["dense_16m"] = {k: v for k, v in dense.items()
+                                    if k in keep + ("spots", "workload")}
 
     base = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -906,9 +1001,11 @@ def run_ours(args):
         else:
             traffic = DRAM_BYTES_PER_FRAME * B
             traffic_source = (
-                "ncu dram__bytes_read.sum + dram__bytes_write.sum over the 8 kernels of a timed "
-                "64-frame launch of this workload, no cache flush between kernels "
-                f"({DRAM_BYTES_PER_FRAME / 1e6:.1f} MB a frame), times the {B} frames of a launch")
+                "ncu dram__bytes_read.sum + dram__bytes_write.sum over the 8 kernels of one timed "
+                "32-frame launch of this workload (32 frames in HBM, the size a capture may "
+                "hold), no cache flush between kernels "
+                f"({DRAM_BYTES_PER_FRAME / 1e6:.1f} MB a frame), times the {B} frames of a launch; "
+                "a frame's traffic grows a little with the batch (16 frames: 163.2 MB)")
         line = {
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -923,6 +1020,7 @@ def run_ours(args):
                                 f"labelling (grouping, filters, spot table), {B} frames a step",
                        "signal_pixels_per_frame": n_signal,
                        "threshold_only_frames_per_s": threshold_only,
+                       "pipelined_frames_per_s": pipelined_fps,
                        "plain_per_frame_frames_per_s": per_frame,
                        "batched_over_plain": threshold_only / per_frame,
                        "threshold_ms_per_step": launch_ms,
@@ -964,6 +1062,8 @@ def main(argv=None):
     ap.add_argument("--e2e-threads", type=int, default=0,
                     help="host threads of the end-to-end legs (0: one a core, as mxi_find -j)")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the plan's default geometry (no tuning launches)")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the 4M/9M tuned-plan and mixed-detector legs")
     ap.add_argument("--no-u16", action="store_true")

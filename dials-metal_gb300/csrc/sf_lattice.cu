@@ -552,25 +552,21 @@ __device__ __noinline__ bool lat_exact(uint32_t n, uint32_t S, uint32_t Q, const
   return stage0_u32(n, S, Q, P, P.root_lo, P.root_hi);
 }
 
-// The stage-0 bit (signal or masked; off the frame counts as set) of pixel
-// (y, x) from the frame with 64-bit sums, for tiles holding a pixel too large
-// for the 32-bit ones.
-__device__ __noinline__ bool lat_wide(const uint32_t *__restrict__ image, int height, int width,
-                                      int y, int x, const LaunchParams &P) {
-  if (y < 0 || y >= height || x < 0 || x >= width ||
-      __ldg(image + (size_t)y * width + x) >= 0xFFFFFFFEu)
+// The stage-0 bit (signal or masked; off the frame counts as set) of the
+// window whose top-left staged pixel is (row, col) of a staged tile, with
+// 64-bit sums, for tiles holding a pixel too large for the 32-bit ones. The
+// staged tile holds pixels off the frame as masked, so they are skipped as
+// the reference's clipped window skips them.
+__device__ __noinline__ bool lat_wide(const uint32_t (*px)[kVerPW], int row, int col,
+                                      const LaunchParams &P) {
+  if (px[row + kLatK][col + kLatK] >= 0xFFFFFFFEu)
     return true;
   uint32_t n = 0;
   unsigned long long S = 0, Q = 0;
-  for (int dy = -kLatK; dy <= kLatK; dy++) {
-    const int yy = y + dy;
-    if (yy < 0 || yy >= height)
-      continue;
-    for (int dx = -kLatK; dx <= kLatK; dx++) {
-      const int xx = x + dx;
-      if (xx < 0 || xx >= width)
-        continue;
-      const uint32_t v = __ldg(image + (size_t)yy * width + xx);
+  for (int dy = 0; dy <= 2 * kLatK; dy++) {
+#pragma unroll
+    for (int dx = 0; dx <= 2 * kLatK; dx++) {
+      const uint32_t v = px[row + dy][col + dx];
       if (v < 0xFFFFFFFEu) {
         n++;
         S += v;
@@ -936,7 +932,6 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
     // Each lane decides its column's needed windows (lane = column, so no
     // two lanes share a result bit): a row's bit clears when its window is
     // not signal.
-    const uint32_t *image = F.image[f];
     uint32_t keep = 0xFFFFFFFFu;  // bit d: row d's window here is signal (or not needed)
     if constexpr (k16) {
       // The reference's float test of every needed window, exactly.
@@ -950,11 +945,12 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
           keep &= ~(1u << d);
       }
     } else if (wide) {
-      // 64-bit sums from the frame (rare).
+      // 64-bit sums from the staged tile (frames with very large counts).
       while (rows) {
         const int d = __ffs(rows) - 1;
         rows &= rows - 1u;
-        if (!lat_wide(image, height, width, r0 - 2 + d, c0 - 2 + lane, P))
+        if (!lat_wide(reinterpret_cast<const uint32_t (*)[kVerPW]>(sm.pix[s].px), d,
+                      off + lane, P))
           keep &= ~(1u << d);
       }
     } else {

@@ -194,7 +194,11 @@ struct SrvSweep {
   }
 };
 
-size_t labeller_capacity(size_t h, size_t w) {
+// Live pixels a sweep's labeller holds (its open components plus one label
+// call's frames): the server's label_capacity, else min(4 Mi, pixels / 2).
+size_t labeller_capacity(const sf_server_options &o, size_t h, size_t w) {
+  if (o.label_capacity)
+    return o.label_capacity;
   return std::min<size_t>((size_t)1 << 22, std::max<size_t>(h * w / 2, 1024));
 }
 
@@ -557,6 +561,7 @@ void sf_default_server_options(sf_server_options *o) {
   o->ring = 32;
   o->capacity_divisor = 16;
   o->coalesce_us = 1000;
+  o->label_capacity = 0;
 }
 
 sf_server *sf_server_open(const sf_server_options *options) {
@@ -623,7 +628,7 @@ size_t sf_server_sweep_bytes(const sf_server *sv, size_t height, size_t width,
   const size_t capacity = std::max<size_t>(1, height * width / sv->opt.capacity_divisor);
   return sv->opt.ring * (height * width * sizeof(uint32_t) + capacity * sizeof(sf_signal_pixel) +
                          sizeof(uint32_t)) +
-         labeller_bytes(height, labeller_capacity(height, width), min_size);
+         labeller_bytes(height, labeller_capacity(sv->opt, height, width), min_size);
 }
 
 int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,
@@ -679,7 +684,7 @@ int sf_server_open_sweep(sf_server *sv, size_t height, size_t width,
     lo = *label;
   else
     sf_default_label_options(&lo);
-  s->lab = sf_label_open(height, width, &lo, labeller_capacity(height, width));
+  s->lab = sf_label_open(height, width, &lo, labeller_capacity(sv->opt, height, width));
   if (!s->lab)
     return SF_EBADARG;
   s->server = sv;

@@ -18,7 +18,7 @@ SF_EBUSY = -5
 class ServerOptions(ctypes.Structure):
     _fields_ = [("hbm_budget", ctypes.c_size_t), ("max_batch", ctypes.c_size_t),
                 ("ring", ctypes.c_size_t), ("capacity_divisor", ctypes.c_size_t),
-                ("coalesce_us", ctypes.c_size_t)]
+                ("coalesce_us", ctypes.c_size_t), ("label_capacity", ctypes.c_size_t)]
 
 
 class FrameDone(ctypes.Structure):
@@ -79,9 +79,10 @@ def _lib():
 
 class Server:
     def __init__(self, hbm_budget: int = 0, max_batch: int = 16, ring: int = 32,
-                 capacity_divisor: int = 16, coalesce_us: int = 1000):
+                 capacity_divisor: int = 16, coalesce_us: int = 1000, label_capacity: int = 0):
         L = _lib()
-        o = ServerOptions(hbm_budget, max_batch, ring, capacity_divisor, coalesce_us)
+        o = ServerOptions(hbm_budget, max_batch, ring, capacity_divisor, coalesce_us,
+                          label_capacity)
         self._s = L.sf_server_open(ctypes.byref(o))
         if not self._s:
             raise api.SpotFinderError("server refused its options: " + api.last_error())

@@ -470,6 +470,9 @@ typedef struct {
   size_t ring;             /* device frame slots per sweep, >= max_batch (32) */
   size_t capacity_divisor; /* signal-list capacity = pixels / this (16) */
   size_t coalesce_us;      /* wait up to this long to fill a launch or a label call (1000) */
+  size_t label_capacity;   /* live pixels each sweep's labeller holds: its open
+                              components plus one label call's frames (0: min(4 Mi,
+                              pixels / 2); dense frames need more) */
 } sf_server_options;
 
 typedef struct {
