@@ -217,7 +217,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": elapsed / max(args.steps, 1) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": WORKLOAD}, "impl": "reference",
+            "config": run_config(args.frames_per_step, args.pool), "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "frames/s", "cores": best["cores"],
                              "kind": "port", "sample": best["sample"] +
                              " (the reference's CPU dext/Labeller restated in C: the "
@@ -552,6 +552,16 @@ def batched_legs(dev, steps: int = 5, warmup: int = 3) -> dict:
                 "2162x2068 and 1065x1030 in one launch sequence, against "
                 "sf_threshold_u32_batch_device once per shape"}
     return out
+
+
+def run_config(frames_per_step: int, pool: int) -> dict:
+    """The workload both arms report (the reference arm names the same)."""
+    return {"workload": WORKLOAD, "frames_per_step": frames_per_step,
+            "frame_pool": f"{pool} distinct frames resident in HBM "
+                          f"({pool * H * W * 4 / 1e9:.2f} GB), cycled",
+            "l2": "inputs larger than L2: each frame is 72.4 MB and consecutive frames differ",
+            "stage": "threshold (all three dext stages + ordered emit) and 3-D labelling "
+                     f"(grouping, filters, spot table), {frames_per_step} frames a step"}
 
 
 def plan_run_rows(plan) -> int:
@@ -1011,14 +1021,8 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "frames_per_step": B,
-                       "frame_pool": f"{pool_n} distinct frames resident in HBM "
-                                     f"({pool_n * H * W * 4 / 1e9:.2f} GB), cycled",
-                       "l2": "inputs larger than L2: each frame is 72.4 MB and "
-                             "consecutive frames differ",
-                       "stage": "threshold (all three dext stages + ordered emit) and 3-D "
-                                f"labelling (grouping, filters, spot table), {B} frames a step",
-                       "signal_pixels_per_frame": n_signal,
+            "config": run_config(B, pool_n),
+            "details": {"signal_pixels_per_frame": n_signal,
                        "threshold_only_frames_per_s": threshold_only,
                        "pipelined_frames_per_s": pipelined_fps,
                        "plain_per_frame_frames_per_s": per_frame,
