@@ -2,15 +2,17 @@
 //
 // k_decode gives each block of a chunk to one warp:
 //
-//   LZ4     every lane follows the same parse of the block: a sequence's
-//           token, offset and length bytes come from one load of the next 32
-//           input bytes (a byte a lane) by shuffles; the literal runs and
-//           matches are copied by the lanes together, 32 bytes apart. A match
-//           whose offset is shorter than its length repeats a pattern of
-//           `offset` bytes: a one-byte run is filled with 16-byte stores,
-//           other patterns are copied in passes of D bytes from D back, D
-//           doubling from the offset up to 128, so that no pass reads what it
-//           writes.
+//   LZ4     every lane follows the same parse of the block, a 32-byte
+//           window of input (a byte a lane) at a time: each lane reads the
+//           sequence that would start at its byte, and the short sequences
+//           chained from the window's start are taken together, their
+//           literals written at once by the lanes that hold them. Matches are
+//           copied by the lanes together, a byte or (long ones, 32-bit
+//           pixels) a word a lane. A match whose offset is shorter than its
+//           length repeats a pattern of `offset` bytes: a one-byte run is
+//           filled with 16-byte stores, other patterns are copied in passes
+//           of D bytes from D back, D doubling from the offset, so that no
+//           pass reads what it writes.
 //   planes  a bitshuffle block decodes into the warp's 8 KB of shared memory
 //           (bitshuffle's default block is 8192 bytes); for each group of 8
 //           elements and each byte j of an element, the group's byte of each
@@ -39,6 +41,7 @@ namespace {
 
 constexpr int kDecWarps = 4;
 constexpr uint32_t kDecBuf = 8192;  // bytes of a warp's decoded block
+constexpr size_t kDecMaxIn = size_t(1) << 31;  // a block's compressed bytes, below
 
 __device__ __forceinline__ void prefetch_l1(const void *p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
@@ -63,16 +66,56 @@ __device__ __forceinline__ void fill_warp(Out *dst, uint8_t v, uint32_t n, int l
   __syncwarp();
 }
 
+// dst[op, op + m) = dst[op - D, op - D + m) for m <= D (so that no byte it
+// reads is one it writes), by the warp, a byte a lane. With kWords, past 32
+// bytes a lane writes a 32-bit word at a time: the bytes up to a 4-byte
+// boundary, the words (each from the two source words it straddles, by a
+// funnel shift), the bytes after the last whole word. The word reads may
+// take up to 2 bytes past the source, which the shift drops.
+template <bool kWords, typename Out>
+__device__ __forceinline__ void copy_pass(Out *dst, uint32_t op, uint32_t D, uint32_t m,
+                                          int lane) {
+  Out *d = dst + op;
+  if (!kWords) {
+    for (uint32_t i = lane; i < m; i += 32)
+      d[i] = d[(int)i - (int)D];
+    return;
+  }
+  if (m <= 32) {
+    if ((uint32_t)lane < m)
+      d[lane] = d[(int)lane - (int)D];
+    return;
+  }
+  const uint32_t head = (uint32_t)(-(uintptr_t)d) & 3u;
+  if ((uint32_t)lane < head)
+    d[lane] = d[(int)lane - (int)D];
+  const uint32_t nw = (m - head) >> 2;
+  uint32_t *dw = reinterpret_cast<uint32_t *>(d + head);
+  const Out *s = d + head - D;
+  const uint32_t sh = (uint32_t)(uintptr_t)s & 3u;
+  const uint32_t *sw = reinterpret_cast<const uint32_t *>(s - sh);
+  if (sh == 0) {
+    for (uint32_t i = lane; i < nw; i += 32)
+      dw[i] = sw[i];
+  } else {
+    for (uint32_t i = lane; i < nw; i += 32)
+      dw[i] = __funnelshift_r(sw[i], sw[i + 1], 8u * sh);
+  }
+  const uint32_t t0 = head + 4u * nw;
+  if ((uint32_t)lane < m - t0)
+    d[t0 + lane] = d[(int)(t0 + lane) - (int)D];
+}
+
 // dst[op, op + ml) = the match at `off` back, by the warp. A match that
 // overlaps what it writes (off < ml) repeats a pattern of `off` bytes: runs
 // of one byte are filled; otherwise it goes in passes of D bytes from D back,
-// D doubling from off up to 128, so that no pass reads what it writes.
-template <typename Out>
+// D doubling from off up to kPass, so that no pass reads what it writes.
+template <bool kWords, typename Out>
 __device__ __forceinline__ void copy_match(Out *dst, uint32_t op, uint32_t off, uint32_t ml,
                                            int lane) {
+  constexpr uint32_t kPass = kWords ? 512u : 128u;
   if (off >= ml) {
-    for (uint32_t i = lane; i < ml; i += 32)
-      dst[op + i] = dst[op - off + i];
+    copy_pass<kWords>(dst, op, off, ml, lane);
     __syncwarp();
     return;
   }
@@ -82,13 +125,11 @@ __device__ __forceinline__ void copy_match(Out *dst, uint32_t op, uint32_t off, 
   }
   uint32_t D = off, done = 0;
   while (done < ml) {
-    const uint32_t m = min(ml - done, min(D, 128u));
-    Out *to = dst + op + done;
-    for (uint32_t i = lane; i < m; i += 32)
-      to[i] = to[(int)i - (int)D];
+    const uint32_t m = min(ml - done, min(D, kPass));
+    copy_pass<kWords>(dst, op + done, D, m, lane);
     __syncwarp();
     done += m;
-    if (m == D && D < 128)
+    if (m == D && D < kPass)
       D *= 2;
   }
 }
@@ -100,49 +141,84 @@ __device__ __forceinline__ void copy_match(Out *dst, uint32_t op, uint32_t off, 
 // block at the input's end; a match must start inside the output and end
 // before its last 5 bytes.
 //
-// Each sequence starts with one load of the next 32 input bytes, a byte a
-// lane. A sequence whose literal run is under 15 bytes and whose match
-// length needs at most one extra byte (most of them) lies within it: the
-// token, offset and length come by shuffles and the literals are written
-// from the lanes that hold them. Any other sequence, and any that would fail
-// a check, takes the byte-by-byte parse, which reports the error.
-template <typename Out>
+// The parse goes a window at a time: one load of the next 32 input bytes, a
+// byte a lane. Every lane reads the sequence that would start at its byte
+// (token, offset, length); the sequences that chain from the window's first
+// byte and lie inside it, with a literal run under 15 bytes and a match
+// length of at most one extra byte (most of them), are taken together: their
+// output positions as the chain is walked, the checks by each sequence's
+// lane, all their literals written at once from the lanes that hold them,
+// then their matches in order. A window whose first sequence is not of that
+// kind, or would fail a check, takes the byte-by-byte parse for that
+// sequence, which reports the error.
+template <bool kWords, typename Out>
 __device__ __forceinline__ long long lz4_warp(const uint8_t *__restrict__ in, uint32_t n,
                                               Out *dst, uint32_t cap, int lane) {
   uint32_t ip = 0, op = 0;
   for (;;) {
     if (ip >= n)
       return -(long long)ip - 1;
+    // (n < 2^31, so that ip + lane cannot wrap: the host refuses larger blocks.)
     const uint32_t w = ip + lane < n ? (uint32_t)__ldg(in + ip + lane) : 0u;
-    const uint32_t token = __shfl_sync(~0u, w, 0);
-    const uint32_t lit0 = token >> 4;
-    if (lit0 < 15 && (unsigned long long)op + lit0 + 12 <= cap &&
-        (unsigned long long)ip + lit0 + 9 <= n) {
-      // Not the last sequence: its offset (and a length byte) are in range.
-      const uint32_t off =
-          __shfl_sync(~0u, w, lit0 + 1) | __shfl_sync(~0u, w, lit0 + 2) << 8;
-      const uint32_t e = __shfl_sync(~0u, w, lit0 + 3);
-      uint32_t ml = (token & 15u) + 4u, used = lit0 + 3;
-      bool take = off != 0 && off <= op + lit0;
-      if ((token & 15u) == 15u) {
-        take = take && e != 255u && (unsigned long long)ip + used + 6 <= n;
-        ml += e;
-        used += 1;
+    {
+      // The sequence a token at this lane's byte would start.
+      const uint32_t l0 = w >> 4, nib = w & 15u;
+      const uint32_t off = __shfl_sync(~0u, w, lane + l0 + 1) |
+                           __shfl_sync(~0u, w, lane + l0 + 2) << 8;
+      const uint32_t e = __shfl_sync(~0u, w, lane + l0 + 3);
+      const uint32_t ext = nib == 15u ? 1u : 0u;
+      const uint32_t len = l0 + 3u + ext;  // its bytes
+      const uint32_t ml = nib + 4u + (ext ? e : 0u);
+      const bool fits = l0 < 15u && (uint32_t)lane + len <= 32u && !(ext && e == 255u);
+      // The chain of such sequences from the window's first byte, and the
+      // output before each (its lane keeps it).
+      const uint32_t step = fits ? len | (l0 + ml) << 8 : 0u;
+      uint32_t toks = 0, acc = 0, before = 0;
+      for (uint32_t p = 0; p < 32u;) {  // warp-uniform
+        const uint32_t s = __shfl_sync(~0u, step, p);
+        if (s == 0)
+          break;
+        toks |= 1u << p;
+        if ((uint32_t)lane == p)
+          before = acc;
+        acc += s >> 8;
+        p += s & 0xFFu;
       }
-      take = take && (unsigned long long)op + lit0 + ml + 5 <= cap;
-      if (take) {
-        if ((uint32_t)lane >= 1 && (uint32_t)lane <= lit0)
-          dst[op + lane - 1] = (Out)w;
-        op += lit0;
-        ip += used;
+      const bool tok = (toks >> lane) & 1u;
+      const unsigned long long at = (unsigned long long)op + before;
+      // Not the last sequence (its literals end 12 bytes before the output's
+      // end and 8 before the input's), the offset inside the output, the
+      // match ending 5 bytes before the output's end.
+      const bool ok = !tok || (at + l0 + 12 <= cap &&
+                               (unsigned long long)ip + lane + l0 + 9 <= n && off != 0 &&
+                               off <= at + l0 && at + l0 + ml + 5 <= cap);
+      const uint32_t bad = __ballot_sync(~0u, !ok);
+      const uint32_t keep = toks & ((bad & (0u - bad)) - 1u);  // those before the first bad
+      if (keep) {
+        // Each lane's byte against the last kept token at or below it.
+        const uint32_t below = keep & ((2u << lane) - 1u);
+        const int t = 31 - __clz(below);
+        const uint32_t tl = __shfl_sync(~0u, l0, t & 31);
+        const uint32_t to = __shfl_sync(~0u, (uint32_t)at, t & 31);
+        const uint32_t r = (uint32_t)(lane - t - 1);
+        if (below && r < tl)
+          dst[to + r] = (Out)w;
         __syncwarp();
-        copy_match(dst, op, off, ml, lane);
-        op += ml;
+        const uint32_t mo = (uint32_t)at + l0, mp = off | ml << 16;
+        for (uint32_t m = keep; m; m &= m - 1u) {  // warp-uniform
+          const int k = __ffs(m) - 1;
+          const uint32_t o = __shfl_sync(~0u, mo, k), q = __shfl_sync(~0u, mp, k);
+          copy_match<kWords>(dst, o, q & 0xFFFFu, q >> 16, lane);
+        }
+        const int last = 31 - __clz(keep);
+        ip += (uint32_t)last + __shfl_sync(~0u, len, last);
+        op = __shfl_sync(~0u, mo + ml, last);
         continue;
       }
     }
+    const uint32_t token = __shfl_sync(~0u, w, 0);
     ip++;
-    uint32_t lit = lit0;
+    uint32_t lit = token >> 4;
     if (lit == 15) {
       uint32_t s;
       do {
@@ -182,7 +258,7 @@ __device__ __forceinline__ long long lz4_warp(const uint8_t *__restrict__ in, ui
     ml += 4;
     if ((unsigned long long)op + ml + 5 > cap)
       return -(long long)ip - 1;
-    copy_match(dst, op, off, ml, lane);
+    copy_match<kWords>(dst, op, off, ml, lane);
     op += ml;
   }
 }
@@ -318,6 +394,9 @@ k_decode(const uint8_t *__restrict__ in, const DecodeBlock *__restrict__ blocks,
          uint32_t nblocks, uint8_t *__restrict__ out, uint8_t *__restrict__ scratch,
          uint32_t *__restrict__ status) {
   __shared__ __align__(16) uint8_t buf[kDecWarps][kDecBuf];
+  // Word copies pay on the planes of 32-bit pixels (long repeats between
+  // planes); on those of 16-bit pixels byte copies measured faster.
+  constexpr bool kWords = E == 4;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (uint32_t b = blockIdx.x * kDecWarps + warp; b < nblocks; b += gridDim.x * kDecWarps) {
     const DecodeBlock d = blocks[b];
@@ -333,7 +412,7 @@ k_decode(const uint8_t *__restrict__ in, const DecodeBlock *__restrict__ blocks,
     for (uint32_t i = (uint32_t)lane * 128u; i < d.in_bytes; i += 32u * 128u)
       prefetch_l1(src + i);
     if (d.mode == kDecLz4) {
-      const long long r = lz4_warp(src, d.in_bytes, dst, d.out_bytes, lane);
+      const long long r = lz4_warp<true>(src, d.in_bytes, dst, d.out_bytes, lane);
       if (r < 0)
         report(status, kDecBad, b, r, lane);
       else if (r != (long long)d.out_bytes)
@@ -342,7 +421,7 @@ k_decode(const uint8_t *__restrict__ in, const DecodeBlock *__restrict__ blocks,
     }
     long long r;
     if (d.out_bytes <= kDecBuf) {
-      r = lz4_warp(src, d.in_bytes, buf[warp], d.out_bytes, lane);
+      r = lz4_warp<kWords>(src, d.in_bytes, buf[warp], d.out_bytes, lane);
       if (r == (long long)d.out_bytes) {
         if (d.elems % 32 == 0)
           unshuffle_words<E>(buf[warp], d.elems, dst, lane);
@@ -351,7 +430,7 @@ k_decode(const uint8_t *__restrict__ in, const DecodeBlock *__restrict__ blocks,
       }
     } else {
       uint8_t *tmp = scratch + d.out_off;
-      r = lz4_warp(src, d.in_bytes, tmp, d.out_bytes, lane);
+      r = lz4_warp<kWords>(src, d.in_bytes, tmp, d.out_bytes, lane);
       if (r == (long long)d.out_bytes)
         unshuffle<E>(tmp, d.elems, dst, lane);
     }
@@ -439,8 +518,9 @@ int plan_chunk(const uint8_t *data, size_t nbytes, const char *algorithm, unsign
       ip += 4;
       if (c > n - ip)
         return bad_data("bitshuffle decompression failed with code -1");
-      if (elems * element > 0xFFFFFFFFull) {
-        t_last_error = "bitshuffle blocks of 4 GB or more are not decoded on the device";
+      if (elems * element > 0xFFFFFFFFull || c >= kDecMaxIn) {
+        t_last_error = "bitshuffle blocks of 4 GB or more (2 GB compressed) are not decoded "
+                       "on the device";
         return SF_EUNSUPPORTED;
       }
       plan->blocks.push_back(
@@ -470,8 +550,9 @@ int plan_chunk(const uint8_t *data, size_t nbytes, const char *algorithm, unsign
       if (c == 0 || read + c > n)
         return bad_data("lz4 block size out of range");
       const size_t want = std::min(expected - written, bsize);
-      if (want > 0xFFFFFFFFull) {
-        t_last_error = "lz4 blocks of 4 GB or more are not decoded on the device";
+      if (want > 0xFFFFFFFFull || c >= kDecMaxIn) {
+        t_last_error = "lz4 blocks of 4 GB or more (2 GB compressed) are not decoded on the "
+                       "device";
         return SF_EUNSUPPORTED;
       }
       plan->blocks.push_back({read, written, (uint32_t)c, (uint32_t)want, 0, kDecLz4});
