@@ -55,7 +55,7 @@ constexpr int kLatCols = 12;                // columns a lane owns
 constexpr int kLatOutLanes = 30;            // lanes 0-29 write, lane 30 feeds lane 29
 constexpr int kLatOut = kLatCols * kLatOutLanes;  // 360 output columns a warp
 constexpr int kLatWarps = 4;                // warps a block
-constexpr int kLatOcc = 6;                  // blocks an SM the kernel is built for
+constexpr int kLatOcc = 5;                  // blocks an SM the kernel is built for
 constexpr uint32_t kLatPS = 26;             // masked count above a 26-bit sum
 constexpr uint32_t kLatMask = (1u << kLatPS) - 1u;
 constexpr uint32_t kLatCap = 32767;         // valid pixels saturate here
@@ -505,7 +505,8 @@ constexpr int kVerDR = kVerRows + 4;         // stage-0 rows
 constexpr int kVerPC = 38;                   // pixel columns
 constexpr int kVerPW = 44;                   // staged columns: 11 16-byte pieces
 constexpr int kVerWarps = 4;
-constexpr int kVerOcc = 5;                   // blocks an SM the kernel is built for
+constexpr int kVerOcc = 6;                   // exact-check blocks an SM (a pixel buffer a warp)
+constexpr int kS2Occ = 5;                    // stage-2 blocks an SM (two pixel buffers a warp)
 
 __host__ __device__ inline int ver_ntx(int w) { return (w + kVerTW - 1) / kVerTW; }
 __host__ __device__ inline int ver_nty(int h) { return (h + kVerRows - 1) / kVerRows; }
@@ -529,9 +530,10 @@ template <typename Pix> struct alignas(128) TileBuf {
 };
 
 template <typename Pix> struct alignas(128) VerWarp {
-  TileBuf<Pix> pix[2];                   // staged pixels, two tiles
-  uint64_t bar[2];                       // their TMA mbarriers
-  uint32_t cw[2][kVerRows][2];           // the tile's candidate words, two tiles
+  TileBuf<Pix> pix[1];                   // staged pixels (the next tile's load goes out
+                                         // once the current one's are read)
+  uint64_t bar[1];                       // its TMA mbarrier
+  uint32_t cw[2][kVerRows][2];           // the tile's candidate words, two tiles (s)
   uint2 vs[kVerDR][kVerPC + 2];          // column sums of 7 rows
   uint32_t msk[kVerPC + 2];              // masked pixels by row, a word a column
 };
@@ -752,10 +754,11 @@ __device__ __forceinline__ void ver_stage(VerWarp<Pix> &sm, int s, uint32_t e, c
   const int f = a.f, r0 = a.r0, c0 = a.c0;
   const int height = F.h[f], width = F.w[f];
   const int xs = tile_xs<Pix>(c0);
+  __syncwarp();  // every lane is done with the pixel buffer
   if (tma)
-    tma_stage<Pix>(sm.pix[s], &sm.bar[s], M, f, r0, xs, lane);
+    tma_stage<Pix>(sm.pix[0], &sm.bar[0], M, f, r0, xs, lane);
   else
-    stage_pixels<Pix>(sm.pix[s].px, reinterpret_cast<const Pix *>(F.image[f]), height, width,
+    stage_pixels<Pix>(sm.pix[0].px, reinterpret_cast<const Pix *>(F.image[f]), height, width,
                       vec, r0, xs, lane);
   if (lane < 2 * kVerRows) {
     const int o = lane >> 1, wdx = (c0 >> 5) + (lane & 1);
@@ -807,7 +810,6 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
   VerWarp<Pix> &sm = warps[warp];
   if (tma && lane == 0) {
     mbar_init(&sm.bar[0], 1);
-    mbar_init(&sm.bar[1], 1);
     mbar_init_fence();
   }
   __syncthreads();
@@ -819,8 +821,11 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
   const uint32_t count = counters[kCtrTiles];
   const uint32_t nw = gridDim.x * kVerWarps;
   uint32_t k = blockIdx.x * kVerWarps + warp;
-  // List entries are read a tile before they are staged, and staged a tile
-  // before they are checked.
+  // List entries are read a tile before they are staged. A warp has one
+  // pixel buffer: the next tile's load goes out as soon as this tile's pixels
+  // have been read (after the column sums, or after the windows summed from
+  // the pixels on a frame with very large counts), and runs under the rest of
+  // this tile's check. The candidate words are staged into the other of two.
   uint32_t e = k < count ? list[k] : 0u;
   uint32_t e1 = k + nw < count ? list[k + nw] : 0u;
   if (k < count)
@@ -828,30 +833,33 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
                    lane);
   cp_async_commit();
   uint32_t e2 = 0u;
-  uint32_t inflight = k < count ? 1u : 0u;  // bit b: a TMA load into buffer b not waited for
+  uint32_t inflight = k < count ? 1u : 0u;  // a TMA load not waited for
   for (int s = 0; k < count; k += nw, s ^= 1, e = e1, e1 = e2) {
     e2 = k + 2 * nw < count ? list[k + 2 * nw] : 0u;
-    if (k + nw < count) {
-      ver_stage<Pix>(sm, s ^ 1, e1, F, M, tma, vec, ntiles, ntx, by_ntiles, by_ntx, final_all,
-                     words, lane);
-      inflight |= 2u >> s;
-    }
-    cp_async_commit();
-    cp_async_wait<1>();  // this tile's pieces have landed
+    cp_async_wait<0>();  // this tile's pieces have landed
     __syncwarp();
     const TileAt a = tile_at(e, ntiles, ntx, by_ntiles, by_ntx);
     const int f = a.f, r0 = a.r0, c0 = a.c0;
     const int height = F.h[f], width = F.w[f], wpr = (width + 31) >> 5;
     if (tma) {
-      inflight &= ~(1u << s);
-      if (!tma_landed<Pix>(sm.pix[s], &sm.bar[s], (parity >> s) & 1u, height, width, r0,
+      inflight = 0u;
+      if (!tma_landed<Pix>(sm.pix[0], &sm.bar[0], parity & 1u, height, width, r0,
                            tile_xs<Pix>(c0), lane)) {
         if (lane == 0)
           atomicOr(counters + kCtrFault, 1u);
         break;  // whole warp
       }
-      parity ^= 1u << s;
+      parity ^= 1u;
     }
+    // The next tile's load, once this tile's pixels have been read.
+    auto stage_next = [&]() {
+      if (k + nw < count) {
+        ver_stage<Pix>(sm, s ^ 1, e1, F, M, tma, vec, ntiles, ntx, by_ntiles, by_ntx,
+                       final_all, words, lane);
+        inflight = 1u;
+      }
+      cp_async_commit();
+    };
     const int off = (c0 - 5) - tile_xs<Pix>(c0);
     const int w0 = c0 >> 5, sh = c0 & 31;
     uint32_t cj[kVerRows];
@@ -883,7 +891,7 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
       uint32_t ns[kVerPR], q[kVerPR], mk = 0;
 #pragma unroll
       for (int r = 0; r < kVerPR; r++) {
-        const uint32_t v = sm.pix[s].px[r][col];
+        const uint32_t v = sm.pix[0].px[r][col];
         const bool masked = is_masked_px<Pix>(v);
         if (!k16)
           mx = max(mx, v + 2u);
@@ -910,6 +918,8 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
     __syncwarp();
     // 16-bit frames sum in 32 bits as the reference does: never wide.
     const bool wide = !k16 && __any_sync(0xffffffffu, mx >= narrow2);
+    if (!wide)
+      stage_next();  // the windows come from the column sums, not the pixels
     if (wide && lane == 0)
       counters[kCtrBatch + (size_t)f * kCtrCount + kCtrWideFrame] = 1u;
     // The stage-0 positions within 2 of a candidate: lane d first forms row
@@ -949,7 +959,7 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
       while (rows) {
         const int d = __ffs(rows) - 1;
         rows &= rows - 1u;
-        if (!lat_wide(reinterpret_cast<const uint32_t (*)[kVerPW]>(sm.pix[s].px), d,
+        if (!lat_wide(reinterpret_cast<const uint32_t (*)[kVerPW]>(sm.pix[0].px), d,
                       off + lane, P))
           keep &= ~(1u << d);
       }
@@ -980,6 +990,8 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
           keep &= ~(1u << d);
       }
     }
+    if (wide)
+      stage_next();
     uint32_t D[kVerDR];
 #pragma unroll
     for (int d = 0; d < kVerDR; d++)
@@ -1015,10 +1027,9 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
     if (lane == 0)
       list2[k] = left ? e : kNoTile;  // same place as in the tile list: no atomics
   }
-  // After a fault: the load still in flight (bounded) before the buffers go.
-  for (int b = 0; b < 2; b++)
-    if (tma && ((inflight >> b) & 1u))
-      (void)mbar_wait(&sm.bar[b], (parity >> b) & 1u);
+  // After a fault: the load still in flight (bounded) before the buffer goes.
+  if (tma && inflight)
+    (void)mbar_wait(&sm.bar[0], parity & 1u);
   cp_async_wait<0>();
 }
 
@@ -1308,7 +1319,7 @@ template <typename Pix> constexpr size_t ver_smem_bytes() {
 }
 static_assert(sizeof(uint4) * 64 % 128 == 0, "the verify warps start 128-byte aligned");
 static_assert((ver_smem_bytes<uint32_t>() + 1024) * kVerOcc <= 228 * 1024,
-              "five exact-check blocks an SM");
+              "six exact-check blocks an SM");
 
 int lat_slots() {
   static int slots = 0;
@@ -1352,7 +1363,7 @@ cudaError_t lattice_stage2(const FramePtrs &F, int nframes, int h, int w, int ve
   static cudaError_t config_error = cudaSuccess;
   static int blocks = 0;
   std::call_once(configured, [] {
-    config_error = persistent_blocks(lat_stage2<kVerOcc, Pix>, s2_smem_bytes<Pix>(), &blocks);
+    config_error = persistent_blocks(lat_stage2<kS2Occ, Pix>, s2_smem_bytes<Pix>(), &blocks);
   });
   if (config_error != cudaSuccess)
     return config_error;
@@ -1362,7 +1373,7 @@ cudaError_t lattice_stage2(const FramePtrs &F, int nframes, int h, int w, int ve
   const uint32_t *list = b.amb + (size_t)nframes * (b.words + tiles);
   TileMaps M;
   const int tma = make_tile_maps<Pix>(F, nframes, h, w, &M);
-  lat_stage2<kVerOcc, Pix><<<blocks * device_sms(), kVerWarps * 32, s2_smem_bytes<Pix>(),
+  lat_stage2<kS2Occ, Pix><<<blocks * device_sms(), kVerWarps * 32, s2_smem_bytes<Pix>(),
                              stream>>>(F, M, tma, h, w, vec, P, b.scr1, b.bits, prefix, b.words,
                                        list, b.counters, b.cand, b.res, b.cand_cap,
                                        make_fastdiv((uint32_t)tiles),
