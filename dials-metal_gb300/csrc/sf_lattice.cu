@@ -52,7 +52,7 @@ namespace {
 constexpr int kLatK = 3;                    // stage-0 half-width
 constexpr int kLatN0 = 49;                  // pixels of a stage-0 window
 constexpr int kLatCols = 12;                // columns a lane owns
-constexpr int kLatOutLanes = 30;            // lanes 0-29 write, lane 30 feeds lane 29
+constexpr int kLatOutLanes = 30;            // lanes 1-30 write; lanes 0 and 31 are their halos
 constexpr int kLatOut = kLatCols * kLatOutLanes;  // 360 output columns a warp
 constexpr int kLatWarps = 4;                // warps a block
 constexpr int kLatOcc = 5;                  // blocks an SM the kernel is built for
@@ -119,8 +119,8 @@ __device__ __forceinline__ int span_frame(const FrameSpans &S, int nframes, int 
 }
 
 // The 12 bound bits of a lane from the lattice bits b0-b4 at its columns
-// -1, 2, 5, 8 and 11 (b4 is the next lane's b0): column c keeps the lattice
-// columns within 2 of it.
+// -1, 2, 5, 8 and 11 (b0 is the lane before's column 11): column c keeps the
+// lattice columns within 2 of it.
 __host__ __device__ constexpr uint32_t lat_bound12(uint32_t b) {
   const uint32_t b0 = b & 1u, b1 = (b >> 1) & 1u, b2 = (b >> 2) & 1u, b3 = (b >> 3) & 1u,
                  b4 = (b >> 4) & 1u;
@@ -130,70 +130,78 @@ __host__ __device__ constexpr uint32_t lat_bound12(uint32_t b) {
 }
 
 __device__ __forceinline__ void lat_load(const uint32_t *__restrict__ image, int height, int width,
-                                         bool interior, int cx, int p, uint32_t v[16]) {
+                                         bool interior, int cx, int p, uint32_t v[kLatCols]) {
   if (p < 0 || p >= height) {
 #pragma unroll
-    for (int i = 0; i < 16; i++)
+    for (int i = 0; i < kLatCols; i++)
       v[i] = 0xFFFFFFFFu;
     return;
   }
-  const uint32_t *row = image + (size_t)p * width + (cx - 4);
+  const uint32_t *row = image + (size_t)p * width + cx;
   if (interior) {
 #pragma unroll
-    for (int f = 0; f < 4; f++) {
+    for (int f = 0; f < kLatCols / 4; f++) {
       const uint4 t = __ldg(reinterpret_cast<const uint4 *>(row) + f);
       v[4 * f] = t.x, v[4 * f + 1] = t.y, v[4 * f + 2] = t.z, v[4 * f + 3] = t.w;
     }
   } else {
 #pragma unroll
-    for (int i = 0; i < 16; i++) {
-      const int gx = cx - 4 + i;
+    for (int i = 0; i < kLatCols; i++) {
+      const int gx = cx + i;
       v[i] = (gx >= 0 && gx < width) ? __ldg(row + i) : 0xFFFFFFFFu;
     }
   }
 }
 
-// One pixel row of a lane: the 16 pixels of columns -4 .. 11 packed (masked
-// as a lone count bit whose square wraps to 0, valid saturated at kLatCap),
-// the row sums of 7 columns at the lattice columns -1, 2, 5, 8, and the
-// masked bits of the lane's own 12 columns.
+// One pixel row of a lane: its 12 pixels packed (masked as a lone count bit
+// whose square wraps to 0, valid saturated at kLatCap), the row sums of 7
+// columns at the lattice columns 2, 5, 8, 11, and the masked bits of the 12
+// columns. The windows reach one column into the lane before (its column 11,
+// by a shuffle) and three into the lane after (its first triple, likewise):
+// lanes 0 and 31 hold the halo columns of the warp's 30 writing lanes.
 // 16-bit frames (Pix = uint16_t) are summed as the reference sums them: in
 // 32 bits, the sum of squares modulo 2^32 (src/spots/dext.hh:31-33); their
 // pixels need no saturation (49 of them sum below 2^22).
 template <typename Pix>
-__device__ __forceinline__ void lat_row(const uint32_t v[16], uint32_t hn[4], uint32_t hq[4],
-                                        uint32_t *m12, uint32_t *mh) {
+__device__ __forceinline__ void lat_row(const uint32_t v[kLatCols], int lane, uint32_t hn[4],
+                                        uint32_t hq[4], uint32_t *m12) {
   constexpr bool k16 = sizeof(Pix) == 2;
-  uint32_t ns[16], q[16];
+  uint32_t ns[kLatCols], q[kLatCols];
 #pragma unroll
-  for (int i = 0; i < 16; i++) {
+  for (int i = 0; i < kLatCols; i++) {
     if (k16)
       ns[i] = v[i] >= 0xFFFEu ? (1u << kLatPS) : v[i];
     else
       ns[i] = v[i] >= 0xFFFFFFFEu ? (1u << kLatPS) : min(v[i], kLatCap);
     q[i] = ns[i] * ns[i];
   }
-  // Triples of columns [3a - 4, 3a - 2], then the 7-column windows.
-  uint32_t gn[5], gq[5];
+  // Triples of columns [3a, 3a + 2], then the 7-column windows.
+  uint32_t gn[4], gq[4];
 #pragma unroll
-  for (int a = 0; a < 5; a++) {
+  for (int a = 0; a < 4; a++) {
     gn[a] = ns[3 * a] + ns[3 * a + 1] + ns[3 * a + 2];
     gq[a] = q[3 * a] + q[3 * a + 1] + q[3 * a + 2];
   }
-#pragma unroll
-  for (int a = 0; a < 4; a++) {
-    hn[a] = gn[a] + gn[a + 1] + ns[3 * a + 6];
-    hq[a] = gq[a] + gq[a + 1] + q[3 * a + 6];
-  }
+  const uint32_t ln = __shfl_sync(0xffffffffu, ns[kLatCols - 1], (lane + 31) & 31);
+  const uint32_t lq = __shfl_sync(0xffffffffu, q[kLatCols - 1], (lane + 31) & 31);
+  const uint32_t rn = __shfl_sync(0xffffffffu, gn[0], (lane + 1) & 31);
+  const uint32_t rq = __shfl_sync(0xffffffffu, gq[0], (lane + 1) & 31);
+  hn[0] = ln + gn[0] + gn[1];
+  hq[0] = lq + gq[0] + gq[1];
+  hn[1] = ns[2] + gn[1] + gn[2];
+  hq[1] = q[2] + gq[1] + gq[2];
+  hn[2] = ns[5] + gn[2] + gn[3];
+  hq[2] = q[5] + gq[2] + gq[3];
+  hn[3] = ns[8] + gn[3] + rn;
+  hq[3] = q[8] + gq[3] + rq;
   // A valid packed 32-bit-frame pixel is below 2^15, so shifting it right by
   // 26 - c (c <= 11) leaves nothing: the shifted words add up to the masked
   // bits. A 16-bit pixel can reach 2^16, so its count bit is isolated first.
   uint32_t m = 0;
 #pragma unroll
   for (int c = 0; c < kLatCols; c++)
-    m += k16 ? (ns[4 + c] >> kLatPS) << c : ns[4 + c] >> (kLatPS - c);
+    m += k16 ? (ns[c] >> kLatPS) << c : ns[c] >> (kLatPS - c);
   *m12 = m;
-  *mh = ns[3] >> kLatPS;  // column -1, the first lattice column
 }
 
 __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
@@ -230,16 +238,16 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
 
 // The ring variant (kRing: 4 | width and 16-byte aligned frames) stages each
 // warp's pixel rows in shared memory by cp.async, kRingSlots - 1 rows ahead:
-// a row is the 95 16-byte pieces from column X - 4 (X the strip's first
-// output column) that the lanes read, 12 columns a lane apart. The other
-// variant loads each lane's 16 columns straight from the frame, a row ahead.
+// a row is the 96 16-byte pieces from column X - 12 (X the strip's first
+// output column) that the lanes read, 12 columns a lane. The other variant
+// loads each lane's 12 columns straight from the frame, a row ahead.
 //
 // A piece is 4 pixels: 16 bytes of a 32-bit frame, 8 of a 16-bit one (whose
-// rows, with 4 | width, start 8-byte aligned). Both fetch 95 pieces from
-// column X - 4, and a lane reads its 16 pixels from column 12 l of the slot.
+// rows, with 4 | width, start 8-byte aligned). Both fetch 96 pieces from
+// column X - 12, and lane l reads its 12 pixels from column 12 l of the slot.
 constexpr int kRingSlots = 4;
-constexpr int kRingPieces = 95;   // pieces fetched a row
-constexpr int kRingStride = 388;  // pixels a slot: what lane 31 reads
+constexpr int kRingPieces = 96;   // pieces fetched a row: 3 a lane
+constexpr int kRingStride = 384;  // pixels a slot
 template <typename Pix>
 constexpr size_t ring_bytes() {
   return (size_t)kLatWarps * kRingSlots * kRingStride * sizeof(Pix);
@@ -278,14 +286,18 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
   const int bytes_per_row = ((width + 31) >> 5) * 4;
   uint8_t *scr1 = scr1_bytes + (size_t)f * mask_bytes;
   uint8_t *fin = final_bytes + (size_t)f * mask_bytes;
-  const int cx = kLatOut * sx + kLatCols * lane;
-  const bool interior = vec && cx - 4 >= 0 && cx + 12 <= width;
-  // This lane's first mask byte (lane pairs share three bytes), and the bits
-  // of its columns inside the frame.
-  const int pair_byte = (kLatOut * sx + 24 * (lane >> 1)) >> 3;
-  const bool writer = lane < kLatOutLanes;
+  // Lane l holds columns X + 12 (l - 1) .. + 11: lanes 1-30 the strip's
+  // 360, lane 0 the 12 before it, lane 31 the 12 after it.
+  const int cx = kLatOut * sx + kLatCols * (lane - 1);
+  const bool interior = vec && cx >= 0 && cx + kLatCols <= width;
+  // This lane's first mask byte (lane pairs 1-2, 3-4, .. share three
+  // bytes), and the bits of its columns inside the frame.
+  const int pair_byte = (kLatOut * sx + 24 * ((lane - 1) >> 1)) >> 3;
+  const bool writer = lane >= 1 && lane <= kLatOutLanes;
+  const bool first_of_pair = (lane & 1) != 0;
   const uint32_t inside12 =
-      cx >= width ? 0u : (cx + kLatCols <= width ? 0xFFFu : ((1u << (width - cx)) - 1u));
+      (cx < 0 || cx >= width) ? 0u
+                              : (cx + kLatCols <= width ? 0xFFFu : ((1u << (width - cx)) - 1u));
   const int ra = ry * run_rows;
   const int rb = min(height, ra + run_rows);
   const int ja = ra / 3;
@@ -306,13 +318,11 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
   // instruction covers 128 contiguous pixels), and whether each lies in the
   // frame.
   const int X = kLatOut * sx;
-  const int x0 = X - 4 + 4 * lane;
-  bool pin[3], pok[3];
+  const int x0 = X - kLatCols + 4 * lane;
+  bool pin[3];
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
-    pok[i] = lane + 32 * i < kRingPieces;
-    pin[i] = pok[i] && x0 + 128 * i >= 0 && x0 + 128 * i + 4 <= width;
-  }
+  for (int i = 0; i < 3; i++)
+    pin[i] = x0 + 128 * i >= 0 && x0 + 128 * i + 4 <= width;
   auto fetch = [&](int p) {
     Pix *dst = ring + ((p - pbeg) % kRingSlots) * kRingStride + 4 * lane;
     const bool rowin = p >= 0 && p < height && p < pend;
@@ -321,15 +331,11 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
     for (int i = 0; i < 3; i++) {
       if (rowin && pin[i])
         cp_async_piece<Pix>(dst + 128 * i, src + 128 * i);
-      else if (pok[i])
+      else
         fill_piece_masked<Pix>(dst + 128 * i);
     }
   };
   if (kRing) {
-    // The pixels past the fetched pieces (read by lane 31 only) stay masked.
-    for (int i = 4 * kRingPieces + lane; i < kRingSlots * kRingStride; i += 32)
-      if (i % kRingStride >= 4 * kRingPieces)
-        ring[i] = (Pix)~0u;
 #pragma unroll
     for (int i = 0; i < kRingSlots - 1; i++) {
       fetch(pbeg + i);
@@ -337,7 +343,7 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
     }
   }
 
-  uint32_t v[16];
+  uint32_t v[kLatCols];
   if constexpr (!kRing)
     lat_load(reinterpret_cast<const uint32_t *>(image), height, width, interior, cx, pbeg, v);
   for (int t = 0; t < ntrip + 3; t++) {
@@ -346,7 +352,7 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       const int p = p0 + k;
-      uint32_t nxt[16];
+      uint32_t nxt[kLatCols];
       if (kRing) {
         // Row p + kRingSlots - 1 goes out; row p has landed.
         __syncwarp();
@@ -358,7 +364,7 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
         if constexpr (k16) {
           const uint2 *src = reinterpret_cast<const uint2 *>(slot + kLatCols * lane);
 #pragma unroll
-          for (int i = 0; i < 4; i++) {
+          for (int i = 0; i < kLatCols / 4; i++) {
             const uint2 x = src[i];
             v[4 * i] = x.x & 0xFFFFu, v[4 * i + 1] = x.x >> 16;
             v[4 * i + 2] = x.y & 0xFFFFu, v[4 * i + 3] = x.y >> 16;
@@ -366,7 +372,7 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
         } else {
           const uint4 *src = reinterpret_cast<const uint4 *>(slot) + 3 * lane;
 #pragma unroll
-          for (int i = 0; i < 4; i++) {
+          for (int i = 0; i < kLatCols / 4; i++) {
             const uint4 x = src[i];
             v[4 * i] = x.x, v[4 * i + 1] = x.y, v[4 * i + 2] = x.z, v[4 * i + 3] = x.w;
           }
@@ -376,11 +382,11 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
         lat_load(reinterpret_cast<const uint32_t *>(image), height, width, interior, cx,
                  p + 1, nxt);
       }
-      uint32_t hn[4], hq[4], mh;
-      lat_row<Pix>(v, hn, hq, &mcur[k], &mh);
+      uint32_t hn[4], hq[4];
+      lat_row<Pix>(v, lane, hn, hq, &mcur[k]);
       if (!kRing) {
 #pragma unroll
-        for (int i = 0; i < 16; i++)
+        for (int i = 0; i < kLatCols; i++)
           v[i] = nxt[i];
       }
 #pragma unroll
@@ -389,10 +395,10 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
         Tq[a] = k == 0 ? hq[a] : Tq[a] + hq[a];
       }
       if (k == 2) {
-        // Masked centres of this row's lattice columns -1, 2, 5, 8: the
+        // Masked centres of this row's lattice columns 2, 5, 8, 11: the
         // lattice row the next triple decides.
         const uint32_t m12 = mcur[2];
-        cm = mh | ((m12 >> 1) & 2u) | ((m12 >> 3) & 4u) | ((m12 >> 5) & 8u);
+        cm = ((m12 >> 2) & 1u) | ((m12 >> 4) & 2u) | ((m12 >> 6) & 4u) | ((m12 >> 8) & 8u);
 #pragma unroll
         for (int a = 0; a < 4; a++) {
           // Window rows p0 - 4 .. p0 + 2, centred on the previous triple's
@@ -434,7 +440,8 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
       }
       b4 |= sig ? 1u << a : 0u;
     }
-    const uint32_t b5 = b4 | (__shfl_down_sync(0xffffffffu, b4, 1) & 1u) << 4;
+    // The bound bits at columns -1 (the lane before's 11), 2, 5, 8, 11.
+    const uint32_t b5 = b4 << 1 | (__shfl_sync(0xffffffffu, b4, (lane + 31) & 31) >> 3 & 1u);
     if (t >= 3) {
       // The previous triple's rows p0 - 3 .. p0 - 1: the first two see the
       // lattice rows p0 - 4 and p0 - 1, the last only p0 - 1.
@@ -445,13 +452,13 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
         const uint32_t bd = k < 2 ? bd01 : bd2;
         const uint32_t mk = mprev[k];
         const uint32_t c12 = bd & ~mk & inside12, s12 = (bd | mk) & inside12;
-        // Lane pairs: the even lane writes the pair's first two bytes, the
-        // odd lane the third.
+        // Lane pairs: the first lane (odd) writes the pair's first two bytes,
+        // the second the third.
         const uint32_t mine = c12 | s12 << 16;
         const uint32_t odd = __shfl_down_sync(0xffffffffu, mine, 1);
         if (writer && r < rb) {
           const size_t at = (size_t)r * bytes_per_row;
-          if ((lane & 1) == 0) {
+          if (first_of_pair) {
             if (pair_byte < bytes_per_row) {
               fin[at + pair_byte] = (uint8_t)c12;
               scr1[at + pair_byte] = (uint8_t)s12;
