@@ -46,6 +46,9 @@ constexpr int kGrid = 2 * 152;          // the bucket partition's chunks
 constexpr int kPassGrid = 8 * 152;      // grid-stride passes over pixels / candidates
 constexpr int kSortGrid = 6 * 152;      // warp sorts: 6 blocks an SM (registers)
 constexpr int kWarpSortMax = 1024;      // members sorted by one warp
+constexpr int kWarpSegMax = 64;         // runs a warp orders without sorting the members
+constexpr uint32_t kRunHead = 0x80000000u;  // a member slot's flag: the first of its run
+constexpr uint32_t kPosMask = 0x7FFFFFFFu;  // a member slot's position (below 2^31)
 constexpr int kBlockSortMax = 8192;     // members sorted by one block
 constexpr int kUnionRetries = 1 << 20;  // cap on a union's CAS retries
 // Frames up to this many rows get per-row start tables, so that a pixel's
@@ -632,8 +635,11 @@ __global__ void k_gather(LabelStatus *st, const uint32_t *__restrict__ root,
     return;
   const uint32_t n = st->n_total;
   const int lane = threadIdx.x & 31;
-  // The lanes of one candidate take their member slots with one atomic (the
-  // members are sorted afterwards, so their order here does not matter).
+  // The lanes of one candidate take their member slots with one atomic: a
+  // run of slots whose positions ascend, from this warp's 32 positions,
+  // which no other warp's run shares. The run's first slot is flagged
+  // (kRunHead: positions are below 2^31, the pool's limit), so that k_sort
+  // can order the runs instead of the members.
   for (uint32_t p0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); p0 < n;
        p0 += gridDim.x * blockDim.x) {
     const uint32_t p = p0 + lane;
@@ -645,7 +651,8 @@ __global__ void k_gather(LabelStatus *st, const uint32_t *__restrict__ root,
       slot = atomicAdd(&cursor[c], (uint32_t)__popc(same));
     slot = __shfl_sync(0xffffffffu, slot, leader);
     if (c != kNone)
-      members[cand_off[c] + slot + __popc(same & ((1u << lane) - 1u))] = p;
+      members[cand_off[c] + slot + __popc(same & ((1u << lane) - 1u))] =
+          p | (lane == leader ? kRunHead : 0u);
   }
 }
 
@@ -920,8 +927,12 @@ __device__ __forceinline__ void put_member(uint32_t q, uint32_t k, uint32_t c, u
 
 // Candidates of up to kWarpSortMax members, a warp each (BLOCK false), or of
 // up to kBlockSortMax, a block each (BLOCK true, from the list the warps
-// made): member positions sorted in shared memory by bitonic sort, then
-// copied out in member order as pixel records.
+// made): member positions put in ascending order in shared memory, then
+// copied out in member order as pixel records. A warp's candidate of at most
+// kWarpSegMax runs (k_gather's runs of ascending positions, each from its
+// own range of positions) is ordered by its runs: a run's place is the
+// total length of the runs whose first position is smaller. Others are
+// sorted by bitonic sort.
 template <bool BLOCK>
 __global__ void __launch_bounds__(kThreads)
 k_sort(LabelStatus *st, const uint32_t *__restrict__ cand_n,
@@ -935,7 +946,8 @@ k_sort(LabelStatus *st, const uint32_t *__restrict__ cand_n,
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
   if (!BLOCK) {
-    uint32_t *s = s_sort + warp * kWarpSortMax;
+    uint32_t *s = s_sort + warp * (kWarpSortMax + 2 * kWarpSegMax);
+    uint32_t *seg = s + kWarpSortMax;  // runs: first slots, then first positions / places
     for (uint32_t c = blockIdx.x * nwarps + warp; c < ncand; c += gridDim.x * nwarps) {
       const uint32_t n = cand_n[c];
       if (n > (uint32_t)kWarpSortMax) {
@@ -946,13 +958,71 @@ k_sort(LabelStatus *st, const uint32_t *__restrict__ cand_n,
       const uint32_t off = cand_off[c];
       const uint32_t *m = members + off;
       if (n <= 32) {
-        const uint32_t q = warp_sort32(lane < (int)n ? m[lane] : kNone, (int)n, lane);
+        const uint32_t q =
+            warp_sort32(lane < (int)n ? m[lane] & kPosMask : kNone, (int)n, lane);
         if (lane < (int)n)
           put_member(q, lane, c, off, frame, index, value, mpix, mcand);
         continue;
       }
+      // The slots into shared memory (flags kept), the runs' first slots and
+      // positions noted.
+      uint32_t nrun = 0;
+      for (uint32_t b = 0; b < n; b += 32) {  // warp-uniform
+        const uint32_t i = b + lane;
+        const uint32_t x = i < n ? m[i] : 0u;
+        const bool head = (x & kRunHead) != 0u;
+        if (i < n)
+          s[i] = x;
+        const unsigned bal = __ballot_sync(0xffffffffu, head);
+        const uint32_t k = nrun + (uint32_t)__popc(bal & ((1u << lane) - 1u));
+        if (head && k < (uint32_t)kWarpSegMax) {
+          seg[k] = i;
+          seg[kWarpSegMax + k] = x & kPosMask;
+        }
+        nrun += (uint32_t)__popc(bal);
+      }
+      __syncwarp();
+      if (nrun <= (uint32_t)kWarpSegMax && seg[0] == 0u) {  // slot 0 always heads a run
+        // A lane's runs j = lane and lane + 32: their first positions, then
+        // the total length of the runs whose first position is smaller.
+        uint32_t first[2], place[2] = {0u, 0u};
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const uint32_t j = (uint32_t)lane + 32u * h;
+          first[h] = j < nrun ? seg[kWarpSegMax + j] : kNone;
+        }
+        for (uint32_t t = 0; t < nrun; t++) {  // warp-uniform
+          const uint32_t ft = seg[kWarpSegMax + t];
+          const uint32_t lt = (t + 1 < nrun ? seg[t + 1] : n) - seg[t];
+#pragma unroll
+          for (int h = 0; h < 2; h++)
+            place[h] += ft < first[h] ? lt : 0u;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const uint32_t j = (uint32_t)lane + 32u * h;
+          if (j < nrun)
+            seg[kWarpSegMax + j] = place[h];
+        }
+        __syncwarp();
+        uint32_t runs = 0;
+        for (uint32_t b = 0; b < n; b += 32) {  // warp-uniform
+          const uint32_t i = b + lane;
+          const uint32_t x = i < n ? s[i] : 0u;
+          const unsigned bal = __ballot_sync(0xffffffffu, (x & kRunHead) != 0u);
+          // The run of slot i: the last head at or before it.
+          const uint32_t g = runs + (uint32_t)__popc(bal & ((2u << lane) - 1u)) - 1u;
+          runs += (uint32_t)__popc(bal);
+          if (i < n)
+            put_member(x & kPosMask, seg[kWarpSegMax + g] + (i - seg[g]), c, off, frame, index,
+                       value, mpix, mcand);
+        }
+        __syncwarp();  // the next candidate reuses the shared rows
+        continue;
+      }
       for (uint32_t i = lane; i < n; i += 32)
-        s[i] = m[i];
+        s[i] &= kPosMask;
       __syncwarp();
       bitonic_sort(s, (int)n, lane, 32, true);
       for (uint32_t i = lane; i < n; i += 32)
@@ -969,7 +1039,7 @@ k_sort(LabelStatus *st, const uint32_t *__restrict__ cand_n,
       const uint32_t off = cand_off[c];
       const uint32_t *m = members + off;
       for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
-        s_sort[i] = m[i];
+        s_sort[i] = m[i] & kPosMask;
       __syncthreads();
       bitonic_sort(s_sort, (int)n, threadIdx.x, blockDim.x, false);
       for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
@@ -1001,6 +1071,9 @@ k_sort_big(LabelStatus *st, const uint32_t *__restrict__ cand_n,
       continue;
     const uint32_t off = cand_off[c];
     uint32_t *m = members + off;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+      m[i] &= kPosMask;  // the run flags (k_gather)
+    __syncthreads();
     uint32_t size = 1;
     while (size < n)
       size <<= 1;
@@ -1696,7 +1769,8 @@ struct Labeller {
                             err, s)) != cudaSuccess)
       return e;
     k_gather<<<kPassGrid, kThreads, 0, s>>>(st, root, candid, cand_off, cursor, members);
-    k_sort<false><<<kSortGrid, kThreads, (kThreads / 32) * kWarpSortMax * 4, s>>>(
+    k_sort<false><<<kSortGrid, kThreads,
+                    (kThreads / 32) * (kWarpSortMax + 2 * kWarpSegMax) * 4, s>>>(
         st, cand_n, cand_off, members, frame[c], index[c], value[c], mpix, mcand, big);
     k_sort<true><<<kGrid / 2, kThreads, kBlockSortMax * 4, s>>>(
         st, cand_n, cand_off, members, frame[c], index[c], value[c], mpix, mcand, big);
