@@ -42,6 +42,104 @@ CHUNKS = [  # shape, dtype, algorithm, block bytes
 ]
 
 
+# Sequences of every shape the device's windowed parse treats differently:
+# literal runs of 0-14 bytes (taken a 32-byte window at a time) and of 15 or
+# more (the byte-by-byte parse), match lengths with no extra byte, one extra
+# byte up to 254 and a 255 (a second extra byte), offsets 1 (a run), 2-31
+# (patterns copied in doubling passes), and longer (whole copies, words for
+# long ones, every source alignment), and sequences that start anywhere in a
+# window, so that some straddle its end.
+_LITS = [0, 0, 0, 0, 1, 1, 2, 3, 4, 5, 7, 11, 13, 14, 15, 16, 17, 33, 270, 300]
+_MLS = [4, 4, 5, 6, 7, 9, 12, 16, 18, 19, 20, 31, 32, 33, 47, 63, 64, 65, 100, 128, 129,
+        200, 272, 273, 274, 300, 512, 513, 600, 1000]
+_OFFS = [1, 2, 3, 4, 5, 6, 7, 8, 9, 13, 16, 17, 31, 32, 33, 63, 100, 126, 127, 128, 129,
+         130, 255, 256, 257, 300, 1000, 4095]
+
+
+def _lz4_length(blk, v):
+    while v >= 255:
+        blk.append(255)
+        v -= 255
+    blk.append(v)
+
+
+def _lz4_random_block(rng, total):
+    """One LZ4 block of random sequences that decodes to `total` bytes (at
+    least 13), keeping LZ4's end-of-block rules (a final literal run of 12
+    bytes or more); returns (block, decoded bytes)."""
+    out, blk = bytearray(), bytearray()
+    while True:
+        left = total - len(out)
+        nl = int(rng.choice(_LITS))
+        ml = int(rng.choice(_MLS))
+        if len(out) + nl == 0:
+            nl = 1
+        if nl + ml + 12 > left:
+            break
+        lits = rng.integers(0, 3 if rng.random() < 0.7 else 256, nl, dtype=np.uint8)
+        off = min(int(rng.choice(_OFFS)), len(out) + nl)
+        blk.append(min(nl, 15) << 4 | min(ml - 4, 15))
+        if nl >= 15:
+            _lz4_length(blk, nl - 15)
+        blk += lits.tobytes()
+        blk += off.to_bytes(2, "little")
+        if ml - 4 >= 15:
+            _lz4_length(blk, ml - 19)
+        out += lits.tobytes()
+        for _ in range(ml):
+            out.append(out[-off])
+    nl = total - len(out)
+    blk.append(min(nl, 15) << 4)
+    if nl >= 15:
+        _lz4_length(blk, nl - 15)
+    blk += rng.integers(0, 256, nl, dtype=np.uint8).tobytes()
+    out += blk[len(blk) - nl:]
+    return bytes(blk), bytes(out)
+
+
+def _lz4_chunk(block, n):
+    """A one-block "lz4" chunk of n decoded bytes."""
+    return n.to_bytes(8, "big") + bytes(4) + len(block).to_bytes(4, "big") + block
+
+
+def _bslz4_chunk(rng, elem, nblocks):
+    """A "bslz4" chunk of nblocks 8192-byte blocks of random sequences (the
+    bit planes of 8192 // elem elements each); returns (chunk, frame bytes),
+    the frame from the planes by bitshuffle's definition."""
+    blocks, frame = [], bytearray()
+    n = 8192 // elem
+    for _ in range(nblocks):
+        blk, planes = _lz4_random_block(rng, 8192)
+        blocks.append(blk)
+        bits = np.unpackbits(np.frombuffer(planes, np.uint8).reshape(8 * elem, n // 8),
+                             axis=1, bitorder="little")  # [plane 8j + k][element]
+        vals = np.zeros(n, np.uint64)
+        for r in range(8 * elem):
+            vals |= bits[r].astype(np.uint64) << np.uint64(r)
+        frame += vals.astype({2: np.uint16, 4: np.uint32}[elem]).tobytes()
+    hdr = len(frame).to_bytes(8, "big") + (8192).to_bytes(4, "big")
+    body = b"".join(len(b).to_bytes(4, "big") + b for b in blocks)
+    return hdr + body, bytes(frame)
+
+
+def test_random_sequences_are_lz4_blocks():
+    # The crafted blocks decode, by the oracle, to what their sequences say;
+    # where the LZ4 library is at hand it reads them too.
+    rng = np.random.default_rng(11)
+    pa = None
+    try:
+        import pyarrow as pa
+    except ImportError:
+        pass
+    for total in [13, 40, 100, 1000, 8192, 20000]:
+        for _ in range(4):
+            blk, out = _lz4_random_block(rng, total)
+            assert O.lz4_decode(blk, total) == out
+            if pa is not None:
+                assert pa.decompress(blk, decompressed_size=total, codec="lz4_raw",
+                                     asbytes=True) == out
+
+
 # ---------------------------------------------------------------------------
 # The oracle and the chunk writer, on the CPU.
 # ---------------------------------------------------------------------------
@@ -281,6 +379,53 @@ def test_device_accepts_what_the_lz4_library_accepts(api):
     f = _frame(20, 30, np.uint32, 5)
     from sfgb import synth
     assert np.array_equal(api.decompress_image(synth.chunk(f), "bslz4", 32, 20, 30), f)
+
+
+@pytest.mark.gpu
+def test_device_decodes_random_sequences(api):
+    # Every sequence shape of the windowed parse, in plain LZ4 blocks
+    # (decoded straight into the frame) and in bitshuffle blocks of 16- and
+    # 32-bit pixels (decoded in shared memory: byte copies and word copies).
+    rng = np.random.default_rng(12)
+    for total in [13, 31, 32, 33, 64, 100, 1000, 8192, 20000, 65536]:
+        for _ in range(3):
+            blk, out = _lz4_random_block(rng, total)
+            got = api.decompress_image(_lz4_chunk(blk, total), "lz4", 8, 1, total)
+            assert got.tobytes() == out, total
+    for elem in (2, 4):
+        for nblocks in (1, 3, 16):
+            chunk, frame = _bslz4_chunk(rng, elem, nblocks)
+            w = len(frame) // elem
+            want = O.decompress_image(chunk, "bslz4", 8 * elem, 1, w)
+            assert want.tobytes() == frame
+            got = api.decompress_image(chunk, "bslz4", 8 * elem, 1, w)
+            assert got.tobytes() == frame, (elem, nblocks)
+
+
+@pytest.mark.gpu
+def test_device_refuses_what_the_oracle_refuses(api):
+    # Random sequences with bytes changed at random: the device accepts the
+    # block with the oracle's bytes, or refuses it, as the oracle does.
+    rng = np.random.default_rng(13)
+    refused = 0
+    for case in range(200):
+        total = int(rng.choice([40, 300, 2000, 8192]))
+        blk, _ = _lz4_random_block(rng, total)
+        bad = bytearray(blk)
+        for _ in range(int(rng.integers(1, 4))):
+            bad[int(rng.integers(0, len(bad)))] = int(rng.integers(0, 256))
+        chunk = _lz4_chunk(bytes(bad), total)
+        try:
+            want = O.decompress_image(chunk, "lz4", 8, 1, total)
+        except RuntimeError as e:
+            with pytest.raises(api.DataError) as d:
+                api.decompress_image(chunk, "lz4", 8, 1, total)
+            assert str(d.value).startswith("lz4 "), case
+            refused += 1
+            continue
+        got = api.decompress_image(chunk, "lz4", 8, 1, total)
+        assert got.tobytes() == want.tobytes(), case
+    assert 20 < refused < 200
 
 
 @pytest.mark.gpu
