@@ -3,10 +3,15 @@
 //
 //   lat_stage01  stage 0 on a lattice of every third row and every third
 //                column only, and the erosion of that lattice: an upper bound
-//                of the eroded mask, written as the eroded and candidate masks
+//                of the eroded mask, written as the candidate mask
 //   lat_verify   the exact stage 0 and erosion on the 8 x 28 tiles that hold
-//                a candidate of the bound; the candidates that fail leave both
-//                masks, which are then the reference's
+//                a candidate of the bound; the candidates that fail leave the
+//                mask, which is then the reference's candidate mask
+//
+// The reference's eroded mask (stage 1's signal after the erosion, which
+// stage 2 keeps out of each background) is the candidate mask with the
+// masked pixels added, and stage 2 reads it so: the candidate mask's bits
+// and its staged pixels' masked values. No separate eroded mask is written.
 //
 // Why the bound holds. The erosion (src/spots/dext.cc:117-142) keeps a valid
 // pixel only if every in-frame pixel of its 5 x 5 neighbourhood is signal or
@@ -258,8 +263,8 @@ __global__ void __launch_bounds__(kLatWarps * 32, kOcc)
 lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
             const __grid_constant__ FrameSpans S, int run_rows,
             const __grid_constant__ StreamTables T,
-            const __grid_constant__ LaunchParams P, uint8_t *__restrict__ scr1_bytes,
-            uint8_t *__restrict__ final_bytes, size_t mask_bytes) {
+            const __grid_constant__ LaunchParams P, uint8_t *__restrict__ final_bytes,
+            size_t mask_bytes) {
   constexpr bool k16 = sizeof(Pix) == 2;
   static_assert(!k16 || kRing, "16-bit frames take the ring variant only");
   extern __shared__ __align__(16) unsigned char lat_ring_raw[];
@@ -284,7 +289,6 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
   const int height = F.h[f], width = F.w[f];
   const Pix *image = reinterpret_cast<const Pix *>(F.image[f]);
   const int bytes_per_row = ((width + 31) >> 5) * 4;
-  uint8_t *scr1 = scr1_bytes + (size_t)f * mask_bytes;
   uint8_t *fin = final_bytes + (size_t)f * mask_bytes;
   // Lane l holds columns X + 12 (l - 1) .. + 11: lanes 1-30 the strip's
   // 360, lane 0 the 12 before it, lane 31 the 12 after it.
@@ -451,25 +455,19 @@ lat_stage01(const __grid_constant__ FramePtrs F, int nframes, int vec,
         const int r = p0 - 3 + k;
         const uint32_t bd = k < 2 ? bd01 : bd2;
         const uint32_t mk = mprev[k];
-        const uint32_t c12 = bd & ~mk & inside12, s12 = (bd | mk) & inside12;
+        const uint32_t c12 = bd & ~mk & inside12;
         // Lane pairs: the first lane (odd) writes the pair's first two bytes,
         // the second the third.
-        const uint32_t mine = c12 | s12 << 16;
-        const uint32_t odd = __shfl_down_sync(0xffffffffu, mine, 1);
+        const uint32_t odd = __shfl_down_sync(0xffffffffu, c12, 1);
         if (writer && r < rb) {
           const size_t at = (size_t)r * bytes_per_row;
           if (first_of_pair) {
-            if (pair_byte < bytes_per_row) {
+            if (pair_byte < bytes_per_row)
               fin[at + pair_byte] = (uint8_t)c12;
-              scr1[at + pair_byte] = (uint8_t)s12;
-            }
-            if (pair_byte + 1 < bytes_per_row) {
+            if (pair_byte + 1 < bytes_per_row)
               fin[at + pair_byte + 1] = (uint8_t)((c12 >> 8) | (odd & 0xFu) << 4);
-              scr1[at + pair_byte + 1] = (uint8_t)((s12 >> 8) | ((odd >> 16) & 0xFu) << 4);
-            }
           } else if (pair_byte + 2 < bytes_per_row) {
             fin[at + pair_byte + 2] = (uint8_t)(c12 >> 4);
-            scr1[at + pair_byte + 2] = (uint8_t)(s12 >> 4);
           }
         }
       }
@@ -800,8 +798,8 @@ template <int kOcc, typename Pix>
 __global__ void __launch_bounds__(kVerWarps * 32, kOcc)
 lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps M, int tma,
            int env_h, int env_w, int vec, const __grid_constant__ LaunchParams P,
-           const __grid_constant__ StreamTables T, uint32_t *__restrict__ scr1_all,
-           uint32_t *__restrict__ final_all, size_t words, const uint32_t *__restrict__ list,
+           const __grid_constant__ StreamTables T, uint32_t *__restrict__ final_all, size_t words,
+           const uint32_t *__restrict__ list,
            uint32_t *__restrict__ counters, FastDiv by_ntiles, FastDiv by_ntx,
            uint32_t *__restrict__ list2) {
   extern __shared__ __align__(128) unsigned char ver_smem_raw[];
@@ -1005,8 +1003,7 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
       D[d] = __ballot_sync(0xffffffffu, (keep >> d) & 1u);
     __syncwarp();  // the next tile rewrites the shared rows
     // The exact erosion of the tile's rows; the candidates that fail leave
-    // both masks, and a tile with a candidate left goes on stage 2's list.
-    uint32_t *scr1 = scr1_all + (size_t)f * words;
+    // the mask, and a tile with a candidate left goes on stage 2's list.
     uint32_t *fin = final_all + (size_t)f * words;
     uint32_t left = 0;
 #pragma unroll
@@ -1026,7 +1023,6 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
         const uint32_t part = (uint32_t)(c64 >> (32 * lane));
         if (part && w0 + lane < wpr) {
           const size_t at = (size_t)(r0 + o) * wpr + w0 + lane;
-          atomicAnd(scr1 + at, ~part);
           atomicAnd(fin + at, ~part);
         }
       }
@@ -1044,8 +1040,9 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
 // Stage 2 (src/spots/dext.cc:151-222) on the listed tiles, after the exact
 // check: a candidate's background is the valid pixels of its clipped 11 x 11
 // window outside the eroded mask, and the tile's 18 x 38 pixels hold every
-// window of its candidates. A warp stages them with the eroded-mask words
-// over them (cp.async, the next tile's while it works on this one), takes
+// window of its candidates. A warp stages them with the candidate-mask words
+// over them (cp.async, the next tile's while it works on this one; a pixel is
+// in the eroded mask when its bit is set or it is masked), takes
 // column sums of 11 rows once per tile, then per candidate adds 11 of them
 // and runs the reference's test (sf_common.cuh). The result goes to the
 // candidate's place in the ascending candidate list, from the per-word list
@@ -1055,7 +1052,7 @@ lat_verify(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
 template <typename Pix> struct alignas(128) S2Warp {
   TileBuf<Pix> pix[2];              // staged pixels, two tiles
   uint64_t bar[2];                  // their TMA mbarriers
-  uint32_t ew[2][kVerPR][3];        // eroded-mask words over the staged columns
+  uint32_t ew[2][kVerPR][3];        // candidate-mask words over the staged columns
   uint32_t cw[2][kVerRows][2];      // candidate-mask words of the tile's rows
   uint32_t pw[2][kVerRows][2];      // their list positions
   uint2 cs[kVerRows][kVerPC + 2];   // {count, sum} of 11 rows of background
@@ -1066,7 +1063,6 @@ __device__ __forceinline__ void s2_stage(S2Warp<Pix> &sm, int s, uint32_t e, con
                                          const TileMaps &M, int tma, int vec, uint32_t ntiles,
                                          int ntx, const FastDiv &by_ntiles,
                                          const FastDiv &by_ntx,
-                                         const uint32_t *__restrict__ scr1_all,
                                          const uint32_t *__restrict__ final_all,
                                          const uint32_t *__restrict__ prefix_all, size_t words,
                                          int lane) {
@@ -1080,13 +1076,13 @@ __device__ __forceinline__ void s2_stage(S2Warp<Pix> &sm, int s, uint32_t e, con
     stage_pixels<Pix>(sm.pix[s].px, reinterpret_cast<const Pix *>(F.image[f]), height, width,
                       vec, r0, xs, lane);
   const int wpr = (width + 31) >> 5;
-  const uint32_t *scr1 = scr1_all + (size_t)f * words;
+  const uint32_t *fin = final_all + (size_t)f * words;
   for (int k = lane; k < kVerPR * 3; k += 32) {
     const int r = k / 3, j = k - 3 * r;
     const int y = r0 - 5 + r, wd = (xs >> 5) + j;
     uint32_t *dst = &sm.ew[s][r][j];
     if (y >= 0 && y < height && wd >= 0 && wd < wpr)
-      cp_async4(dst, scr1 + (size_t)y * wpr + wd);
+      cp_async4(dst, fin + (size_t)y * wpr + wd);
     else
       *dst = 0u;
   }
@@ -1108,8 +1104,8 @@ template <int kOcc, typename Pix>
 __global__ void __launch_bounds__(kVerWarps * 32, kOcc)
 lat_stage2(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps M, int tma,
            int env_h, int env_w, int vec, const __grid_constant__ LaunchParams P,
-           const uint32_t *__restrict__ scr1_all, const uint32_t *__restrict__ final_all,
-           const uint32_t *__restrict__ prefix_all, size_t words,
+           const uint32_t *__restrict__ final_all, const uint32_t *__restrict__ prefix_all,
+           size_t words,
            const uint32_t *__restrict__ list, uint32_t *__restrict__ counters,
            uint32_t *__restrict__ cand_all, uint2 *__restrict__ res_all, uint32_t cand_cap,
            FastDiv by_ntiles, FastDiv by_ntx) {
@@ -1153,14 +1149,14 @@ lat_stage2(const __grid_constant__ FramePtrs F, const __grid_constant__ TileMaps
   uint32_t e = next_live(blockIdx.x * kVerWarps + (threadIdx.x >> 5), &k);
   uint32_t e1 = next_live(k + nw, &k1);
   if (k < count)
-    s2_stage<Pix>(sm, 0, e, F, M, tma, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
-                  final_all, prefix_all, words, lane);
+    s2_stage<Pix>(sm, 0, e, F, M, tma, vec, ntiles, ntx, by_ntiles, by_ntx, final_all,
+                  prefix_all, words, lane);
   cp_async_commit();
   uint32_t inflight = k < count ? 1u : 0u;  // bit b: a TMA load into buffer b not waited for
   for (int s = 0; k < count; s ^= 1) {
     if (k1 < count) {
-      s2_stage<Pix>(sm, s ^ 1, e1, F, M, tma, vec, ntiles, ntx, by_ntiles, by_ntx, scr1_all,
-                    final_all, prefix_all, words, lane);
+      s2_stage<Pix>(sm, s ^ 1, e1, F, M, tma, vec, ntiles, ntx, by_ntiles, by_ntx, final_all,
+                    prefix_all, words, lane);
       inflight |= 2u >> s;
     }
     cp_async_commit();
@@ -1381,7 +1377,7 @@ cudaError_t lattice_stage2(const FramePtrs &F, int nframes, int h, int w, int ve
   TileMaps M;
   const int tma = make_tile_maps<Pix>(F, nframes, h, w, &M);
   lat_stage2<kS2Occ, Pix><<<blocks * device_sms(), kVerWarps * 32, s2_smem_bytes<Pix>(),
-                             stream>>>(F, M, tma, h, w, vec, P, b.scr1, b.bits, prefix, b.words,
+                             stream>>>(F, M, tma, h, w, vec, P, b.bits, prefix, b.words,
                                        list, b.counters, b.cand, b.res, b.cand_cap,
                                        make_fastdiv((uint32_t)tiles),
                                        make_fastdiv((uint32_t)ver_ntx(w)));
@@ -1406,13 +1402,13 @@ cudaError_t lattice(const FramePtrs &F, int nframes, int h, int w, int vec, cons
   }
   const size_t mask_bytes = b.words * sizeof(uint32_t);
   const unsigned lb = (unsigned)((S.start[nframes] + kLatWarps - 1) / kLatWarps);
-  uint8_t *scr1 = reinterpret_cast<uint8_t *>(b.scr1), *fin = reinterpret_cast<uint8_t *>(b.bits);
+  uint8_t *fin = reinterpret_cast<uint8_t *>(b.bits);
   if (sizeof(Pix) == 2 || vec)
     lat_stage01<kLatOcc, true, Pix><<<lb, kLatWarps * 32, ring_bytes<Pix>(), stream>>>(
-        F, nframes, vec, S, run_rows, T, P, scr1, fin, mask_bytes);
+        F, nframes, vec, S, run_rows, T, P, fin, mask_bytes);
   else
     lat_stage01<kLatOcc, false, uint32_t><<<lb, kLatWarps * 32, 0, stream>>>(
-        F, nframes, vec, S, run_rows, T, P, scr1, fin, mask_bytes);
+        F, nframes, vec, S, run_rows, T, P, fin, mask_bytes);
   static std::once_flag configured;
   static cudaError_t config_error = cudaSuccess;
   static int ver_blocks = 0;
@@ -1449,7 +1445,7 @@ cudaError_t lattice(const FramePtrs &F, int nframes, int h, int w, int vec, cons
   TileMaps M;
   const int tma = make_tile_maps<Pix>(F, nframes, h, w, &M);
   lat_verify<kVerOcc, Pix><<<ver_blocks * device_sms(), kVerWarps * 32, ver_smem_bytes<Pix>(),
-                             stream>>>(F, M, tma, h, w, vec, P, T, b.scr1, b.bits, b.words, list,
+                             stream>>>(F, M, tma, h, w, vec, P, T, b.bits, b.words, list,
                                        b.counters, by_ntiles, by_ntx,
                                        list + (size_t)nframes * tiles);
   return cudaGetLastError();

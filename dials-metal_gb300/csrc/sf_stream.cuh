@@ -126,8 +126,9 @@ cudaError_t launch_lattice_stage2(const FramePtrs &frames, int nframes, int h, i
                                   int pixel_bytes, const LaunchParams &P, const StreamBuffers &b,
                                   cudaStream_t stream);
 // Stage 0 and the erosion for kernel 3,3: the lattice bound, then the exact
-// check of its candidates; writes b.scr1 and b.bits as the first pass of
-// launch_stream does (vec: the frames allow 16-byte loads).
+// check of its candidates; writes b.bits as the first pass of launch_stream
+// does (vec: the frames allow 16-byte loads). b.scr1 is not used: stage 2
+// takes the eroded mask as b.bits plus the masked pixels.
 // pixel_bytes 4 (32-bit frames) or 2 (16-bit frames: 4 | w, 8-byte aligned).
 cudaError_t launch_lattice(const FramePtrs &frames, int nframes, int h, int w, int vec,
                            int pixel_bytes, const LaunchParams &P, const StreamTables &T,
