@@ -56,7 +56,7 @@ H, W = 4362, 4148
 # capture of this bench without cache flushes between kernels (11,235 MB for
 # the launch: lat_stage01 5,266 MB, lat_verify 2,098 MB, lat_stage2 2,621 MB,
 # the scans and the list 1,250 MB); the algorithmic bytes are 76.5 MB a frame.
-DRAM_BYTES_PER_FRAME = 169.1e6
+DRAM_BYTES_PER_FRAME = 161.2e6
 
 
 # Kernels a timed step launches: the threshold plan's graph (lat_stage01,
@@ -1015,7 +1015,7 @@ def run_ours(args):
                 "32-frame launch of this workload (32 frames in HBM, the size a capture may "
                 "hold), no cache flush between kernels "
                 f"({DRAM_BYTES_PER_FRAME / 1e6:.1f} MB a frame), times the {B} frames of a launch; "
-                "a frame's traffic grows a little with the batch (16 frames: 163.2 MB)")
+                "a frame's traffic grows a little with the batch")
         line = {
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
