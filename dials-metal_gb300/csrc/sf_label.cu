@@ -484,6 +484,14 @@ __global__ void k_closing_list(LabelStatus *st, const BatchArgs *__restrict__ ap
 // Stable partition of the closing roots by emission event.
 constexpr int kBuckets = kLabelMaxBatch + 1;
 
+// This block's share [lo, hi) of n items (the histogram and the scatter
+// split them alike).
+__device__ __forceinline__ void bucket_chunk(uint32_t n, uint32_t *lo, uint32_t *hi) {
+  const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  *lo = min(n, blockIdx.x * chunk);
+  *hi = min(n, *lo + chunk);
+}
+
 __global__ void __launch_bounds__(kThreads)
 k_bucket_hist(LabelStatus *st, const uint32_t *__restrict__ cbucket, uint32_t *hist) {
   if (st->error)
@@ -493,7 +501,7 @@ k_bucket_hist(LabelStatus *st, const uint32_t *__restrict__ cbucket, uint32_t *h
     h[b] = 0;
   __syncthreads();
   uint32_t lo, hi;
-  scan_chunk(st->n_closing, &lo, &hi);
+  bucket_chunk(st->n_closing, &lo, &hi);
   for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x)
     atomicAdd(&h[cbucket[k]], 1u);
   __syncthreads();
@@ -543,7 +551,7 @@ k_bucket_scatter(LabelStatus *st, const uint32_t *__restrict__ clist,
   for (int b = threadIdx.x; b < kBuckets; b += blockDim.x)
     running[b] = hist[blockIdx.x * kBuckets + b];
   uint32_t lo, hi;
-  scan_chunk(st->n_closing, &lo, &hi);
+  bucket_chunk(st->n_closing, &lo, &hi);
   for (uint32_t base = lo; base < hi; base += blockDim.x) {
     for (int i = threadIdx.x; i < W * kBuckets; i += blockDim.x)
       (&wcnt[0][0])[i] = 0;

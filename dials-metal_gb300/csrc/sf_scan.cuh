@@ -1,7 +1,9 @@
 // Device-wide exclusive scan of uint32 values whose count lives on the
 // device, so a pipeline of kernels never has to read a size back to the host.
 // Three launches on a fixed grid: per-block chunk sums, a one-block scan of
-// those, then each block rescans its chunk with its offset.
+// those, then each block rescans its chunk with its offset. A thread takes
+// kScanItems consecutive values (two 16-byte loads where the chunk allows),
+// so a block scans kScanThreads * kScanItems values a step.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -11,6 +13,8 @@ namespace sf {
 
 constexpr int kScanBlocks = 512;
 constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr uint32_t kScanStep = kScanThreads * kScanItems;  // values a block step
 
 // Block-wide exclusive scan of one value per thread; returns the exclusive
 // prefix and writes the block total to *total (all threads see it).
@@ -50,11 +54,30 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *t
   return r;
 }
 
+// This block's share [lo, hi) of n values, in whole steps (so a share starts
+// 16-byte aligned when the array does).
 __device__ __forceinline__ void scan_chunk(uint32_t n, uint32_t *lo, uint32_t *hi) {
-  const uint32_t chunk = (n + gridDim.x - 1) / gridDim.x;
-  *lo = min(n, blockIdx.x * chunk);
-  *hi = min(n, *lo + chunk);
+  const uint32_t per = (n + gridDim.x - 1) / gridDim.x;
+  const uint32_t chunk = (per + kScanStep - 1) / kScanStep * kScanStep;
+  *lo = (uint32_t)min((unsigned long long)n, (unsigned long long)blockIdx.x * chunk);
+  *hi = (uint32_t)min((unsigned long long)n, (unsigned long long)*lo + chunk);
 }
+
+// A thread's kScanItems values from i (zero past hi).
+__device__ __forceinline__ void scan_load(const uint32_t *__restrict__ in, uint32_t i,
+                                          uint32_t hi, bool vec, uint32_t v[kScanItems]) {
+  if (vec && i + kScanItems <= hi) {
+    const uint4 a = *reinterpret_cast<const uint4 *>(in + i);
+    const uint4 b = *reinterpret_cast<const uint4 *>(in + i + 4);
+    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w;
+    v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+    return;
+  }
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++)
+    v[k] = i + k < hi ? in[i + k] : 0u;
+}
+static_assert(kScanItems == 8, "two 16-byte loads a thread");
 
 static __global__ void __launch_bounds__(kScanThreads)
 scan_sums(const uint32_t *__restrict__ in, const uint32_t *__restrict__ d_n,
@@ -63,9 +86,15 @@ scan_sums(const uint32_t *__restrict__ in, const uint32_t *__restrict__ d_n,
     return;
   uint32_t lo, hi;
   scan_chunk(*d_n, &lo, &hi);
+  const bool vec = reinterpret_cast<uintptr_t>(in) % 16 == 0;
   uint32_t acc = 0;
-  for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-    acc += in[i];
+  for (uint32_t i = lo + threadIdx.x * kScanItems; i < hi; i += kScanStep) {
+    uint32_t v[kScanItems];
+    scan_load(in, i, hi, vec, v);
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++)
+      acc += v[k];
+  }
   for (int o = 16; o; o >>= 1)
     acc += __shfl_xor_sync(0xffffffffu, acc, o);
   __shared__ uint32_t s[32];
@@ -102,14 +131,32 @@ scan_apply(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
     return;
   uint32_t lo, hi;
   scan_chunk(*d_n, &lo, &hi);
+  const bool vec = reinterpret_cast<uintptr_t>(in) % 16 == 0 &&
+                   reinterpret_cast<uintptr_t>(out) % 16 == 0;
   uint32_t carry = block_sums[blockIdx.x];
-  for (uint32_t base = lo; base < hi; base += blockDim.x) {
-    const uint32_t i = base + threadIdx.x;
-    const uint32_t v = i < hi ? in[i] : 0u;
+  for (uint32_t base = lo; base < hi; base += kScanStep) {  // block-uniform
+    const uint32_t i = base + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    scan_load(in, i, hi, vec, v);  // all read before any is written (in may be out)
+    uint32_t t = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+      const uint32_t x = v[k];
+      v[k] = t;
+      t += x;
+    }
     uint32_t total;
-    const uint32_t e = block_exclusive_scan(v, &total);
-    if (i < hi)
-      out[i] = carry + e;
+    const uint32_t e = carry + block_exclusive_scan(t, &total);
+    if (vec && i + kScanItems <= hi) {
+      *reinterpret_cast<uint4 *>(out + i) = make_uint4(e + v[0], e + v[1], e + v[2], e + v[3]);
+      *reinterpret_cast<uint4 *>(out + i + 4) =
+          make_uint4(e + v[4], e + v[5], e + v[6], e + v[7]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < kScanItems; k++)
+        if (i + k < hi)
+          out[i + k] = e + v[k];
+    }
     carry += total;
   }
 }
