@@ -109,7 +109,8 @@ int sf_find_u16_params(const uint16_t *image, size_t height, size_t width,
  * (bitshuffle+LZ4, 16- or 32-bit pixels), "lz4" or "" (uncompressed).
  * Returns 0; -6 (SF_EDATA) where the reference throws, with its text in
  * sf_last_error(); -1 for null pointers; -4 for bitshuffle chunks of other
- * pixel sizes; -3.
+ * pixel sizes, and for blocks of 4 GB or more decoded (2 GB or more
+ * compressed); -3.
  *
  * sf_decompress_image writes the frame to host memory `out`;
  * sf_decompress_device to device memory d_out (16-byte aligned), returning
