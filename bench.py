@@ -56,7 +56,7 @@ H, W = 4362, 4148
 # capture of this bench without cache flushes between kernels (11,235 MB for
 # the launch: lat_stage01 5,266 MB, lat_verify 2,098 MB, lat_stage2 2,621 MB,
 # the scans and the list 1,250 MB); the algorithmic bytes are 76.5 MB a frame.
-DRAM_BYTES_PER_FRAME = 161.2e6
+DRAM_BYTES_PER_FRAME = 162.0e6
 
 
 # Kernels a timed step launches: the threshold plan's graph (lat_stage01,
@@ -1011,9 +1011,9 @@ def run_ours(args):
         else:
             traffic = DRAM_BYTES_PER_FRAME * B
             traffic_source = (
-                "ncu dram__bytes_read.sum + dram__bytes_write.sum over the 8 kernels of one timed "
-                "32-frame launch of this workload (32 frames in HBM, the size a capture may "
-                "hold), no cache flush between kernels "
+                "ncu dram__bytes_read.sum + dram__bytes_write.sum of one timed 32-frame launch "
+                "of this workload (32 frames in HBM), one capture a kernel for its 8 kernels, no "
+                "cache flush between kernels "
                 f"({DRAM_BYTES_PER_FRAME / 1e6:.1f} MB a frame), times the {B} frames of a launch; "
                 "a frame's traffic grows a little with the batch")
         line = {
