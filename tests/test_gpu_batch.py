@@ -91,6 +91,26 @@ def test_batch_parameters(api, params):
         _same(b.result(j), O.dext(f, O.Params(**params)), f"{params} frame {j}")
 
 
+@pytest.mark.parametrize("h,w,n", [(300, 480, 3), (257, 700, 5), (120, 722, 4), (40, 364, 64)])
+def test_batch_16bit_against_oracle(api, h, w, n):
+    # 16-bit frames in one launch (sf_threshold_u16_batch_device): the
+    # lattice path where 4 | width, the tile path otherwise; each frame's
+    # list and mask as the oracle gives them for it alone.
+    import torch
+    frames = []
+    for f in _mixed_frames(h, w, n, seed=h * 7 + w + n):
+        g = np.minimum(f, 0xFFFD).astype(np.uint16)  # valid counts below the markers
+        g[f >= 0xFFFFFFFE] = 0xFFFF
+        frames.append(g)
+    b = api.DeviceBatch(h, w, n, capacity=h * w)
+    b([torch.from_numpy(g.view(np.int16)).cuda() for g in frames])
+    torch.cuda.synchronize()
+    for j, g in enumerate(frames):
+        want, mask = O.dext(g, with_mask=True)
+        _same(b.result(j), want, f"{h}x{w} u16 frame {j} of {n}")
+        assert np.array_equal(b.mask(j), mask.astype(bool)), f"mask of u16 frame {j}"
+
+
 def test_batch_unaligned_frames(api):
     frames = _mixed_frames(180, 400, 4, seed=3)
     b = _run(api, frames, offset=1)
