@@ -379,8 +379,9 @@ public:
     if ((e = cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking)) != cudaSuccess)
       return fail(e, "cudaStreamCreate");
     // The small results read back: the count (word 0), the decoder's error
-    // record (1-3), the narrowing's largest value (4), a frame scan (words
-    // 6-13, four 64-bit counts); the same layout on both sides.
+    // record (1-3), the narrowing's largest value (4), the decoder's block
+    // counter (5, device only), a frame scan (words 6-13, four 64-bit
+    // counts); the same layout on both sides.
     if ((e = cudaMalloc(&count_, kWords * sizeof(uint32_t))) != cudaSuccess)
       return fail(e, "cudaMalloc for the count");
     if ((e = cudaMallocHost(&host_count_, kWords * sizeof(uint32_t))) != cudaSuccess)
@@ -388,7 +389,7 @@ public:
     return SF_OK;
   }
 
-  static constexpr int kWords = 16, kWorst = 4, kScan = 6;
+  static constexpr int kWords = 16, kWorst = 4, kNext = 5, kScan = 6;
   unsigned long long *scan_words() {
     return reinterpret_cast<unsigned long long *>(count_ + kScan);
   }
@@ -446,10 +447,11 @@ public:
     if ((e = cudaMemcpyAsync(table_, table_host_, table_bytes, cudaMemcpyHostToDevice,
                              stream_)) != cudaSuccess)
       return fail(e, "copying the block table to the device");
-    if ((e = cudaMemsetAsync(count_ + 1, 0, 3 * sizeof(uint32_t), stream_)) != cudaSuccess)
+    if ((e = cudaMemsetAsync(count_ + 1, 0, 3 * sizeof(uint32_t), stream_)) != cudaSuccess ||
+        (e = cudaMemsetAsync(count_ + kNext, 0, sizeof(uint32_t), stream_)) != cudaSuccess)
       return fail(e, "cudaMemsetAsync");
     if ((e = launch_decode(chunk_, table_, plan.blocks.size(), plan.element, d_frame,
-                           scratch_, count_ + 1, stream_)) != cudaSuccess)
+                           scratch_, count_ + 1, count_ + kNext, stream_)) != cudaSuccess)
       return fail(e, "launching the decoder");
     if ((e = cudaMemcpyAsync(host_count_ + 1, count_ + 1, 3 * sizeof(uint32_t),
                              cudaMemcpyDeviceToHost, stream_)) != cudaSuccess)

@@ -392,13 +392,21 @@ template <int E>
 __global__ void __launch_bounds__(kDecWarps * 32)
 k_decode(const uint8_t *__restrict__ in, const DecodeBlock *__restrict__ blocks,
          uint32_t nblocks, uint8_t *__restrict__ out, uint8_t *__restrict__ scratch,
-         uint32_t *__restrict__ status) {
+         uint32_t *__restrict__ status, uint32_t *__restrict__ next) {
   __shared__ __align__(16) uint8_t buf[kDecWarps][kDecBuf];
   // Word copies pay on the planes of 32-bit pixels (long repeats between
   // planes); on those of 16-bit pixels byte copies measured faster.
   constexpr bool kWords = E == 4;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (uint32_t b = blockIdx.x * kDecWarps + warp; b < nblocks; b += gridDim.x * kDecWarps) {
+  // Blocks are taken in turn from one counter: a warp that finishes early
+  // takes the next, so that blocks of uneven cost even out.
+  auto take = [&]() {
+    uint32_t b = 0;
+    if (lane == 0)
+      b = atomicAdd(next, 1u);
+    return __shfl_sync(0xffffffffu, b, 0);
+  };
+  for (uint32_t b = take(); b < nblocks; b = take()) {
     const DecodeBlock d = blocks[b];
     const uint8_t *src = in + d.in_off;
     uint8_t *dst = out + d.out_off;
@@ -567,7 +575,7 @@ int plan_chunk(const uint8_t *data, size_t nbytes, const char *algorithm, unsign
 
 cudaError_t launch_decode(const uint8_t *d_payload, const DecodeBlock *d_blocks, size_t nblocks,
                           unsigned element, uint8_t *d_frame, uint8_t *d_scratch,
-                          uint32_t *d_status, cudaStream_t stream) {
+                          uint32_t *d_status, uint32_t *d_next, cudaStream_t stream) {
   if (nblocks == 0)
     return cudaSuccess;
   // One wave: the shared buffers allow 6 blocks of 4 warps an SM.
@@ -575,10 +583,10 @@ cudaError_t launch_decode(const uint8_t *d_payload, const DecodeBlock *d_blocks,
   const int grid = (int)std::min<size_t>(want, (size_t)device_sms() * 6);
   if (element == 2)
     k_decode<2><<<grid, kDecWarps * 32, 0, stream>>>(d_payload, d_blocks, (uint32_t)nblocks,
-                                                     d_frame, d_scratch, d_status);
+                                                     d_frame, d_scratch, d_status, d_next);
   else
     k_decode<4><<<grid, kDecWarps * 32, 0, stream>>>(d_payload, d_blocks, (uint32_t)nblocks,
-                                                     d_frame, d_scratch, d_status);
+                                                     d_frame, d_scratch, d_status, d_next);
   return cudaGetLastError();
 }
 

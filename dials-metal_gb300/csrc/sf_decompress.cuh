@@ -50,10 +50,11 @@ int plan_chunk(const uint8_t *data, size_t nbytes, const char *algorithm, unsign
 
 // Decodes the table's blocks of d_payload into d_frame (16-byte aligned).
 // d_scratch (plan.frame_bytes) is needed when plan.scratch is set; d_status
-// (3 words, zeroed by the caller) receives the first error seen.
+// (3 words, zeroed by the caller) receives the first error seen; d_next (a
+// word, zeroed by the caller) hands the blocks out to the warps.
 cudaError_t launch_decode(const uint8_t *d_payload, const DecodeBlock *d_blocks, size_t nblocks,
                           unsigned element, uint8_t *d_frame, uint8_t *d_scratch,
-                          uint32_t *d_status, cudaStream_t stream);
+                          uint32_t *d_status, uint32_t *d_next, cudaStream_t stream);
 
 // The reference's exception text for a decoder error record.
 std::string decode_error_text(const ChunkPlan &plan, const uint32_t status[3]);

@@ -316,11 +316,11 @@ cudaError_t sf_server::upload_chunk(SrvSweep &s, const SrvFrame &f, int ci) {
           cudaSuccess ||
       (e = cudaMemcpyAsync(s.tables[k], s.host_tables[k], tb, cudaMemcpyHostToDevice, cs)) !=
           cudaSuccess ||
-      (e = cudaMemsetAsync(s.dec_status + 4 * k, 0, 3 * sizeof(uint32_t), cs)) != cudaSuccess)
+      (e = cudaMemsetAsync(s.dec_status + 4 * k, 0, 4 * sizeof(uint32_t), cs)) != cudaSuccess)
     return e;
   return sf::launch_decode(st.chunk, s.tables[k], p.blocks.size(), p.element,
                            reinterpret_cast<uint8_t *>(s.slots[k]), st.scratch,
-                           s.dec_status + 4 * k, cs);
+                           s.dec_status + 4 * k, s.dec_status + 4 * k + 3, cs);
 }
 
 void sf_server::label_loop(SrvSweep *s) {
