@@ -152,25 +152,40 @@ __device__ __forceinline__ uint32_t lower_bound_warp(const uint32_t *__restrict_
 // Kernels of one batch, in launch order.
 // ---------------------------------------------------------------------------
 
+// Each frame's offset in the batch, the exclusive prefix of the counts: one
+// warp, frames 2l and 2l + 1 on lane l.
+static_assert(kLabelMaxBatch <= 64, "two frames a lane");
 __global__ void k_offsets(LabelStatus *st, const BatchArgs *__restrict__ ap,
                           uint32_t capacity) {
-  if (threadIdx.x != 0 || st->error)
+  if (st->error)
     return;
   const BatchArgs &a = *ap;
-  const uint32_t *counts = a.counts;
-  const size_t stride = a.stride;
-  uint32_t off = 0;
-  for (int j = 0; j < a.nb; j++) {
-    st->frame_off[j] = off;
-    // A list whose count exceeds its stride is one that overflowed its
-    // threshold's capacity: it is incomplete, and refused.
-    if (counts[j] > stride) {
+  const int lane = threadIdx.x & 31, nb = a.nb;
+  const int j0 = 2 * lane, j1 = j0 + 1;
+  const uint32_t c0 = j0 < nb ? a.counts[j0] : 0u, c1 = j1 < nb ? a.counts[j1] : 0u;
+  // A list whose count exceeds its stride is one that overflowed its
+  // threshold's capacity: it is incomplete, and refused.
+  if (__any_sync(0xffffffffu, c0 > a.stride || c1 > a.stride)) {
+    if (lane == 0)
       st->error |= kErrListOverflow;
-      return;
-    }
-    off += counts[j];
+    return;
   }
-  st->frame_off[a.nb] = off;
+  uint32_t incl = c0 + c1;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o)
+      incl += t;
+  }
+  const uint32_t excl = incl - c0 - c1;
+  if (j0 < nb)
+    st->frame_off[j0] = excl;
+  if (j1 < nb)
+    st->frame_off[j1] = excl + c0;
+  const uint32_t off = __shfl_sync(0xffffffffu, incl, 31);
+  if (lane != 0)
+    return;
+  st->frame_off[nb] = off;
   st->n_big = 0;
   st->n_edges = 0;
   const unsigned long long total = (unsigned long long)st->n_live + off;
@@ -509,19 +524,39 @@ k_bucket_hist(LabelStatus *st, const uint32_t *__restrict__ cbucket, uint32_t *h
     hist[blockIdx.x * kBuckets + b] = h[b];
 }
 
-// Exclusive scan over (bucket, block) in bucket-major order, in place.
+// Exclusive scan over (bucket, block) in bucket-major order, in place: a warp
+// scans a bucket's counts (each lane a run of blocks), then the buckets'
+// totals are scanned and added.
 __global__ void __launch_bounds__(1024) k_bucket_offsets(LabelStatus *st, uint32_t *hist) {
   if (st->error)
     return;
   __shared__ uint32_t btotal[kBuckets];
-  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) {
-    uint32_t run = 0;
-    for (int blk = 0; blk < kGrid; blk++) {
-      const uint32_t v = hist[blk * kBuckets + b];
-      hist[blk * kBuckets + b] = run;
-      run += v;
+  constexpr int kPer = (kGrid + 31) / 32;  // blocks a lane
+  const int lane = threadIdx.x & 31;
+  const int lo = min(kGrid, lane * kPer), hi = min(kGrid, lo + kPer);
+  for (int b = threadIdx.x >> 5; b < kBuckets; b += blockDim.x >> 5) {  // warp-uniform
+    uint32_t v[kPer], sum = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+      v[k] = lo + k < hi ? hist[(lo + k) * kBuckets + b] : 0u;
+      sum += v[k];
     }
-    btotal[b] = run;
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o)
+        incl += t;
+    }
+    uint32_t run = incl - sum;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+      if (lo + k < hi)
+        hist[(lo + k) * kBuckets + b] = run;
+      run += v[k];
+    }
+    if (lane == 31)
+      btotal[b] = incl;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -533,9 +568,8 @@ __global__ void __launch_bounds__(1024) k_bucket_offsets(LabelStatus *st, uint32
     }
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < kBuckets; b += blockDim.x)
-    for (int blk = 0; blk < kGrid; blk++)
-      hist[blk * kBuckets + b] += btotal[b];
+  for (int i = threadIdx.x; i < kGrid * kBuckets; i += blockDim.x)
+    hist[i] += btotal[i % kBuckets];
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -1555,8 +1589,7 @@ static cudaError_t load_label_kernels() {
       (const void *)k_sort_big,       (const void *)k_perm_hist,     (const void *)k_perm_offsets,
       (const void *)k_perm_scatter,   (const void *)k_first,         (const void *)k_pix,
       (const void *)k_terms,          (const void *)k_var,           (const void *)k_compact,
-      (const void *)k_end_batch,      (const void *)scan_sums,       (const void *)scan_block_sums,
-      (const void *)scan_apply};
+      (const void *)k_end_batch,      (const void *)scan_sums,       (const void *)scan_apply};
   for (const void *k : kernels) {
     cudaFuncAttributes a;
     const cudaError_t e = cudaFuncGetAttributes(&a, k);
@@ -1765,7 +1798,7 @@ struct Labeller {
       return e;
     k_closing_list<<<kPassGrid, kThreads, 0, s>>>(st, ap, flag, posa, zlast, clist, cbucket);
     k_bucket_hist<<<kGrid, kThreads, 0, s>>>(st, cbucket, hist);
-    k_bucket_offsets<<<1, 128, 0, s>>>(st, hist);
+    k_bucket_offsets<<<1, 1024, 0, s>>>(st, hist);
     k_bucket_scatter<<<kGrid, kThreads, 0, s>>>(st, clist, cbucket, hist, order);
     k_size_filter<<<kPassGrid, kThreads, 0, s>>>(st, ap, order, csize, cflag);
     if ((e = exclusive_scan(cflag, cpos, &st->n_closing, &st->n_cand, block_sums, err, s)) !=

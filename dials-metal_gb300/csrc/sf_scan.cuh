@@ -1,9 +1,10 @@
 // Device-wide exclusive scan of uint32 values whose count lives on the
 // device, so a pipeline of kernels never has to read a size back to the host.
-// Three launches on a fixed grid: per-block chunk sums, a one-block scan of
-// those, then each block rescans its chunk with its offset. A thread takes
-// kScanItems consecutive values (two 16-byte loads where the chunk allows),
-// so a block scans kScanThreads * kScanItems values a step.
+// Two launches on a fixed grid: per-block chunk sums, then each block rescans
+// its chunk with its offset, which it takes from its own block scan of the
+// chunk sums (block 0 also writes the total). A thread takes kScanItems
+// consecutive values (two 16-byte loads where the chunk allows), so a block
+// scans kScanThreads * kScanItems values a step.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -15,6 +16,7 @@ constexpr int kScanBlocks = 512;
 constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
 constexpr uint32_t kScanStep = kScanThreads * kScanItems;  // values a block step
+static_assert(kScanBlocks <= kScanThreads, "a chunk sum a thread in the offset scan");
 
 // Block-wide exclusive scan of one value per thread; returns the exclusive
 // prefix and writes the block total to *total (all threads see it).
@@ -109,31 +111,27 @@ scan_sums(const uint32_t *__restrict__ in, const uint32_t *__restrict__ d_n,
   }
 }
 
-static __global__ void __launch_bounds__(kScanBlocks)
-scan_block_sums(uint32_t *__restrict__ block_sums, uint32_t *__restrict__ d_total,
-                const uint32_t *__restrict__ d_error) {
-  if (d_error && *d_error)
-    return;
-  uint32_t total;
-  const uint32_t v = threadIdx.x < kScanBlocks ? block_sums[threadIdx.x] : 0u;
-  const uint32_t e = block_exclusive_scan(v, &total);
-  if (threadIdx.x < kScanBlocks)
-    block_sums[threadIdx.x] = e;
-  if (threadIdx.x == 0 && d_total)
-    *d_total = total;
-}
-
 static __global__ void __launch_bounds__(kScanThreads)
 scan_apply(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
            const uint32_t *__restrict__ d_n, const uint32_t *__restrict__ block_sums,
-           const uint32_t *__restrict__ d_error) {
+           uint32_t *__restrict__ d_total, const uint32_t *__restrict__ d_error) {
   if (d_error && *d_error)
     return;
+  // This block's offset: the chunk sums of the blocks before it.
+  __shared__ uint32_t s_carry;
+  uint32_t all;
+  const uint32_t bs = threadIdx.x < kScanBlocks ? block_sums[threadIdx.x] : 0u;
+  const uint32_t be = block_exclusive_scan(bs, &all);
+  if (threadIdx.x == blockIdx.x)
+    s_carry = be;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && d_total)
+    *d_total = all;
+  __syncthreads();
   uint32_t lo, hi;
   scan_chunk(*d_n, &lo, &hi);
   const bool vec = reinterpret_cast<uintptr_t>(in) % 16 == 0 &&
                    reinterpret_cast<uintptr_t>(out) % 16 == 0;
-  uint32_t carry = block_sums[blockIdx.x];
+  uint32_t carry = s_carry;
   for (uint32_t base = lo; base < hi; base += kScanStep) {  // block-uniform
     const uint32_t i = base + threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
@@ -162,14 +160,15 @@ scan_apply(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
 }
 
 // out[i] = sum of in[0..i) for i < *d_n; *d_total = sum of all. `in` and
-// `out` may alias. block_sums holds kScanBlocks words. Skipped entirely when
+// `out` may alias; d_total may not be d_n (block 0 writes it while the others
+// read d_n). block_sums holds kScanBlocks words. Skipped entirely when
 // *d_error is non-zero (d_error may be null).
 inline cudaError_t exclusive_scan(const uint32_t *in, uint32_t *out, const uint32_t *d_n,
                                   uint32_t *d_total, uint32_t *block_sums,
                                   const uint32_t *d_error, cudaStream_t stream) {
   scan_sums<<<kScanBlocks, kScanThreads, 0, stream>>>(in, d_n, block_sums, d_error);
-  scan_block_sums<<<1, kScanBlocks, 0, stream>>>(block_sums, d_total, d_error);
-  scan_apply<<<kScanBlocks, kScanThreads, 0, stream>>>(in, out, d_n, block_sums, d_error);
+  scan_apply<<<kScanBlocks, kScanThreads, 0, stream>>>(in, out, d_n, block_sums, d_total,
+                                                       d_error);
   return cudaGetLastError();
 }
 
