@@ -45,8 +45,9 @@ constexpr int kThreads = 256;
 constexpr int kGrid = 2 * 152;          // the bucket partition's chunks
 constexpr int kPassGrid = 8 * 152;      // grid-stride passes over pixels / candidates
 constexpr int kSortGrid = 6 * 152;      // warp sorts: 6 blocks an SM (registers)
-constexpr int kWarpSortMax = 1024;      // members sorted by one warp
-constexpr int kWarpSegMax = 64;         // runs a warp orders without sorting the members
+constexpr int kWarpSortMax = 512;       // members ordered by one warp
+constexpr int kWarpSegMax = 128;        // runs a warp orders without sorting the members
+constexpr int kSegPerLane = kWarpSegMax / 32;
 constexpr uint32_t kRunHead = 0x80000000u;  // a member slot's flag: the first of its run
 constexpr uint32_t kPosMask = 0x7FFFFFFFu;  // a member slot's position (below 2^31)
 constexpr int kBlockSortMax = 8192;     // members sorted by one block
@@ -704,7 +705,7 @@ __global__ void k_gather(LabelStatus *st, const uint32_t *__restrict__ root,
 // length needs no padding: a comparator whose second element lies at or
 // beyond n would leave the first in place, as if against +infinity, and is
 // skipped. Threads walk the comparators, not the elements.
-__device__ void bitonic_sort(uint32_t *s, int n, int t, int nt, bool warp_only) {
+__device__ void bitonic_sort(uint32_t *s, int n, int t, int nt) {
   int size = 1;
   while (size < n)
     size <<= 1;
@@ -729,10 +730,7 @@ __device__ void bitonic_sort(uint32_t *s, int n, int t, int nt, bool warp_only) 
           }
         }
       }
-      if (warp_only)
-        __syncwarp();
-      else
-        __syncthreads();
+      __syncthreads();
     }
   }
 }
@@ -817,7 +815,8 @@ __device__ __forceinline__ bool fp_finish(FirstPass &f) {
 // the reference's, in its order; the work is laid out so that the lanes of
 // each FP64 instruction are busy:
 //
-//   k_sort         a warp per candidate (a block beyond kWarpSortMax members,
+//   k_sort         a warp per candidate (a block beyond kWarpSortMax members
+//                  or kWarpSegMax runs,
 //                  a block sorting in global memory beyond kBlockSortMax):
 //                  members sorted into (frame, index) order and copied out as
 //                  pixel records, each tagged with its candidate.
@@ -967,14 +966,14 @@ __device__ __forceinline__ void put_member(uint32_t q, uint32_t k, uint32_t c, u
   mcand[off + k] = c;
 }
 
-// Candidates of up to kWarpSortMax members, a warp each (BLOCK false), or of
-// up to kBlockSortMax, a block each (BLOCK true, from the list the warps
-// made): member positions put in ascending order in shared memory, then
-// copied out in member order as pixel records. A warp's candidate of at most
-// kWarpSegMax runs (k_gather's runs of ascending positions, each from its
-// own range of positions) is ordered by its runs: a run's place is the
-// total length of the runs whose first position is smaller. Others are
-// sorted by bitonic sort.
+// Member positions put in ascending order, then copied out in member order
+// as pixel records. A warp each (BLOCK false): a candidate of up to 32
+// members is sorted in registers; one of up to kWarpSortMax members in at
+// most kWarpSegMax runs (k_gather's runs of ascending positions, each from
+// its own range of positions) is ordered by its runs: a run's place is the
+// total length of the runs whose first position is smaller. The others, up
+// to kBlockSortMax members, go on a list for a block each (BLOCK true),
+// which sorts them in shared memory (bitonic).
 template <bool BLOCK>
 __global__ void __launch_bounds__(kThreads)
 k_sort(LabelStatus *st, const uint32_t *__restrict__ cand_n,
@@ -1025,24 +1024,27 @@ k_sort(LabelStatus *st, const uint32_t *__restrict__ cand_n,
       }
       __syncwarp();
       if (nrun <= (uint32_t)kWarpSegMax && seg[0] == 0u) {  // slot 0 always heads a run
-        // A lane's runs j = lane and lane + 32: their first positions, then
-        // the total length of the runs whose first position is smaller.
-        uint32_t first[2], place[2] = {0u, 0u};
+        // A lane's runs j = lane + 32 h: their first positions, then the
+        // total length of the runs whose first position is smaller.
+        const int hn = (int)((nrun + 31u) >> 5);  // a lane's runs in use (warp-uniform)
+        uint32_t first[kSegPerLane], place[kSegPerLane];
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < kSegPerLane; h++) {
           const uint32_t j = (uint32_t)lane + 32u * h;
           first[h] = j < nrun ? seg[kWarpSegMax + j] : kNone;
+          place[h] = 0u;
         }
         for (uint32_t t = 0; t < nrun; t++) {  // warp-uniform
           const uint32_t ft = seg[kWarpSegMax + t];
           const uint32_t lt = (t + 1 < nrun ? seg[t + 1] : n) - seg[t];
 #pragma unroll
-          for (int h = 0; h < 2; h++)
-            place[h] += ft < first[h] ? lt : 0u;
+          for (int h = 0; h < kSegPerLane; h++)
+            if (h < hn)
+              place[h] += ft < first[h] ? lt : 0u;
         }
         __syncwarp();
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < kSegPerLane; h++) {
           const uint32_t j = (uint32_t)lane + 32u * h;
           if (j < nrun)
             seg[kWarpSegMax + j] = place[h];
@@ -1063,12 +1065,10 @@ k_sort(LabelStatus *st, const uint32_t *__restrict__ cand_n,
         __syncwarp();  // the next candidate reuses the shared rows
         continue;
       }
-      for (uint32_t i = lane; i < n; i += 32)
-        s[i] &= kPosMask;
-      __syncwarp();
-      bitonic_sort(s, (int)n, lane, 32, true);
-      for (uint32_t i = lane; i < n; i += 32)
-        put_member(s[i], i, c, off, frame, index, value, mpix, mcand);
+      // More runs than a warp orders: a block sorts the members (a warp's
+      // sort of a few hundred members would hold up its SM's last wave).
+      if (lane == 0)
+        big[atomicAdd(&st->n_big, 1u)] = c;
       __syncwarp();  // the next candidate reuses the shared rows
     }
   } else {
@@ -1083,7 +1083,7 @@ k_sort(LabelStatus *st, const uint32_t *__restrict__ cand_n,
       for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
         s_sort[i] = m[i] & kPosMask;
       __syncthreads();
-      bitonic_sort(s_sort, (int)n, threadIdx.x, blockDim.x, false);
+      bitonic_sort(s_sort, (int)n, threadIdx.x, blockDim.x);
       for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
         put_member(s_sort[i], i, c, off, frame, index, value, mpix, mcand);
       __syncthreads();
@@ -1742,7 +1742,9 @@ struct Labeller {
     if (height <= kRowTableMaxRows)
       SF_ALLOC(rows, (size_t)(kLabelMaxBatch + 1) * (height + 1));
     SF_ALLOC(mcand, n);
-    SF_ALLOC(big, n / (kWarpSortMax + 1) + 1);
+    // Every candidate a block sorts has more than 32 members (fewer are
+    // sorted in a warp's registers).
+    SF_ALLOC(big, n / 33 + 1);
     SF_ALLOC(mpix, n);
     SF_ALLOC(cspots, spots_cap);
     SF_ALLOC(perm, spots_cap);

@@ -300,3 +300,40 @@ def test_spots_beyond_shared_memory_sorts_against_oracle(max_spot_size):
     d.add_device([0, 1, 2, 3], dev.data_ptr(), cap, counts.data_ptr(),
                  torch.cuda.current_stream().cuda_stream)
     _same(d.finish(), want, f"one call, max_spot_size {max_spot_size}")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bad", [0, 33, 63])
+def test_device_list_beyond_its_stride_is_refused(bad):
+    """A count above the lists' stride (a threshold that overflowed) fails the
+    whole call, wherever the frame sits in a 64-frame batch; the same batch
+    with every count in range labels as the oracle does."""
+    import torch
+    from sfgb import labeller
+    h, w, nb, cap = 20, 30, 64, 40
+    rng = np.random.default_rng(5 + bad)
+    lists = []
+    for f in range(nb):
+        idx = np.sort(rng.choice(h * w, size=int(rng.integers(0, cap + 1)), replace=False))
+        s = np.zeros(len(idx), O.SIGNAL_DTYPE)
+        s["index"] = idx
+        s["value"] = rng.integers(1, 100, len(idx))
+        lists.append(s)
+    dev = torch.zeros((nb, cap * 16), dtype=torch.uint8, device="cuda")
+    for j, s in enumerate(lists):
+        dev[j, : len(s) * 16] = torch.from_numpy(s.view(np.uint8).copy()).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    counts = [len(s) for s in lists]
+    lab = O.Labeller(h, w)
+    for f, s in enumerate(lists):
+        lab.add(f, s)
+    want = lab.finish()
+    d = labeller.DeviceLabeller(h, w)
+    ok = torch.tensor(counts, dtype=torch.int32, device="cuda")
+    d.add_device(list(range(nb)), dev.data_ptr(), cap, ok.data_ptr(), stream)
+    _same(d.finish(), want, "64 frames in one call")
+    counts[bad] = cap + 1
+    over = torch.tensor(counts, dtype=torch.int32, device="cuda")
+    d = labeller.DeviceLabeller(h, w)
+    with pytest.raises(RuntimeError, match="exceeds its capacity"):
+        d.add_device(list(range(nb)), dev.data_ptr(), cap, over.data_ptr(), stream)
