@@ -220,8 +220,9 @@ def run_reference(args):
             "config": run_config(args.frames_per_step, args.pool), "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "frames/s", "cores": best["cores"],
                              "kind": "port", "sample": best["sample"] +
-                             " (the reference's CPU dext/Labeller restated in C: the "
-                             "reference tree is not on this host)"},
+                             " (the reference's CPU dext/Labeller restated in C and pinned "
+                             "to the reference's own output; the reference's own build "
+                             "does not travel to the GPU host)"},
             "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

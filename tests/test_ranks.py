@@ -67,3 +67,26 @@ def test_reference_arm_runs_on_rank_0_only(monkeypatch, capsys):
     assert bench.main(["--impl", "reference", "--gpus", "2", "--steps", "1",
                        "--warmup", "0"]) == 0
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line_on_rank_0(monkeypatch, capsys):
+    """At N=1 the reference arm prints one line in the bench's contract: the
+    CPU port's frames/s as the value, described by its cpu_baseline, and an
+    e2e with no device copies."""
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    assert bench.main(["--impl", "reference", "--steps", "1", "--warmup", "0"]) == 0
+    lines = [l for l in capsys.readouterr().out.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "frames/s" and d["n_gpus"] == 1
+    assert d["higher_is_better"] is True and d["steps"] == 1 and d["value"] > 0
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "frames/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"].startswith("eiger_16m")
