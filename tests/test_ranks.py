@@ -90,3 +90,17 @@ def test_reference_arm_line_on_rank_0(monkeypatch, capsys):
     assert d["e2e"] == {"value": d["value"], "unit": "frames/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
     assert d["config"]["workload"].startswith("eiger_16m")
+
+
+def test_our_arm_fails_loudly_without_a_device(monkeypatch):
+    """No CPU stand-in: without a usable GPU the bench's own arm stops with the
+    reason instead of printing a line."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from sfgb import api
+    if api.available():
+        pytest.skip("a device is present")
+    monkeypatch.setenv("RANK", "0")
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    with pytest.raises(SystemExit, match="no usable GB300"):
+        bench.main(["--steps", "1", "--warmup", "0"])
